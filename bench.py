@@ -1,0 +1,359 @@
+"""Benchmark of the 2-D Jacobi sweep hot path on GB300.
+
+Workload (one bench step): box2d2r (25-point) Jacobi on an 8192 x 8192
+interior with a 2-cell zero halo (8196^2 grid), FP16 storage / FP32
+accumulate, 100 ping-pong timesteps, tensor-core engine — the plain box2d2r
+configuration of the reference's headline comparison.  Inputs are seeded
+synthetic U[-1,1) grids with coefficients U[0,1) normalised to sum 1 (the
+reference ships no datasets; its benchmark meshes are synthetic too).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is device-timed Gpts/s (point-updates per
+second) with the grid resident in HBM; `e2e` is the same metric through the
+public one-call C-ABI (tcs_sweep_host) with pinned host buffers, host<->device
+copies inside the timed region.  Each brick plane is 134 MB and a sweep
+alternates two of them, so the working set (269 MB) exceeds the 129 MB L2.
+`--impl reference` times the CPU gold code (the oracle's restatement of
+common/gold_box2d2r.cpp) on the host cores.  With torchrun (N > 1) every rank
+sweeps its own replica grid (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+INTERIOR = 8192
+HALO = 2
+TIMESTEPS = 100
+STENCIL = "box2d2r"
+BYTES_PER_UPDATE = {"f16": 4, "split": 8, "f32": 8}
+FLOPS_PER_UPDATE = {"star2d1r": 10, "star2d2r": 18, "box2d1r": 18, "box2d2r": 50}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--stencil", default=STENCIL)
+    ap.add_argument("--engine", default="tensor")
+    ap.add_argument("--precision", default="f16")
+    ap.add_argument("--interior", type=int, default=INTERIOR)
+    ap.add_argument("--timesteps", type=int, default=TIMESTEPS)
+    ap.add_argument("--no-extras", action="store_true", help="skip comparator and CPU legs")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling driver: upload the grid, run --timesteps single-step "
+                         "launches (no graph), exit; for ncu captures")
+    return ap.parse_args()
+
+
+def run_profile(args):
+    import torch
+
+    import tcstencil_gb300 as tcs
+
+    n = args.interior + 2 * HALO
+    A, B = make_inputs(n, args.stencil, 1000)
+    plan = tcs.Plan(n, n, args.stencil, B, engine=args.engine, precision=args.precision)
+    plan.upload(A)
+    plan.run(args.timesteps, use_graph=False)
+    torch.cuda.synchronize()
+    assert tcs.device_error() == 0
+    plan.close()
+    print(f"profile run: {args.stencil}/{args.engine}/{args.precision} {n}^2 x {args.timesteps}")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
+
+
+def make_inputs(n_grid: int, stencil: str, seed: int):
+    rng = np.random.default_rng(seed)
+    r = 1 if stencil in ("star2d1r", "box2d1r") else 2
+    n = 2 * r + 1
+    A = np.zeros((n_grid, n_grid), np.float32)
+    A[HALO:-HALO, HALO:-HALO] = rng.uniform(-1, 1, (n_grid - 2 * HALO,) * 2).astype(np.float32)
+    B = rng.random((n, n))
+    if stencil.startswith("star"):
+        m = np.zeros((n, n), bool)
+        m[r, :] = True
+        m[:, r] = True
+        B = np.where(m, B, 0.0)
+    return A, (B / B.sum()).astype(np.float32)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(stencil, engine, precision):
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    e = d.get(f"{stencil}/{engine}/{precision}")
+    return e.get("dram_bytes_per_launch") if e else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-i", str(gpu_index),
+                                       "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [ln.split(", ") for ln in self.f.read().strip().splitlines() if ln.count(",") >= 9]
+        os.unlink(self.f.name)
+        return rows
+
+    @staticmethod
+    def summarize(rows):
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        smax = [float(r[3]) for r in rows if r[3].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[6 + i].strip() == "Active"})
+        loaded = [s for s in sm if smax and s > 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows),
+                "power_w_max": max((float(r[4]) for r in rows if r[4].strip().replace(".", "").isdigit()),
+                                   default=None)}
+
+
+def cpu_baseline(stencil: str, budget_s: float = 8.0):
+    """Gold (oracle restatement of common/gold_*.cpp) on every host core: each
+    thread sweeps its own 1028^2 grid copy (1024^2 interior)."""
+    import oracle
+
+    threads = os.cpu_count() or 1
+    A, B = make_inputs(1024 + 2 * HALO, stencil, 7)
+    t1 = oracle.gold_bench(A, B, stencil, 1, threads)
+    steps = max(1, int(budget_s / max(t1, 1e-3)))
+    t = oracle.gold_bench(A, B, stencil, steps, threads)
+    pts = threads * 1024 * 1024 * steps
+    return {"value": pts / t / 1e9, "unit": "Gpts/s", "cores": threads, "kind": "port",
+            "sample": f"{threads} threads x {steps} {stencil} gold steps on a 1028^2 grid "
+                      f"(1024^2 interior), {t:.1f} s"}
+
+
+def run_reference(args):
+    rank, _, ws = dist_env()
+    if rank != 0:
+        return
+    import oracle
+
+    threads = os.cpu_count() or 1
+    A, B = make_inputs(1024 + 2 * HALO, args.stencil, 7)
+    for _ in range(args.warmup):
+        oracle.gold_bench(A, B, args.stencil, 1, threads)
+    t = 0.0
+    for _ in range(args.steps):
+        t += oracle.gold_bench(A, B, args.stencil, 1, threads)
+    pts = threads * 1024 * 1024 * args.steps
+    v = pts / t / 1e9
+    print(json.dumps({
+        "impl": "reference", "metric": f"{args.stencil} Jacobi point-updates per second",
+        "value": v, "unit": "Gpts/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": v, "unit": "Gpts/s", "cores": threads, "kind": "port",
+                         "sample": f"each step: {threads} threads x 1 gold step on its own "
+                                   "1028^2 grid (1024^2 interior)"},
+        "e2e": {"value": v, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def workload_config(args):
+    n = args.interior + 2 * HALO
+    return {"workload": f"{args.stencil} Jacobi, {args.interior}x{args.interior} interior + "
+                        f"{HALO}-cell zero halo ({n}^2 grid), {args.timesteps} ping-pong "
+                        f"timesteps per bench step",
+            "stencil": args.stencil, "grid": [n, n], "timesteps": args.timesteps,
+            "engine": args.engine, "precision": args.precision,
+            "storage": "f32" if args.precision == "f32" else "f16",
+            "accumulate": "f32", "parallelism": "replicas",
+            "l2": "inputs larger than L2 (two 134 MB brick planes > 129 MB L2)"}
+
+
+def timed_sweeps(torch, tcs, plan, K, W, timesteps, stream):
+    for _ in range(W):
+        plan.run(timesteps, use_graph=True, stream=stream)
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(K):
+        plan.run(timesteps, use_graph=True, stream=stream)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop) / 1e3
+
+
+def run_ours(args):
+    import torch
+
+    import tcstencil_gb300 as tcs
+
+    rank, local_rank, ws = dist_env()
+    torch.cuda.set_device(local_rank)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    n = args.interior + 2 * HALO
+    A, B = make_inputs(n, args.stencil, 1000 + rank)
+    stream = torch.cuda.current_stream()
+    plan = tcs.Plan(n, n, args.stencil, B, engine=args.engine, precision=args.precision)
+    plan.upload(A)
+    torch.cuda.synchronize()
+    updates_per_step = args.interior * args.interior * args.timesteps
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up, then the timed region with clocks sampled during it
+    for _ in range(args.warmup):
+        plan.run(args.timesteps, use_graph=True, stream=stream)
+    barrier()
+    sampler = ClockSampler(local_rank) if rank == 0 else None
+    barrier()
+    t = timed_sweeps(torch, tcs, plan, args.steps, 0, args.timesteps, stream)
+    clocks = ClockSampler.summarize(sampler.stop()) if sampler else None
+    tmax = t
+    if ws > 1:
+        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        tmax = float(tt.item())
+    assert tcs.device_error() == 0
+    value = ws * updates_per_step * args.steps / tmax / 1e9
+    launch_s = t / (args.steps * args.timesteps)
+    bpu = BYTES_PER_UPDATE[args.precision]
+    achieved = bpu * args.interior * args.interior / launch_s / 1e9
+    peak, peak_kind = load_peaks()
+    traffic = load_traffic(args.stencil, args.engine, args.precision)
+
+    # e2e through the one-call C-ABI with pinned host buffers
+    h_in = torch.from_numpy(A).pin_memory().numpy()
+    h_out = torch.empty((n, n), dtype=torch.float32).pin_memory().numpy()
+    e2e_steps = max(3, args.steps // 4)
+    for _ in range(2):
+        tcs.sweep_host(h_in, args.timesteps, args.stencil, B, engine=args.engine,
+                       precision=args.precision, h_out=h_out)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        tcs.sweep_host(h_in, args.timesteps, args.stencil, B, engine=args.engine,
+                       precision=args.precision, h_out=h_out)
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    if ws > 1:
+        tt = torch.tensor([te], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        te = float(tt.item())
+    e2e = {"value": ws * updates_per_step * e2e_steps / te / 1e9, "unit": "Gpts/s",
+           "h2d_bytes_per_step": n * n * 4, "d2h_bytes_per_step": n * n * 4,
+           "api": "tcs_sweep_host (pinned host FP32 grid in/out, cached plan)"}
+    plan.close()
+    tcs.lib().tcs_release_cache()
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        # the other engine and stencil of the same configuration, same GPU
+        for st in ("box2d2r", "star2d2r"):
+            for eng in ("tensor", "cudacore"):
+                if st == args.stencil and eng == args.engine:
+                    continue
+                A2, B2 = make_inputs(n, st, 2000)
+                p2 = tcs.Plan(n, n, st, B2, engine=eng, precision="f16")
+                p2.upload(A2)
+                t2 = timed_sweeps(torch, tcs, p2, max(5, args.steps // 4), 2, args.timesteps, stream)
+                p2.close()
+                extras[f"{st}/{eng}/f16"] = round(updates_per_step * max(5, args.steps // 4) / t2 / 1e9, 2)
+    if ws > 1:
+        torch.distributed.barrier()
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+    line = {
+        "metric": f"{args.stencil} Jacobi point-updates per second (Gpts/s; %HBM roofline in 'roofline')",
+        "value": round(value, 3), "unit": "Gpts/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * tmax / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f16" if args.precision != "f32" else "f32",
+        "data": "synthetic (seeded U[-1,1) grid, normalised U[0,1) coefficients)",
+        "config": workload_config(args),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_kind": peak_kind,
+                     "basis": f"{bpu} B per point-update x {args.interior}^2 updates per launch / "
+                              f"mean launch time {launch_s * 1e6:.2f} us (CUDA events)"},
+        "e2e": e2e,
+        "gpu_launches": args.steps * args.timesteps,
+        "clocks": clocks,
+        "tflops_useful": round(value * FLOPS_PER_UPDATE[args.stencil] / 1e3, 2),
+        "comparators_gpts": extras,
+    }
+    if not args.no_extras:
+        line["cpu_baseline"] = cpu_baseline(args.stencil)
+    print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

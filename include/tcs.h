@@ -1,0 +1,183 @@
+/*
+ * tcs.h — C-ABI of tcstencil_gb300, a GB300 (sm_103a) engine for the 2-D
+ * Jacobi sweeps star2d1r, star2d2r, box2d1r and box2d2r of TCStencil.
+ *
+ * Plain C: pointers, sizes and ints only.  Every int-returning entry point
+ * returns a TCS_* status; tcs_last_error() gives the message of the last
+ * failure on the calling thread.  Device pointers are CUDA device pointers of
+ * the current device; `stream` is a cudaStream_t (NULL = legacy default).
+ *
+ * Stencil semantics (common/gold_*.cpp): out[i][j] = sum over taps of
+ * B[dy+r][dx+r] * in[i+dy][j+dx] on an update rectangle; star stencils read
+ * only the centre row and column of the n x n coefficient matrix B (n = 2r+1).
+ * Cells outside the rectangle keep their value (a fixed border): a multi-step
+ * sweep is a ping-pong whose border never changes, as gold's is.
+ *
+ * Device grid format ("layout16", brick_layout_2D of layout16/host_*.cu:77-88
+ * generalised to any ny x nx): nby = ceil(ny/16) by nbx = ceil(nx/16) bricks
+ * of 16 x 16 cells, brick (i, j) at element (i*nbx + j)*256, cell (y, x) of a
+ * brick at y*16 + x.  FP16 grids hold IEEE binary16 bits (uint16_t); FP32
+ * grids hold floats in the same brick order; a split grid is two FP16 brick
+ * planes, value = hi + lo * 2^-11.
+ */
+#ifndef TCS_H_
+#define TCS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define TCS_OK 0
+#define TCS_ERR_INVALID 1     /* an argument is out of range                  */
+#define TCS_ERR_CUDA 2        /* a CUDA runtime or driver call failed         */
+#define TCS_ERR_UNSUPPORTED 3 /* valid request this build/device cannot run   */
+#define TCS_ERR_NOMEM 4       /* device allocation failed or budget exceeded  */
+#define TCS_ERR_TIMEOUT 5     /* a bounded device wait gave up                */
+
+enum tcs_stencil { TCS_STAR2D1R = 0, TCS_STAR2D2R = 1, TCS_BOX2D1R = 2, TCS_BOX2D2R = 3 };
+/* TENSOR: tcgen05 banded-matrix kernel; CUDACORE: FP32 FMA warp-strip kernel */
+enum tcs_engine { TCS_ENGINE_TENSOR = 0, TCS_ENGINE_CUDACORE = 1 };
+/* F16: FP16 storage, FP32 accumulate.  SPLIT: hi+lo FP16 pair storage, three
+ * tensor-core products (tensor engine only).  F32: FP32 storage with gold's
+ * exact arithmetic (CUDA-core engine only). */
+enum tcs_precision { TCS_PREC_F16 = 0, TCS_PREC_SPLIT = 1, TCS_PREC_F32 = 2 };
+
+const char *tcs_status_string(int status);
+const char *tcs_last_error(void);
+/* Radius of a stencil (1 or 2), or -1. */
+int tcs_stencil_radius(int stencil);
+/* Elements of one brick plane for an ny x nx grid: ceil(ny/16)*ceil(nx/16)*256. */
+size_t tcs_brick_elems(int ny, int nx);
+/* Reads and clears the device error word that bounded in-kernel waits set on
+ * timeout (0 = none).  Synchronises the device. */
+int tcs_device_error(int *code);
+
+/* ------------------------------------------------ drop-in host entry points
+ * Same signature, arguments and behaviour as the reference's
+ *   extern "C" void host_code(float *h_A, float *h_B, float *h_C, int N, int n)
+ * (tensor form: layout16/host_<stencil>.cu, e.g. layout16/host_star2d1r.cu:129;
+ *  CUDA-core form: baseline/host_<stencil>.cu, e.g. baseline/host_star2d1r.cu:78):
+ * h_A is N x N FP32 (N a multiple of 16), h_B is n x n, the grid is padded by
+ * 16 cells of value 1.0, stored as FP16 bricks, swept once per launch for
+ * RUN_TIMES launches (timed from launch SKIP_TIMES on, printed as
+ * "[Time] Time used: %f ms"), and all N x N cells of the result are written to
+ * h_C as FP32.  Device memory is allocated and freed inside the call.  On a
+ * CUDA error the message is printed and the process exits, as the reference's
+ * check_error does (common/common.hpp:10-16). */
+void host_star2d1r(float *h_A, float *h_B, float *h_C, int N, int n);
+void host_star2d2r(float *h_A, float *h_B, float *h_C, int N, int n);
+void host_box2d1r(float *h_A, float *h_B, float *h_C, int N, int n);
+void host_box2d2r(float *h_A, float *h_B, float *h_C, int N, int n);
+void host_cc_star2d1r(float *h_A, float *h_B, float *h_C, int N, int n);
+void host_cc_star2d2r(float *h_A, float *h_B, float *h_C, int N, int n);
+void host_cc_box2d1r(float *h_A, float *h_B, float *h_C, int N, int n);
+void host_cc_box2d2r(float *h_A, float *h_B, float *h_C, int N, int n);
+
+/* The parametrised form behind the eight entry points above and behind the
+ * per-variant `host_code` shims, with the common/param.hpp macros as
+ * arguments (RUN_TIMES, SKIP_TIMES, STEP_TIMES, TILE_SIZE; tile_size is
+ * accepted and ignored: tiles are chosen by the engine).  Returns a status
+ * instead of exiting. */
+int tcs_host_code(float *h_A, float *h_B, float *h_C, int N, int n, int stencil, int engine,
+                  int run_times, int skip_times, int step_times, int tile_size);
+
+/* ------------------------------------------- layout transforms (device)
+ * Bit-exact device forms of the reference's host helpers
+ * (layout16/host_star2d1r.cu:63-101, common/common.hpp:146-160). */
+
+/* padding_2D (layout16/host_star2d1r.cu:63-75): d_in size x size FP16 ->
+ * d_out (size+2*halo)^2 FP16, border cells = value16 (FP16 bits). */
+int tcs_padding_2d(const uint16_t *d_in, uint16_t *d_out, int size, int halo, uint16_t value16,
+                   void *stream);
+/* brick_layout_2D (layout16/host_star2d1r.cu:77-88), generalised to ny x nx;
+ * cells of partial bricks past the grid are 0. */
+int tcs_brick_layout_2d(const uint16_t *d_in, uint16_t *d_out, int ny, int nx, void *stream);
+/* reverse_layout_2D (layout16/host_star2d1r.cu:90-101), generalised likewise. */
+int tcs_reverse_layout_2d(const uint16_t *d_in, uint16_t *d_out, int ny, int nx, void *stream);
+/* array_float2half + padding_2D + brick_layout_2D in one pass: d_in is an
+ * ny x nx FP32 row-major grid, the result is the FP16 brick grid of
+ * (ny+2*pad) x (nx+2*pad) cells with border cells = pad_value. */
+int tcs_pack_f16(const float *d_in, int ny, int nx, int pad, float pad_value, uint16_t *d_bricks,
+                 void *stream);
+/* reverse_layout_2D + interior copy + array_half2float: the ny x nx cells at
+ * offset (pad, pad) of the (ny+2*pad) x (nx+2*pad) brick grid, as FP32. */
+int tcs_unpack_f16(const uint16_t *d_bricks, int ny, int nx, int pad, float *d_out, void *stream);
+/* FP32 and split counterparts of the two above. */
+int tcs_pack_f32(const float *d_in, int ny, int nx, int pad, float pad_value, float *d_bricks,
+                 void *stream);
+int tcs_unpack_f32(const float *d_bricks, int ny, int nx, int pad, float *d_out, void *stream);
+int tcs_pack_split(const float *d_in, int ny, int nx, int pad, float pad_value, uint16_t *d_hi,
+                   uint16_t *d_lo, void *stream);
+int tcs_unpack_split(const uint16_t *d_hi, const uint16_t *d_lo, int ny, int nx, int pad,
+                     float *d_out, void *stream);
+
+/* Band builders (host): the reference's init_coe, bit-exact.  B16 is n x n
+ * FP16 bits.  Star (layout16/host_star2d1r.cu:33-61, host_star2d2r.cu:33-67):
+ * a, b are 16x16.  Box (layout16/host_box2d1r.cu:29-46, host_box2d2r.cu:29-50):
+ * coe is n bands of 16x16. */
+int tcs_init_coe_star(const uint16_t *B16, int n, uint16_t *a, uint16_t *b);
+int tcs_init_coe_box(const uint16_t *B16, int n, uint16_t *coe);
+
+/* ------------------------------------------------------ one sweep step
+ * One Jacobi step on caller-owned device brick grids (the device kernel the
+ * reference launches as mma_run / kernel_run, layout16/kernel_*.cu,
+ * baseline/kernel_*.cu).  `coeffs` is the n x n FP32 matrix in host memory;
+ * the update rectangle is [y0,y1) x [x0,x1), or gold's interior
+ * [r, ny-r) x [r, nx-r) when all four are 0; it must lie inside
+ * [r, ny-r) x [r, nx-r).  d_out cells outside the rectangle receive d_in's.
+ * For TCS_PREC_SPLIT, *_lo are the lo planes; otherwise pass NULL.
+ * For TCS_PREC_F32 the planes are float bricks. */
+typedef struct tcs_step_args {
+    int ny, nx;
+    int stencil;   /* enum tcs_stencil   */
+    int engine;    /* enum tcs_engine    */
+    int precision; /* enum tcs_precision */
+    int y0, y1, x0, x1;
+    const float *coeffs; /* host, n*n */
+} tcs_step_args;
+
+int tcs_sweep_step(const tcs_step_args *args, const void *d_in, const void *d_in_lo, void *d_out,
+                   void *d_out_lo, void *stream);
+
+/* ------------------------------------------------------------------ plans
+ * A plan owns the device state of one grid (ping-pong brick planes) and runs
+ * multi-step sweeps; steps > 1 run as one captured CUDA graph per step count. */
+typedef struct tcs_plan_s *tcs_plan;
+
+typedef struct tcs_problem {
+    int ny, nx;
+    int stencil, engine, precision;
+    int y0, y1, x0, x1; /* all 0 = [r, ny-r) x [r, nx-r) */
+    const float *coeffs; /* host, n*n; copied into the plan */
+} tcs_problem;
+
+int tcs_plan_create(const tcs_problem *problem, tcs_plan *out);
+int tcs_plan_destroy(tcs_plan plan);
+/* Loads an ny x nx FP32 row-major grid (host or device memory). */
+int tcs_plan_upload(tcs_plan plan, const float *grid, int grid_on_host, void *stream);
+/* Writes the current state as an ny x nx FP32 row-major grid. */
+int tcs_plan_download(tcs_plan plan, float *grid, int grid_on_host, void *stream);
+/* Runs `steps` sweep steps.  use_graph != 0 replays a CUDA graph of the steps. */
+int tcs_plan_run(tcs_plan plan, int steps, int use_graph, void *stream);
+/* Device pointers of the current state planes (lo = NULL unless split), and
+ * the bytes of one plane. */
+int tcs_plan_state(tcs_plan plan, void **hi, void **lo, size_t *plane_bytes);
+/* Replaces the coefficients (host n*n). */
+int tcs_plan_set_coeffs(tcs_plan plan, const float *coeffs);
+
+/* One-call form: host FP32 grid in, `steps` steps, host FP32 grid out.  Device
+ * state is kept in a per-thread cache keyed by shape and mode, so repeated
+ * calls of one shape do not reallocate. */
+int tcs_sweep_host(const float *h_in, float *h_out, const tcs_problem *problem, int steps);
+/* Frees the calling thread's cached plans. */
+void tcs_release_cache(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TCS_H_ */

@@ -1,0 +1,539 @@
+/*
+ * CPU oracle for the 2-D Jacobi sweep hot path (star2d1r, star2d2r, box2d1r,
+ * box2d2r).  TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py use it as the checker.  Nothing in the
+ * tcstencil_gb300 product links, loads or calls this file.
+ *
+ * What is restated here, and from where (paths are inside buaa-hipo/TCStencil):
+ *
+ *   oracle_gold_step_f32   common/gold_star2d1r.cpp:4-14, gold_star2d2r.cpp:4-16,
+ *                          gold_box2d1r.cpp:3-15, gold_box2d2r.cpp:3-15.
+ *                          Same tap order, same non-fused float arithmetic
+ *                          (build with -ffp-contract=off), generalised to a
+ *                          ny x nx grid and an explicit update rectangle.
+ *   oracle_pad_2d          layout16/host_star2d1r.cu:63-75   (padding_2D)
+ *   oracle_brick_2d        layout16/host_star2d1r.cu:77-88   (brick_layout_2D)
+ *   oracle_unbrick_2d      layout16/host_star2d1r.cu:90-101  (reverse_layout_2D)
+ *   oracle_f32_to_f16 /    common/common.hpp:146-160         (array_float2half /
+ *   oracle_f16_to_f32                                         array_half2float)
+ *   oracle_init_coe_star   layout16/host_star2d1r.cu:33-61, host_star2d2r.cu:33-67
+ *   oracle_init_coe_box    layout16/host_box2d1r.cu:29-46,  host_box2d2r.cu:29-50
+ *   oracle_check_error_2d  common/common.hpp:38-92 (checkError2D /
+ *                          checkRelativeError2D; RMS, without the printing)
+ *
+ * Arithmetic contracts of the GPU engine (used as tighter checks than gold):
+ *   oracle_step_f16cc   FP16 storage, FP32 coefficients, fmaf chain in gold's
+ *                       tap order, RNE to FP16  (CUDA-core FP16 kernel).
+ *   oracle_step_f16tc   FP16 storage, FP16 coefficients, exact products summed
+ *                       in double, RNE to FP16   (tensor-core FP16 kernel).
+ *   oracle_step_split   hi + lo*2^-11 FP16 pair storage, coefficients in three
+ *                       FP16 pieces, four products, sum in double (split
+ *                       tensor kernel).
+ *   oracle_step_f64     the same stencil in double (error reference).
+ *
+ * The FP16 conversion below is the IEEE-754 binary16 round-to-nearest-even
+ * rule, written from the format definition.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+enum { ST_STAR2D1R = 0, ST_STAR2D2R = 1, ST_BOX2D1R = 2, ST_BOX2D2R = 3 };
+
+#define MAX_TAPS 25
+
+/* Tap list of a stencil in the order gold sums it.  Returns the tap count;
+ * fills the radius r and the coefficient-matrix width n = 2r+1. */
+static int taps_for(int stencil, int *r, int *n, int *tdy, int *tdx) {
+    int k = 0;
+    switch (stencil) {
+    case ST_STAR2D1R: /* gold_star2d1r.cpp:10-12: up, centre, down, left, right */
+        *r = 1;
+        tdy[k] = -1; tdx[k++] = 0;
+        tdy[k] = 0;  tdx[k++] = 0;
+        tdy[k] = 1;  tdx[k++] = 0;
+        tdy[k] = 0;  tdx[k++] = -1;
+        tdy[k] = 0;  tdx[k++] = 1;
+        break;
+    case ST_STAR2D2R: /* gold_star2d2r.cpp:10-14: column top to bottom, then row */
+        *r = 2;
+        for (int d = -2; d <= 2; d++) { tdy[k] = d; tdx[k++] = 0; }
+        tdy[k] = 0; tdx[k++] = -2;
+        tdy[k] = 0; tdx[k++] = -1;
+        tdy[k] = 0; tdx[k++] = 1;
+        tdy[k] = 0; tdx[k++] = 2;
+        break;
+    case ST_BOX2D1R: /* gold_box2d1r.cpp:11-13: k = 0..8, (k/3-1, k%3-1) */
+    case ST_BOX2D2R: /* gold_box2d2r.cpp:11-13: k = 0..24, (k/5-2, k%5-2) */
+        *r = stencil == ST_BOX2D1R ? 1 : 2;
+        for (int i = 0; i < (2 * *r + 1) * (2 * *r + 1); i++) {
+            tdy[k] = i / (2 * *r + 1) - *r;
+            tdx[k++] = i % (2 * *r + 1) - *r;
+        }
+        break;
+    default:
+        return -1;
+    }
+    *n = 2 * *r + 1;
+    return k;
+}
+
+int oracle_stencil_radius(int stencil) {
+    int r, n, dy[MAX_TAPS], dx[MAX_TAPS];
+    return taps_for(stencil, &r, &n, dy, dx) < 0 ? -1 : r;
+}
+
+/* Copies the tap table out (for tests that check the GPU tap order). */
+int oracle_stencil_taps(int stencil, int *tdy, int *tdx) {
+    int r, n;
+    return taps_for(stencil, &r, &n, tdy, tdx);
+}
+
+static int is_box(int stencil) { return stencil == ST_BOX2D1R || stencil == ST_BOX2D2R; }
+
+/* ---------------------------------------------------------------- FP16 --- */
+
+static uint16_t f64_to_f16(double v) {
+    uint16_t sign = signbit(v) ? 0x8000u : 0u;
+    double a = fabs(v);
+    if (isnan(v)) return 0x7e00u;
+    if (a >= 65520.0) return sign | 0x7c00u;
+    if (a < 6.103515625e-05) { /* below 2^-14: subnormal, step 2^-24 */
+        double m = nearbyint(a * 16777216.0);
+        return sign | (uint16_t)m; /* m == 1024 is the smallest normal */
+    }
+    int e;
+    frexp(a, &e); /* a in [2^(e-1), 2^e) */
+    int E = e - 1;
+    double m = nearbyint(ldexp(a, 10 - E)); /* in [1024, 2048] */
+    if (m == 2048.0) { m = 1024.0; E += 1; }
+    if (E > 15) return sign | 0x7c00u;
+    return sign | (uint16_t)((E + 15) << 10) | (uint16_t)((int)m - 1024);
+}
+
+static double f16_to_f64(uint16_t h) {
+    int s = h >> 15, e = (h >> 10) & 0x1f, m = h & 0x3ff;
+    double v;
+    if (e == 0) v = ldexp((double)m, -24);
+    else if (e == 31) v = m ? NAN : INFINITY;
+    else v = ldexp((double)(m | 0x400), e - 25);
+    return s ? -v : v;
+}
+
+uint16_t oracle_f16_from_f64(double v) { return f64_to_f16(v); }
+double oracle_f64_from_f16(uint16_t h) { return f16_to_f64(h); }
+
+void oracle_f32_to_f16(const float *in, uint16_t *out, long n) {
+    for (long i = 0; i < n; i++) out[i] = f64_to_f16((double)in[i]);
+}
+
+void oracle_f16_to_f32(const uint16_t *in, float *out, long n) {
+    for (long i = 0; i < n; i++) out[i] = (float)f16_to_f64(in[i]);
+}
+
+/* ------------------------------------------------------------- layouts --- */
+
+/* padding_2D (layout16/host_star2d1r.cu:63-75): size^2 -> (size+2h)^2. */
+void oracle_pad_2d(const uint16_t *in, uint16_t *out, int size, int halo, uint16_t value) {
+    int p = size + 2 * halo;
+    for (int i = 0; i < p; i++)
+        for (int j = 0; j < p; j++) {
+            int in_range = i >= halo && i < size + halo && j >= halo && j < size + halo;
+            out[(long)i * p + j] = in_range ? in[(long)(i - halo) * size + (j - halo)] : value;
+        }
+}
+
+/* brick_layout_2D (layout16/host_star2d1r.cu:77-88) generalised to ny x nx:
+ * nby = ceil(ny/b), nbx = ceil(nx/b) bricks of b x b; cells past the grid are
+ * `fill`.  For ny == nx == a multiple of b it is the reference transform. */
+void oracle_brick_2d(const uint16_t *in, uint16_t *out, int ny, int nx, int b, uint16_t fill) {
+    int nby = (ny + b - 1) / b, nbx = (nx + b - 1) / b;
+    for (int i = 0; i < nby; i++)
+        for (int j = 0; j < nbx; j++)
+            for (int x = 0; x < b; x++)
+                for (int y = 0; y < b; y++) {
+                    int gy = i * b + x, gx = j * b + y;
+                    long o = ((long)i * nbx + j) * b * b + x * b + y;
+                    out[o] = (gy < ny && gx < nx) ? in[(long)gy * nx + gx] : fill;
+                }
+}
+
+/* reverse_layout_2D (layout16/host_star2d1r.cu:90-101), generalised likewise. */
+void oracle_unbrick_2d(const uint16_t *in, uint16_t *out, int ny, int nx, int b) {
+    int nbx = (nx + b - 1) / b;
+    for (int gy = 0; gy < ny; gy++)
+        for (int gx = 0; gx < nx; gx++) {
+            int i = gy / b, x = gy % b, j = gx / b, y = gx % b;
+            out[(long)gy * nx + gx] = in[((long)i * nbx + j) * b * b + x * b + y];
+        }
+}
+
+/* init_coe for the star stencils (layout16/host_star2d1r.cu:33-61 for n = 3,
+ * layout16/host_star2d2r.cu:33-67 for n = 5): `a` is the 16x16 vertical band
+ * (A operand), `b` the horizontal band with its centre zeroed (B operand),
+ * both clipped at the brick edge.  B is n x n FP16, row-major. */
+void oracle_init_coe_star(const uint16_t *B, int n, uint16_t *a, uint16_t *b) {
+    int r = n / 2;
+    memset(a, 0, 256 * sizeof(uint16_t));
+    memset(b, 0, 256 * sizeof(uint16_t));
+    uint16_t vert[5], hori[5];
+    for (int i = 0; i < n; i++) {
+        hori[i] = B[r * n + i];
+        vert[i] = B[r + i * n];
+    }
+    hori[r] = 0;
+    /* interior rows of the band: entry (row i+r, col i+j) of a, (row i+j,
+     * col i+r) of b */
+    for (int i = 0; i < 16 - 2 * r; i++)
+        for (int j = 0; j < n; j++) {
+            a[(i + r) * 16 + i + j] = vert[j];
+            b[(i + j) * 16 + i + r] = hori[j];
+        }
+    /* clipped rows at the top/bottom (a) and left/right columns (b): the
+     * n-d taps of an edge row d cells from the brick edge that stay inside */
+    for (int d = 1; d <= r; d++)
+        for (int t = 0; t < n - d; t++) {
+            a[(r - d) * 16 + t] = vert[d + t];                        /* top    */
+            a[(15 - r + d) * 16 + (16 - (n - d)) + t] = vert[t];      /* bottom */
+            b[t * 16 + (r - d)] = hori[d + t];                        /* left   */
+            b[((16 - (n - d)) + t) * 16 + (15 - r + d)] = hori[t];    /* right  */
+        }
+}
+
+/* init_coe for the box stencils (layout16/host_box2d1r.cu:29-46 for n = 3,
+ * layout16/host_box2d2r.cu:29-50 for n = 5): n horizontal 16x16 bands, band z
+ * built from row z of B, clipped at the brick edge. */
+void oracle_init_coe_box(const uint16_t *B, int n, uint16_t *coe) {
+    int r = n / 2;
+    memset(coe, 0, (size_t)256 * n * sizeof(uint16_t));
+    for (int z = 0; z < n; z++) {
+        uint16_t *c = coe + z * 256;
+        for (int i = 0; i < 16 - 2 * r; i++)
+            for (int j = 0; j < n; j++)
+                c[(i + j) * 16 + i + r] = B[z * n + j];
+        for (int d = 1; d <= r; d++)
+            for (int t = 0; t < n - d; t++) {
+                c[t * 16 + (r - d)] = B[z * n + d + t];
+                c[((16 - (n - d)) + t) * 16 + (15 - r + d)] = B[z * n + t];
+            }
+    }
+}
+
+/* ------------------------------------------------------------- sweeps --- */
+
+static void rect_default(int ny, int nx, int r, int *y0, int *y1, int *x0, int *x1) {
+    if (*y0 == 0 && *y1 == 0 && *x0 == 0 && *x1 == 0) {
+        *y0 = r; *y1 = ny - r; *x0 = r; *x1 = nx - r;
+    }
+}
+
+/* One gold step in FP32 over the update rectangle [y0,y1) x [x0,x1) (all zero
+ * = gold's interior [r, n-r)).  C outside the rectangle is not written. */
+int oracle_gold_step_f32(const float *A, const float *B, float *C, int ny, int nx, int stencil,
+                         int y0, int y1, int x0, int x1) {
+    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
+    int nt = taps_for(stencil, &r, &n, tdy, tdx);
+    if (nt < 0) return -1;
+    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
+    float cf[MAX_TAPS];
+    long off[MAX_TAPS];
+    for (int k = 0; k < nt; k++) {
+        cf[k] = B[(tdy[k] + r) * n + tdx[k] + r];
+        off[k] = (long)tdy[k] * nx + tdx[k];
+    }
+    int box = is_box(stencil);
+    for (int i = y0; i < y1; i++)
+        for (int j = x0; j < x1; j++) {
+            const float *p = A + (long)i * nx + j;
+            float s;
+            int k0;
+            if (box) { s = 0.0f; k0 = 0; }         /* C[i][j] = 0; C += ... */
+            else { s = p[off[0]] * cf[0]; k0 = 1; } /* a*b + c*d + ...      */
+            for (int k = k0; k < nt; k++) s = s + p[off[k]] * cf[k];
+            C[(long)i * nx + j] = s;
+        }
+    return 0;
+}
+
+int oracle_step_f64(const double *A, const double *B, double *C, int ny, int nx, int stencil,
+                    int y0, int y1, int x0, int x1) {
+    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
+    int nt = taps_for(stencil, &r, &n, tdy, tdx);
+    if (nt < 0) return -1;
+    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
+    for (int i = y0; i < y1; i++)
+        for (int j = x0; j < x1; j++) {
+            double s = 0.0;
+            for (int k = 0; k < nt; k++)
+                s += A[(long)(i + tdy[k]) * nx + j + tdx[k]] * B[(tdy[k] + r) * n + tdx[k] + r];
+            C[(long)i * nx + j] = s;
+        }
+    return 0;
+}
+
+/* CUDA-core FP16 contract: FP16 in, FP32 coefficients, acc = fmaf chain in
+ * gold's tap order starting from 0, RNE to FP16.  Cells outside the update
+ * rectangle copy the input. */
+int oracle_step_f16cc(const uint16_t *A, const float *B, uint16_t *C, int ny, int nx, int stencil,
+                      int y0, int y1, int x0, int x1) {
+    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
+    int nt = taps_for(stencil, &r, &n, tdy, tdx);
+    if (nt < 0) return -1;
+    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
+    for (int i = 0; i < ny; i++)
+        for (int j = 0; j < nx; j++) {
+            long o = (long)i * nx + j;
+            if (i < y0 || i >= y1 || j < x0 || j >= x1) { C[o] = A[o]; continue; }
+            float acc = 0.0f;
+            for (int k = 0; k < nt; k++) {
+                float x = (float)f16_to_f64(A[o + (long)tdy[k] * nx + tdx[k]]);
+                acc = fmaf(x, B[(tdy[k] + r) * n + tdx[k] + r], acc);
+            }
+            C[o] = f64_to_f16((double)acc);
+        }
+    return 0;
+}
+
+/* FP32-storage contract: gold's exact arithmetic, cells outside the rectangle
+ * copy the input (this is gold plus the fixed-border copy of a ping-pong). */
+int oracle_step_f32(const float *A, const float *B, float *C, int ny, int nx, int stencil,
+                    int y0, int y1, int x0, int x1) {
+    int r = oracle_stencil_radius(stencil);
+    if (r < 0) return -1;
+    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
+    for (int i = 0; i < ny; i++)
+        for (int j = 0; j < nx; j++)
+            if (i < y0 || i >= y1 || j < x0 || j >= x1) C[(long)i * nx + j] = A[(long)i * nx + j];
+    return oracle_gold_step_f32(A, B, C, ny, nx, stencil, y0, y1, x0, x1);
+}
+
+/* Tensor-core FP16 contract: FP16 in, coefficients rounded to FP16, exact
+ * products, the sum taken in double, RNE to FP16. */
+int oracle_step_f16tc(const uint16_t *A, const float *B, uint16_t *C, int ny, int nx, int stencil,
+                      int y0, int y1, int x0, int x1) {
+    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
+    int nt = taps_for(stencil, &r, &n, tdy, tdx);
+    if (nt < 0) return -1;
+    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
+    double ch[MAX_TAPS];
+    for (int k = 0; k < nt; k++) ch[k] = f16_to_f64(f64_to_f16(B[(tdy[k] + r) * n + tdx[k] + r]));
+    for (int i = 0; i < ny; i++)
+        for (int j = 0; j < nx; j++) {
+            long o = (long)i * nx + j;
+            if (i < y0 || i >= y1 || j < x0 || j >= x1) { C[o] = A[o]; continue; }
+            double s = 0.0;
+            for (int k = 0; k < nt; k++) s += f16_to_f64(A[o + (long)tdy[k] * nx + tdx[k]]) * ch[k];
+            C[o] = f64_to_f16(s);
+        }
+    return 0;
+}
+
+#define SPLIT_SCALE 2048.0 /* lo is stored scaled by 2^11 */
+
+/* Splits x into hi = fp16(x), lo = fp16((x - hi) * 2^11). */
+void oracle_split_f64(const double *x, uint16_t *hi, uint16_t *lo, long n) {
+    for (long i = 0; i < n; i++) {
+        uint16_t h = f64_to_f16(x[i]);
+        hi[i] = h;
+        lo[i] = f64_to_f16((x[i] - f16_to_f64(h)) * SPLIT_SCALE);
+    }
+}
+
+void oracle_join_f64(const uint16_t *hi, const uint16_t *lo, double *x, long n) {
+    for (long i = 0; i < n; i++) x[i] = f16_to_f64(hi[i]) + f16_to_f64(lo[i]) / SPLIT_SCALE;
+}
+
+/* Split-precision contract.  Data x = xh + xl 2^-11; an FP32 coefficient c is
+ * held as three FP16 pieces c = ch + 2^-11 (cl + c3) (c3 carries the bits a
+ * two-piece split would drop; without it the operator is off by ~2^-23
+ * relative and the error grows linearly with the step count).  Four products:
+ *   v = sum ch*xh + 2^-11 (ch*xl + cl*xh + c3*xh)      (sum in double here)
+ * then hi' = fp16(v), lo' = fp16((v - hi') 2^11). */
+int oracle_step_split(const uint16_t *Ah, const uint16_t *Al, const float *B, uint16_t *Ch,
+                      uint16_t *Cl, int ny, int nx, int stencil, int y0, int y1, int x0, int x1) {
+    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
+    int nt = taps_for(stencil, &r, &n, tdy, tdx);
+    if (nt < 0) return -1;
+    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
+    double chi[MAX_TAPS], clo[MAX_TAPS], c3[MAX_TAPS];
+    for (int k = 0; k < nt; k++) {
+        double c = B[(tdy[k] + r) * n + tdx[k] + r];
+        chi[k] = f16_to_f64(f64_to_f16(c));
+        clo[k] = f16_to_f64(f64_to_f16((c - chi[k]) * SPLIT_SCALE));
+        c3[k] = f16_to_f64(f64_to_f16((c - chi[k]) * SPLIT_SCALE - clo[k]));
+    }
+    for (int i = 0; i < ny; i++)
+        for (int j = 0; j < nx; j++) {
+            long o = (long)i * nx + j;
+            if (i < y0 || i >= y1 || j < x0 || j >= x1) { Ch[o] = Ah[o]; Cl[o] = Al[o]; continue; }
+            double main = 0.0, corr = 0.0;
+            for (int k = 0; k < nt; k++) {
+                long q = o + (long)tdy[k] * nx + tdx[k];
+                double xh = f16_to_f64(Ah[q]), xl = f16_to_f64(Al[q]);
+                main += chi[k] * xh;
+                corr += chi[k] * xl + clo[k] * xh + c3[k] * xh;
+            }
+            double v = main + corr / SPLIT_SCALE;
+            uint16_t h = f64_to_f16(v);
+            Ch[o] = h;
+            Cl[o] = f64_to_f16((v - f16_to_f64(h)) * SPLIT_SCALE);
+        }
+    return 0;
+}
+
+/* ------------------------------------------------- multi-step sweeps --- */
+/* Ping-pong with a fixed border: both buffers start as the input, each step
+ * writes the update rectangle of the other buffer.  `grid` is updated in
+ * place with the result after `steps` steps. */
+
+int oracle_sweep_f32(float *grid, const float *B, int ny, int nx, int stencil, int steps,
+                     int y0, int y1, int x0, int x1) {
+    long cells = (long)ny * nx;
+    float *tmp = (float *)malloc(cells * sizeof(float));
+    if (!tmp) return -2;
+    memcpy(tmp, grid, cells * sizeof(float));
+    float *cur = grid, *nxt = tmp;
+    for (int t = 0; t < steps; t++) {
+        if (oracle_gold_step_f32(cur, B, nxt, ny, nx, stencil, y0, y1, x0, x1)) { free(tmp); return -1; }
+        float *s = cur; cur = nxt; nxt = s;
+    }
+    if (cur != grid) memcpy(grid, cur, cells * sizeof(float));
+    free(tmp);
+    return 0;
+}
+
+int oracle_sweep_f64(double *grid, const double *B, int ny, int nx, int stencil, int steps,
+                     int y0, int y1, int x0, int x1) {
+    long cells = (long)ny * nx;
+    double *tmp = (double *)malloc(cells * sizeof(double));
+    if (!tmp) return -2;
+    memcpy(tmp, grid, cells * sizeof(double));
+    double *cur = grid, *nxt = tmp;
+    for (int t = 0; t < steps; t++) {
+        if (oracle_step_f64(cur, B, nxt, ny, nx, stencil, y0, y1, x0, x1)) { free(tmp); return -1; }
+        double *s = cur; cur = nxt; nxt = s;
+    }
+    if (cur != grid) memcpy(grid, cur, cells * sizeof(double));
+    free(tmp);
+    return 0;
+}
+
+typedef int (*step16_fn)(const uint16_t *, const float *, uint16_t *, int, int, int, int, int, int, int);
+
+static int sweep16(step16_fn fn, uint16_t *grid, const float *B, int ny, int nx, int stencil,
+                   int steps, int y0, int y1, int x0, int x1) {
+    long cells = (long)ny * nx;
+    uint16_t *tmp = (uint16_t *)malloc(cells * sizeof(uint16_t));
+    if (!tmp) return -2;
+    uint16_t *cur = grid, *nxt = tmp;
+    for (int t = 0; t < steps; t++) {
+        if (fn(cur, B, nxt, ny, nx, stencil, y0, y1, x0, x1)) { free(tmp); return -1; }
+        uint16_t *s = cur; cur = nxt; nxt = s;
+    }
+    if (cur != grid) memcpy(grid, cur, cells * sizeof(uint16_t));
+    free(tmp);
+    return 0;
+}
+
+int oracle_sweep_f16cc(uint16_t *grid, const float *B, int ny, int nx, int stencil, int steps,
+                       int y0, int y1, int x0, int x1) {
+    return sweep16(oracle_step_f16cc, grid, B, ny, nx, stencil, steps, y0, y1, x0, x1);
+}
+
+int oracle_sweep_f16tc(uint16_t *grid, const float *B, int ny, int nx, int stencil, int steps,
+                       int y0, int y1, int x0, int x1) {
+    return sweep16(oracle_step_f16tc, grid, B, ny, nx, stencil, steps, y0, y1, x0, x1);
+}
+
+int oracle_sweep_split(uint16_t *hi, uint16_t *lo, const float *B, int ny, int nx, int stencil,
+                       int steps, int y0, int y1, int x0, int x1) {
+    long cells = (long)ny * nx;
+    uint16_t *th = (uint16_t *)malloc(cells * sizeof(uint16_t));
+    uint16_t *tl = (uint16_t *)malloc(cells * sizeof(uint16_t));
+    if (!th || !tl) { free(th); free(tl); return -2; }
+    uint16_t *ch = hi, *cl = lo, *nh = th, *nl = tl;
+    for (int t = 0; t < steps; t++) {
+        if (oracle_step_split(ch, cl, B, nh, nl, ny, nx, stencil, y0, y1, x0, x1)) {
+            free(th); free(tl); return -1;
+        }
+        uint16_t *s = ch; ch = nh; nh = s;
+        s = cl; cl = nl; nl = s;
+    }
+    if (ch != hi) { memcpy(hi, ch, cells * 2); memcpy(lo, cl, cells * 2); }
+    free(th); free(tl);
+    return 0;
+}
+
+/* ------------------------------------------------------ error metrics --- */
+/* checkError2D / checkRelativeError2D (common/common.hpp:38-92) without the
+ * printing: out[0] = RMS absolute error, out[1] = max absolute error,
+ * out[2] = RMS relative error with |ref| < min_number dividing by min_number,
+ * over rows [y_lb, y_ub) and columns [x_lb, x_ub) of an N-wide grid. */
+void oracle_check_error_2d(int N, const float *output, const float *reference, int y_lb, int y_ub,
+                           int x_lb, int x_ub, double min_number, double *out) {
+    double e2 = 0.0, emax = 0.0, r2 = 0.0;
+    for (int j = y_lb; j < y_ub; j++)
+        for (int k = x_lb; k < x_ub; k++) {
+            double ref = reference[(long)j * N + k];
+            double d = (double)output[(long)j * N + k] - ref;
+            double ad = d < 0 ? -d : d;
+            e2 += ad * ad;
+            if (ad > emax) emax = ad;
+            double rel = fabs(ref) < min_number ? d / min_number : d / ref;
+            r2 += rel * rel;
+        }
+    double cnt = (double)(y_ub - y_lb) * (double)(x_ub - x_lb);
+    out[0] = sqrt(e2 / cnt);
+    out[1] = emax;
+    out[2] = sqrt(r2 / cnt);
+}
+
+/* ---------------------------------------------- CPU throughput harness --- */
+/* Runs `threads` POSIX threads, each sweeping its own copy of an ny x nx FP32
+ * grid with gold for `steps` steps (the all-cores plan: independent copies,
+ * gold itself unchanged).  Returns elapsed wall seconds, or < 0 on error. */
+
+typedef struct {
+    float *a, *b;
+    const float *B;
+    int ny, nx, stencil, steps;
+} bench_arg;
+
+static void *bench_worker(void *p) {
+    bench_arg *g = (bench_arg *)p;
+    float *cur = g->a, *nxt = g->b;
+    for (int t = 0; t < g->steps; t++) {
+        oracle_gold_step_f32(cur, g->B, nxt, g->ny, g->nx, g->stencil, 0, 0, 0, 0);
+        float *s = cur; cur = nxt; nxt = s;
+    }
+    return NULL;
+}
+
+double oracle_gold_bench(const float *init, const float *B, int ny, int nx, int stencil, int steps,
+                         int threads) {
+    if (threads < 1) threads = 1;
+    long cells = (long)ny * nx;
+    bench_arg *args = (bench_arg *)calloc(threads, sizeof(bench_arg));
+    pthread_t *tid = (pthread_t *)calloc(threads, sizeof(pthread_t));
+    if (!args || !tid) { free(args); free(tid); return -2.0; }
+    for (int t = 0; t < threads; t++) {
+        args[t].a = (float *)malloc(cells * sizeof(float));
+        args[t].b = (float *)malloc(cells * sizeof(float));
+        if (!args[t].a || !args[t].b) return -2.0;
+        memcpy(args[t].a, init, cells * sizeof(float));
+        memcpy(args[t].b, init, cells * sizeof(float));
+        args[t].B = B; args[t].ny = ny; args[t].nx = nx;
+        args[t].stencil = stencil; args[t].steps = steps;
+    }
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int t = 0; t < threads; t++) pthread_create(&tid[t], NULL, bench_worker, &args[t]);
+    for (int t = 0; t < threads; t++) pthread_join(tid[t], NULL);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    for (int t = 0; t < threads; t++) { free(args[t].a); free(args[t].b); }
+    free(args); free(tid);
+    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}

@@ -1,0 +1,269 @@
+"""tcstencil_gb300 — GB300 (sm_103a) engine for TCStencil's 2-D Jacobi sweeps.
+
+Python mirror of the C-ABI in include/tcs.h (ctypes over the in-tree
+libtcs.so).  The reference's interface is kept: `host_code(h_A, h_B, h_C, N, n)`
+per stencil (layout16/host_*.cu, baseline/host_*.cu), with the same argument
+meaning; the extended interface adds non-square grids, update rectangles,
+multi-step plans, split precision and device-resident state.
+
+There is no CPU fallback: if the native library is missing, every entry point
+raises.  Build it with `tcstencil_gb300.build.build()`.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = [
+    "STENCILS", "ENGINES", "PRECISIONS", "RADIUS", "TcsError", "lib", "host_code",
+    "host_star2d1r", "host_star2d2r", "host_box2d1r", "host_box2d2r", "host_cc_star2d1r",
+    "host_cc_star2d2r", "host_cc_box2d1r", "host_cc_box2d2r", "sweep_step", "Plan",
+    "sweep_host", "brick_elems", "device_error",
+]
+
+STENCILS = {"star2d1r": 0, "star2d2r": 1, "box2d1r": 2, "box2d2r": 3}
+RADIUS = {"star2d1r": 1, "star2d2r": 2, "box2d1r": 1, "box2d2r": 2}
+ENGINES = {"tensor": 0, "cudacore": 1}
+PRECISIONS = {"f16": 0, "split": 1, "f32": 2}
+
+TCS_OK, TCS_ERR_INVALID, TCS_ERR_CUDA, TCS_ERR_UNSUPPORTED, TCS_ERR_NOMEM, TCS_ERR_TIMEOUT = range(6)
+
+LIB_PATH = _build.LIB
+
+
+class TcsError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+class StepArgs(ctypes.Structure):
+    _fields_ = [("ny", ctypes.c_int), ("nx", ctypes.c_int), ("stencil", ctypes.c_int),
+                ("engine", ctypes.c_int), ("precision", ctypes.c_int), ("y0", ctypes.c_int),
+                ("y1", ctypes.c_int), ("x0", ctypes.c_int), ("x1", ctypes.c_int),
+                ("coeffs", ctypes.POINTER(ctypes.c_float))]
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [("ny", ctypes.c_int), ("nx", ctypes.c_int), ("stencil", ctypes.c_int),
+                ("engine", ctypes.c_int), ("precision", ctypes.c_int), ("y0", ctypes.c_int),
+                ("y1", ctypes.c_int), ("x0", ctypes.c_int), ("x1", ctypes.c_int),
+                ("coeffs", ctypes.POINTER(ctypes.c_float))]
+
+
+_lib = None
+
+# name -> (restype, argtypes) for every function include/tcs.h declares
+_P, _I, _F, _SZ, _U16 = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_size_t, ctypes.c_uint16
+_HOST = [_P, _P, _P, _I, _I]
+SIGNATURES = {
+    "tcs_status_string": (ctypes.c_char_p, [_I]),
+    "tcs_last_error": (ctypes.c_char_p, []),
+    "tcs_stencil_radius": (_I, [_I]),
+    "tcs_brick_elems": (_SZ, [_I, _I]),
+    "tcs_device_error": (_I, [_P]),
+    "host_star2d1r": (None, _HOST), "host_star2d2r": (None, _HOST),
+    "host_box2d1r": (None, _HOST), "host_box2d2r": (None, _HOST),
+    "host_cc_star2d1r": (None, _HOST), "host_cc_star2d2r": (None, _HOST),
+    "host_cc_box2d1r": (None, _HOST), "host_cc_box2d2r": (None, _HOST),
+    "tcs_host_code": (_I, _HOST + [_I, _I, _I, _I, _I, _I]),
+    "tcs_padding_2d": (_I, [_P, _P, _I, _I, _U16, _P]),
+    "tcs_brick_layout_2d": (_I, [_P, _P, _I, _I, _P]),
+    "tcs_reverse_layout_2d": (_I, [_P, _P, _I, _I, _P]),
+    "tcs_pack_f16": (_I, [_P, _I, _I, _I, _F, _P, _P]),
+    "tcs_unpack_f16": (_I, [_P, _I, _I, _I, _P, _P]),
+    "tcs_pack_f32": (_I, [_P, _I, _I, _I, _F, _P, _P]),
+    "tcs_unpack_f32": (_I, [_P, _I, _I, _I, _P, _P]),
+    "tcs_pack_split": (_I, [_P, _I, _I, _I, _F, _P, _P, _P]),
+    "tcs_unpack_split": (_I, [_P, _P, _I, _I, _I, _P, _P]),
+    "tcs_init_coe_star": (_I, [_P, _I, _P, _P]),
+    "tcs_init_coe_box": (_I, [_P, _I, _P]),
+    "tcs_sweep_step": (_I, [ctypes.POINTER(StepArgs), _P, _P, _P, _P, _P]),
+    "tcs_plan_create": (_I, [ctypes.POINTER(Problem), ctypes.POINTER(_P)]),
+    "tcs_plan_destroy": (_I, [_P]),
+    "tcs_plan_upload": (_I, [_P, _P, _I, _P]),
+    "tcs_plan_download": (_I, [_P, _P, _I, _P]),
+    "tcs_plan_run": (_I, [_P, _I, _I, _P]),
+    "tcs_plan_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_SZ)]),
+    "tcs_plan_set_coeffs": (_I, [_P, _P]),
+    "tcs_sweep_host": (_I, [_P, _P, ctypes.POINTER(Problem), _I]),
+    "tcs_release_cache": (None, []),
+}
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded native library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build the CUDA engine with tcstencil_gb300.build.build() "
+                "(there is no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int) -> None:
+    if status != TCS_OK:
+        L = lib()
+        raise TcsError(status, f"{L.tcs_status_string(status).decode()}: "
+                               f"{L.tcs_last_error().decode()}")
+
+
+def _ptr(x) -> int | None:
+    """Device/host address of a torch tensor, numpy array or int (None -> NULL)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+def _coeffs(coeffs, stencil: str) -> np.ndarray:
+    n = 2 * RADIUS[stencil] + 1
+    c = np.ascontiguousarray(coeffs, dtype=np.float32).reshape(-1)
+    if c.size != n * n:
+        raise ValueError(f"{stencil} needs {n}x{n} coefficients, got {c.size}")
+    return c
+
+
+def brick_elems(ny: int, nx: int) -> int:
+    return lib().tcs_brick_elems(ny, nx)
+
+
+def device_error() -> int:
+    """Reads and clears the device error word (raises TcsError on a timeout)."""
+    code = ctypes.c_int(0)
+    _check(lib().tcs_device_error(ctypes.byref(code)))
+    return code.value
+
+
+# --------------------------------------------------------------- drop-in --
+def host_code(h_A: np.ndarray, h_B: np.ndarray, h_C: np.ndarray, N: int, n: int,
+              stencil: str, engine: str = "tensor", run_times: int = 500,
+              skip_times: int = 400, step_times: int = 1, tile_size: int = 1) -> None:
+    """The reference's host_code(h_A, h_B, h_C, N, n) (layout16/host_star2d1r.cu:129),
+    with the common/param.hpp macros as keyword arguments."""
+    for a, shape in ((h_A, (N, N)), (h_C, (N, N)), (h_B, (n, n))):
+        if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"] or a.size != shape[0] * shape[1]:
+            raise ValueError("host_code takes C-contiguous float32 arrays")
+    _check(lib().tcs_host_code(_ptr(h_A), _ptr(h_B), _ptr(h_C), N, n, STENCILS[stencil],
+                               ENGINES[engine], run_times, skip_times, step_times, tile_size))
+
+
+def _drop_in(stencil, engine):
+    def f(h_A, h_B, h_C, N, n, **kw):
+        host_code(h_A, h_B, h_C, N, n, stencil, engine, **kw)
+    f.__name__ = ("host_cc_" if engine == "cudacore" else "host_") + stencil
+    f.__doc__ = f"host_code of the reference's {stencil} ({engine} form)."
+    return f
+
+
+host_star2d1r = _drop_in("star2d1r", "tensor")
+host_star2d2r = _drop_in("star2d2r", "tensor")
+host_box2d1r = _drop_in("box2d1r", "tensor")
+host_box2d2r = _drop_in("box2d2r", "tensor")
+host_cc_star2d1r = _drop_in("star2d1r", "cudacore")
+host_cc_star2d2r = _drop_in("star2d2r", "cudacore")
+host_cc_box2d1r = _drop_in("box2d1r", "cudacore")
+host_cc_box2d2r = _drop_in("box2d2r", "cudacore")
+
+
+# --------------------------------------------------------------- extended --
+def _rect(rect):
+    return (0, 0, 0, 0) if rect is None else tuple(int(v) for v in rect)
+
+
+def sweep_step(d_in, d_out, ny: int, nx: int, stencil: str, coeffs, engine: str = "tensor",
+               precision: str = "f16", rect=None, d_in_lo=None, d_out_lo=None,
+               stream=None) -> None:
+    """One step on caller-owned device brick planes (tcs_sweep_step)."""
+    c = _coeffs(coeffs, stencil)
+    y0, y1, x0, x1 = _rect(rect)
+    a = StepArgs(ny, nx, STENCILS[stencil], ENGINES[engine], PRECISIONS[precision], y0, y1, x0,
+                 x1, c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    _check(lib().tcs_sweep_step(ctypes.byref(a), _ptr(d_in), _ptr(d_in_lo), _ptr(d_out),
+                                _ptr(d_out_lo), _stream(stream)))
+
+
+class Plan:
+    """Device-resident sweep of one grid (tcs_plan_*)."""
+
+    def __init__(self, ny: int, nx: int, stencil: str, coeffs, engine: str = "tensor",
+                 precision: str = "f16", rect=None):
+        self._c = _coeffs(coeffs, stencil)
+        y0, y1, x0, x1 = _rect(rect)
+        self.ny, self.nx, self.stencil, self.engine, self.precision = ny, nx, stencil, engine, precision
+        pr = Problem(ny, nx, STENCILS[stencil], ENGINES[engine], PRECISIONS[precision], y0, y1,
+                     x0, x1, self._c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        h = ctypes.c_void_p()
+        _check(lib().tcs_plan_create(ctypes.byref(pr), ctypes.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().tcs_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, grid, stream=None) -> None:
+        """grid: ny x nx float32 (numpy = host memory, torch CUDA tensor = device)."""
+        on_host = isinstance(grid, np.ndarray) or (hasattr(grid, "is_cuda") and not grid.is_cuda)
+        _check(lib().tcs_plan_upload(self._h, _ptr(grid), int(on_host), _stream(stream)))
+
+    def download(self, out, stream=None) -> None:
+        on_host = isinstance(out, np.ndarray) or (hasattr(out, "is_cuda") and not out.is_cuda)
+        _check(lib().tcs_plan_download(self._h, _ptr(out), int(on_host), _stream(stream)))
+
+    def run(self, steps: int, use_graph: bool = True, stream=None) -> None:
+        _check(lib().tcs_plan_run(self._h, steps, int(use_graph), _stream(stream)))
+
+    def state(self):
+        """(hi device pointer, lo device pointer or None, bytes per plane)."""
+        hi, lo, nb = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_size_t()
+        _check(lib().tcs_plan_state(self._h, ctypes.byref(hi), ctypes.byref(lo), ctypes.byref(nb)))
+        return hi.value, lo.value, nb.value
+
+    def set_coeffs(self, coeffs) -> None:
+        self._c = _coeffs(coeffs, self.stencil)
+        _check(lib().tcs_plan_set_coeffs(self._h, _ptr(self._c)))
+
+
+def sweep_host(h_in: np.ndarray, steps: int, stencil: str, coeffs, engine: str = "tensor",
+               precision: str = "f16", rect=None, h_out: np.ndarray | None = None) -> np.ndarray:
+    """Host FP32 grid in, `steps` Jacobi steps, host FP32 grid out (tcs_sweep_host)."""
+    h_in = np.ascontiguousarray(h_in, dtype=np.float32)
+    ny, nx = h_in.shape
+    out = np.empty_like(h_in) if h_out is None else h_out
+    c = _coeffs(coeffs, stencil)
+    y0, y1, x0, x1 = _rect(rect)
+    pr = Problem(ny, nx, STENCILS[stencil], ENGINES[engine], PRECISIONS[precision], y0, y1, x0,
+                 x1, c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    _check(lib().tcs_sweep_host(_ptr(h_in), _ptr(out), ctypes.byref(pr), steps))
+    return out

@@ -1,0 +1,308 @@
+// Device layout transforms: the reference's host-side array_float2half,
+// padding_2D, brick_layout_2D and reverse_layout_2D (common/common.hpp:146-160,
+// layout16/host_star2d1r.cu:63-101), as bit-exact device kernels, plus fused
+// pack/unpack forms used on the sweep path.
+//
+// Thread granularity is one 16-byte slice of a brick row (8 FP16 or 4 FP32
+// cells), so brick-side accesses are 128-bit and consecutive threads touch
+// consecutive bytes of a brick.
+#include "tcs_device.cuh"
+#include "tcs_internal.h"
+
+namespace tcs {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ uint16_t f2h_bits(float v) {
+    __half h = __float2half_rn(v);
+    return *reinterpret_cast<uint16_t *>(&h);
+}
+
+__device__ __forceinline__ float h2f_bits(uint16_t b) {
+    __half h = *reinterpret_cast<__half *>(&b);
+    return __half2float(h);
+}
+
+// Value of padded-grid cell (Y, X) of a (ny+2pad) x (nx+2pad) grid whose
+// interior is the FP32 row-major input.
+__device__ __forceinline__ float padded_cell(const float *in, int ny, int nx, int pad,
+                                             float pad_value, int Y, int X) {
+    const int iy = Y - pad, ix = X - pad;
+    return (iy >= 0 && iy < ny && ix >= 0 && ix < nx) ? in[(size_t)iy * nx + ix] : pad_value;
+}
+
+// slice id -> (brick, row, first column) for `per` cells per slice
+struct Slice {
+    int brick, row, col;
+};
+__device__ __forceinline__ Slice slice_of(size_t id, int per) {
+    const int slices_per_row = 16 / per;
+    Slice s;
+    s.brick = static_cast<int>(id / (16 * slices_per_row));
+    const int rem = static_cast<int>(id % (16 * slices_per_row));
+    s.row = rem / slices_per_row;
+    s.col = (rem % slices_per_row) * per;
+    return s;
+}
+
+__global__ void pack_f16_kernel(const float *__restrict__ in, int ny, int nx, int pad,
+                                float pad_value, uint16_t *__restrict__ out, int nyo, int nxo,
+                                int nbx, size_t n_slices) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_slices) return;
+    const Slice s = slice_of(id, 8);
+    const int Y = (s.brick / nbx) * 16 + s.row;
+    const int X0 = (s.brick % nbx) * 16 + s.col;
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        uint16_t h[2];
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int X = X0 + 2 * i + j;
+            h[j] = (Y < nyo && X < nxo) ? f2h_bits(padded_cell(in, ny, nx, pad, pad_value, Y, X))
+                                        : (uint16_t)0;
+        }
+        w[i] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+    }
+    reinterpret_cast<uint4 *>(out)[id] = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__global__ void unpack_f16_kernel(const uint16_t *__restrict__ in, int ny, int nx, int pad,
+                                  float *__restrict__ out, int nbx, size_t n_slices) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_slices) return;
+    const Slice s = slice_of(id, 8);
+    const int iy = (s.brick / nbx) * 16 + s.row - pad;
+    if (iy < 0 || iy >= ny) return;
+    const uint4 v = reinterpret_cast<const uint4 *>(in)[id];
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    const int ix0 = (s.brick % nbx) * 16 + s.col - pad;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int ix = ix0 + i;
+        if (ix >= 0 && ix < nx)
+            out[(size_t)iy * nx + ix] = h2f_bits((uint16_t)(w[i >> 1] >> (16 * (i & 1))));
+    }
+}
+
+__global__ void pack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
+                                float pad_value, float *__restrict__ out, int nyo, int nxo,
+                                int nbx, size_t n_slices) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_slices) return;
+    const Slice s = slice_of(id, 4);
+    const int Y = (s.brick / nbx) * 16 + s.row;
+    const int X0 = (s.brick % nbx) * 16 + s.col;
+    float v[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int X = X0 + i;
+        v[i] = (Y < nyo && X < nxo) ? padded_cell(in, ny, nx, pad, pad_value, Y, X) : 0.0f;
+    }
+    reinterpret_cast<float4 *>(out)[id] = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+__global__ void unpack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
+                                  float *__restrict__ out, int nbx, size_t n_slices) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_slices) return;
+    const Slice s = slice_of(id, 4);
+    const int iy = (s.brick / nbx) * 16 + s.row - pad;
+    if (iy < 0 || iy >= ny) return;
+    const float4 v = reinterpret_cast<const float4 *>(in)[id];
+    const float f[4] = {v.x, v.y, v.z, v.w};
+    const int ix0 = (s.brick % nbx) * 16 + s.col - pad;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int ix = ix0 + i;
+        if (ix >= 0 && ix < nx) out[(size_t)iy * nx + ix] = f[i];
+    }
+}
+
+// hi = fp16(x), lo = fp16((x - hi) * 2^11); both steps before the last
+// rounding are exact in FP32.
+__global__ void pack_split_kernel(const float *__restrict__ in, int ny, int nx, int pad,
+                                  float pad_value, uint16_t *__restrict__ hi,
+                                  uint16_t *__restrict__ lo, int nyo, int nxo, int nbx,
+                                  size_t n_slices) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_slices) return;
+    const Slice s = slice_of(id, 8);
+    const int Y = (s.brick / nbx) * 16 + s.row;
+    const int X0 = (s.brick % nbx) * 16 + s.col;
+    uint32_t wh[4], wl[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        uint16_t h[2], l[2];
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int X = X0 + 2 * i + j;
+            h[j] = 0;
+            l[j] = 0;
+            if (Y < nyo && X < nxo) {
+                const float x = padded_cell(in, ny, nx, pad, pad_value, Y, X);
+                h[j] = f2h_bits(x);
+                l[j] = f2h_bits((x - h2f_bits(h[j])) * 2048.0f);
+            }
+        }
+        wh[i] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+        wl[i] = (uint32_t)l[0] | ((uint32_t)l[1] << 16);
+    }
+    reinterpret_cast<uint4 *>(hi)[id] = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+    reinterpret_cast<uint4 *>(lo)[id] = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+}
+
+__global__ void unpack_split_kernel(const uint16_t *__restrict__ hi,
+                                    const uint16_t *__restrict__ lo, int ny, int nx, int pad,
+                                    float *__restrict__ out, int nbx, size_t n_slices) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_slices) return;
+    const Slice s = slice_of(id, 8);
+    const int iy = (s.brick / nbx) * 16 + s.row - pad;
+    if (iy < 0 || iy >= ny) return;
+    const uint4 vh = reinterpret_cast<const uint4 *>(hi)[id];
+    const uint4 vl = reinterpret_cast<const uint4 *>(lo)[id];
+    const uint32_t wh[4] = {vh.x, vh.y, vh.z, vh.w};
+    const uint32_t wl[4] = {vl.x, vl.y, vl.z, vl.w};
+    const int ix0 = (s.brick % nbx) * 16 + s.col - pad;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int ix = ix0 + i;
+        if (ix >= 0 && ix < nx) {
+            const float h = h2f_bits((uint16_t)(wh[i >> 1] >> (16 * (i & 1))));
+            const float l = h2f_bits((uint16_t)(wl[i >> 1] >> (16 * (i & 1))));
+            out[(size_t)iy * nx + ix] = fmaf(l, 1.0f / 2048.0f, h);
+        }
+    }
+}
+
+// padding_2D: one thread per output cell.
+__global__ void padding_2d_kernel(const uint16_t *__restrict__ in, uint16_t *__restrict__ out,
+                                  int size, int halo, uint16_t value) {
+    const int p = size + 2 * halo;
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)p * p) return;
+    const int i = static_cast<int>(id / p), j = static_cast<int>(id % p);
+    const bool inside = i >= halo && i < size + halo && j >= halo && j < size + halo;
+    out[id] = inside ? in[(size_t)(i - halo) * size + (j - halo)] : value;
+}
+
+// brick_layout_2D: one thread per 8-cell slice of the brick output.
+__global__ void brick_2d_kernel(const uint16_t *__restrict__ in, uint16_t *__restrict__ out,
+                                int ny, int nx, int nbx, size_t n_slices) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_slices) return;
+    const Slice s = slice_of(id, 8);
+    const int Y = (s.brick / nbx) * 16 + s.row;
+    const int X0 = (s.brick % nbx) * 16 + s.col;
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        uint32_t h[2];
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int X = X0 + 2 * i + j;
+            h[j] = (Y < ny && X < nx) ? in[(size_t)Y * nx + X] : 0u;
+        }
+        w[i] = h[0] | (h[1] << 16);
+    }
+    reinterpret_cast<uint4 *>(out)[id] = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// reverse_layout_2D: one thread per 8-cell slice of the brick input.
+__global__ void unbrick_2d_kernel(const uint16_t *__restrict__ in, uint16_t *__restrict__ out,
+                                  int ny, int nx, int nbx, size_t n_slices) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_slices) return;
+    const Slice s = slice_of(id, 8);
+    const int Y = (s.brick / nbx) * 16 + s.row;
+    if (Y >= ny) return;
+    const uint4 v = reinterpret_cast<const uint4 *>(in)[id];
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    const int X0 = (s.brick % nbx) * 16 + s.col;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int X = X0 + i;
+        if (X < nx) out[(size_t)Y * nx + X] = (uint16_t)(w[i >> 1] >> (16 * (i & 1)));
+    }
+}
+
+inline unsigned blocks_for(size_t n) { return static_cast<unsigned>((n + kThreads - 1) / kThreads); }
+inline int nb(int n) { return (n + 15) / 16; }
+
+}  // namespace
+
+cudaError_t launch_pack_f16(const float *in, int ny, int nx, int pad, float pad_value,
+                            uint16_t *bricks, cudaStream_t s) {
+    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
+    const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
+    pack_f16_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, bricks, nyo,
+                                                       nxo, nb(nxo), n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_f16(const uint16_t *bricks, int ny, int nx, int pad, float *out,
+                              cudaStream_t s) {
+    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
+    const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
+    unpack_f16_kernel<<<blocks_for(n), kThreads, 0, s>>>(bricks, ny, nx, pad, out, nb(nxo), n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_f32(const float *in, int ny, int nx, int pad, float pad_value,
+                            float *bricks, cudaStream_t s) {
+    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
+    const size_t n = (size_t)nb(nyo) * nb(nxo) * 64;
+    pack_f32_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, bricks, nyo,
+                                                       nxo, nb(nxo), n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_f32(const float *bricks, int ny, int nx, int pad, float *out,
+                              cudaStream_t s) {
+    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
+    const size_t n = (size_t)nb(nyo) * nb(nxo) * 64;
+    unpack_f32_kernel<<<blocks_for(n), kThreads, 0, s>>>(bricks, ny, nx, pad, out, nb(nxo), n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_split(const float *in, int ny, int nx, int pad, float pad_value,
+                              uint16_t *hi, uint16_t *lo, cudaStream_t s) {
+    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
+    const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
+    pack_split_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, hi, lo, nyo,
+                                                         nxo, nb(nxo), n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_split(const uint16_t *hi, const uint16_t *lo, int ny, int nx, int pad,
+                                float *out, cudaStream_t s) {
+    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
+    const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
+    unpack_split_kernel<<<blocks_for(n), kThreads, 0, s>>>(hi, lo, ny, nx, pad, out, nb(nxo), n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_padding_2d(const uint16_t *in, uint16_t *out, int size, int halo,
+                              uint16_t value, cudaStream_t s) {
+    const size_t p = (size_t)(size + 2 * halo);
+    padding_2d_kernel<<<blocks_for(p * p), kThreads, 0, s>>>(in, out, size, halo, value);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_brick_2d(const uint16_t *in, uint16_t *out, int ny, int nx, cudaStream_t s) {
+    const size_t n = (size_t)nb(ny) * nb(nx) * 32;
+    brick_2d_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, out, ny, nx, nb(nx), n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unbrick_2d(const uint16_t *in, uint16_t *out, int ny, int nx, cudaStream_t s) {
+    const size_t n = (size_t)nb(ny) * nb(nx) * 32;
+    unbrick_2d_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, out, ny, nx, nb(nx), n);
+    return cudaGetLastError();
+}
+
+}  // namespace tcs

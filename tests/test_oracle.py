@@ -1,0 +1,108 @@
+"""The oracle pinned against the reference's own outputs (CPU only).
+
+The golden fixtures were produced by the reference's unchanged gold_*.cpp and
+layout16 helpers (tests/golden/make_golden.py); the in-repo restatement must
+reproduce them bit for bit."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import STENCILS
+
+
+@pytest.mark.parametrize("stencil", STENCILS)
+def test_gold_step_matches_reference_fixtures(golden, stencil):
+    g = golden(f"gold_{stencil}.npz")
+    for N in (16, 37, 64):
+        for tag in ("refB", "normB"):
+            A, B = g[f"A_{N}_{tag}"], g[f"B_{N}_{tag}"]
+            out = oracle.gold_step(A, B, stencil, g[f"Cin_{N}_{tag}"])
+            np.testing.assert_array_equal(out.view(np.uint32), g[f"Cout_{N}_{tag}"].view(np.uint32))
+
+
+@pytest.mark.parametrize("stencil", STENCILS)
+def test_gold_sweep_matches_reference_fixtures(golden, stencil):
+    g = golden(f"gold_{stencil}.npz")
+    for N in (16, 37, 64):
+        out = oracle.sweep_f32(g[f"A_{N}_normB"], g[f"B_{N}_normB"], stencil, 5)
+        np.testing.assert_array_equal(out.view(np.uint32), g[f"sweep5_{N}"].view(np.uint32))
+
+
+def test_layout_helpers_match_reference_fixtures(golden):
+    g = golden("layout16.npz")
+    one = int(np.float16(1.0).view(np.uint16))
+    for N in (16, 48):
+        p = oracle.pad_2d(g[f"in_{N}"], 16, one)
+        np.testing.assert_array_equal(p, g[f"padded_{N}"])
+        b = oracle.brick_2d(p)
+        np.testing.assert_array_equal(b, g[f"bricks_{N}"])
+        np.testing.assert_array_equal(oracle.unbrick_2d(b, N + 32, N + 32), g[f"reversed_{N}"])
+
+
+@pytest.mark.parametrize("stencil", STENCILS)
+def test_init_coe_matches_reference_fixtures(golden, stencil):
+    g = golden("init_coe.npz")
+    n = 2 * oracle.RADIUS[stencil] + 1
+    for tag in ("refB", "randB"):
+        B16 = g[f"{stencil}_{tag}_B16"]
+        if stencil.startswith("star"):
+            a, b = oracle.init_coe_star(B16, n)
+            np.testing.assert_array_equal(a, g[f"{stencil}_{tag}_a"])
+            np.testing.assert_array_equal(b, g[f"{stencil}_{tag}_b"])
+        else:
+            np.testing.assert_array_equal(oracle.init_coe_box(B16, n), g[f"{stencil}_{tag}_coe"])
+
+
+def test_f16_conversion_is_ieee_rne():
+    rng = np.random.default_rng(7)
+    x = np.concatenate([
+        (rng.standard_normal(200000) * 300).astype(np.float32),
+        (rng.standard_normal(20000) * 1e-5).astype(np.float32),
+        np.array([0.0, -0.0, 65504.0, 65519.99, 65520.0, 1e9, 2.0 ** -24, 2.0 ** -25,
+                  3 * 2.0 ** -26, 6.1035156e-05, 6.0975552e-05], np.float32)])
+    with np.errstate(over="ignore"):
+        expect = x.astype(np.float16).view(np.uint16)
+    np.testing.assert_array_equal(oracle.f32_to_f16(x), expect)
+    h = expect
+    np.testing.assert_array_equal(oracle.f16_to_f32(h), h.view(np.float16).astype(np.float32))
+
+
+def test_split_round_trip_precision():
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, 100000)
+    hi, lo = oracle.split(x)
+    back = oracle.join(hi, lo)
+    rel = np.abs(back - x) / np.maximum(np.abs(x), 1e-3)
+    assert rel.max() < 2.0 ** -21
+
+
+@pytest.mark.parametrize("stencil", STENCILS)
+def test_arithmetic_contracts_agree(stencil):
+    """The FP16 contracts differ from each other by at most one FP16 step."""
+    rng = np.random.default_rng(11)
+    n = 2 * oracle.RADIUS[stencil] + 1
+    B = rng.random((n, n)).astype(np.float32)
+    B /= B.sum()
+    A = rng.uniform(-1, 1, (40, 53)).astype(np.float32)
+    A16 = oracle.f32_to_f16(A)
+    cc = oracle.f16_to_f32(oracle.sweep_f16cc(A16, B, stencil, 1)).astype(np.float64)
+    tc = oracle.f16_to_f32(oracle.sweep_f16tc(A16, B, stencil, 1)).astype(np.float64)
+    gold = oracle.sweep_f32(A, B, stencil, 1).astype(np.float64)
+    assert np.max(np.abs(cc - tc)) <= 2.0 ** -9
+    assert np.max(np.abs(cc - gold)) <= 2.0 ** -9
+
+
+def test_reference_build_matches_restatement_on_random_cases():
+    """Direct comparison with the compiled reference, where it was built."""
+    R = oracle.Ref()
+    if not R.available():
+        pytest.skip("reference not compiled here (oracle/_ref)")
+    rng = np.random.default_rng(5)
+    for st in STENCILS:
+        n = 2 * oracle.RADIUS[st] + 1
+        for N in (5, 17, 100):
+            A = rng.uniform(-3, 3, (N, N)).astype(np.float32)
+            B = rng.uniform(-2, 2, (n, n)).astype(np.float32)
+            C = rng.random((N, N)).astype(np.float32)
+            np.testing.assert_array_equal(R.gold(A, B, st, C).view(np.uint32),
+                                          oracle.gold_step(A, B, st, C).view(np.uint32))
