@@ -41,8 +41,9 @@ extern "C" {
 enum tcs_stencil { TCS_STAR2D1R = 0, TCS_STAR2D2R = 1, TCS_BOX2D1R = 2, TCS_BOX2D2R = 3 };
 /* TENSOR: tcgen05 banded-matrix kernel; CUDACORE: FP32 FMA warp-strip kernel */
 enum tcs_engine { TCS_ENGINE_TENSOR = 0, TCS_ENGINE_CUDACORE = 1 };
-/* F16: FP16 storage, FP32 accumulate.  SPLIT: hi+lo FP16 pair storage, three
- * tensor-core products (tensor engine only).  F32: FP32 storage with gold's
+/* F16: FP16 storage, FP32 accumulate.  SPLIT: hi+lo FP16 pair storage, four
+ * tensor-core products, FP32-level accuracy (tensor engine only; needs a
+ * non-expanding stencil, sum of |c| <= 1).  F32: FP32 storage with gold's
  * exact arithmetic (CUDA-core engine only). */
 enum tcs_precision { TCS_PREC_F16 = 0, TCS_PREC_SPLIT = 1, TCS_PREC_F32 = 2 };
 
@@ -106,14 +107,21 @@ int tcs_pack_f16(const float *d_in, int ny, int nx, int pad, float pad_value, ui
 /* reverse_layout_2D + interior copy + array_half2float: the ny x nx cells at
  * offset (pad, pad) of the (ny+2*pad) x (nx+2*pad) brick grid, as FP32. */
 int tcs_unpack_f16(const uint16_t *d_bricks, int ny, int nx, int pad, float *d_out, void *stream);
-/* FP32 and split counterparts of the two above. */
+/* FP32 counterparts of the two above. */
 int tcs_pack_f32(const float *d_in, int ny, int nx, int pad, float pad_value, float *d_bricks,
                  void *stream);
 int tcs_unpack_f32(const float *d_bricks, int ny, int nx, int pad, float *d_out, void *stream);
-int tcs_pack_split(const float *d_in, int ny, int nx, int pad, float pad_value, uint16_t *d_hi,
-                   uint16_t *d_lo, void *stream);
+/* Split counterparts.  A split grid stores x' = x 2^-scale_exp as
+ * hi = rint(x' 2^11) 2^-11 (FP16, fixed point) and lo = fp16((x' - hi) 2^11);
+ * scale_exp should make max|x'| <= 1 (tcs_split_scale_exp). */
+int tcs_pack_split(const float *d_in, int ny, int nx, int pad, float pad_value, int scale_exp,
+                   uint16_t *d_hi, uint16_t *d_lo, void *stream);
 int tcs_unpack_split(const uint16_t *d_hi, const uint16_t *d_lo, int ny, int nx, int pad,
-                     float *d_out, void *stream);
+                     int scale_exp, float *d_out, void *stream);
+/* max |x| of n device floats, returned in host memory (synchronous). */
+int tcs_max_abs_f32(const float *d_in, size_t n, float *h_max, void *stream);
+/* Smallest E with max_abs 2^-E <= 1 (0 when max_abs is 0). */
+int tcs_split_scale_exp(float max_abs);
 
 /* Band builders (host): the reference's init_coe, bit-exact.  B16 is n x n
  * FP16 bits.  Star (layout16/host_star2d1r.cu:33-61, host_star2d2r.cu:33-67):
@@ -166,6 +174,8 @@ int tcs_plan_run(tcs_plan plan, int steps, int use_graph, void *stream);
 /* Device pointers of the current state planes (lo = NULL unless split), and
  * the bytes of one plane. */
 int tcs_plan_state(tcs_plan plan, void **hi, void **lo, size_t *plane_bytes);
+/* Scale exponent of a split plan's planes (0 for other precisions). */
+int tcs_plan_scale_exp(tcs_plan plan, int *scale_exp);
 /* Replaces the coefficients (host n*n). */
 int tcs_plan_set_coeffs(tcs_plan plan, const float *coeffs);
 

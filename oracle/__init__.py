@@ -58,8 +58,8 @@ def lib() -> ctypes.CDLL:
         L.oracle_sweep_split.restype = I
         L.oracle_f32_to_f16.argtypes = [P, P, ctypes.c_long]
         L.oracle_f16_to_f32.argtypes = [P, P, ctypes.c_long]
-        L.oracle_split_f64.argtypes = [P, P, P, ctypes.c_long]
-        L.oracle_join_f64.argtypes = [P, P, P, ctypes.c_long]
+        L.oracle_split_f64.argtypes = [P, P, P, ctypes.c_long, I]
+        L.oracle_join_f64.argtypes = [P, P, P, ctypes.c_long, I]
         L.oracle_pad_2d.argtypes = [P, P, I, I, ctypes.c_uint16]
         L.oracle_brick_2d.argtypes = [P, P, I, I, I, ctypes.c_uint16]
         L.oracle_unbrick_2d.argtypes = [P, P, I, I, I]
@@ -104,19 +104,25 @@ def f16_to_f32(h: np.ndarray) -> np.ndarray:
     return out
 
 
-def split(x: np.ndarray):
+def split_scale_exp(x: np.ndarray) -> int:
+    """Smallest E with max|x| 2^-E <= 1 (the engine's choice; 0 for all-zero)."""
+    m = float(np.max(np.abs(x))) if x.size else 0.0
+    return 0 if m == 0.0 else int(np.frexp(np.float32(m))[1])
+
+
+def split(x: np.ndarray, scale_exp: int = 0):
     x = np.ascontiguousarray(x, dtype=np.float64)
     hi = np.empty(x.shape, np.uint16)
     lo = np.empty(x.shape, np.uint16)
-    lib().oracle_split_f64(_p(x), _p(hi), _p(lo), x.size)
+    lib().oracle_split_f64(_p(x), _p(hi), _p(lo), x.size, scale_exp)
     return hi, lo
 
 
-def join(hi: np.ndarray, lo: np.ndarray) -> np.ndarray:
+def join(hi: np.ndarray, lo: np.ndarray, scale_exp: int = 0) -> np.ndarray:
     hi = np.ascontiguousarray(hi, np.uint16)
     lo = np.ascontiguousarray(lo, np.uint16)
     out = np.empty(hi.shape, np.float64)
-    lib().oracle_join_f64(_p(hi), _p(lo), _p(out), hi.size)
+    lib().oracle_join_f64(_p(hi), _p(lo), _p(out), hi.size, scale_exp)
     return out
 
 

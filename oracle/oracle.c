@@ -26,9 +26,9 @@
  *                       tap order, RNE to FP16  (CUDA-core FP16 kernel).
  *   oracle_step_f16tc   FP16 storage, FP16 coefficients, exact products summed
  *                       in double, RNE to FP16   (tensor-core FP16 kernel).
- *   oracle_step_split   hi + lo*2^-11 FP16 pair storage, coefficients in three
- *                       FP16 pieces, four products, sum in double (split
- *                       tensor kernel).
+ *   oracle_step_split   fixed-point hi + lo*2^-11 FP16 pair storage,
+ *                       coefficients in three FP16 pieces, four products,
+ *                       sum in double (split tensor kernel).
  *   oracle_step_f64     the same stencil in double (error reference).
  *
  * The FP16 conversion below is the IEEE-754 binary16 round-to-nearest-even
@@ -333,37 +333,44 @@ int oracle_step_f16tc(const uint16_t *A, const float *B, uint16_t *C, int ny, in
 
 #define SPLIT_SCALE 2048.0 /* lo is stored scaled by 2^11 */
 
-/* Splits x into hi = fp16(x), lo = fp16((x - hi) * 2^11). */
-void oracle_split_f64(const double *x, uint16_t *hi, uint16_t *lo, long n) {
+/* Split storage of x (the engine's split planes): x' = x 2^-e,
+ * hi = fp16(rint(x' 2^11) 2^-11) (fixed point), lo = fp16((x' - hi) 2^11). */
+void oracle_split_f64(const double *x, uint16_t *hi, uint16_t *lo, long n, int e) {
     for (long i = 0; i < n; i++) {
-        uint16_t h = f64_to_f16(x[i]);
+        double xs = ldexp(x[i], -e);
+        uint16_t h = f64_to_f16(nearbyint(xs * SPLIT_SCALE) / SPLIT_SCALE);
         hi[i] = h;
-        lo[i] = f64_to_f16((x[i] - f16_to_f64(h)) * SPLIT_SCALE);
+        lo[i] = f64_to_f16((xs - f16_to_f64(h)) * SPLIT_SCALE);
     }
 }
 
-void oracle_join_f64(const uint16_t *hi, const uint16_t *lo, double *x, long n) {
-    for (long i = 0; i < n; i++) x[i] = f16_to_f64(hi[i]) + f16_to_f64(lo[i]) / SPLIT_SCALE;
+void oracle_join_f64(const uint16_t *hi, const uint16_t *lo, double *x, long n, int e) {
+    for (long i = 0; i < n; i++)
+        x[i] = ldexp(f16_to_f64(hi[i]) + f16_to_f64(lo[i]) / SPLIT_SCALE, e);
 }
 
-/* Split-precision contract.  Data x = xh + xl 2^-11; an FP32 coefficient c is
- * held as three FP16 pieces c = ch + 2^-11 (cl + c3) (c3 carries the bits a
- * two-piece split would drop; without it the operator is off by ~2^-23
- * relative and the error grows linearly with the step count).  Four products:
- *   v = sum ch*xh + 2^-11 (ch*xl + cl*xh + c3*xh)      (sum in double here)
- * then hi' = fp16(v), lo' = fp16((v - hi') 2^11). */
+/* Split-precision contract (planes as oracle_split_f64 stores them; the
+ * stencil is linear, so the scale exponent does not enter a step).  An FP32
+ * coefficient c is held as ch = rint(c 2^11) 2^-11 (fixed point) plus
+ * rem = (c - ch) 2^11 in two FP16 pieces, cl = fp16(rem), c3 = fp16(rem - cl),
+ * and cf = fp16(c).  Four products:
+ *   v = sum ch*xh + 2^-11 sum (cf*xl + cl*xh + c3*xh)      (in double here)
+ * then hi' = fp16(rint(v 2^11) 2^-11), lo' = fp16((v - hi') 2^11).  Every
+ * ch*xh is a multiple of 2^-22, so the first sum is exact on the GPU too. */
 int oracle_step_split(const uint16_t *Ah, const uint16_t *Al, const float *B, uint16_t *Ch,
                       uint16_t *Cl, int ny, int nx, int stencil, int y0, int y1, int x0, int x1) {
     int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
     int nt = taps_for(stencil, &r, &n, tdy, tdx);
     if (nt < 0) return -1;
     rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
-    double chi[MAX_TAPS], clo[MAX_TAPS], c3[MAX_TAPS];
+    double chi[MAX_TAPS], cfl[MAX_TAPS], clo[MAX_TAPS], c3[MAX_TAPS];
     for (int k = 0; k < nt; k++) {
         double c = B[(tdy[k] + r) * n + tdx[k] + r];
-        chi[k] = f16_to_f64(f64_to_f16(c));
-        clo[k] = f16_to_f64(f64_to_f16((c - chi[k]) * SPLIT_SCALE));
-        c3[k] = f16_to_f64(f64_to_f16((c - chi[k]) * SPLIT_SCALE - clo[k]));
+        chi[k] = nearbyint(c * SPLIT_SCALE) / SPLIT_SCALE;
+        cfl[k] = f16_to_f64(f64_to_f16(c));
+        double rem = (c - chi[k]) * SPLIT_SCALE;
+        clo[k] = f16_to_f64(f64_to_f16(rem));
+        c3[k] = f16_to_f64(f64_to_f16(rem - clo[k]));
     }
     for (int i = 0; i < ny; i++)
         for (int j = 0; j < nx; j++) {
@@ -374,10 +381,10 @@ int oracle_step_split(const uint16_t *Ah, const uint16_t *Al, const float *B, ui
                 long q = o + (long)tdy[k] * nx + tdx[k];
                 double xh = f16_to_f64(Ah[q]), xl = f16_to_f64(Al[q]);
                 main += chi[k] * xh;
-                corr += chi[k] * xl + clo[k] * xh + c3[k] * xh;
+                corr += cfl[k] * xl + clo[k] * xh + c3[k] * xh;
             }
             double v = main + corr / SPLIT_SCALE;
-            uint16_t h = f64_to_f16(v);
+            uint16_t h = f64_to_f16(nearbyint(v * SPLIT_SCALE) / SPLIT_SCALE);
             Ch[o] = h;
             Cl[o] = f64_to_f16((v - f16_to_f64(h)) * SPLIT_SCALE);
         }

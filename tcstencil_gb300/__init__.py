@@ -78,8 +78,11 @@ SIGNATURES = {
     "tcs_unpack_f16": (_I, [_P, _I, _I, _I, _P, _P]),
     "tcs_pack_f32": (_I, [_P, _I, _I, _I, _F, _P, _P]),
     "tcs_unpack_f32": (_I, [_P, _I, _I, _I, _P, _P]),
-    "tcs_pack_split": (_I, [_P, _I, _I, _I, _F, _P, _P, _P]),
-    "tcs_unpack_split": (_I, [_P, _P, _I, _I, _I, _P, _P]),
+    "tcs_pack_split": (_I, [_P, _I, _I, _I, _F, _I, _P, _P, _P]),
+    "tcs_unpack_split": (_I, [_P, _P, _I, _I, _I, _I, _P, _P]),
+    "tcs_max_abs_f32": (_I, [_P, _SZ, ctypes.POINTER(ctypes.c_float), _P]),
+    "tcs_split_scale_exp": (_I, [_F]),
+    "tcs_plan_scale_exp": (_I, [_P, ctypes.POINTER(_I)]),
     "tcs_init_coe_star": (_I, [_P, _I, _P, _P]),
     "tcs_init_coe_box": (_I, [_P, _I, _P]),
     "tcs_sweep_step": (_I, [ctypes.POINTER(StepArgs), _P, _P, _P, _P, _P]),
@@ -249,6 +252,12 @@ class Plan:
         hi, lo, nb = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_size_t()
         _check(lib().tcs_plan_state(self._h, ctypes.byref(hi), ctypes.byref(lo), ctypes.byref(nb)))
         return hi.value, lo.value, nb.value
+
+    def scale_exp(self) -> int:
+        """Split plans store x 2^-E; returns E (0 for other precisions)."""
+        e = ctypes.c_int(0)
+        _check(lib().tcs_plan_scale_exp(self._h, ctypes.byref(e)))
+        return e.value
 
     def set_coeffs(self, coeffs) -> None:
         self._c = _coeffs(coeffs, self.stencil)

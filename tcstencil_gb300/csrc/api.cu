@@ -1,6 +1,7 @@
 // Host side of the C-ABI in include/tcs.h: argument checks, tensor-map
 // encoding, plans (device state + captured multi-step graphs), the one-call
 // host form, and the drop-in replacements of the reference's host_code.
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -65,6 +66,21 @@ TapCoeffs tap_coeffs(int stencil, const float *B) {
     return c;
 }
 
+double tap_abs_sum(int stencil, const float *B) {
+    const TapCoeffs c = tap_coeffs(stencil, B);
+    double s = 0.0;
+    for (int k = 0; k < tap_count(stencil); k++) s += std::fabs((double)c.c[k]);
+    return s;
+}
+
+int split_scale_exp(float max_abs) {
+    if (!(max_abs > 0.0f) || !std::isfinite(max_abs)) return 0;
+    int e = 0;
+    const float m = std::frexp(max_abs, &e);  // max_abs = m 2^e, m in [0.5, 1)
+    (void)m;
+    return e;  // max_abs < 2^e, so max_abs 2^-e < 1
+}
+
 // ------------------------------------------------------------ tensor maps --
 namespace {
 
@@ -90,7 +106,7 @@ EncodeTiledFn encode_fn() {
 
 }  // namespace
 
-int encode_plane_maps(const void *plane, int nby, int nbx, PlaneMaps *maps) {
+int encode_plane_maps(const void *plane, int nby, int nbx, int tbx, PlaneMaps *maps) {
     EncodeTiledFn enc = encode_fn();
     if (!enc) return fail(TCS_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
     if (reinterpret_cast<uintptr_t>(plane) % 16)
@@ -98,8 +114,8 @@ int encode_plane_maps(const void *plane, int nby, int nbx, PlaneMaps *maps) {
     // (8 cells, 16 rows, brick rows, 2 halves, brick columns); strides in bytes
     const cuuint64_t dims[5] = {8, 16, (cuuint64_t)nby, 2, (cuuint64_t)nbx};
     const cuuint64_t strides[4] = {32, (cuuint64_t)nbx * 512, 16, 512};
-    const cuuint32_t box_main[5] = {8, 16, kTcTileBricks + 2, 2, kTcTileBricks};
-    const cuuint32_t box_halo[5] = {8, 16, kTcTileBricks + 2, 1, 1};
+    const cuuint32_t box_main[5] = {8, 16, kTcTileBricksY + 2, 2, (cuuint32_t)tbx};
+    const cuuint32_t box_halo[5] = {8, 16, kTcTileBricksY + 2, 1, 1};
     const cuuint32_t es[5] = {1, 1, 1, 1, 1};
     CUresult r1 = enc(&maps->main, CU_TENSOR_MAP_DATA_TYPE_UINT16, 5, const_cast<void *>(plane),
                       dims, strides, box_main, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -116,6 +132,18 @@ int encode_plane_maps(const void *plane, int nby, int nbx, PlaneMaps *maps) {
 
 // --------------------------------------------------------- one sweep step --
 namespace {
+
+// The split form keeps its fixed-point hi plane exact only for stencils that
+// do not expand the data (sum of |c| <= 1, with slack for FP32 rounding of a
+// normalised set).
+int check_split_coeffs(int stencil, int precision, const float *B) {
+    if (precision != TCS_PREC_SPLIT) return TCS_OK;
+    const double s = tap_abs_sum(stencil, B);
+    if (!(s <= kSplitMaxAbsSum))
+        return fail(TCS_ERR_UNSUPPORTED,
+                    "split precision needs a non-expanding stencil (sum of |c| <= 1), got %g", s);
+    return TCS_OK;
+}
 
 int check_mode(int engine, int precision) {
     if (engine != TCS_ENGINE_TENSOR && engine != TCS_ENGINE_CUDACORE)
@@ -234,16 +262,32 @@ int tcs_unpack_f32(const float *d_in, int ny, int nx, int pad, float *d_out, voi
     TCS_CHECK_PACK("tcs_unpack_f32");
     return cuda_status(launch_unpack_f32(d_in, ny, nx, pad, d_out, (cudaStream_t)stream), "unpack_f32 launch");
 }
-int tcs_pack_split(const float *d_in, int ny, int nx, int pad, float pad_value, uint16_t *d_hi,
-                   uint16_t *d_lo, void *stream) {
+int tcs_pack_split(const float *d_in, int ny, int nx, int pad, float pad_value, int scale_exp,
+                   uint16_t *d_hi, uint16_t *d_lo, void *stream) {
     TCS_CHECK_PACK("tcs_pack_split");
-    return cuda_status(launch_pack_split(d_in, ny, nx, pad, pad_value, d_hi, d_lo, (cudaStream_t)stream), "pack_split launch");
+    return cuda_status(launch_pack_split(d_in, ny, nx, pad, pad_value, scale_exp, d_hi, d_lo, (cudaStream_t)stream), "pack_split launch");
 }
+int tcs_max_abs_f32(const float *d_in, size_t n, float *h_max, void *stream) {
+    if (!d_in || !h_max) return fail(TCS_ERR_INVALID, "tcs_max_abs_f32: null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned *d = nullptr, bits = 0;
+    int st = cuda_status(cudaMalloc(&d, sizeof(unsigned)), "cudaMalloc(max)");
+    if (!st) st = cuda_status(cudaMemsetAsync(d, 0, sizeof(unsigned), s), "memset(max)");
+    if (!st) st = cuda_status(launch_max_abs(d_in, n, d, s), "max_abs launch");
+    if (!st) st = cuda_status(cudaMemcpyAsync(&bits, d, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "max copy");
+    if (!st) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (d) cudaFree(d);
+    if (!st) std::memcpy(h_max, &bits, sizeof(float));
+    return st;
+}
+
+int tcs_split_scale_exp(float max_abs) { return split_scale_exp(max_abs); }
+
 int tcs_unpack_split(const uint16_t *d_hi, const uint16_t *d_lo, int ny, int nx, int pad,
-                     float *d_out, void *stream) {
+                     int scale_exp, float *d_out, void *stream) {
     const void *d_in = d_hi;
     TCS_CHECK_PACK("tcs_unpack_split");
-    return cuda_status(launch_unpack_split(d_hi, d_lo, ny, nx, pad, d_out, (cudaStream_t)stream), "unpack_split launch");
+    return cuda_status(launch_unpack_split(d_hi, d_lo, ny, nx, pad, scale_exp, d_out, (cudaStream_t)stream), "unpack_split launch");
 }
 
 // ---------------------------------------------------------- band builders --
@@ -297,13 +341,18 @@ int tcs_sweep_step(const tcs_step_args *a, const void *d_in, const void *d_in_lo
     if (st) return st;
     if (a->precision == TCS_PREC_SPLIT && (!d_in_lo || !d_out_lo))
         return fail(TCS_ERR_INVALID, "tcs_sweep_step: split precision needs lo planes");
+    if (a->stencil < TCS_STAR2D1R || a->stencil > TCS_BOX2D2R)
+        return fail(TCS_ERR_INVALID, "unknown stencil %d", a->stencil);
+    st = check_split_coeffs(a->stencil, a->precision, a->coeffs);
+    if (st) return st;
     GridGeom g;
     st = make_geom(a->ny, a->nx, a->stencil, a->y0, a->y1, a->x0, a->x1, &g);
     if (st) return st;
     PlaneMaps maps[2];
     if (a->engine == TCS_ENGINE_TENSOR) {
-        st = encode_plane_maps(d_in, g.nby, g.nbx, &maps[0]);
-        if (!st && a->precision == TCS_PREC_SPLIT) st = encode_plane_maps(d_in_lo, g.nby, g.nbx, &maps[1]);
+        const int tbx = tc_tile_bricks_x(a->precision == TCS_PREC_SPLIT);
+        st = encode_plane_maps(d_in, g.nby, g.nbx, tbx, &maps[0]);
+        if (!st && a->precision == TCS_PREC_SPLIT) st = encode_plane_maps(d_in_lo, g.nby, g.nbx, tbx, &maps[1]);
         if (st) return st;
     }
     return run_step(g, a->stencil, a->engine, a->precision, a->coeffs, maps, d_in, d_in_lo, d_out,
@@ -321,7 +370,9 @@ struct tcs_plan_s {
     void *buf[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [state][hi, lo]
     PlaneMaps maps[2][2];
     int cur = 0;
-    float *staging = nullptr;  // ny*nx FP32, for host/row-major transfers
+    int scale_exp = 0;          // split form: planes hold x 2^-scale_exp
+    unsigned *d_max = nullptr;  // split form: max |x| scratch (float bits)
+    float *staging = nullptr;   // ny*nx FP32, for host/row-major transfers
     cudaStream_t capture_stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, start state)
 
@@ -338,6 +389,7 @@ struct tcs_plan_s {
             for (auto &p : s)
                 if (p) cudaFree(p);
         if (staging) cudaFree(staging);
+        if (d_max) cudaFree(d_max);
         if (capture_stream) cudaStreamDestroy(capture_stream);
     }
 
@@ -368,6 +420,8 @@ int tcs_plan_create(const tcs_problem *pr, tcs_plan *out) {
     p->prob = *pr;
     st = make_geom(pr->ny, pr->nx, pr->stencil, pr->y0, pr->y1, pr->x0, pr->x1, &p->g);
     if (st) return st;
+    st = check_split_coeffs(pr->stencil, pr->precision, pr->coeffs);
+    if (st) return st;
     const int n = 2 * stencil_r(pr->stencil) + 1;
     for (int k = 0; k < 25; k++) p->coeffs[k] = k < n * n ? pr->coeffs[k] : 0.0f;
     p->prob.coeffs = p->coeffs;
@@ -385,7 +439,8 @@ int tcs_plan_create(const tcs_problem *pr, tcs_plan *out) {
     if (pr->engine == TCS_ENGINE_TENSOR)
         for (int s = 0; s < 2; s++)
             for (int pl = 0; pl < p->planes(); pl++) {
-                st = encode_plane_maps(p->buf[s][pl], p->g.nby, p->g.nbx, &p->maps[s][pl]);
+                st = encode_plane_maps(p->buf[s][pl], p->g.nby, p->g.nbx,
+                                       tc_tile_bricks_x(pr->precision == TCS_PREC_SPLIT), &p->maps[s][pl]);
                 if (st) return st;
             }
     *out = p.release();
@@ -400,6 +455,8 @@ int tcs_plan_destroy(tcs_plan plan) {
 int tcs_plan_set_coeffs(tcs_plan p, const float *coeffs) {
     if (!p || !coeffs) return fail(TCS_ERR_INVALID, "tcs_plan_set_coeffs: null argument");
     const int n = 2 * stencil_r(p->prob.stencil) + 1;
+    int st = check_split_coeffs(p->prob.stencil, p->prob.precision, coeffs);
+    if (st) return st;
     if (std::memcmp(p->coeffs, coeffs, n * n * sizeof(float)) != 0) {
         std::memcpy(p->coeffs, coeffs, n * n * sizeof(float));
         p->drop_graphs();  // graphs hold the coefficients as kernel parameters
@@ -423,9 +480,22 @@ int tcs_plan_upload(tcs_plan p, const float *grid, int on_host, void *stream) {
     cudaError_t e;
     if (p->prob.precision == TCS_PREC_F32)
         e = launch_pack_f32(src, p->prob.ny, p->prob.nx, 0, 0.0f, static_cast<float *>(p->buf[0][0]), s);
-    else if (p->prob.precision == TCS_PREC_SPLIT)
-        e = launch_pack_split(src, p->prob.ny, p->prob.nx, 0, 0.0f, static_cast<uint16_t *>(p->buf[0][0]),
-                              static_cast<uint16_t *>(p->buf[0][1]), s);
+    else if (p->prob.precision == TCS_PREC_SPLIT) {
+        // scale so that max |x| 2^-E <= 1 (needs the maximum on the host)
+        int st = TCS_OK;
+        if (!p->d_max) st = cuda_status(cudaMalloc(&p->d_max, sizeof(unsigned)), "cudaMalloc(max)");
+        if (!st) st = cuda_status(cudaMemsetAsync(p->d_max, 0, sizeof(unsigned), s), "memset(max)");
+        if (!st) st = cuda_status(launch_max_abs(src, (size_t)p->prob.ny * p->prob.nx, p->d_max, s), "max_abs launch");
+        unsigned bits = 0;
+        if (!st) st = cuda_status(cudaMemcpyAsync(&bits, p->d_max, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "max copy");
+        if (!st) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        if (st) return st;
+        float mx;
+        std::memcpy(&mx, &bits, sizeof(mx));
+        p->scale_exp = split_scale_exp(mx);
+        e = launch_pack_split(src, p->prob.ny, p->prob.nx, 0, 0.0f, p->scale_exp,
+                              static_cast<uint16_t *>(p->buf[0][0]), static_cast<uint16_t *>(p->buf[0][1]), s);
+    }
     else
         e = launch_pack_f16(src, p->prob.ny, p->prob.nx, 0, 0.0f, static_cast<uint16_t *>(p->buf[0][0]), s);
     return cuda_status(e, "pack launch");
@@ -446,7 +516,7 @@ int tcs_plan_download(tcs_plan p, float *grid, int on_host, void *stream) {
         e = launch_unpack_f32(static_cast<float *>(p->buf[c][0]), p->prob.ny, p->prob.nx, 0, dst, s);
     else if (p->prob.precision == TCS_PREC_SPLIT)
         e = launch_unpack_split(static_cast<uint16_t *>(p->buf[c][0]), static_cast<uint16_t *>(p->buf[c][1]),
-                                p->prob.ny, p->prob.nx, 0, dst, s);
+                                p->prob.ny, p->prob.nx, 0, p->scale_exp, dst, s);
     else
         e = launch_unpack_f16(static_cast<uint16_t *>(p->buf[c][0]), p->prob.ny, p->prob.nx, 0, dst, s);
     int st = cuda_status(e, "unpack launch");
@@ -460,6 +530,12 @@ int tcs_plan_state(tcs_plan p, void **hi, void **lo, size_t *plane_bytes) {
     if (hi) *hi = p->buf[p->cur][0];
     if (lo) *lo = p->buf[p->cur][1];
     if (plane_bytes) *plane_bytes = p->plane_bytes;
+    return TCS_OK;
+}
+
+int tcs_plan_scale_exp(tcs_plan p, int *scale_exp) {
+    if (!p || !scale_exp) return fail(TCS_ERR_INVALID, "tcs_plan_scale_exp: null argument");
+    *scale_exp = p->scale_exp;
     return TCS_OK;
 }
 
@@ -595,7 +671,7 @@ int tcs_host_code(float *h_A, float *h_B, float *h_C, int N, int n, int stencil,
     // array_float2half + padding_2D(pad 16, value 1.0) + brick_layout_2D
     if (!st) st = cuda_status(launch_pack_f16(d_f32, N, N, pad, 1.0f, d_A, nullptr), "pack launch");
     PlaneMaps maps[2];
-    if (!st && engine == TCS_ENGINE_TENSOR) st = encode_plane_maps(d_A, g.nby, g.nbx, &maps[0]);
+    if (!st && engine == TCS_ENGINE_TENSOR) st = encode_plane_maps(d_A, g.nby, g.nbx, tc_tile_bricks_x(false), &maps[0]);
     if (!st) st = cuda_status(cudaEventCreate(&start), "cudaEventCreate");
     if (!st) st = cuda_status(cudaEventCreate(&stop), "cudaEventCreate");
     double sum = 0.0;

@@ -122,10 +122,17 @@ __global__ void unpack_f32_kernel(const float *__restrict__ in, int ny, int nx, 
     }
 }
 
-// hi = fp16(x), lo = fp16((x - hi) * 2^11); both steps before the last
-// rounding are exact in FP32.
+// Split storage of x: x' = x 2^-E, hi = fp16(rint(x' 2^11) 2^-11) (fixed
+// point), lo = fp16((x' - hi) 2^11).  Every step before the final rounding
+// of lo is exact in FP32.
+__device__ __forceinline__ void split_value(float x, float scale, uint16_t &h, uint16_t &l) {
+    const float xs = x * scale;
+    h = f2h_bits(rintf(xs * 2048.0f) * (1.0f / 2048.0f));
+    l = f2h_bits((xs - h2f_bits(h)) * 2048.0f);
+}
+
 __global__ void pack_split_kernel(const float *__restrict__ in, int ny, int nx, int pad,
-                                  float pad_value, uint16_t *__restrict__ hi,
+                                  float pad_value, float scale, uint16_t *__restrict__ hi,
                                   uint16_t *__restrict__ lo, int nyo, int nxo, int nbx,
                                   size_t n_slices) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -142,11 +149,8 @@ __global__ void pack_split_kernel(const float *__restrict__ in, int ny, int nx, 
             const int X = X0 + 2 * i + j;
             h[j] = 0;
             l[j] = 0;
-            if (Y < nyo && X < nxo) {
-                const float x = padded_cell(in, ny, nx, pad, pad_value, Y, X);
-                h[j] = f2h_bits(x);
-                l[j] = f2h_bits((x - h2f_bits(h[j])) * 2048.0f);
-            }
+            if (Y < nyo && X < nxo)
+                split_value(padded_cell(in, ny, nx, pad, pad_value, Y, X), scale, h[j], l[j]);
         }
         wh[i] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
         wl[i] = (uint32_t)l[0] | ((uint32_t)l[1] << 16);
@@ -157,7 +161,8 @@ __global__ void pack_split_kernel(const float *__restrict__ in, int ny, int nx, 
 
 __global__ void unpack_split_kernel(const uint16_t *__restrict__ hi,
                                     const uint16_t *__restrict__ lo, int ny, int nx, int pad,
-                                    float *__restrict__ out, int nbx, size_t n_slices) {
+                                    float scale, float *__restrict__ out, int nbx,
+                                    size_t n_slices) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_slices) return;
     const Slice s = slice_of(id, 8);
@@ -174,9 +179,19 @@ __global__ void unpack_split_kernel(const uint16_t *__restrict__ hi,
         if (ix >= 0 && ix < nx) {
             const float h = h2f_bits((uint16_t)(wh[i >> 1] >> (16 * (i & 1))));
             const float l = h2f_bits((uint16_t)(wl[i >> 1] >> (16 * (i & 1))));
-            out[(size_t)iy * nx + ix] = fmaf(l, 1.0f / 2048.0f, h);
+            out[(size_t)iy * nx + ix] = fmaf(l, 1.0f / 2048.0f, h) * scale;
         }
     }
+}
+
+// max |x| as float bits (non-negative floats order like their bit patterns).
+__global__ void max_abs_kernel(const float *__restrict__ in, size_t n, unsigned *out_bits) {
+    float m = 0.0f;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(in[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(m));
 }
 
 // padding_2D: one thread per output cell.
@@ -270,19 +285,28 @@ cudaError_t launch_unpack_f32(const float *bricks, int ny, int nx, int pad, floa
 }
 
 cudaError_t launch_pack_split(const float *in, int ny, int nx, int pad, float pad_value,
-                              uint16_t *hi, uint16_t *lo, cudaStream_t s) {
+                              int scale_exp, uint16_t *hi, uint16_t *lo, cudaStream_t s) {
     const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
     const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
-    pack_split_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, hi, lo, nyo,
+    pack_split_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, ny, nx, pad, pad_value,
+                                                         ldexpf(1.0f, -scale_exp), hi, lo, nyo,
                                                          nxo, nb(nxo), n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_unpack_split(const uint16_t *hi, const uint16_t *lo, int ny, int nx, int pad,
-                                float *out, cudaStream_t s) {
+                                int scale_exp, float *out, cudaStream_t s) {
     const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
     const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
-    unpack_split_kernel<<<blocks_for(n), kThreads, 0, s>>>(hi, lo, ny, nx, pad, out, nb(nxo), n);
+    unpack_split_kernel<<<blocks_for(n), kThreads, 0, s>>>(hi, lo, ny, nx, pad,
+                                                           ldexpf(1.0f, scale_exp), out, nb(nxo), n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_max_abs(const float *in, size_t n, unsigned *out_bits, cudaStream_t s) {
+    const size_t want = (n + kThreads - 1) / kThreads;
+    const unsigned blocks = static_cast<unsigned>(want < 2048 ? (want ? want : 1) : 2048);
+    max_abs_kernel<<<blocks, kThreads, 0, s>>>(in, n, out_bits);
     return cudaGetLastError();
 }
 

@@ -63,15 +63,24 @@ cudaError_t launch_cc_f16(const GridGeom &g, int stencil, const TapCoeffs &c, co
 cudaError_t launch_cc_f32(const GridGeom &g, int stencil, const TapCoeffs &c, const float *in,
                           float *out, cudaStream_t s);
 
-// Tensor-core tile: kTcTileBricks x kTcTileBricks bricks (128 x 128 cells).
-constexpr int kTcTileBricks = 8;
+// Tensor-core tile: 8 bricks (128 rows) high; 8 bricks wide in the FP16 form
+// and 6 in the split form (whose two accumulators per tile take more TMEM).
+constexpr int kTcTileBricksY = 8;
+__host__ __device__ constexpr int tc_tile_bricks_x(bool split) { return split ? 6 : 8; }
 
 // Tensor maps of one FP16 brick plane for the tensor-core kernel.
 struct PlaneMaps {
     CUtensorMap main; // box: 8 x 16 x (tile bricks y + 2) x 2 x (tile bricks x)
     CUtensorMap halo; // box: 8 x 16 x (tile bricks y + 2) x 1 x 1
 };
-int encode_plane_maps(const void *plane, int nby, int nbx, PlaneMaps *maps);
+int encode_plane_maps(const void *plane, int nby, int nbx, int tile_bricks_x, PlaneMaps *maps);
+
+// Scale exponent of a split-precision grid: values are stored as x 2^-E,
+// with E the smallest integer such that max|x| 2^-E <= 1 (0 for max|x| = 0).
+int split_scale_exp(float max_abs);
+// Sum of |c| over a stencil's taps (the split form needs it <= 1 + 2^-8).
+double tap_abs_sum(int stencil, const float *B);
+constexpr double kSplitMaxAbsSum = 1.0 + 1.0 / 256.0;
 
 // Reads and clears the tensor kernels' device error word.
 cudaError_t tc_take_error(int *code);
@@ -95,9 +104,11 @@ cudaError_t launch_pack_f32(const float *in, int ny, int nx, int pad, float pad_
 cudaError_t launch_unpack_f32(const float *bricks, int ny, int nx, int pad, float *out,
                               cudaStream_t s);
 cudaError_t launch_pack_split(const float *in, int ny, int nx, int pad, float pad_value,
-                              uint16_t *hi, uint16_t *lo, cudaStream_t s);
+                              int scale_exp, uint16_t *hi, uint16_t *lo, cudaStream_t s);
 cudaError_t launch_unpack_split(const uint16_t *hi, const uint16_t *lo, int ny, int nx, int pad,
-                                float *out, cudaStream_t s);
+                                int scale_exp, float *out, cudaStream_t s);
+// max |x| over n floats into *out_bits (float bits; *out_bits must start at 0)
+cudaError_t launch_max_abs(const float *in, size_t n, unsigned *out_bits, cudaStream_t s);
 cudaError_t launch_padding_2d(const uint16_t *in, uint16_t *out, int size, int halo,
                               uint16_t value, cudaStream_t s);
 cudaError_t launch_brick_2d(const uint16_t *in, uint16_t *out, int ny, int nx, cudaStream_t s);

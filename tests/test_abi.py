@@ -109,3 +109,12 @@ def test_reference_driver_links_against_the_shim(tcs, tmp_path):
         r = subprocess.run(cmd, capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
         assert exe.exists()
+
+
+def test_split_rejects_expanding_stencils(tcs):
+    """Split storage needs sum |c| <= 1; the check runs before any device work."""
+    B = np.full((3, 3), 0.2, np.float32)  # sum 1.8
+    with pytest.raises(tcs.TcsError) as e:
+        tcs.sweep_step(1 << 20, 2 << 20, 64, 64, "box2d1r", B, precision="split",
+                       d_in_lo=3 << 20, d_out_lo=4 << 20)
+    assert e.value.status == tcs.TCS_ERR_UNSUPPORTED

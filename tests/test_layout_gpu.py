@@ -75,12 +75,18 @@ def test_pack_unpack_f32_and_split(tcs, torch_cuda):
     np.testing.assert_array_equal(d_o.cpu().numpy(), A)
     d_h = torch.empty(n, dtype=torch.int16, device="cuda")
     d_l = torch.empty(n, dtype=torch.int16, device="cuda")
-    assert L.tcs_pack_split(d_A.data_ptr(), ny, nx, pad, 0.0, d_h.data_ptr(), d_l.data_ptr(), None) == 0
+    import ctypes
+    mx = ctypes.c_float(0.0)
+    assert L.tcs_max_abs_f32(d_A.data_ptr(), ny * nx, ctypes.byref(mx), None) == 0
+    assert mx.value == np.max(np.abs(A))
+    e = L.tcs_split_scale_exp(mx.value)
+    assert e == oracle.split_scale_exp(A)
+    assert L.tcs_pack_split(d_A.data_ptr(), ny, nx, pad, 0.0, e, d_h.data_ptr(), d_l.data_ptr(), None) == 0
     padded = np.zeros((ny + 2, nx + 2), np.float64)
     padded[1:-1, 1:-1] = A
-    hi, lo = oracle.split(padded)
+    hi, lo = oracle.split(padded, e)
     np.testing.assert_array_equal(d_h.cpu().numpy().view(np.uint16), oracle.brick_2d(hi))
     np.testing.assert_array_equal(d_l.cpu().numpy().view(np.uint16), oracle.brick_2d(lo))
-    assert L.tcs_unpack_split(d_h.data_ptr(), d_l.data_ptr(), ny, nx, pad, d_o.data_ptr(), None) == 0
+    assert L.tcs_unpack_split(d_h.data_ptr(), d_l.data_ptr(), ny, nx, pad, e, d_o.data_ptr(), None) == 0
     back = d_o.cpu().numpy().astype(np.float64)
-    assert np.max(np.abs(back - A) / np.maximum(np.abs(A), 1e-3)) < 2.0 ** -21
+    assert np.max(np.abs(back - A)) <= 2.0 ** (e - 23)

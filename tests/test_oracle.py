@@ -68,12 +68,18 @@ def test_f16_conversion_is_ieee_rne():
 
 
 def test_split_round_trip_precision():
+    """Fixed-point hi (multiples of 2^-11) + FP16 lo: absolute error <= 2^-23
+    of the scaled value, i.e. FP32-level for the largest values."""
     rng = np.random.default_rng(3)
-    x = rng.uniform(-1, 1, 100000)
-    hi, lo = oracle.split(x)
-    back = oracle.join(hi, lo)
-    rel = np.abs(back - x) / np.maximum(np.abs(x), 1e-3)
-    assert rel.max() < 2.0 ** -21
+    for scale in (1.0, 37.5, 1e-3):
+        x = rng.uniform(-1, 1, 100000) * scale
+        e = oracle.split_scale_exp(x)
+        assert np.max(np.abs(x)) * 2.0 ** -e <= 1.0
+        hi, lo = oracle.split(x, e)
+        h = oracle.f16_to_f32(hi).astype(np.float64)
+        assert np.all(np.round(h * 2048) == h * 2048)  # hi is fixed point
+        back = oracle.join(hi, lo, e)
+        assert np.max(np.abs(back - x)) <= 2.0 ** (e - 23)
 
 
 @pytest.mark.parametrize("stencil", STENCILS)

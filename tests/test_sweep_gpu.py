@@ -87,23 +87,44 @@ def test_tensor_f16_within_one_step_per_sweep(tcs, torch_cuda, stencil, shape, s
     assert np.max(np.abs(got - expect)) <= tol
 
 
+def smooth_plus_noise(rng, ny, nx):
+    """U[-1,1) plus sin(2 pi x) sin(2 pi y), the split-precision test field."""
+    yy, xx = np.meshgrid(np.arange(ny) / ny, np.arange(nx) / nx, indexing="ij")
+    return (rng.uniform(-1, 1, (ny, nx)) + np.sin(2 * np.pi * xx) * np.sin(2 * np.pi * yy)).astype(np.float32)
+
+
 @pytest.mark.parametrize("stencil", STENCILS)
 @pytest.mark.parametrize("shape", [(40, 70), (130, 300)])
 def test_tensor_split_contract_and_fp64_error(tcs, torch_cuda, stencil, shape):
     rng = np.random.default_rng(23)
-    ny, nx = shape
-    yy, xx = np.meshgrid(np.arange(ny) / ny, np.arange(nx) / nx, indexing="ij")
-    A = (rng.uniform(-1, 1, shape) + np.sin(2 * np.pi * xx) * np.sin(2 * np.pi * yy)).astype(np.float32)
+    A = smooth_plus_noise(rng, *shape)
     B = normalized_coeffs(rng, stencil)
     steps = 10
     got = run_plan(tcs, A, B, stencil, steps, "tensor", "split").astype(np.float64)
-    hi, lo = oracle.split(A.astype(np.float64))
+    e = oracle.split_scale_exp(A)
+    hi, lo = oracle.split(A.astype(np.float64), e)
     h, l = oracle.sweep_split(hi, lo, B, stencil, steps)
-    contract = oracle.join(h, l)
-    assert np.max(np.abs(got - contract)) <= steps * 4e-7 * np.abs(contract).max()
+    contract = oracle.join(h, l, e)
+    # FP32 (not double) combination of the two accumulators: a few 2^-24 per step
+    assert np.max(np.abs(got - contract)) <= steps * 2.0 ** (e - 22)
     ref64 = oracle.sweep_f64(A.astype(np.float64), B.astype(np.float64), stencil, steps)
     rel_l2 = np.linalg.norm(got - ref64) / np.linalg.norm(ref64)
     assert rel_l2 <= 1e-6, rel_l2
+
+
+@pytest.mark.parametrize("stencil", ["box2d1r", "box2d2r"])
+def test_tensor_split_200_steps_within_1e6_of_fp64(tcs, torch_cuda, stencil):
+    """The split-precision configuration's bar (FP32 grid as hi+lo FP16,
+    200 steps, error vs FP64 <= 1e-6) on a 258^2 grid."""
+    rng = np.random.default_rng(200)
+    A = smooth_plus_noise(rng, 258, 258)
+    B = normalized_coeffs(rng, stencil)
+    got = run_plan(tcs, A, B, stencil, 200, "tensor", "split").astype(np.float64)
+    ref64 = oracle.sweep_f64(A.astype(np.float64), B.astype(np.float64), stencil, 200)
+    rel_l2 = np.linalg.norm(got - ref64) / np.linalg.norm(ref64)
+    gold = oracle.sweep_f32(A, B, stencil, 200).astype(np.float64)
+    rel_gold = np.linalg.norm(gold - ref64) / np.linalg.norm(ref64)
+    assert rel_l2 <= 1e-6, (rel_l2, rel_gold)
 
 
 @pytest.mark.parametrize("engine", ["tensor", "cudacore"])
