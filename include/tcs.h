@@ -151,6 +151,26 @@ typedef struct tcs_step_args {
 int tcs_sweep_step(const tcs_step_args *args, const void *d_in, const void *d_in_lo, void *d_out,
                    void *d_out_lo, void *stream);
 
+/* ------------------------------------------------ sweeps without allocation
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * where they sweep: code running while a CUDA graph is being captured, real-
+ * time loops that forbid allocator calls and the synchronisation they bring,
+ * and hosts whose device memory is all handed out by a pool or budget they do
+ * not own.  d_out receives `steps` FP16 Jacobi steps of d_in (brick planes as
+ * in tcs_sweep_step; d_in is only read; precision must be TCS_PREC_F16).  The
+ * ping-pong partner plane is a library-owned static device array of
+ * tcs_noalloc_scratch_bytes() = 32 MiB, held by every GPU that loads the
+ * library until exit: grids of up to 16,777,216 cells (e.g. 4096 x 4096);
+ * larger ones are rejected with TCS_ERR_INVALID.  No device memory is
+ * allocated.  The first call on a device looks up the array's device address
+ * (and configures the tensor kernel): make that first call before any stream
+ * capture.  All calls on a device share the array, so calls that overlap on
+ * the GPU (other streams or threads) race on it; each call overwrites what it
+ * uses, so nothing needs clearing between calls. */
+size_t tcs_noalloc_scratch_bytes(void);
+int tcs_sweep_steps_noalloc(const tcs_step_args *args, const void *d_in, void *d_out, int steps,
+                            void *stream);
+
 /* ------------------------------------------------------------------ plans
  * A plan owns the device state of one grid (ping-pong brick planes) and runs
  * multi-step sweeps; steps > 1 run as one captured CUDA graph per step count. */

@@ -94,6 +94,8 @@ SIGNATURES = {
     "tcs_plan_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_SZ)]),
     "tcs_plan_set_coeffs": (_I, [_P, _P]),
     "tcs_sweep_host": (_I, [_P, _P, ctypes.POINTER(Problem), _I]),
+    "tcs_noalloc_scratch_bytes": (_SZ, []),
+    "tcs_sweep_steps_noalloc": (_I, [ctypes.POINTER(StepArgs), _P, _P, _I, _P]),
     "tcs_release_cache": (None, []),
 }
 
@@ -208,6 +210,21 @@ def sweep_step(d_in, d_out, ny: int, nx: int, stencil: str, coeffs, engine: str 
                  x1, c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
     _check(lib().tcs_sweep_step(ctypes.byref(a), _ptr(d_in), _ptr(d_in_lo), _ptr(d_out),
                                 _ptr(d_out_lo), _stream(stream)))
+
+
+def sweep_steps_noalloc(d_in, d_out, ny: int, nx: int, stencil: str, coeffs, steps: int,
+                        engine: str = "tensor", rect=None, stream=None) -> None:
+    """`steps` FP16 sweep steps from d_in to d_out with no device allocation
+    (tcs_sweep_steps_noalloc): for callers that may not call cudaMalloc where
+    they sweep, e.g. inside CUDA graph capture.  The ping-pong plane is a
+    32 MiB static device array shared by all calls on a GPU, so overlapping
+    calls race; make the first call on a device before any capture."""
+    c = _coeffs(coeffs, stencil)
+    y0, y1, x0, x1 = _rect(rect)
+    a = StepArgs(ny, nx, STENCILS[stencil], ENGINES[engine], PRECISIONS["f16"], y0, y1, x0, x1,
+                 c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    _check(lib().tcs_sweep_steps_noalloc(ctypes.byref(a), _ptr(d_in), _ptr(d_out), steps,
+                                         _stream(stream)))
 
 
 class Plan:

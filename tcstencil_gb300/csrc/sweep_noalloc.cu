@@ -1,0 +1,114 @@
+// Multi-step sweeps for callers that must not allocate device memory.
+//
+// A sweep of T > 1 steps from a read-only input to an output needs a third
+// brick plane for the ping-pong.  tcs_plan_* and tcs_sweep_host get it from
+// cudaMalloc.  Some callers cannot call cudaMalloc at the point where they
+// sweep: code running while a CUDA graph is being captured (allocation is not
+// a stream operation and breaks the capture), real-time loops that forbid
+// allocator calls and the synchronisation they may cause, and hosts whose
+// device memory is entirely handed out by a pool or budget they do not own.
+// For them, tcs_sweep_steps_noalloc keeps that third plane in a file-scope
+// device array of kNoAllocScratchBytes, which every GPU that loads this
+// library holds until the process exits.
+#include <mutex>
+
+#include "tcs_internal.h"
+
+namespace tcs {
+
+namespace {
+
+// 32 MiB: one FP16 brick plane of up to 16,777,216 cells (e.g. 4096 x 4096).
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch per device ordinal, looked up once per
+// device with that device current.  (In host code the array's name is only a
+// host-side stand-in, never a device address.)
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+void *g_scratch_ptr[kMaxDevices] = {};
+
+int scratch_for_current_device(void **out) {
+    int dev = 0;
+    int st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (st) return st;
+    if (dev < 0 || dev >= kMaxDevices) return fail(TCS_ERR_UNSUPPORTED, "device ordinal %d", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch),
+                         "cudaGetSymbolAddress(no-alloc scratch)");
+        if (st) return st;
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return TCS_OK;
+}
+
+}  // namespace
+
+}  // namespace tcs
+
+using namespace tcs;
+
+extern "C" {
+
+size_t tcs_noalloc_scratch_bytes(void) { return kNoAllocScratchBytes; }
+
+int tcs_sweep_steps_noalloc(const tcs_step_args *a, const void *d_in, void *d_out, int steps,
+                            void *stream) {
+    if (!a || !a->coeffs || !d_in || !d_out || steps < 0)
+        return fail(TCS_ERR_INVALID, "tcs_sweep_steps_noalloc: bad arguments");
+    if (d_in == d_out)
+        return fail(TCS_ERR_INVALID, "tcs_sweep_steps_noalloc: input and output must differ");
+    if (a->precision != TCS_PREC_F16)
+        return fail(TCS_ERR_UNSUPPORTED, "tcs_sweep_steps_noalloc: FP16 planes only");
+    if (a->engine != TCS_ENGINE_TENSOR && a->engine != TCS_ENGINE_CUDACORE)
+        return fail(TCS_ERR_INVALID, "unknown engine %d", a->engine);
+    GridGeom g;
+    int st = make_geom(a->ny, a->nx, a->stencil, a->y0, a->y1, a->x0, a->x1, &g);
+    if (st) return st;
+    const size_t plane_bytes = (size_t)g.nby * g.nbx * 256 * sizeof(uint16_t);
+    if (plane_bytes > kNoAllocScratchBytes)
+        return fail(TCS_ERR_INVALID,
+                    "tcs_sweep_steps_noalloc: a %d x %d grid needs %zu bytes of scratch; the "
+                    "static scratch holds %zu (at most %zu FP16 cells)",
+                    a->ny, a->nx, plane_bytes, kNoAllocScratchBytes, kNoAllocScratchBytes / 2);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (steps == 0)
+        return cuda_status(cudaMemcpyAsync(d_out, d_in, plane_bytes, cudaMemcpyDeviceToDevice, s),
+                           "no-alloc copy");
+    void *scratch = nullptr;
+    st = scratch_for_current_device(&scratch);
+    if (st) return st;
+    if (a->engine == TCS_ENGINE_TENSOR) {
+        st = cuda_status(tc_prepare(a->stencil, false), "tensor kernel set-up");
+        if (st) return st;
+    }
+    const TapCoeffs c = tap_coeffs(a->stencil, a->coeffs);
+    // Steps alternate between d_out and the scratch plane so that the last
+    // one lands in d_out; d_in is only read.
+    const void *src = d_in;
+    for (int t = 1; t <= steps; t++) {
+        void *dst = ((steps - t) % 2 == 0) ? d_out : scratch;
+        cudaError_t e;
+        if (a->engine == TCS_ENGINE_CUDACORE) {
+            e = launch_cc_f16(g, a->stencil, c, static_cast<const uint16_t *>(src),
+                              static_cast<uint16_t *>(dst), s);
+        } else {
+            PlaneMaps maps;
+            st = encode_plane_maps(src, g.nby, g.nbx, tc_tile_bricks_x(false), &maps);
+            if (st) return st;
+            e = launch_tc_f16(g, a->stencil, a->coeffs, maps, static_cast<const uint16_t *>(src),
+                              static_cast<uint16_t *>(dst), s);
+        }
+        st = cuda_status(e, "no-alloc sweep launch");
+        if (st) return st;
+        src = dst;
+    }
+    return TCS_OK;
+}
+
+}  // extern "C"
