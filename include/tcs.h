@@ -13,12 +13,19 @@
  * Cells outside the rectangle keep their value (a fixed border): a multi-step
  * sweep is a ping-pong whose border never changes, as gold's is.
  *
- * Device grid format ("layout16", brick_layout_2D of layout16/host_*.cu:77-88
- * generalised to any ny x nx): nby = ceil(ny/16) by nbx = ceil(nx/16) bricks
- * of 16 x 16 cells, brick (i, j) at element (i*nbx + j)*256, cell (y, x) of a
- * brick at y*16 + x.  FP16 grids hold IEEE binary16 bits (uint16_t); FP32
- * grids hold floats in the same brick order; a split grid is two FP16 brick
- * planes, value = hi + lo * 2^-11.
+ * Device plane format of the sweep engine ("panel planes"): 16-row
+ * half-bricks of 16 bytes per row (8 FP16 or 4 FP32 cells) in column-major
+ * brick order, i.e. column panels of 16 bytes per row with the rows of a
+ * panel contiguous.  With cpp = 8 (FP16) or 4 (FP32) cells per panel row,
+ * nyp = ceil(ny/128)*128 + 8 rows per panel and npan = ceil(nx/128)*128/cpp
+ * + 2 panels, cell (y, x) is at element
+ *     ((x/cpp + 1) * nyp + (y + 4)) * cpp + x % cpp,
+ * and tcs_plane_elems() gives the element count.  Padding rows and panels
+ * must hold finite values (tcs_pack_* writes every element; zero-fill planes
+ * that are only written by sweeps).  FP16 planes hold IEEE binary16 bits
+ * (uint16_t); a split grid is two FP16 planes (hi, lo, see tcs_pack_split).
+ * The reference's own 16 x 16 brick layout (layout16, brick_layout_2D of
+ * layout16/host_*.cu:77-88) is produced by tcs_brick_layout_2d.
  */
 #ifndef TCS_H_
 #define TCS_H_
@@ -51,8 +58,12 @@ const char *tcs_status_string(int status);
 const char *tcs_last_error(void);
 /* Radius of a stencil (1 or 2), or -1. */
 int tcs_stencil_radius(int stencil);
-/* Elements of one brick plane for an ny x nx grid: ceil(ny/16)*ceil(nx/16)*256. */
+/* Elements of the reference's layout16 bricks of an ny x nx grid:
+ * ceil(ny/16)*ceil(nx/16)*256. */
 size_t tcs_brick_elems(int ny, int nx);
+/* Elements of one engine plane of an ny x nx grid for a precision (uint16_t
+ * elements for F16 and SPLIT, floats for F32). */
+size_t tcs_plane_elems(int ny, int nx, int precision);
 /* Reads and clears the device error word that bounded in-kernel waits set on
  * timeout (0 = none).  Synchronises the device. */
 int tcs_device_error(int *code);
@@ -63,7 +74,7 @@ int tcs_device_error(int *code);
  * (tensor form: layout16/host_<stencil>.cu, e.g. layout16/host_star2d1r.cu:129;
  *  CUDA-core form: baseline/host_<stencil>.cu, e.g. baseline/host_star2d1r.cu:78):
  * h_A is N x N FP32 (N a multiple of 16), h_B is n x n, the grid is padded by
- * 16 cells of value 1.0, stored as FP16 bricks, swept once per launch for
+ * 16 cells of value 1.0, stored as an FP16 plane, swept once per launch for
  * RUN_TIMES launches (timed from launch SKIP_TIMES on, printed as
  * "[Time] Time used: %f ms"), and all N x N cells of the result are written to
  * h_C as FP32.  Device memory is allocated and freed inside the call.  On a
@@ -99,18 +110,18 @@ int tcs_padding_2d(const uint16_t *d_in, uint16_t *d_out, int size, int halo, ui
 int tcs_brick_layout_2d(const uint16_t *d_in, uint16_t *d_out, int ny, int nx, void *stream);
 /* reverse_layout_2D (layout16/host_star2d1r.cu:90-101), generalised likewise. */
 int tcs_reverse_layout_2d(const uint16_t *d_in, uint16_t *d_out, int ny, int nx, void *stream);
-/* array_float2half + padding_2D + brick_layout_2D in one pass: d_in is an
- * ny x nx FP32 row-major grid, the result is the FP16 brick grid of
- * (ny+2*pad) x (nx+2*pad) cells with border cells = pad_value. */
-int tcs_pack_f16(const float *d_in, int ny, int nx, int pad, float pad_value, uint16_t *d_bricks,
+/* array_float2half + padding_2D + the layout change in one pass: d_in is an
+ * ny x nx FP32 row-major grid, the result is the FP16 engine plane of the
+ * (ny+2*pad) x (nx+2*pad) grid whose border cells are pad_value. */
+int tcs_pack_f16(const float *d_in, int ny, int nx, int pad, float pad_value, uint16_t *d_plane,
                  void *stream);
-/* reverse_layout_2D + interior copy + array_half2float: the ny x nx cells at
- * offset (pad, pad) of the (ny+2*pad) x (nx+2*pad) brick grid, as FP32. */
-int tcs_unpack_f16(const uint16_t *d_bricks, int ny, int nx, int pad, float *d_out, void *stream);
+/* The inverse (reverse layout + interior copy + array_half2float): the ny x nx
+ * cells at offset (pad, pad) of the (ny+2*pad) x (nx+2*pad) plane, as FP32. */
+int tcs_unpack_f16(const uint16_t *d_plane, int ny, int nx, int pad, float *d_out, void *stream);
 /* FP32 counterparts of the two above. */
-int tcs_pack_f32(const float *d_in, int ny, int nx, int pad, float pad_value, float *d_bricks,
+int tcs_pack_f32(const float *d_in, int ny, int nx, int pad, float pad_value, float *d_plane,
                  void *stream);
-int tcs_unpack_f32(const float *d_bricks, int ny, int nx, int pad, float *d_out, void *stream);
+int tcs_unpack_f32(const float *d_plane, int ny, int nx, int pad, float *d_out, void *stream);
 /* Split counterparts.  A split grid stores x' = x 2^-scale_exp as
  * hi = rint(x' 2^11) 2^-11 (FP16, fixed point) and lo = fp16((x' - hi) 2^11);
  * scale_exp should make max|x'| <= 1 (tcs_split_scale_exp). */
@@ -131,14 +142,14 @@ int tcs_init_coe_star(const uint16_t *B16, int n, uint16_t *a, uint16_t *b);
 int tcs_init_coe_box(const uint16_t *B16, int n, uint16_t *coe);
 
 /* ------------------------------------------------------ one sweep step
- * One Jacobi step on caller-owned device brick grids (the device kernel the
+ * One Jacobi step on caller-owned device planes (the device kernel the
  * reference launches as mma_run / kernel_run, layout16/kernel_*.cu,
  * baseline/kernel_*.cu).  `coeffs` is the n x n FP32 matrix in host memory;
  * the update rectangle is [y0,y1) x [x0,x1), or gold's interior
  * [r, ny-r) x [r, nx-r) when all four are 0; it must lie inside
  * [r, ny-r) x [r, nx-r).  d_out cells outside the rectangle receive d_in's.
  * For TCS_PREC_SPLIT, *_lo are the lo planes; otherwise pass NULL.
- * For TCS_PREC_F32 the planes are float bricks. */
+ * For TCS_PREC_F32 the planes are float planes. */
 typedef struct tcs_step_args {
     int ny, nx;
     int stencil;   /* enum tcs_stencil   */
@@ -156,12 +167,13 @@ int tcs_sweep_step(const tcs_step_args *args, const void *d_in, const void *d_in
  * where they sweep: code running while a CUDA graph is being captured, real-
  * time loops that forbid allocator calls and the synchronisation they bring,
  * and hosts whose device memory is all handed out by a pool or budget they do
- * not own.  d_out receives `steps` FP16 Jacobi steps of d_in (brick planes as
- * in tcs_sweep_step; d_in is only read; precision must be TCS_PREC_F16).  The
+ * not own.  d_out receives `steps` FP16 Jacobi steps of d_in (planes as in
+ * tcs_sweep_step; d_in is only read; precision must be TCS_PREC_F16).  The
  * ping-pong partner plane is a library-owned static device array of
  * tcs_noalloc_scratch_bytes() = 32 MiB, held by every GPU that loads the
- * library until exit: grids of up to 16,777,216 cells (e.g. 4096 x 4096);
- * larger ones are rejected with TCS_ERR_INVALID.  No device memory is
+ * library until exit: grids whose plane (tcs_plane_elems) has up to
+ * 16,777,216 cells (e.g. 4000 x 4000); larger ones are rejected with
+ * TCS_ERR_INVALID.  No device memory is
  * allocated.  The first call on a device looks up the array's device address
  * (and configures the tensor kernel): make that first call before any stream
  * capture.  All calls on a device share the array, so calls that overlap on
@@ -172,7 +184,7 @@ int tcs_sweep_steps_noalloc(const tcs_step_args *args, const void *d_in, void *d
                             void *stream);
 
 /* ------------------------------------------------------------------ plans
- * A plan owns the device state of one grid (ping-pong brick planes) and runs
+ * A plan owns the device state of one grid (ping-pong planes) and runs
  * multi-step sweeps; steps > 1 run as one captured CUDA graph per step count. */
 typedef struct tcs_plan_s *tcs_plan;
 

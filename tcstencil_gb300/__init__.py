@@ -22,7 +22,7 @@ __all__ = [
     "STENCILS", "ENGINES", "PRECISIONS", "RADIUS", "TcsError", "lib", "host_code",
     "host_star2d1r", "host_star2d2r", "host_box2d1r", "host_box2d2r", "host_cc_star2d1r",
     "host_cc_star2d2r", "host_cc_box2d1r", "host_cc_box2d2r", "sweep_step", "Plan",
-    "sweep_host", "brick_elems", "device_error",
+    "sweep_host", "brick_elems", "plane_elems", "device_error", "sweep_steps_noalloc",
 ]
 
 STENCILS = {"star2d1r": 0, "star2d2r": 1, "box2d1r": 2, "box2d2r": 3}
@@ -65,6 +65,7 @@ SIGNATURES = {
     "tcs_last_error": (ctypes.c_char_p, []),
     "tcs_stencil_radius": (_I, [_I]),
     "tcs_brick_elems": (_SZ, [_I, _I]),
+    "tcs_plane_elems": (_SZ, [_I, _I, _I]),
     "tcs_device_error": (_I, [_P]),
     "host_star2d1r": (None, _HOST), "host_star2d2r": (None, _HOST),
     "host_box2d1r": (None, _HOST), "host_box2d2r": (None, _HOST),
@@ -154,7 +155,13 @@ def _coeffs(coeffs, stencil: str) -> np.ndarray:
 
 
 def brick_elems(ny: int, nx: int) -> int:
+    """Elements of the reference's layout16 bricks of an ny x nx grid."""
     return lib().tcs_brick_elems(ny, nx)
+
+
+def plane_elems(ny: int, nx: int, precision: str = "f16") -> int:
+    """Elements of one engine plane (panel layout, see include/tcs.h)."""
+    return lib().tcs_plane_elems(ny, nx, PRECISIONS[precision])
 
 
 def device_error() -> int:
@@ -203,7 +210,7 @@ def _rect(rect):
 def sweep_step(d_in, d_out, ny: int, nx: int, stencil: str, coeffs, engine: str = "tensor",
                precision: str = "f16", rect=None, d_in_lo=None, d_out_lo=None,
                stream=None) -> None:
-    """One step on caller-owned device brick planes (tcs_sweep_step)."""
+    """One step on caller-owned device planes (tcs_sweep_step)."""
     c = _coeffs(coeffs, stencil)
     y0, y1, x0, x1 = _rect(rect)
     a = StepArgs(ny, nx, STENCILS[stencil], ENGINES[engine], PRECISIONS[precision], y0, y1, x0,

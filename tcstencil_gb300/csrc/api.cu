@@ -51,9 +51,9 @@ int make_geom(int ny, int nx, int stencil, int y0, int y1, int x0, int x1, GridG
                     x0, x1, r, ny - r, r, nx - r);
     geom->ny = ny;
     geom->nx = nx;
-    geom->nby = (ny + 15) / 16;
-    geom->nbx = (nx + 15) / 16;
     geom->y0 = y0; geom->y1 = y1; geom->x0 = x0; geom->x1 = x1;
+    geom->p16 = plane_geom(ny, nx, 8);
+    geom->p32 = plane_geom(ny, nx, 4);
     return TCS_OK;
 }
 
@@ -79,55 +79,6 @@ int split_scale_exp(float max_abs) {
     const float m = std::frexp(max_abs, &e);  // max_abs = m 2^e, m in [0.5, 1)
     (void)m;
     return e;  // max_abs < 2^e, so max_abs 2^-e < 1
-}
-
-// ------------------------------------------------------------ tensor maps --
-namespace {
-
-using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-    static EncodeTiledFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
-                                             cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(p);
-    }
-    return fn;
-}
-
-}  // namespace
-
-int encode_plane_maps(const void *plane, int nby, int nbx, int tbx, PlaneMaps *maps) {
-    EncodeTiledFn enc = encode_fn();
-    if (!enc) return fail(TCS_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
-    if (reinterpret_cast<uintptr_t>(plane) % 16)
-        return fail(TCS_ERR_INVALID, "brick plane must be 16-byte aligned");
-    // (8 cells, 16 rows, brick rows, 2 halves, brick columns); strides in bytes
-    const cuuint64_t dims[5] = {8, 16, (cuuint64_t)nby, 2, (cuuint64_t)nbx};
-    const cuuint64_t strides[4] = {32, (cuuint64_t)nbx * 512, 16, 512};
-    const cuuint32_t box_main[5] = {8, 16, kTcTileBricksY + 2, 2, (cuuint32_t)tbx};
-    const cuuint32_t box_halo[5] = {8, 16, kTcTileBricksY + 2, 1, 1};
-    const cuuint32_t es[5] = {1, 1, 1, 1, 1};
-    CUresult r1 = enc(&maps->main, CU_TENSOR_MAP_DATA_TYPE_UINT16, 5, const_cast<void *>(plane),
-                      dims, strides, box_main, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r1 != CUDA_SUCCESS) return fail(TCS_ERR_CUDA, "cuTensorMapEncodeTiled(main) failed: %d", (int)r1);
-    CUresult r2 = enc(&maps->halo, CU_TENSOR_MAP_DATA_TYPE_UINT16, 5, const_cast<void *>(plane),
-                      dims, strides, box_halo, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r2 != CUDA_SUCCESS) return fail(TCS_ERR_CUDA, "cuTensorMapEncodeTiled(halo) failed: %d", (int)r2);
-    return TCS_OK;
 }
 
 // --------------------------------------------------------- one sweep step --
@@ -157,10 +108,9 @@ int check_mode(int engine, int precision) {
     return TCS_OK;
 }
 
-// One step with already-encoded maps of the input planes (tensor engine).
+// One step from the input planes to the output planes.
 int run_step(const GridGeom &g, int stencil, int engine, int precision, const float *B,
-             const PlaneMaps *in_maps, const void *in, const void *in_lo, void *out, void *out_lo,
-             cudaStream_t s) {
+             const void *in, const void *in_lo, void *out, void *out_lo, cudaStream_t s) {
     cudaError_t e;
     if (engine == TCS_ENGINE_CUDACORE) {
         const TapCoeffs c = tap_coeffs(stencil, B);
@@ -171,11 +121,11 @@ int run_step(const GridGeom &g, int stencil, int engine, int precision, const fl
             e = launch_cc_f16(g, stencil, c, static_cast<const uint16_t *>(in),
                               static_cast<uint16_t *>(out), s);
     } else if (precision == TCS_PREC_SPLIT) {
-        e = launch_tc_split(g, stencil, B, in_maps[0], in_maps[1],
-                            static_cast<const uint16_t *>(in), static_cast<const uint16_t *>(in_lo),
-                            static_cast<uint16_t *>(out), static_cast<uint16_t *>(out_lo), s);
+        e = launch_tc_split(g, stencil, B, static_cast<const uint16_t *>(in),
+                            static_cast<const uint16_t *>(in_lo), static_cast<uint16_t *>(out),
+                            static_cast<uint16_t *>(out_lo), s);
     } else {
-        e = launch_tc_f16(g, stencil, B, in_maps[0], static_cast<const uint16_t *>(in),
+        e = launch_tc_f16(g, stencil, B, static_cast<const uint16_t *>(in),
                           static_cast<uint16_t *>(out), s);
     }
     return cuda_status(e, "sweep kernel launch");
@@ -211,6 +161,11 @@ int tcs_stencil_radius(int stencil) {
 size_t tcs_brick_elems(int ny, int nx) {
     if (ny <= 0 || nx <= 0) return 0;
     return (size_t)((ny + 15) / 16) * (size_t)((nx + 15) / 16) * 256;
+}
+
+size_t tcs_plane_elems(int ny, int nx, int precision) {
+    if (ny <= 0 || nx <= 0 || precision < TCS_PREC_F16 || precision > TCS_PREC_F32) return 0;
+    return plane_elems(plane_geom(ny, nx, precision == TCS_PREC_F32 ? 4 : 8));
 }
 
 int tcs_device_error(int *code) {
@@ -348,14 +303,14 @@ int tcs_sweep_step(const tcs_step_args *a, const void *d_in, const void *d_in_lo
     GridGeom g;
     st = make_geom(a->ny, a->nx, a->stencil, a->y0, a->y1, a->x0, a->x1, &g);
     if (st) return st;
-    PlaneMaps maps[2];
+    if (reinterpret_cast<uintptr_t>(d_in) % 16 || reinterpret_cast<uintptr_t>(d_out) % 16 ||
+        reinterpret_cast<uintptr_t>(d_in_lo) % 16 || reinterpret_cast<uintptr_t>(d_out_lo) % 16)
+        return fail(TCS_ERR_INVALID, "tcs_sweep_step: planes must be 16-byte aligned");
     if (a->engine == TCS_ENGINE_TENSOR) {
-        const int tbx = tc_tile_bricks_x(a->precision == TCS_PREC_SPLIT);
-        st = encode_plane_maps(d_in, g.nby, g.nbx, tbx, &maps[0]);
-        if (!st && a->precision == TCS_PREC_SPLIT) st = encode_plane_maps(d_in_lo, g.nby, g.nbx, tbx, &maps[1]);
+        st = cuda_status(tc_prepare(a->stencil, a->precision == TCS_PREC_SPLIT), "tensor kernel set-up");
         if (st) return st;
     }
-    return run_step(g, a->stencil, a->engine, a->precision, a->coeffs, maps, d_in, d_in_lo, d_out,
+    return run_step(g, a->stencil, a->engine, a->precision, a->coeffs, d_in, d_in_lo, d_out,
                     d_out_lo, (cudaStream_t)stream);
 }
 
@@ -368,7 +323,6 @@ struct tcs_plan_s {
     GridGeom g;
     size_t plane_bytes = 0;
     void *buf[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [state][hi, lo]
-    PlaneMaps maps[2][2];
     int cur = 0;
     int scale_exp = 0;          // split form: planes hold x 2^-scale_exp
     unsigned *d_max = nullptr;  // split form: max |x| scratch (float bits)
@@ -394,8 +348,8 @@ struct tcs_plan_s {
     }
 
     int step(int from, cudaStream_t s) {
-        return run_step(g, prob.stencil, prob.engine, prob.precision, coeffs, maps[from],
-                        buf[from][0], buf[from][1], buf[1 - from][0], buf[1 - from][1], s);
+        return run_step(g, prob.stencil, prob.engine, prob.precision, coeffs, buf[from][0],
+                        buf[from][1], buf[1 - from][0], buf[1 - from][1], s);
     }
 };
 
@@ -425,24 +379,20 @@ int tcs_plan_create(const tcs_problem *pr, tcs_plan *out) {
     const int n = 2 * stencil_r(pr->stencil) + 1;
     for (int k = 0; k < 25; k++) p->coeffs[k] = k < n * n ? pr->coeffs[k] : 0.0f;
     p->prob.coeffs = p->coeffs;
-    const size_t elems = tcs_brick_elems(pr->ny, pr->nx);
+    const size_t elems = tcs_plane_elems(pr->ny, pr->nx, pr->precision);
     p->plane_bytes = elems * (pr->precision == TCS_PREC_F32 ? 4 : 2);
+    // Zeroed, so that padding cells, which no sweep writes, are finite: a
+    // zero band entry times a NaN would still poison an MMA sum.
     for (int s = 0; s < 2; s++)
         for (int pl = 0; pl < p->planes(); pl++) {
-            st = cuda_status(cudaMalloc(&p->buf[s][pl], p->plane_bytes), "cudaMalloc(brick plane)");
+            st = cuda_status(cudaMalloc(&p->buf[s][pl], p->plane_bytes), "cudaMalloc(plane)");
+            if (!st) st = cuda_status(cudaMemset(p->buf[s][pl], 0, p->plane_bytes), "cudaMemset(plane)");
             if (st) return st;
         }
     if (pr->engine == TCS_ENGINE_TENSOR) {
         st = cuda_status(tc_prepare(pr->stencil, pr->precision == TCS_PREC_SPLIT), "tensor kernel set-up");
         if (st) return st;
     }
-    if (pr->engine == TCS_ENGINE_TENSOR)
-        for (int s = 0; s < 2; s++)
-            for (int pl = 0; pl < p->planes(); pl++) {
-                st = encode_plane_maps(p->buf[s][pl], p->g.nby, p->g.nbx,
-                                       tc_tile_bricks_x(pr->precision == TCS_PREC_SPLIT), &p->maps[s][pl]);
-                if (st) return st;
-            }
     *out = p.release();
     return TCS_OK;
 }
@@ -653,7 +603,7 @@ int tcs_host_code(float *h_A, float *h_B, float *h_C, int N, int n, int stencil,
     st = make_geom(Np, Np, stencil, a.y0, a.y1, a.x0, a.x1, &g);
     if (st) return st;
 
-    const size_t cells = (size_t)N * N, plane = tcs_brick_elems(Np, Np) * sizeof(uint16_t);
+    const size_t cells = (size_t)N * N, plane = tcs_plane_elems(Np, Np, TCS_PREC_F16) * sizeof(uint16_t);
     float *d_f32 = nullptr;
     uint16_t *d_A = nullptr, *d_C = nullptr;
     cudaEvent_t start = nullptr, stop = nullptr;
@@ -667,11 +617,12 @@ int tcs_host_code(float *h_A, float *h_B, float *h_C, int N, int n, int stencil,
     st = cuda_status(cudaMalloc(&d_f32, cells * sizeof(float)), "Failed to allocate device memory for A");
     if (!st) st = cuda_status(cudaMalloc(&d_A, plane), "Failed to allocate device memory for A");
     if (!st) st = cuda_status(cudaMalloc(&d_C, plane), "Failed to allocate device memory for C");
+    if (!st) st = cuda_status(cudaMemset(d_C, 0, plane), "cudaMemset(C)");
     if (!st) st = cuda_status(cudaMemcpy(d_f32, h_A, cells * sizeof(float), cudaMemcpyHostToDevice), "H2D copy of A");
     // array_float2half + padding_2D(pad 16, value 1.0) + brick_layout_2D
     if (!st) st = cuda_status(launch_pack_f16(d_f32, N, N, pad, 1.0f, d_A, nullptr), "pack launch");
-    PlaneMaps maps[2];
-    if (!st && engine == TCS_ENGINE_TENSOR) st = encode_plane_maps(d_A, g.nby, g.nbx, tc_tile_bricks_x(false), &maps[0]);
+    if (!st && engine == TCS_ENGINE_TENSOR)
+        st = cuda_status(tc_prepare(stencil, false), "tensor kernel set-up");
     if (!st) st = cuda_status(cudaEventCreate(&start), "cudaEventCreate");
     if (!st) st = cuda_status(cudaEventCreate(&stop), "cudaEventCreate");
     double sum = 0.0;
@@ -679,7 +630,7 @@ int tcs_host_code(float *h_A, float *h_B, float *h_C, int N, int n, int stencil,
         float elapsed = 0.0f;
         st = cuda_status(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
         if (!st) st = cuda_status(cudaEventRecord(start, nullptr), "cudaEventRecord");
-        if (!st) st = run_step(g, stencil, engine, TCS_PREC_F16, h_B, maps, d_A, nullptr, d_C, nullptr, nullptr);
+        if (!st) st = run_step(g, stencil, engine, TCS_PREC_F16, h_B, d_A, nullptr, d_C, nullptr, nullptr);
         if (!st) st = cuda_status(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
         if (!st) st = cuda_status(cudaEventRecord(stop, nullptr), "cudaEventRecord");
         if (!st) st = cuda_status(cudaEventSynchronize(stop), "cudaEventSynchronize");

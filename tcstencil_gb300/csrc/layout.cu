@@ -1,11 +1,13 @@
-// Device layout transforms: the reference's host-side array_float2half,
-// padding_2D, brick_layout_2D and reverse_layout_2D (common/common.hpp:146-160,
-// layout16/host_star2d1r.cu:63-101), as bit-exact device kernels, plus fused
-// pack/unpack forms used on the sweep path.
+// Device layout transforms.
 //
-// Thread granularity is one 16-byte slice of a brick row (8 FP16 or 4 FP32
-// cells), so brick-side accesses are 128-bit and consecutive threads touch
-// consecutive bytes of a brick.
+//  - The reference's host-side layout16 helpers, padding_2D, brick_layout_2D
+//    and reverse_layout_2D (layout16/host_star2d1r.cu:63-101), as bit-exact
+//    device kernels (16 x 16 bricks, row-major inside a brick).
+//  - pack / unpack between FP32 row-major grids and the engine's panel
+//    planes: array_float2half (common/common.hpp:146-160) + padding_2D +
+//    layout change in one pass, and the inverse.  One thread writes or reads
+//    one 16-byte panel row, so plane-side accesses are 128-bit and
+//    consecutive threads touch consecutive bytes of a panel.
 #include "tcs_device.cuh"
 #include "tcs_internal.h"
 
@@ -26,100 +28,24 @@ __device__ __forceinline__ float h2f_bits(uint16_t b) {
 }
 
 // Value of padded-grid cell (Y, X) of a (ny+2pad) x (nx+2pad) grid whose
-// interior is the FP32 row-major input.
+// interior is the FP32 row-major input; 0 outside the padded grid.
 __device__ __forceinline__ float padded_cell(const float *in, int ny, int nx, int pad,
                                              float pad_value, int Y, int X) {
+    if (Y < 0 || X < 0 || Y >= ny + 2 * pad || X >= nx + 2 * pad) return 0.0f;
     const int iy = Y - pad, ix = X - pad;
     return (iy >= 0 && iy < ny && ix >= 0 && ix < nx) ? in[(size_t)iy * nx + ix] : pad_value;
 }
 
-// slice id -> (brick, row, first column) for `per` cells per slice
-struct Slice {
-    int brick, row, col;
+// A panel row: thread id -> (panel, row) -> first cell (Y, X0).
+struct PanelRow {
+    int Y, X0;
 };
-__device__ __forceinline__ Slice slice_of(size_t id, int per) {
-    const int slices_per_row = 16 / per;
-    Slice s;
-    s.brick = static_cast<int>(id / (16 * slices_per_row));
-    const int rem = static_cast<int>(id % (16 * slices_per_row));
-    s.row = rem / slices_per_row;
-    s.col = (rem % slices_per_row) * per;
-    return s;
-}
-
-__global__ void pack_f16_kernel(const float *__restrict__ in, int ny, int nx, int pad,
-                                float pad_value, uint16_t *__restrict__ out, int nyo, int nxo,
-                                int nbx, size_t n_slices) {
-    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n_slices) return;
-    const Slice s = slice_of(id, 8);
-    const int Y = (s.brick / nbx) * 16 + s.row;
-    const int X0 = (s.brick % nbx) * 16 + s.col;
-    uint32_t w[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        uint16_t h[2];
-#pragma unroll
-        for (int j = 0; j < 2; j++) {
-            const int X = X0 + 2 * i + j;
-            h[j] = (Y < nyo && X < nxo) ? f2h_bits(padded_cell(in, ny, nx, pad, pad_value, Y, X))
-                                        : (uint16_t)0;
-        }
-        w[i] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
-    }
-    reinterpret_cast<uint4 *>(out)[id] = make_uint4(w[0], w[1], w[2], w[3]);
-}
-
-__global__ void unpack_f16_kernel(const uint16_t *__restrict__ in, int ny, int nx, int pad,
-                                  float *__restrict__ out, int nbx, size_t n_slices) {
-    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n_slices) return;
-    const Slice s = slice_of(id, 8);
-    const int iy = (s.brick / nbx) * 16 + s.row - pad;
-    if (iy < 0 || iy >= ny) return;
-    const uint4 v = reinterpret_cast<const uint4 *>(in)[id];
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-    const int ix0 = (s.brick % nbx) * 16 + s.col - pad;
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const int ix = ix0 + i;
-        if (ix >= 0 && ix < nx)
-            out[(size_t)iy * nx + ix] = h2f_bits((uint16_t)(w[i >> 1] >> (16 * (i & 1))));
-    }
-}
-
-__global__ void pack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
-                                float pad_value, float *__restrict__ out, int nyo, int nxo,
-                                int nbx, size_t n_slices) {
-    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n_slices) return;
-    const Slice s = slice_of(id, 4);
-    const int Y = (s.brick / nbx) * 16 + s.row;
-    const int X0 = (s.brick % nbx) * 16 + s.col;
-    float v[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int X = X0 + i;
-        v[i] = (Y < nyo && X < nxo) ? padded_cell(in, ny, nx, pad, pad_value, Y, X) : 0.0f;
-    }
-    reinterpret_cast<float4 *>(out)[id] = make_float4(v[0], v[1], v[2], v[3]);
-}
-
-__global__ void unpack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
-                                  float *__restrict__ out, int nbx, size_t n_slices) {
-    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n_slices) return;
-    const Slice s = slice_of(id, 4);
-    const int iy = (s.brick / nbx) * 16 + s.row - pad;
-    if (iy < 0 || iy >= ny) return;
-    const float4 v = reinterpret_cast<const float4 *>(in)[id];
-    const float f[4] = {v.x, v.y, v.z, v.w};
-    const int ix0 = (s.brick % nbx) * 16 + s.col - pad;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int ix = ix0 + i;
-        if (ix >= 0 && ix < nx) out[(size_t)iy * nx + ix] = f[i];
-    }
+__device__ __forceinline__ PanelRow panel_row(size_t id, const PlaneGeom &p) {
+    PanelRow r;
+    const int pan = static_cast<int>(id / p.nyp);
+    r.Y = static_cast<int>(id % p.nyp) - kPadTop;
+    r.X0 = (pan - 1) * p.cpp;
+    return r;
 }
 
 // Split storage of x: x' = x 2^-E, hi = fp16(rint(x' 2^11) 2^-11) (fixed
@@ -131,27 +57,81 @@ __device__ __forceinline__ void split_value(float x, float scale, uint16_t &h, u
     l = f2h_bits((xs - h2f_bits(h)) * 2048.0f);
 }
 
+__global__ void pack_f16_kernel(const float *__restrict__ in, int ny, int nx, int pad,
+                                float pad_value, uint16_t *__restrict__ out, PlaneGeom p,
+                                size_t n_rows) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_rows) return;
+    const PanelRow r = panel_row(id, p);
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint32_t a = f2h_bits(padded_cell(in, ny, nx, pad, pad_value, r.Y, r.X0 + 2 * i));
+        const uint32_t b = f2h_bits(padded_cell(in, ny, nx, pad, pad_value, r.Y, r.X0 + 2 * i + 1));
+        w[i] = a | (b << 16);
+    }
+    reinterpret_cast<uint4 *>(out)[id] = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__global__ void unpack_f16_kernel(const uint16_t *__restrict__ in, int ny, int nx, int pad,
+                                  float *__restrict__ out, PlaneGeom p, size_t n_rows) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_rows) return;
+    const PanelRow r = panel_row(id, p);
+    const int iy = r.Y - pad;
+    if (iy < 0 || iy >= ny) return;
+    const uint4 v = reinterpret_cast<const uint4 *>(in)[id];
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int ix = r.X0 + i - pad;
+        if (ix >= 0 && ix < nx)
+            out[(size_t)iy * nx + ix] = h2f_bits((uint16_t)(w[i >> 1] >> (16 * (i & 1))));
+    }
+}
+
+__global__ void pack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
+                                float pad_value, float *__restrict__ out, PlaneGeom p,
+                                size_t n_rows) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_rows) return;
+    const PanelRow r = panel_row(id, p);
+    float v[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) v[i] = padded_cell(in, ny, nx, pad, pad_value, r.Y, r.X0 + i);
+    reinterpret_cast<float4 *>(out)[id] = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+__global__ void unpack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
+                                  float *__restrict__ out, PlaneGeom p, size_t n_rows) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_rows) return;
+    const PanelRow r = panel_row(id, p);
+    const int iy = r.Y - pad;
+    if (iy < 0 || iy >= ny) return;
+    const float4 v = reinterpret_cast<const float4 *>(in)[id];
+    const float f[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int ix = r.X0 + i - pad;
+        if (ix >= 0 && ix < nx) out[(size_t)iy * nx + ix] = f[i];
+    }
+}
+
 __global__ void pack_split_kernel(const float *__restrict__ in, int ny, int nx, int pad,
                                   float pad_value, float scale, uint16_t *__restrict__ hi,
-                                  uint16_t *__restrict__ lo, int nyo, int nxo, int nbx,
-                                  size_t n_slices) {
+                                  uint16_t *__restrict__ lo, PlaneGeom p, size_t n_rows) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n_slices) return;
-    const Slice s = slice_of(id, 8);
-    const int Y = (s.brick / nbx) * 16 + s.row;
-    const int X0 = (s.brick % nbx) * 16 + s.col;
+    if (id >= n_rows) return;
+    const PanelRow r = panel_row(id, p);
     uint32_t wh[4], wl[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         uint16_t h[2], l[2];
 #pragma unroll
-        for (int j = 0; j < 2; j++) {
-            const int X = X0 + 2 * i + j;
-            h[j] = 0;
-            l[j] = 0;
-            if (Y < nyo && X < nxo)
-                split_value(padded_cell(in, ny, nx, pad, pad_value, Y, X), scale, h[j], l[j]);
-        }
+        for (int j = 0; j < 2; j++)
+            split_value(padded_cell(in, ny, nx, pad, pad_value, r.Y, r.X0 + 2 * i + j), scale,
+                        h[j], l[j]);
         wh[i] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
         wl[i] = (uint32_t)l[0] | ((uint32_t)l[1] << 16);
     }
@@ -161,21 +141,20 @@ __global__ void pack_split_kernel(const float *__restrict__ in, int ny, int nx, 
 
 __global__ void unpack_split_kernel(const uint16_t *__restrict__ hi,
                                     const uint16_t *__restrict__ lo, int ny, int nx, int pad,
-                                    float scale, float *__restrict__ out, int nbx,
-                                    size_t n_slices) {
+                                    float scale, float *__restrict__ out, PlaneGeom p,
+                                    size_t n_rows) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n_slices) return;
-    const Slice s = slice_of(id, 8);
-    const int iy = (s.brick / nbx) * 16 + s.row - pad;
+    if (id >= n_rows) return;
+    const PanelRow r = panel_row(id, p);
+    const int iy = r.Y - pad;
     if (iy < 0 || iy >= ny) return;
     const uint4 vh = reinterpret_cast<const uint4 *>(hi)[id];
     const uint4 vl = reinterpret_cast<const uint4 *>(lo)[id];
     const uint32_t wh[4] = {vh.x, vh.y, vh.z, vh.w};
     const uint32_t wl[4] = {vl.x, vl.y, vl.z, vl.w};
-    const int ix0 = (s.brick % nbx) * 16 + s.col - pad;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-        const int ix = ix0 + i;
+        const int ix = r.X0 + i - pad;
         if (ix >= 0 && ix < nx) {
             const float h = h2f_bits((uint16_t)(wh[i >> 1] >> (16 * (i & 1))));
             const float l = h2f_bits((uint16_t)(wl[i >> 1] >> (16 * (i & 1))));
@@ -194,6 +173,20 @@ __global__ void max_abs_kernel(const float *__restrict__ in, size_t n, unsigned 
     if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(m));
 }
 
+// ------------------------------------------- reference layout16 helpers ---
+// 16 x 16 bricks: brick (i, j) at (i*nbx + j)*256, cell (y, x) at y*16 + x.
+struct Slice {
+    int brick, row, col;
+};
+__device__ __forceinline__ Slice slice_of(size_t id) {
+    Slice s;
+    s.brick = static_cast<int>(id / 32);
+    const int rem = static_cast<int>(id % 32);
+    s.row = rem / 2;
+    s.col = (rem % 2) * 8;
+    return s;
+}
+
 // padding_2D: one thread per output cell.
 __global__ void padding_2d_kernel(const uint16_t *__restrict__ in, uint16_t *__restrict__ out,
                                   int size, int halo, uint16_t value) {
@@ -210,7 +203,7 @@ __global__ void brick_2d_kernel(const uint16_t *__restrict__ in, uint16_t *__res
                                 int ny, int nx, int nbx, size_t n_slices) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_slices) return;
-    const Slice s = slice_of(id, 8);
+    const Slice s = slice_of(id);
     const int Y = (s.brick / nbx) * 16 + s.row;
     const int X0 = (s.brick % nbx) * 16 + s.col;
     uint32_t w[4];
@@ -232,7 +225,7 @@ __global__ void unbrick_2d_kernel(const uint16_t *__restrict__ in, uint16_t *__r
                                   int ny, int nx, int nbx, size_t n_slices) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_slices) return;
-    const Slice s = slice_of(id, 8);
+    const Slice s = slice_of(id);
     const int Y = (s.brick / nbx) * 16 + s.row;
     if (Y >= ny) return;
     const uint4 v = reinterpret_cast<const uint4 *>(in)[id];
@@ -248,58 +241,64 @@ __global__ void unbrick_2d_kernel(const uint16_t *__restrict__ in, uint16_t *__r
 inline unsigned blocks_for(size_t n) { return static_cast<unsigned>((n + kThreads - 1) / kThreads); }
 inline int nb(int n) { return (n + 15) / 16; }
 
+struct PackShape {
+    PlaneGeom p;
+    size_t rows;
+};
+inline PackShape pack_shape(int ny, int nx, int pad, int cpp) {
+    PackShape s;
+    s.p = plane_geom(ny + 2 * pad, nx + 2 * pad, cpp);
+    s.rows = (size_t)s.p.nyp * s.p.npan;
+    return s;
+}
+
 }  // namespace
 
 cudaError_t launch_pack_f16(const float *in, int ny, int nx, int pad, float pad_value,
-                            uint16_t *bricks, cudaStream_t s) {
-    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
-    const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
-    pack_f16_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, bricks, nyo,
-                                                       nxo, nb(nxo), n);
+                            uint16_t *plane, cudaStream_t s) {
+    const PackShape ps = pack_shape(ny, nx, pad, 8);
+    pack_f16_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, plane,
+                                                             ps.p, ps.rows);
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack_f16(const uint16_t *bricks, int ny, int nx, int pad, float *out,
+cudaError_t launch_unpack_f16(const uint16_t *plane, int ny, int nx, int pad, float *out,
                               cudaStream_t s) {
-    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
-    const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
-    unpack_f16_kernel<<<blocks_for(n), kThreads, 0, s>>>(bricks, ny, nx, pad, out, nb(nxo), n);
+    const PackShape ps = pack_shape(ny, nx, pad, 8);
+    unpack_f16_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(plane, ny, nx, pad, out, ps.p,
+                                                               ps.rows);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pack_f32(const float *in, int ny, int nx, int pad, float pad_value,
-                            float *bricks, cudaStream_t s) {
-    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
-    const size_t n = (size_t)nb(nyo) * nb(nxo) * 64;
-    pack_f32_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, bricks, nyo,
-                                                       nxo, nb(nxo), n);
+                            float *plane, cudaStream_t s) {
+    const PackShape ps = pack_shape(ny, nx, pad, 4);
+    pack_f32_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, plane,
+                                                             ps.p, ps.rows);
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack_f32(const float *bricks, int ny, int nx, int pad, float *out,
+cudaError_t launch_unpack_f32(const float *plane, int ny, int nx, int pad, float *out,
                               cudaStream_t s) {
-    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
-    const size_t n = (size_t)nb(nyo) * nb(nxo) * 64;
-    unpack_f32_kernel<<<blocks_for(n), kThreads, 0, s>>>(bricks, ny, nx, pad, out, nb(nxo), n);
+    const PackShape ps = pack_shape(ny, nx, pad, 4);
+    unpack_f32_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(plane, ny, nx, pad, out, ps.p,
+                                                               ps.rows);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pack_split(const float *in, int ny, int nx, int pad, float pad_value,
                               int scale_exp, uint16_t *hi, uint16_t *lo, cudaStream_t s) {
-    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
-    const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
-    pack_split_kernel<<<blocks_for(n), kThreads, 0, s>>>(in, ny, nx, pad, pad_value,
-                                                         ldexpf(1.0f, -scale_exp), hi, lo, nyo,
-                                                         nxo, nb(nxo), n);
+    const PackShape ps = pack_shape(ny, nx, pad, 8);
+    pack_split_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(
+        in, ny, nx, pad, pad_value, ldexpf(1.0f, -scale_exp), hi, lo, ps.p, ps.rows);
     return cudaGetLastError();
 }
 
 cudaError_t launch_unpack_split(const uint16_t *hi, const uint16_t *lo, int ny, int nx, int pad,
                                 int scale_exp, float *out, cudaStream_t s) {
-    const int nyo = ny + 2 * pad, nxo = nx + 2 * pad;
-    const size_t n = (size_t)nb(nyo) * nb(nxo) * 32;
-    unpack_split_kernel<<<blocks_for(n), kThreads, 0, s>>>(hi, lo, ny, nx, pad,
-                                                           ldexpf(1.0f, scale_exp), out, nb(nxo), n);
+    const PackShape ps = pack_shape(ny, nx, pad, 8);
+    unpack_split_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(
+        hi, lo, ny, nx, pad, ldexpf(1.0f, scale_exp), out, ps.p, ps.rows);
     return cudaGetLastError();
 }
 

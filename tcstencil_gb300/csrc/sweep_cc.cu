@@ -1,13 +1,17 @@
 // CUDA-core sweep kernels (the counterpart of the reference's baseline/
 // kernel_*.cu `kernel_run`, rebuilt for GB300).
 //
-// One warp sweeps a vertical strip of bricks top to bottom.  Each lane owns a
-// 16-byte slice of a brick row (8 FP16 cells, or 4 FP32 cells), loaded with one
-// 128-bit load, so a warp reads whole 32-byte sectors of 16 (FP16) or 8 (FP32)
-// adjacent bricks per row.  Horizontal halo cells come from the neighbouring
-// lanes by warp shuffle; the two outer lanes fetch the strip's edge cells.
-// The vertical taps come from a register window of the last 2r+1 rows, so each
-// input row is loaded and converted once per strip.
+// One warp sweeps a vertical strip of 16 panels (128 FP16 or 64 FP32 columns)
+// top to bottom, two rows per step.  Lanes 2p and 2p+1 own panel p: each
+// loads one 16-byte panel row (the two rows of a step are one 32-byte sector
+// of the panel), the pair swaps them with shuffles, and each lane then
+// computes both rows for its half of the panel's columns.  Horizontal halo
+// cells come from the neighbouring panel's lanes by shuffle; the two outer
+// lanes fetch the strip's edge cells.  The vertical taps come from a register
+// window of six rows, so each input row is loaded and converted once per
+// strip.  Before storing, the pair swaps halves again so that each lane
+// writes one full 16-byte panel row.  The plane's padding rows and panels
+// keep every read in bounds.
 //
 // Arithmetic follows gold's tap order (common/gold_*.cpp):
 //  - FP16 storage: acc = fmaf chain from 0, FP32 coefficients, RNE to FP16.
@@ -23,10 +27,12 @@ namespace tcs {
 namespace {
 
 constexpr int kCcWarps = 4;     // warps per block
-constexpr int kStripRows = 64;  // rows per warp strip
+constexpr int kStripRows = 64;  // rows per warp strip (even)
 
 struct CcParams {
     GridGeom g;
+    PlaneGeom p;   // plane of this precision
+    int nchunks;   // panels that hold grid cells
     int strip_h;
     int strips_x;
     int n_strips;
@@ -40,33 +46,18 @@ __device__ __forceinline__ uint4 ldg_v4(const void *p) {
     return v;
 }
 
-template <bool F32>
-struct Lane;
-
-// FP16: 2 lanes per brick row, 8 cells per lane.
-template <>
-struct Lane<false> {
-    static constexpr int kVec = 8;
-    static constexpr int kLanesPerBrick = 2;
-};
-// FP32: 4 lanes per brick row, 4 cells per lane.
-template <>
-struct Lane<true> {
-    static constexpr int kVec = 4;
-    static constexpr int kLanesPerBrick = 4;
-};
-
 template <int S, bool F32>
 __global__ void __launch_bounds__(kCcWarps * 32)
     cc_sweep_kernel(const void *__restrict__ in_, void *__restrict__ out_, CcParams p,
                     TapCoeffs c) {
     constexpr int R = stencil_r(S);
-    constexpr int NW = 2 * R + 1;          // window rows
-    constexpr int V = Lane<F32>::kVec;     // cells per lane
-    constexpr int LPB = Lane<F32>::kLanesPerBrick;
-    constexpr int W = V + 2 * R;           // window columns
+    constexpr int V = F32 ? 4 : 8;    // cells per panel row
+    constexpr int H = V / 2;          // cells per lane
+    constexpr int W = H + 2 * R;      // window columns of a lane
     constexpr int NT = tap_count(S);
     constexpr bool BOX = stencil_box(S);
+    constexpr int WPC = F32 ? 1 : 2;              // cells per 32-bit word
+    constexpr int HW = (R + WPC - 1) / WPC;       // halo words per row
     using T = typename std::conditional<F32, float, uint16_t>::type;
     const T *__restrict__ in = static_cast<const T *>(in_);
     T *__restrict__ out = static_cast<T *>(out_);
@@ -75,156 +66,169 @@ __global__ void __launch_bounds__(kCcWarps * 32)
     const int strip = blockIdx.x * kCcWarps + (threadIdx.x >> 5);
     if (strip >= p.n_strips) return;  // uniform across the warp
     const int sx = strip % p.strips_x, sy = strip / p.strips_x;
-    const int nbx = p.g.nbx;
-    const int bx = sx * (32 / LPB) + lane / LPB;
-    const int sub = lane % LPB;            // slice of the brick row
-    const bool active = bx < nbx;
-    const int xb = bx * 16 + V * sub;      // first column of this lane
-    const int rows = p.g.nby * 16;
+    const int par = lane & 1;                 // 0: left half of the panel, 1: right half
+    const int chunk = sx * 16 + (lane >> 1);  // panel of this lane pair
+    const bool active = chunk < p.nchunks;
+    const int xb = chunk * V;                 // first column of the panel
+    const int xl = xb + par * H;              // first column this lane computes
     const int ys = sy * p.strip_h;
-    const int ye = min(ys + p.strip_h, rows);
+    const int ye = min(ys + p.strip_h, p.g.ny);
+    const bool right_edge_ok = chunk + 2 < p.p.npan;  // the next panel is allocated
+    const int ymax = p.g.ny + 3;  // rows past this are never needed
 
+    // Raw words of one step: both rows of this lane pair's panel, and the
+    // halo words on this lane's outer side for both rows.
     struct Raw {
-        uint4 v;
-        uint32_t e0, e1;  // edge cells fetched by lanes 0 and 31
+        uint32_t w[2][4];
+        uint32_t h[2][HW];
     };
 
-    auto row_base = [&](int y) -> size_t {
-        return (size_t)(y >> 4) * nbx * 256 + (size_t)(y & 15) * 16;
-    };
-
-    auto load_row = [&](int y) -> Raw {
+    // Row pair (y0, y0+1): this lane loads row y0 + par and swaps with its pair.
+    auto load_pair = [&](int y0) -> Raw {
         Raw r;
-        r.v = make_uint4(0u, 0u, 0u, 0u);
-        r.e0 = 0u;
-        r.e1 = 0u;
-        if (y >= 0 && y < rows) {
-            const T *rowp = in + row_base(y);
-            if (active) r.v = ldg_v4(rowp + (size_t)bx * 256 + V * sub);
-            if constexpr (!F32) {
-                // one 32-bit word = 2 FP16 cells
-                if (lane == 0 && bx >= 1)
-                    r.e0 = __ldg(reinterpret_cast<const uint32_t *>(rowp + (size_t)(bx - 1) * 256 + 14));
-                if (lane == 31 && bx + 1 < nbx)
-                    r.e0 = __ldg(reinterpret_cast<const uint32_t *>(rowp + (size_t)(bx + 1) * 256));
-            } else {
-                if (lane == 0 && bx >= 1) {
-                    const uint32_t *q = reinterpret_cast<const uint32_t *>(rowp + (size_t)(bx - 1) * 256 + 14);
-                    r.e0 = __ldg(q);
-                    r.e1 = __ldg(q + 1);
-                }
-                if (lane == 31 && bx + 1 < nbx) {
-                    const uint32_t *q = reinterpret_cast<const uint32_t *>(rowp + (size_t)(bx + 1) * 256);
-                    r.e0 = __ldg(q);
-                    r.e1 = __ldg(q + 1);
-                }
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (active) v = ldg_v4(in + plane_index(p.p, min(y0 + par, ymax), xb));
+        const uint32_t mine[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t other = __shfl_xor_sync(0xffffffffu, mine[i], 1);
+            r.w[0][i] = par ? other : mine[i];
+            r.w[1][i] = par ? mine[i] : other;
+        }
+        // the left half needs the last R cells of the panel to the left, the
+        // right half the first R cells of the panel to the right
+#pragma unroll
+        for (int row = 0; row < 2; row++)
+#pragma unroll
+            for (int k = 0; k < HW; k++) {
+                const uint32_t from_left = __shfl_up_sync(0xffffffffu, r.w[row][4 - HW + k], 2);
+                const uint32_t from_right = __shfl_down_sync(0xffffffffu, r.w[row][k], 2);
+                r.h[row][k] = par ? from_right : from_left;
+            }
+        if (lane == 0 || lane == 31) {
+            const bool ok = lane == 0 || right_edge_ok;
+            const int xe = lane == 0 ? xb - V : xb + V;
+#pragma unroll
+            for (int row = 0; row < 2; row++) {
+                const uint32_t *q = reinterpret_cast<const uint32_t *>(
+                    in + plane_index(p.p, min(y0 + row, ymax), xe));
+#pragma unroll
+                for (int k = 0; k < HW; k++)
+                    r.h[row][k] = ok ? __ldg(q + (lane == 0 ? 4 - HW + k : k)) : 0u;
             }
         }
         return r;
     };
 
-    // Converts a raw row into window columns [0, W): R left halo cells, the
-    // lane's V cells, R right halo cells.  All lanes take part (shuffles).
-    auto to_window = [&](const Raw &r, float (&w)[W]) {
+    // Window columns [0, W) of this lane for one row: cells xl-R .. xl+H+R-1.
+    auto to_window = [&](const Raw &r, int row, float (&w)[W]) {
+        float cells[V];
+        float halo[2];
         if constexpr (!F32) {
-            uint32_t left = __shfl_up_sync(0xffffffffu, r.v.w, 1);   // cells x-2, x-1
-            uint32_t right = __shfl_down_sync(0xffffffffu, r.v.x, 1); // cells x+8, x+9
-            if (lane == 0) left = r.e0;
-            if (lane == 31) right = r.e0;
-            const uint32_t words[4] = {r.v.x, r.v.y, r.v.z, r.v.w};
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                float2 f = unpack_half2(words[i]);
-                w[R + 2 * i] = f.x;
-                w[R + 2 * i + 1] = f.y;
+                const float2 f = unpack_half2(r.w[row][i]);
+                cells[2 * i] = f.x;
+                cells[2 * i + 1] = f.y;
             }
-            float2 fl = unpack_half2(left), fr = unpack_half2(right);
-            if constexpr (R == 1) {
-                w[0] = fl.y;
-                w[W - 1] = fr.x;
-            } else {
-                w[0] = fl.x;
-                w[1] = fl.y;
-                w[W - 2] = fr.x;
-                w[W - 1] = fr.y;
-            }
+            const float2 hf = unpack_half2(r.h[row][0]);
+            // left half: cells 6, 7 of the left panel; right half: 0, 1 of the right
+            halo[0] = hf.x;
+            halo[1] = hf.y;
         } else {
-            uint32_t l1 = __shfl_up_sync(0xffffffffu, r.v.w, 1);   // cell x-1
-            uint32_t l2 = __shfl_up_sync(0xffffffffu, r.v.z, 1);   // cell x-2
-            uint32_t r1 = __shfl_down_sync(0xffffffffu, r.v.x, 1); // cell x+4
-            uint32_t r2 = __shfl_down_sync(0xffffffffu, r.v.y, 1); // cell x+5
-            if (lane == 0) { l2 = r.e0; l1 = r.e1; }
-            if (lane == 31) { r1 = r.e0; r2 = r.e1; }
-            w[R + 0] = __uint_as_float(r.v.x);
-            w[R + 1] = __uint_as_float(r.v.y);
-            w[R + 2] = __uint_as_float(r.v.z);
-            w[R + 3] = __uint_as_float(r.v.w);
-            if constexpr (R == 1) {
-                w[0] = __uint_as_float(l1);
-                w[W - 1] = __uint_as_float(r1);
-            } else {
-                w[0] = __uint_as_float(l2);
-                w[1] = __uint_as_float(l1);
-                w[W - 2] = __uint_as_float(r1);
-                w[W - 1] = __uint_as_float(r2);
-            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) cells[i] = __uint_as_float(r.w[row][i]);
+            halo[0] = __uint_as_float(r.h[row][0]);
+            halo[1] = __uint_as_float(r.h[row][HW - 1]);
+        }
+#pragma unroll
+        for (int k = 0; k < W; k++) {
+            // left half: R halo cells (the left panel's last R), then cells 0..H+R-1
+            const float left = k < R ? (F32 ? halo[k] : halo[2 - R + k]) : cells[k - R];
+            // right half: cells H-R..V-1, then R halo cells (the right panel's first R)
+            const float right = k < H + R ? cells[H - R + k] : halo[k - H - R];
+            w[k] = par ? right : left;
         }
     };
 
-    float win[NW][W];
-#pragma unroll
-    for (int k = 0; k < 2 * R; k++) to_window(load_row(ys - R + k), win[k]);
-    Raw next = load_row(ys + R);
+    // window: pair slot j holds rows (y0-2+2j, y0-1+2j), rotated over steps
+    float win[3][2][W];
+    {
+        const Raw a = load_pair(ys - 2);
+        to_window(a, 0, win[0][0]);
+        to_window(a, 1, win[0][1]);
+        const Raw b = load_pair(ys);
+        to_window(b, 0, win[1][0]);
+        to_window(b, 1, win[1][1]);
+    }
+    Raw next = load_pair(ys + 2);
 
-    for (int y = ys; y < ye; y += NW) {
+    for (int y = ys; y < ye; y += 6) {
 #pragma unroll
-        for (int u = 0; u < NW; u++) {
-            const int yy = y + u;
-            if (yy < ye) {
-                to_window(next, win[(u + 2 * R) % NW]);  // row yy + R
-                next = load_row(yy + R + 1);
+        for (int u = 0; u < 3; u++) {
+            const int y0 = y + 2 * u;
+            if (y0 < ye) {
+                to_window(next, 0, win[(u + 2) % 3][0]);
+                to_window(next, 1, win[(u + 2) % 3][1]);
+                next = load_pair(y0 + 4);
 
-                float acc[V];
+                float acc[2][H];
 #pragma unroll
-                for (int i = 0; i < V; i++) {
-                    constexpr int dy0 = tap_dy(S, 0), dx0 = tap_dx(S, 0);
-                    const float x0 = win[(u + R + dy0) % NW][R + i + dx0];
-                    if constexpr (F32) acc[i] = BOX ? __fadd_rn(0.0f, __fmul_rn(x0, c.c[0]))
-                                                    : __fmul_rn(x0, c.c[0]);
-                    else acc[i] = fmaf(x0, c.c[0], 0.0f);
-                }
+                for (int q = 0; q < 2; q++) {
+                    {
+                        constexpr int dy0 = tap_dy(S, 0), dx0 = tap_dx(S, 0);
+                        const int wr = 2 + q + dy0;  // window row of y0 + q + dy
 #pragma unroll
-                for (int k = 1; k < NT; k++) {
-                    const int dy = tap_dy(S, k), dx = tap_dx(S, k);
-#pragma unroll
-                    for (int i = 0; i < V; i++) {
-                        const float x = win[(u + R + dy) % NW][R + i + dx];
-                        if constexpr (F32) acc[i] = __fadd_rn(acc[i], __fmul_rn(x, c.c[k]));
-                        else acc[i] = fmaf(x, c.c[k], acc[i]);
-                    }
-                }
-
-                if (active) {
-                    const bool row_in = yy >= p.g.y0 && yy < p.g.y1;
-                    const bool all_in = row_in && xb >= p.g.x0 && xb + V <= p.g.x1;
-                    if (!all_in) {
-#pragma unroll
-                        for (int i = 0; i < V; i++) {
-                            const int x = xb + i;
-                            const bool upd = row_in && x >= p.g.x0 && x < p.g.x1;
-                            if (!upd) acc[i] = win[(u + R) % NW][R + i];
+                        for (int i = 0; i < H; i++) {
+                            const float x0 = win[(u + wr / 2) % 3][wr % 2][R + i + dx0];
+                            if constexpr (F32) acc[q][i] = BOX ? __fadd_rn(0.0f, __fmul_rn(x0, c.c[0]))
+                                                               : __fmul_rn(x0, c.c[0]);
+                            else acc[q][i] = fmaf(x0, c.c[0], 0.0f);
                         }
                     }
-                    T *dst = out + row_base(yy) + (size_t)bx * 256 + V * sub;
-                    uint4 pk;
-                    if constexpr (F32) {
-                        pk = make_uint4(__float_as_uint(acc[0]), __float_as_uint(acc[1]),
-                                        __float_as_uint(acc[2]), __float_as_uint(acc[3]));
-                    } else {
-                        pk = make_uint4(pack_half2(acc[0], acc[1]), pack_half2(acc[2], acc[3]),
-                                        pack_half2(acc[4], acc[5]), pack_half2(acc[6], acc[7]));
+#pragma unroll
+                    for (int k = 1; k < NT; k++) {
+                        const int dy = tap_dy(S, k), dx = tap_dx(S, k);
+                        const int wr = 2 + q + dy;
+#pragma unroll
+                        for (int i = 0; i < H; i++) {
+                            const float x = win[(u + wr / 2) % 3][wr % 2][R + i + dx];
+                            if constexpr (F32) acc[q][i] = __fadd_rn(acc[q][i], __fmul_rn(x, c.c[k]));
+                            else acc[q][i] = fmaf(x, c.c[k], acc[q][i]);
+                        }
                     }
-                    *reinterpret_cast<uint4 *>(dst) = pk;
+                    // cells outside the update rectangle keep their value
+                    const int yy = y0 + q;
+                    const bool row_in = yy >= p.g.y0 && yy < p.g.y1;
+                    if (!(row_in && xl >= p.g.x0 && xl + H <= p.g.x1)) {
+#pragma unroll
+                        for (int i = 0; i < H; i++) {
+                            const int x = xl + i;
+                            if (!(row_in && x >= p.g.x0 && x < p.g.x1))
+                                acc[q][i] = win[(u + (2 + q) / 2) % 3][(2 + q) % 2][R + i];
+                        }
+                    }
+                }
+                // this lane's half of both rows; the pair swaps halves so that
+                // lane par stores all of row y0 + par
+                uint32_t mine[2][2];
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    if constexpr (F32) {
+                        mine[q][0] = __float_as_uint(acc[q][0]);
+                        mine[q][1] = __float_as_uint(acc[q][1]);
+                    } else {
+                        mine[q][0] = pack_half2(acc[q][0], acc[q][1]);
+                        mine[q][1] = pack_half2(acc[q][2], acc[q][3]);
+                    }
+                }
+                const uint32_t s0 = __shfl_xor_sync(0xffffffffu, par ? mine[0][0] : mine[1][0], 1);
+                const uint32_t s1 = __shfl_xor_sync(0xffffffffu, par ? mine[0][1] : mine[1][1], 1);
+                const int yy = y0 + par;
+                if (active && yy < ye) {
+                    const uint4 v = par ? make_uint4(s0, s1, mine[1][0], mine[1][1])
+                                        : make_uint4(mine[0][0], mine[0][1], s0, s1);
+                    *reinterpret_cast<uint4 *>(out + plane_index(p.p, yy, xb)) = v;
                 }
             }
         }
@@ -236,10 +240,11 @@ cudaError_t launch_cc(const GridGeom &g, int stencil, const TapCoeffs &c, const 
                       void *out, cudaStream_t s) {
     CcParams p;
     p.g = g;
+    p.p = F32 ? g.p32 : g.p16;
+    p.nchunks = (g.nx + p.p.cpp - 1) / p.p.cpp;
     p.strip_h = kStripRows;
-    const int bricks_per_warp = 32 / Lane<F32>::kLanesPerBrick;
-    p.strips_x = (g.nbx + bricks_per_warp - 1) / bricks_per_warp;
-    const int strips_y = (g.nby * 16 + p.strip_h - 1) / p.strip_h;
+    p.strips_x = (p.nchunks + 15) / 16;
+    const int strips_y = (g.ny + p.strip_h - 1) / p.strip_h;
     p.n_strips = p.strips_x * strips_y;
     dim3 block(kCcWarps * 32);
     dim3 grid((p.n_strips + kCcWarps - 1) / kCcWarps);

@@ -18,7 +18,8 @@ namespace tcs {
 
 namespace {
 
-// 32 MiB: one FP16 brick plane of up to 16,777,216 cells (e.g. 4096 x 4096).
+// 32 MiB: one FP16 plane of up to 16,777,216 cells, padding included (e.g. a
+// 4000 x 4000 grid; tcs_plane_elems gives a grid's plane size).
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -70,7 +71,7 @@ int tcs_sweep_steps_noalloc(const tcs_step_args *a, const void *d_in, void *d_ou
     GridGeom g;
     int st = make_geom(a->ny, a->nx, a->stencil, a->y0, a->y1, a->x0, a->x1, &g);
     if (st) return st;
-    const size_t plane_bytes = (size_t)g.nby * g.nbx * 256 * sizeof(uint16_t);
+    const size_t plane_bytes = plane_elems(g.p16) * sizeof(uint16_t);
     if (plane_bytes > kNoAllocScratchBytes)
         return fail(TCS_ERR_INVALID,
                     "tcs_sweep_steps_noalloc: a %d x %d grid needs %zu bytes of scratch; the "
@@ -98,10 +99,7 @@ int tcs_sweep_steps_noalloc(const tcs_step_args *a, const void *d_in, void *d_ou
             e = launch_cc_f16(g, a->stencil, c, static_cast<const uint16_t *>(src),
                               static_cast<uint16_t *>(dst), s);
         } else {
-            PlaneMaps maps;
-            st = encode_plane_maps(src, g.nby, g.nbx, tc_tile_bricks_x(false), &maps);
-            if (st) return st;
-            e = launch_tc_f16(g, a->stencil, a->coeffs, maps, static_cast<const uint16_t *>(src),
+            e = launch_tc_f16(g, a->stencil, a->coeffs, static_cast<const uint16_t *>(src),
                               static_cast<uint16_t *>(dst), s);
         }
         st = cuda_status(e, "no-alloc sweep launch");

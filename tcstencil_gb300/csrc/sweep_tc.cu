@@ -3,27 +3,29 @@
 // reference's wmma `mma_run` (layout16/kernel_*.cu).
 //
 // Formulation.  An output tile is 128 rows (the MMA's M, one row per TMEM
-// lane) by TW = 16*TBX columns.  Rows are shifted by the smem descriptor; the
-// horizontal taps are a band.  The tile's input columns are cut into TBX+1
-// windows of 16 columns (K = 16), window w = [X0-8+16w, X0+8+16w).  For each
-// coefficient row dy, window w is multiplied (A = staged input shifted by dy,
-// B = 16 x 32 band of row dy) into the 32 output columns [X0-16+16w,
-// X0+16+16w) (N = 32) that it can reach: every staged input chunk is read
-// once per dy, and each read feeds 32 outputs.  Windows overlap their
-// neighbours' outputs by 16 columns, so even windows are issued first (their
-// output ranges are disjoint and cover the accumulator, the first of them
-// with accumulate = 0) and odd windows then add in.  Star stencils use the
-// same windows with a one-tap (diagonal) band on the off-centre rows.  FP16
-// operands, FP32 accumulators in tensor memory (TMEM).
+// lane) by 128 columns.  Rows are shifted by the smem descriptor; the
+// horizontal taps are a band.  The tile's input columns are cut into 16-column
+// windows (K = 16), window w = [X0-8+16w, X0+8+16w).  For each coefficient row
+// dy, window w is multiplied (A = staged input shifted by dy, B = 16 x 32 band
+// of row dy) into the 32 output columns [X0-16+16w, X0+16+16w) (N = 32) that
+// it can reach: every staged input chunk is read once per dy, and each read
+// feeds 32 outputs.  Windows overlap their neighbours' outputs by 16 columns,
+// so even windows are issued first (their output ranges are disjoint and
+// cover the accumulator, the first of them with accumulate = 0) and odd
+// windows then add in.  Star stencils use the same windows with a one-tap
+// (diagonal) band on the off-centre rows.  FP16 operands, FP32 accumulators
+// in tensor memory (TMEM).  The split form works in two 64-column sub-tiles
+// so that its two accumulators per sub-tile still double-buffer in TMEM.
 //
-// Staging.  The tile's input (its bricks plus one brick row above and below
-// and one 8-column chunk left and right) is fetched by TMA from the brick grid
-// through a 5-D view (8 cells, 16 rows, brick row, half brick, brick column)
-// into a chunk-planar shared-memory image: chunk s holds all 160 staged rows
-// of 8 columns at a 16-byte row stride.  That image is directly a no-swizzle
-// K-major UMMA operand (8-row x 16-byte core matrices, SBO = 128 B between
-// row groups, LBO = 160*16 B between K chunks), and a row shift dy is +16*dy
-// bytes on the descriptor start address.
+// Staging.  Planes are column panels (8 cells x all rows, 16 bytes per row,
+// rows contiguous; see tcs_internal.h), so the 132 input rows a tile needs
+// from one panel (two halo rows above and below) are one contiguous 2112-byte
+// run: the producer fetches the 18 panels of a tile (16 + one each side) with
+// 18 1-D bulk copies.  The shared-memory image, chunk s = all 132 rows of
+// panel s at a 16-byte row stride, is directly a no-swizzle K-major UMMA
+// operand (8-row x 16-byte core matrices, SBO = 128 B between row groups,
+// LBO = 2112 B between K chunks), and a row shift dy is +16*dy bytes on the
+// descriptor start address.
 //
 // Split precision (hi + lo planes).  Data are stored as x' = x 2^-E with
 // hi = rint(x' 2^11) 2^-11 (fixed point) and lo = fp16((x' - hi) 2^11); a
@@ -37,12 +39,12 @@
 // FP32 with round-to-nearest in the epilogue.
 //
 // Pipeline (persistent, one CTA per SM, 6 warps):
-//   warp 0      TMA producer (3 loads per tile and plane) into NS stages
+//   warp 0      producer: bulk copies of each tile's panels into NS stages
 //   warp 1      TMEM allocator and single-thread MMA issuer
 //   warps 2..5  epilogue: TMEM -> registers -> FP16 (or hi/lo) -> global
-// Two accumulator buffers let the epilogue of tile i overlap the MMAs of i+1.
-// Every wait is bounded; on timeout the kernel records an error word, stops,
-// drains its own copies and MMAs, frees TMEM and returns.
+// Two accumulator buffers let the epilogue of one (sub-)tile overlap the MMAs
+// of the next.  Every wait is bounded; on timeout the kernel records an error
+// word, stops, drains its own copies and MMAs, frees TMEM and returns.
 #include "tcs_device.cuh"
 #include "tcs_internal.h"
 
@@ -52,32 +54,31 @@ namespace {
 
 __device__ int g_tc_error = 0;
 
-constexpr int kTileRows = 128;                 // = UMMA M = TMEM lanes
-constexpr int kTBY = kTileRows / 16;           // tile height in bricks
-constexpr int kStagedRows = kTileRows + 32;    // one brick row above and below
-constexpr int kChunkBytes = kStagedRows * 16;  // one 8-column chunk of the stage
-constexpr int kBandBytes = 32 * 16 * 2;        // one 16(K) x 32(N) FP16 band
-constexpr int kThreads = 192;
+constexpr int kRowsStaged = kTile + 4;           // two halo rows above and below
+constexpr int kChunkBytes = kRowsStaged * 16;    // one panel of the stage
+constexpr int kSlots = kTile / 8 + 2;            // 16 panels + one each side
+constexpr int kPlaneStage = kSlots * kChunkBytes;
+constexpr int kBandBytes = 32 * 16 * 2;          // one 16(K) x 32(N) FP16 band
+constexpr int kEpiWarps = 8;                     // two warpgroups, one per column half
+constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kIdesc = idesc_f16_f32(128, 32);
 
 template <int S, bool SPLIT>
 struct Cfg {
     static constexpr int R = stencil_r(S);
     static constexpr bool BOX = stencil_box(S);
-    static constexpr int NDY = 2 * R + 1;                // coefficient rows
-    static constexpr int TBX = tc_tile_bricks_x(SPLIT);  // tile width in bricks
-    static constexpr int TW = TBX * 16;
-    static constexpr int NWIN = TBX + 1;                 // 16-column input windows
-    static constexpr int SLOTS = 2 * TBX + 2;            // 8-column chunks staged
-    static constexpr int PLANE_STAGE = SLOTS * kChunkBytes;
-    static constexpr int PLANES = SPLIT ? 2 : 1;         // hi (and lo) data planes
-    static constexpr int BAND_PLANES = SPLIT ? 4 : 1;    // ch (and cf, cl, c3)
-    static constexpr int STAGES = SPLIT ? 2 : 3;
-    static constexpr int ACC_PLANE = 16 * (TBX + 2);     // TMEM columns per accumulator
+    static constexpr int NDY = 2 * R + 1;                 // coefficient rows
+    static constexpr int NSUB = SPLIT ? 2 : 1;            // sub-tiles per tile
+    static constexpr int SUB_BLOCKS = kTile / 16 / NSUB;  // 16-column output blocks per sub-tile
+    static constexpr int SUB_WIN = SUB_BLOCKS + 1;        // input windows per sub-tile
+    static constexpr int ACC_PLANE = 16 * (SUB_BLOCKS + 2);  // TMEM columns per accumulator
     static constexpr int ACC = ACC_PLANE * (SPLIT ? 2 : 1);
     static constexpr int TMEM_COLS = 512;
     static_assert(2 * ACC <= TMEM_COLS, "two accumulator buffers must fit in TMEM");
-    static constexpr size_t SMEM = 1024 + (size_t)STAGES * PLANES * PLANE_STAGE +
+    static constexpr int PLANES = SPLIT ? 2 : 1;          // hi (and lo) data planes
+    static constexpr int BAND_PLANES = SPLIT ? 4 : 1;     // ch (and cf, cl, c3)
+    static constexpr int STAGES = SPLIT ? 2 : 4;
+    static constexpr size_t SMEM = 1024 + (size_t)STAGES * PLANES * kPlaneStage +
                                    (size_t)BAND_PLANES * NDY * kBandBytes + 256;
     static_assert(SMEM <= 232448, "shared memory budget");
 };
@@ -85,7 +86,7 @@ struct Cfg {
 struct TcParams {
     GridGeom g;
     int tiles_x, n_tiles;
-    const uint16_t *in_hi, *in_lo;  // input planes (border copies)
+    const uint16_t *in_hi, *in_lo;  // input planes
     uint16_t *out_hi, *out_lo;
     float coef[25];                 // n x n, row-major
 };
@@ -107,22 +108,18 @@ __device__ __forceinline__ void split_fixed(float v, uint16_t &hi, uint16_t &lo)
 }
 
 template <int S, bool SPLIT>
-__global__ void __launch_bounds__(kThreads, 1)
-    tc_sweep_kernel(const __grid_constant__ CUtensorMap map_hi_main,
-                    const __grid_constant__ CUtensorMap map_hi_halo,
-                    const __grid_constant__ CUtensorMap map_lo_main,
-                    const __grid_constant__ CUtensorMap map_lo_halo, const TcParams p) {
+__global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p) {
     using C = Cfg<S, SPLIT>;
     constexpr int R = C::R;
     constexpr int NS = C::STAGES;
     constexpr int NP = C::PLANES;
-    constexpr int TBX = C::TBX;
+    constexpr int NSUB = C::NSUB;
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                 ~static_cast<uintptr_t>(1023));
-    uint8_t *stage_base = smem;                                          // [NS][NP][stage]
-    uint8_t *band_base = smem + (size_t)NS * NP * C::PLANE_STAGE;        // [BAND_PLANES][NDY]
+    uint8_t *stage_base = smem;                                    // [NS][NP][stage]
+    uint8_t *band_base = smem + (size_t)NS * NP * kPlaneStage;     // [BAND_PLANES][NDY]
     uint64_t *bars =
         reinterpret_cast<uint64_t *>(band_base + C::BAND_PLANES * C::NDY * kBandBytes);
     uint64_t *full = bars;                    // [NS]
@@ -135,6 +132,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
+    const PlaneGeom pg = p.g.p16;
 
     // ---------------------------------------------------------- set-up ---
     if (threadIdx.x == 0) {
@@ -144,17 +142,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 4);
+            mbar_init(&acc_empty[b], kEpiWarps);
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
         fence_mbar_init();
-        tma_prefetch_map(&map_hi_main);
-        tma_prefetch_map(&map_hi_halo);
-        if (SPLIT) {
-            tma_prefetch_map(&map_lo_main);
-            tma_prefetch_map(&map_lo_halo);
-        }
     }
     if (warp == 1) {
         __syncwarp();
@@ -179,9 +171,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             const float ch = rintf(c * 2048.0f) * (1.0f / 2048.0f);
             const float rem = (c - ch) * 2048.0f;  // exact
             const uint16_t cl = h_bits(rem);
-            band[off] = h_bits(ch);                             // ch: fixed point
-            band[C::NDY * 512 + off] = h_bits(c);               // cf: fp16(c), multiplies lo
-            band[2 * C::NDY * 512 + off] = cl;                  // cl
+            band[off] = h_bits(ch);                                  // ch: fixed point
+            band[C::NDY * 512 + off] = h_bits(c);                    // cf: fp16(c), multiplies lo
+            band[2 * C::NDY * 512 + off] = cl;                       // cl
             band[3 * C::NDY * 512 + off] = h_bits(rem - h_val(cl));  // c3
         }
     }
@@ -207,18 +199,19 @@ __global__ void __launch_bounds__(kThreads, 1)
                     *abort_flag = 1;
                     break;
                 }
-                const int by0 = (t / tiles_x) * kTBY;
-                const int bx0 = (t % tiles_x) * TBX;
-                mbar_arrive_expect_tx(&full[s], NP * C::PLANE_STAGE);
+                const int Y0 = (t / tiles_x) * kTile;
+                const int X0 = (t % tiles_x) * kTile;
+                mbar_arrive_expect_tx(&full[s], NP * kPlaneStage);
+                // rows Y0-2 .. Y0+129 of panels X0/8 - 1 .. X0/8 + 16
+                const size_t src0 = plane_index(pg, Y0 - 2, X0 - 8);
 #pragma unroll
                 for (int pl = 0; pl < NP; pl++) {
-                    const CUtensorMap *mm = pl ? &map_lo_main : &map_hi_main;
-                    const CUtensorMap *mh = pl ? &map_lo_halo : &map_hi_halo;
-                    uint8_t *st = stage_base + ((size_t)s * NP + pl) * C::PLANE_STAGE;
-                    tma_load_5d(st + kChunkBytes, mm, &full[s], 0, 0, by0 - 1, 0, bx0);
-                    tma_load_5d(st, mh, &full[s], 0, 0, by0 - 1, 1, bx0 - 1);
-                    tma_load_5d(st + (C::SLOTS - 1) * kChunkBytes, mh, &full[s], 0, 0, by0 - 1,
-                                0, bx0 + TBX);
+                    const uint16_t *src = (pl ? p.in_lo : p.in_hi) + src0;
+                    uint8_t *st = stage_base + ((size_t)s * NP + pl) * kPlaneStage;
+#pragma unroll 1
+                    for (int c = 0; c < kSlots; c++)
+                        bulk_load(st + c * kChunkBytes, src + (size_t)c * pg.nyp * 8, kChunkBytes,
+                                  &full[s]);
                 }
                 last_issued = i;
             }
@@ -239,54 +232,62 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) {
             int i = 0;
             bool issued_any = false;
+            bool stop = false;
             const uint64_t b_desc0 = smem_desc(smem_u32(band_base), 512, 128);
-            for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, i++) {
+            for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
                 const int s = i % NS;
-                const int b = i & 1;
                 if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
                     record_error(&g_tc_error, kErrWaitFull);
                     *abort_flag = 1;
                     break;
                 }
-                if (!mbar_wait(&acc_empty[b], ((i >> 1) & 1) ^ 1, abort_flag)) {
-                    record_error(&g_tc_error, kErrWaitAccum);
-                    *abort_flag = 1;
-                    break;
-                }
-                tc_fence_after();
-                const uint32_t d_main = tmem_base + b * C::ACC;
-                const uint32_t d_corr = d_main + C::ACC_PLANE;
-                // Descriptors: the start-address field holds (address >> 4) in
-                // its low bits, so a descriptor for base + offset is the base
-                // descriptor plus offset >> 4 (all offsets compile-time here).
+                // Descriptors: the start-address field holds (address >> 4)
+                // in its low bits, so a descriptor for base + offset is the
+                // base descriptor plus offset >> 4 (compile-time offsets).
                 const uint64_t a_hi0 =
-                    smem_desc(smem_u32(stage_base + ((size_t)s * NP) * C::PLANE_STAGE), kChunkBytes, 128);
-                const uint64_t a_lo0 = a_hi0 + (C::PLANE_STAGE >> 4);
-                // even windows (disjoint outputs, initialise), then odd windows
+                    smem_desc(smem_u32(stage_base + ((size_t)s * NP) * kPlaneStage), kChunkBytes, 128);
+                const uint64_t a_lo0 = a_hi0 + (kPlaneStage >> 4);
 #pragma unroll
-                for (int parity = 0; parity < 2; parity++) {
+                for (int h = 0; h < NSUB; h++) {
+                    const int k = i * NSUB + h;  // sub-tile counter
+                    const int b = k & 1;
+                    if (!mbar_wait(&acc_empty[b], ((k >> 1) & 1) ^ 1, abort_flag)) {
+                        record_error(&g_tc_error, kErrWaitAccum);
+                        *abort_flag = 1;
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d_main = tmem_base + b * C::ACC;
+                    const uint32_t d_corr = d_main + C::ACC_PLANE;
+                    // even windows (disjoint outputs, initialise), then odd windows
 #pragma unroll
-                    for (int dy = 0; dy < C::NDY; dy++) {
-                        const uint64_t b_ch = b_desc0 + (uint64_t)((dy * kBandBytes) >> 4);
-                        const uint32_t acc = (parity == 1 || dy > 0) ? 1u : 0u;
+                    for (int parity = 0; parity < 2; parity++) {
 #pragma unroll
-                        for (int w = parity; w < C::NWIN; w += 2) {
-                            const uint64_t a_off = (uint64_t)((2 * w * kChunkBytes + (16 - R + dy) * 16) >> 4);
-                            umma_f16(d_main + 16 * w, a_hi0 + a_off, b_ch, kIdesc, acc);
-                            if (SPLIT) {
-                                const uint64_t b_cf = b_desc0 + (uint64_t)(((C::NDY + dy) * kBandBytes) >> 4);
-                                const uint64_t b_cl = b_desc0 + (uint64_t)(((2 * C::NDY + dy) * kBandBytes) >> 4);
-                                const uint64_t b_c3 = b_desc0 + (uint64_t)(((3 * C::NDY + dy) * kBandBytes) >> 4);
-                                umma_f16(d_corr + 16 * w, a_lo0 + a_off, b_cf, kIdesc, acc);
-                                umma_f16(d_corr + 16 * w, a_hi0 + a_off, b_cl, kIdesc, 1);
-                                umma_f16(d_corr + 16 * w, a_hi0 + a_off, b_c3, kIdesc, 1);
+                        for (int dy = 0; dy < C::NDY; dy++) {
+                            const uint64_t b_ch = b_desc0 + (uint64_t)((dy * kBandBytes) >> 4);
+                            const uint32_t acc = (parity == 1 || dy > 0) ? 1u : 0u;
+#pragma unroll
+                            for (int w = parity; w < C::SUB_WIN; w += 2) {
+                                const int wg = h * C::SUB_BLOCKS + w;  // window in the tile
+                                const uint64_t a_off =
+                                    (uint64_t)((2 * wg * kChunkBytes + (2 - R + dy) * 16) >> 4);
+                                umma_f16(d_main + 16 * w, a_hi0 + a_off, b_ch, kIdesc, acc);
+                                if (SPLIT) {
+                                    const uint64_t b_cf = b_desc0 + (uint64_t)(((C::NDY + dy) * kBandBytes) >> 4);
+                                    const uint64_t b_cl = b_desc0 + (uint64_t)(((2 * C::NDY + dy) * kBandBytes) >> 4);
+                                    const uint64_t b_c3 = b_desc0 + (uint64_t)(((3 * C::NDY + dy) * kBandBytes) >> 4);
+                                    umma_f16(d_corr + 16 * w, a_lo0 + a_off, b_cf, kIdesc, acc);
+                                    umma_f16(d_corr + 16 * w, a_hi0 + a_off, b_cl, kIdesc, 1);
+                                    umma_f16(d_corr + 16 * w, a_hi0 + a_off, b_c3, kIdesc, 1);
+                                }
                             }
                         }
                     }
+                    umma_commit(&acc_full[b]);
+                    issued_any = true;
                 }
                 umma_commit(&empty[s]);
-                umma_commit(&acc_full[b]);
-                issued_any = true;
             }
             if (issued_any) {
                 umma_commit(drain);
@@ -302,117 +303,117 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;       // TMEM lane quarter of this warp
+        const int half = (warp - 2) >> 2;  // which half of a sub-tile's column blocks
         const int m = q * 32 + lane;  // output row within the tile
         const GridGeom &g = p.g;
         int i = 0;
-        for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, i++) {
-            const int b = i & 1;
-            bool ok = mbar_wait(&acc_full[b], (i >> 1) & 1, abort_flag);
-            ok = __all_sync(0xffffffffu, ok);
-            if (!ok) {
-                if (lane == 0) {
-                    record_error(&g_tc_error, kErrWaitResult);
-                    *abort_flag = 1;
-                }
-                break;
-            }
-            tc_fence_after();
-            const int by0 = (t / tiles_x) * kTBY;
-            const int bx0 = (t % tiles_x) * TBX;
-            const int Y0 = by0 * 16, X0 = bx0 * 16;
-            const bool fast = Y0 >= g.y0 && Y0 + kTileRows <= g.y1 && X0 >= g.x0 &&
-                              X0 + C::TW <= g.x1;
+        bool stop = false;
+        for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
+            const int Y0 = (t / tiles_x) * kTile;
+            const int X0 = (t % tiles_x) * kTile;
+            const bool fast = Y0 >= g.y0 && Y0 + kTile <= g.y1 && X0 >= g.x0 && X0 + kTile <= g.x1;
             const int y = Y0 + m;
-            const int by = by0 + (m >> 4);
             const bool row_in = y >= g.y0 && y < g.y1;
-            // output block j (columns X0+16j ..) is accumulator column 16(j+1)
-            const uint32_t lane_addr =
-                tmem_base + ((uint32_t)(q * 32) << 16) + b * C::ACC + 16;
-            // G blocks per TMEM round trip: all their loads are issued before
-            // one wait, so the load latency is paid once per group.
-            constexpr int G = SPLIT ? 2 : 4;
-            static_assert(TBX % G == 0, "group size");
 #pragma unroll 1
-            for (int j0 = 0; j0 < TBX; j0 += G) {
-                uint32_t v[G][16];
-                uint32_t w[SPLIT ? G : 1][16];
-#pragma unroll
-                for (int gg = 0; gg < G; gg++) {
-                    tmem_ld_x16(lane_addr + 16 * (j0 + gg), v[gg]);
-                    if (SPLIT) tmem_ld_x16(lane_addr + C::ACC_PLANE + 16 * (j0 + gg), w[SPLIT ? gg : 0]);
-                }
-                tmem_ld_wait();
-#pragma unroll
-                for (int gg = 0; gg < G; gg++) {
-                    const int j = j0 + gg;
-                    const int bx = bx0 + j;
-                    if (by >= g.nby || bx >= g.nbx) continue;
-                    const size_t off = ((size_t)by * g.nbx + bx) * 256 + (size_t)(m & 15) * 16;
-                    float f[16];
-#pragma unroll
-                    for (int c = 0; c < 16; c++) {
-                        f[c] = __uint_as_float(v[gg][c]);
-                        if (SPLIT) f[c] = fmaf(__uint_as_float(w[SPLIT ? gg : 0][c]), 1.0f / 2048.0f, f[c]);
+            for (int h = 0; h < NSUB; h++) {
+                const int k = i * NSUB + h;
+                const int b = k & 1;
+                bool ok = mbar_wait(&acc_full[b], (k >> 1) & 1, abort_flag);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) {
+                    if (lane == 0) {
+                        record_error(&g_tc_error, kErrWaitResult);
+                        *abort_flag = 1;
                     }
-                    uint32_t hw[8], lw[8];
-                    if (fast) {
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                // output block jl of the sub-tile is accumulator column 16(jl+1)
+                const uint32_t lane_addr =
+                    tmem_base + ((uint32_t)(q * 32) << 16) + b * C::ACC + 16;
+                // G blocks per TMEM round trip: all their loads are issued
+                // before one wait, so the load latency is paid once per group.
+                constexpr int G = C::SUB_BLOCKS / 2;  // this warp's blocks, one round trip
+                {
+                    const int j0 = half * G;
+                    uint32_t v[G][16];
+                    uint32_t w[SPLIT ? G : 1][16];
 #pragma unroll
-                        for (int c = 0; c < 8; c++) {
-                            uint16_t h0, h1, l0 = 0, l1 = 0;
-                            if (SPLIT) {
-                                split_fixed(f[2 * c], h0, l0);
-                                split_fixed(f[2 * c + 1], h1, l1);
-                            } else {
-                                h0 = h_bits(f[2 * c]);
-                                h1 = h_bits(f[2 * c + 1]);
-                            }
-                            hw[c] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-                            lw[c] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+                    for (int gg = 0; gg < G; gg++) {
+                        tmem_ld_x16(lane_addr + 16 * (j0 + gg), v[gg]);
+                        if (SPLIT) tmem_ld_x16(lane_addr + C::ACC_PLANE + 16 * (j0 + gg), w[SPLIT ? gg : 0]);
+                    }
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int gg = 0; gg < G; gg++) {
+                        const int xb = X0 + 16 * (h * C::SUB_BLOCKS + j0 + gg);
+                        const size_t off0 = plane_index(pg, y, xb);      // cells xb .. xb+7
+                        const size_t off1 = off0 + (size_t)pg.nyp * 8;   // cells xb+8 .. xb+15
+                        float f[16];
+#pragma unroll
+                        for (int c = 0; c < 16; c++) {
+                            f[c] = __uint_as_float(v[gg][c]);
+                            if (SPLIT) f[c] = fmaf(__uint_as_float(w[SPLIT ? gg : 0][c]), 1.0f / 2048.0f, f[c]);
                         }
-                    } else {
-                        // Border tile: cells outside the update rectangle copy the input.
-                        const uint4 *ih = reinterpret_cast<const uint4 *>(p.in_hi + off);
-                        const uint4 i0 = ih[0], i1 = ih[1];
-                        const uint32_t iw[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
-                        uint32_t il[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                        if (SPLIT) {
-                            const uint4 *iq = reinterpret_cast<const uint4 *>(p.in_lo + off);
-                            const uint4 l0 = iq[0], l1 = iq[1];
-                            il[0] = l0.x; il[1] = l0.y; il[2] = l0.z; il[3] = l0.w;
-                            il[4] = l1.x; il[5] = l1.y; il[6] = l1.z; il[7] = l1.w;
-                        }
+                        uint32_t hw[8], lw[8];
+                        if (fast) {
 #pragma unroll
-                        for (int c = 0; c < 8; c++) {
-                            uint16_t hh[2], ll[2];
-#pragma unroll
-                            for (int u = 0; u < 2; u++) {
-                                const int x = X0 + 16 * j + 2 * c + u;
-                                const bool upd = row_in && x >= g.x0 && x < g.x1;
-                                if (upd) {
-                                    if (SPLIT) split_fixed(f[2 * c + u], hh[u], ll[u]);
-                                    else { hh[u] = h_bits(f[2 * c + u]); ll[u] = 0; }
+                            for (int c = 0; c < 8; c++) {
+                                uint16_t h0, h1, l0 = 0, l1 = 0;
+                                if (SPLIT) {
+                                    split_fixed(f[2 * c], h0, l0);
+                                    split_fixed(f[2 * c + 1], h1, l1);
                                 } else {
-                                    hh[u] = (uint16_t)(iw[c] >> (16 * u));
-                                    ll[u] = (uint16_t)(il[c] >> (16 * u));
+                                    h0 = h_bits(f[2 * c]);
+                                    h1 = h_bits(f[2 * c + 1]);
                                 }
+                                hw[c] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+                                lw[c] = (uint32_t)l0 | ((uint32_t)l1 << 16);
                             }
-                            hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
-                            lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
+                        } else {
+                            // Border tile: cells outside the update rectangle copy the input.
+                            const uint4 i0 = *reinterpret_cast<const uint4 *>(p.in_hi + off0);
+                            const uint4 i1 = *reinterpret_cast<const uint4 *>(p.in_hi + off1);
+                            const uint32_t iw[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
+                            uint32_t il[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                            if (SPLIT) {
+                                const uint4 l0 = *reinterpret_cast<const uint4 *>(p.in_lo + off0);
+                                const uint4 l1 = *reinterpret_cast<const uint4 *>(p.in_lo + off1);
+                                il[0] = l0.x; il[1] = l0.y; il[2] = l0.z; il[3] = l0.w;
+                                il[4] = l1.x; il[5] = l1.y; il[6] = l1.z; il[7] = l1.w;
+                            }
+#pragma unroll
+                            for (int c = 0; c < 8; c++) {
+                                uint16_t hh[2], ll[2];
+#pragma unroll
+                                for (int u = 0; u < 2; u++) {
+                                    const int x = xb + 2 * c + u;
+                                    const bool upd = row_in && x >= g.x0 && x < g.x1;
+                                    if (upd) {
+                                        if (SPLIT) split_fixed(f[2 * c + u], hh[u], ll[u]);
+                                        else { hh[u] = h_bits(f[2 * c + u]); ll[u] = 0; }
+                                    } else {
+                                        hh[u] = (uint16_t)(iw[c] >> (16 * u));
+                                        ll[u] = (uint16_t)(il[c] >> (16 * u));
+                                    }
+                                }
+                                hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
+                                lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
+                            }
+                        }
+                        *reinterpret_cast<uint4 *>(p.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                        *reinterpret_cast<uint4 *>(p.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+                        if (SPLIT) {
+                            *reinterpret_cast<uint4 *>(p.out_lo + off0) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                            *reinterpret_cast<uint4 *>(p.out_lo + off1) = make_uint4(lw[4], lw[5], lw[6], lw[7]);
                         }
                     }
-                    uint4 *oh = reinterpret_cast<uint4 *>(p.out_hi + off);
-                    oh[0] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                    oh[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
-                    if (SPLIT) {
-                        uint4 *ol = reinterpret_cast<uint4 *>(p.out_lo + off);
-                        ol[0] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-                        ol[1] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
-                    }
                 }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[b]);
             }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&acc_empty[b]);
         }
     }
 
@@ -450,16 +451,15 @@ cudaError_t prepare_tc() {
 }
 
 template <int S, bool SPLIT>
-cudaError_t launch_tc(const GridGeom &g, const float *B, const PlaneMaps &hi, const PlaneMaps *lo,
-                      const uint16_t *in_hi, const uint16_t *in_lo, uint16_t *out_hi,
-                      uint16_t *out_lo, cudaStream_t s) {
+cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
+                      const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s) {
     using C = Cfg<S, SPLIT>;
     cudaError_t pe = prepare_tc<S, SPLIT>();
     if (pe != cudaSuccess) return pe;
     TcParams p;
     p.g = g;
-    const int tiles_y = (g.nby + kTBY - 1) / kTBY;
-    p.tiles_x = (g.nbx + C::TBX - 1) / C::TBX;
+    const int tiles_y = (g.ny + kTile - 1) / kTile;
+    p.tiles_x = (g.nx + kTile - 1) / kTile;
     p.n_tiles = tiles_y * p.tiles_x;
     p.in_hi = in_hi;
     p.in_lo = in_lo;
@@ -468,20 +468,18 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const PlaneMaps &hi, co
     for (int k = 0; k < 25; k++) p.coef[k] = 0.0f;
     for (int k = 0; k < C::NDY * C::NDY; k++) p.coef[k] = B[k];
     const int grid = p.n_tiles < g_num_sms ? p.n_tiles : g_num_sms;
-    const PlaneMaps &l = lo ? *lo : hi;
-    tc_sweep_kernel<S, SPLIT><<<grid, kThreads, C::SMEM, s>>>(hi.main, hi.halo, l.main, l.halo, p);
+    tc_sweep_kernel<S, SPLIT><<<grid, kThreads, C::SMEM, s>>>(p);
     return cudaGetLastError();
 }
 
 template <bool SPLIT>
-cudaError_t dispatch_tc(const GridGeom &g, int stencil, const float *B, const PlaneMaps &hi,
-                        const PlaneMaps *lo, const uint16_t *in_hi, const uint16_t *in_lo,
-                        uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s) {
+cudaError_t dispatch_tc(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
+                        const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s) {
     switch (stencil) {
-    case TCS_STAR2D1R: return launch_tc<TCS_STAR2D1R, SPLIT>(g, B, hi, lo, in_hi, in_lo, out_hi, out_lo, s);
-    case TCS_STAR2D2R: return launch_tc<TCS_STAR2D2R, SPLIT>(g, B, hi, lo, in_hi, in_lo, out_hi, out_lo, s);
-    case TCS_BOX2D1R: return launch_tc<TCS_BOX2D1R, SPLIT>(g, B, hi, lo, in_hi, in_lo, out_hi, out_lo, s);
-    case TCS_BOX2D2R: return launch_tc<TCS_BOX2D2R, SPLIT>(g, B, hi, lo, in_hi, in_lo, out_hi, out_lo, s);
+    case TCS_STAR2D1R: return launch_tc<TCS_STAR2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s);
+    case TCS_STAR2D2R: return launch_tc<TCS_STAR2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s);
+    case TCS_BOX2D1R: return launch_tc<TCS_BOX2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s);
+    case TCS_BOX2D2R: return launch_tc<TCS_BOX2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -505,17 +503,15 @@ cudaError_t tc_take_error(int *code) {
     return *code ? cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(int)) : cudaSuccess;
 }
 
-cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const PlaneMaps &in_maps,
-                          const uint16_t *in, uint16_t *out, cudaStream_t s) {
-    return dispatch_tc<false>(g, stencil, B, in_maps, nullptr, in, nullptr, out, nullptr, s);
+cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
+                          uint16_t *out, cudaStream_t s) {
+    return dispatch_tc<false>(g, stencil, B, in, nullptr, out, nullptr, s);
 }
 
-cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B,
-                            const PlaneMaps &in_hi_maps, const PlaneMaps &in_lo_maps,
-                            const uint16_t *in_hi, const uint16_t *in_lo, uint16_t *out_hi,
-                            uint16_t *out_lo, cudaStream_t s) {
-    return dispatch_tc<true>(g, stencil, B, in_hi_maps, &in_lo_maps, in_hi, in_lo, out_hi, out_lo,
-                             s);
+cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
+                            const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
+                            cudaStream_t s) {
+    return dispatch_tc<true>(g, stencil, B, in_hi, in_lo, out_hi, out_lo, s);
 }
 
 }  // namespace tcs

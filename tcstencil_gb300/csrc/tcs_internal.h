@@ -3,6 +3,7 @@
 
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "../../include/tcs.h"
@@ -40,11 +41,50 @@ struct TapCoeffs {
     float c[25];
 };
 
-// Geometry of one brick grid and its update rectangle.
+// ----------------------------------------------------------------- planes --
+// The engine's plane format: column panels of 16 bytes per row (8 FP16 or 4
+// FP32 cells), panel after panel, rows contiguous inside a panel -- i.e.
+// 16-row half-bricks (16 x 8 FP16 cells) in column-major brick order.  Rows
+// are padded to a multiple of the 128-row tile plus kPadTop rows above and
+// (kPadRows - kPadTop) below, columns to a multiple of the 128-column tile
+// plus one panel on each side, so every tile's staged neighbourhood lies
+// inside the allocation.  Cell (y, x) is at
+//   ((x / cpp + 1) * nyp + (y + kPadTop)) * cpp + x % cpp.
+constexpr int kTile = 128;
+constexpr int kPadTop = 4;
+constexpr int kPadRows = 8;
+
+__host__ __device__ constexpr int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+struct PlaneGeom {
+    int nyp;   // rows per panel, padding included
+    int npan;  // panels, padding included
+    int cpp;   // cells per panel row: 8 (FP16) or 4 (FP32)
+};
+
+__host__ __device__ inline PlaneGeom plane_geom(int ny, int nx, int cpp) {
+    PlaneGeom p;
+    p.nyp = round_up(ny, kTile) + kPadRows;
+    p.npan = round_up(nx, kTile) / cpp + 2;
+    p.cpp = cpp;
+    return p;
+}
+__host__ __device__ inline size_t plane_elems(const PlaneGeom &p) {
+    return (size_t)p.nyp * p.npan * p.cpp;
+}
+// Index of cell (y, x) for y >= -kPadTop and x >= -cpp (x a multiple of cpp
+// or any column of a panel).
+__host__ __device__ inline size_t plane_index(const PlaneGeom &p, int y, int x) {
+    const int xs = x + p.cpp;
+    return ((size_t)(xs / p.cpp) * p.nyp + (size_t)(y + kPadTop)) * p.cpp + (size_t)(xs % p.cpp);
+}
+
+// Geometry of one grid and its update rectangle.
 struct GridGeom {
-    int ny, nx;   // cells
-    int nby, nbx; // bricks
+    int ny, nx;  // cells
     int y0, y1, x0, x1;
+    PlaneGeom p16;  // FP16 (and split) planes
+    PlaneGeom p32;  // FP32 planes
 };
 
 // Sets the thread's last-error message and returns `status`.
@@ -57,24 +97,6 @@ int make_geom(int ny, int nx, int stencil, int y0, int y1, int x0, int x1, GridG
 // Gold's coefficients for a stencil from an n x n row-major matrix.
 TapCoeffs tap_coeffs(int stencil, const float *B);
 
-// --- kernels (launch wrappers; return cudaError_t of the launch) ---------
-cudaError_t launch_cc_f16(const GridGeom &g, int stencil, const TapCoeffs &c, const uint16_t *in,
-                          uint16_t *out, cudaStream_t s);
-cudaError_t launch_cc_f32(const GridGeom &g, int stencil, const TapCoeffs &c, const float *in,
-                          float *out, cudaStream_t s);
-
-// Tensor-core tile: 8 bricks (128 rows) high; 8 bricks wide in the FP16 form
-// and 6 in the split form (whose two accumulators per tile take more TMEM).
-constexpr int kTcTileBricksY = 8;
-__host__ __device__ constexpr int tc_tile_bricks_x(bool split) { return split ? 6 : 8; }
-
-// Tensor maps of one FP16 brick plane for the tensor-core kernel.
-struct PlaneMaps {
-    CUtensorMap main; // box: 8 x 16 x (tile bricks y + 2) x 2 x (tile bricks x)
-    CUtensorMap halo; // box: 8 x 16 x (tile bricks y + 2) x 1 x 1
-};
-int encode_plane_maps(const void *plane, int nby, int nbx, int tile_bricks_x, PlaneMaps *maps);
-
 // Scale exponent of a split-precision grid: values are stored as x 2^-E,
 // with E the smallest integer such that max|x| 2^-E <= 1 (0 for max|x| = 0).
 int split_scale_exp(float max_abs);
@@ -82,26 +104,34 @@ int split_scale_exp(float max_abs);
 double tap_abs_sum(int stencil, const float *B);
 constexpr double kSplitMaxAbsSum = 1.0 + 1.0 / 256.0;
 
+// --- kernels (launch wrappers; return cudaError_t of the launch) ---------
+cudaError_t launch_cc_f16(const GridGeom &g, int stencil, const TapCoeffs &c, const uint16_t *in,
+                          uint16_t *out, cudaStream_t s);
+cudaError_t launch_cc_f32(const GridGeom &g, int stencil, const TapCoeffs &c, const float *in,
+                          float *out, cudaStream_t s);
+
 // Reads and clears the tensor kernels' device error word.
 cudaError_t tc_take_error(int *code);
 // Configures the tensor kernel of (stencil, split) ahead of its first launch.
 cudaError_t tc_prepare(int stencil, bool split);
 
-cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const PlaneMaps &in_maps,
-                          const uint16_t *in, uint16_t *out, cudaStream_t s);
-cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B,
-                            const PlaneMaps &in_hi_maps, const PlaneMaps &in_lo_maps,
-                            const uint16_t *in_hi, const uint16_t *in_lo, uint16_t *out_hi,
-                            uint16_t *out_lo, cudaStream_t s);
+cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
+                          uint16_t *out, cudaStream_t s);
+cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
+                            const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
+                            cudaStream_t s);
 
 // --- layout kernels -------------------------------------------------------
+// pack/unpack between an FP32 row-major grid and an engine plane of the
+// (ny + 2 pad) x (nx + 2 pad) padded grid; every plane cell is written by
+// pack (cells outside the padded grid are 0).
 cudaError_t launch_pack_f16(const float *in, int ny, int nx, int pad, float pad_value,
-                            uint16_t *bricks, cudaStream_t s);
-cudaError_t launch_unpack_f16(const uint16_t *bricks, int ny, int nx, int pad, float *out,
+                            uint16_t *plane, cudaStream_t s);
+cudaError_t launch_unpack_f16(const uint16_t *plane, int ny, int nx, int pad, float *out,
                               cudaStream_t s);
 cudaError_t launch_pack_f32(const float *in, int ny, int nx, int pad, float pad_value,
-                            float *bricks, cudaStream_t s);
-cudaError_t launch_unpack_f32(const float *bricks, int ny, int nx, int pad, float *out,
+                            float *plane, cudaStream_t s);
+cudaError_t launch_unpack_f32(const float *plane, int ny, int nx, int pad, float *out,
                               cudaStream_t s);
 cudaError_t launch_pack_split(const float *in, int ny, int nx, int pad, float pad_value,
                               int scale_exp, uint16_t *hi, uint16_t *lo, cudaStream_t s);
@@ -109,6 +139,7 @@ cudaError_t launch_unpack_split(const uint16_t *hi, const uint16_t *lo, int ny, 
                                 int scale_exp, float *out, cudaStream_t s);
 // max |x| over n floats into *out_bits (float bits; *out_bits must start at 0)
 cudaError_t launch_max_abs(const float *in, size_t n, unsigned *out_bits, cudaStream_t s);
+// the reference's layout16 transforms (bricks of 16 x 16, row-major inside)
 cudaError_t launch_padding_2d(const uint16_t *in, uint16_t *out, int size, int halo,
                               uint16_t value, cudaStream_t s);
 cudaError_t launch_brick_2d(const uint16_t *in, uint16_t *out, int ny, int nx, cudaStream_t s);

@@ -30,29 +30,33 @@ def f16_ulp(x: np.ndarray) -> np.ndarray:
     return 2.0 ** (np.floor(np.log2(a)) - 10)
 
 
+def plane_shape(ny: int, nx: int, cpp: int = 8):
+    """(rows per panel, panels) of the engine's panel plane (include/tcs.h)."""
+    return -(-ny // 128) * 128 + 8, -(-nx // 128) * 128 // cpp + 2
+
+
+def plane_index(ny: int, nx: int, cpp: int = 8) -> np.ndarray:
+    """Element index of every cell (y, x) in the panel plane."""
+    nyp, _ = plane_shape(ny, nx, cpp)
+    y = np.arange(ny)[:, None]
+    x = np.arange(nx)[None, :]
+    return ((x // cpp + 1) * nyp + (y + 4)) * cpp + x % cpp
+
+
+def to_plane(g: np.ndarray, cpp: int = 8) -> np.ndarray:
+    """Host panel plane of a row-major grid (padding cells 0)."""
+    ny, nx = g.shape
+    nyp, npan = plane_shape(ny, nx, cpp)
+    flat = np.zeros(nyp * npan * cpp, g.dtype)
+    flat[plane_index(ny, nx, cpp)] = g
+    return flat
+
+
 def plane16(torch, g16: np.ndarray):
-    """Device FP16 brick plane (uint16 tensor) of a row-major FP16-bits grid."""
-    return torch.from_numpy(oracle.brick_2d(g16).view(np.int16)).cuda()
+    """Device FP16 panel plane (int16 tensor) of a row-major FP16-bits grid."""
+    return torch.from_numpy(to_plane(g16).view(np.int16)).cuda()
 
 
 def grid16(plane, ny: int, nx: int) -> np.ndarray:
-    """Row-major FP16 bits of a device brick plane."""
-    return oracle.unbrick_2d(plane.cpu().numpy().view(np.uint16), ny, nx)
-
-
-def brick_index(ny: int, nx: int) -> np.ndarray:
-    nbx = (nx + 15) // 16
-    y = np.arange(ny)[:, None]
-    x = np.arange(nx)[None, :]
-    return ((y // 16) * nbx + (x // 16)) * 256 + (y % 16) * 16 + (x % 16)
-
-
-def plane32(torch, g: np.ndarray):
-    ny, nx = g.shape
-    flat = np.zeros(((ny + 15) // 16) * ((nx + 15) // 16) * 256, np.float32)
-    flat[brick_index(ny, nx)] = g
-    return torch.from_numpy(flat).cuda()
-
-
-def grid32(plane, ny: int, nx: int) -> np.ndarray:
-    return plane.cpu().numpy()[brick_index(ny, nx)]
+    """Row-major FP16 bits of a device panel plane."""
+    return plane.cpu().numpy().view(np.uint16)[plane_index(ny, nx)]

@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 import oracle
+from helpers import to_plane
 
 pytestmark = pytest.mark.gpu
 
@@ -41,19 +42,22 @@ def test_brick_and_reverse_layout(tcs, torch_cuda, ny, nx):
 
 
 @pytest.mark.parametrize("ny,nx,pad", [(32, 32, 16), (45, 70, 2), (64, 17, 0)])
-def test_pack_unpack_f16_is_float2half_pad_brick(tcs, torch_cuda, ny, nx, pad):
-    """tcs_pack_f16 = array_float2half + padding_2D + brick_layout_2D."""
+def test_pack_unpack_f16_is_float2half_pad_layout(tcs, torch_cuda, ny, nx, pad):
+    """tcs_pack_f16 = array_float2half + padding_2D + the panel layout, with
+    every padding cell of the plane written (0)."""
     torch = torch_cuda
     rng = np.random.default_rng(pad + ny)
     A = (rng.standard_normal((ny, nx)) * 10).astype(np.float32)
     d_A = _dev(torch, A)
     nyo, nxo = ny + 2 * pad, nx + 2 * pad
-    d_b = torch.empty(tcs.brick_elems(nyo, nxo), dtype=torch.int16, device="cuda")
+    n = tcs.plane_elems(nyo, nxo)
+    assert n == len(to_plane(np.zeros((nyo, nxo), np.uint16)))
+    d_b = torch.full((n,), 12345, dtype=torch.int16, device="cuda")
     L = tcs.lib()
     assert L.tcs_pack_f16(d_A.data_ptr(), ny, nx, pad, 1.0, d_b.data_ptr(), None) == 0
     padded = np.ones((nyo, nxo), np.float32)
     padded[pad:pad + ny, pad:pad + nx] = A
-    expect = oracle.brick_2d(oracle.f32_to_f16(padded))
+    expect = to_plane(oracle.f32_to_f16(padded))
     np.testing.assert_array_equal(d_b.cpu().numpy().view(np.uint16), expect)
     d_out = torch.empty((ny, nx), dtype=torch.float32, device="cuda")
     assert L.tcs_unpack_f16(d_b.data_ptr(), ny, nx, pad, d_out.data_ptr(), None) == 0
@@ -67,12 +71,16 @@ def test_pack_unpack_f32_and_split(tcs, torch_cuda):
     A = rng.uniform(-1, 1, (ny, nx)).astype(np.float32)
     d_A = _dev(torch, A)
     L = tcs.lib()
-    n = tcs.brick_elems(ny + 2, nx + 2)
+    n = tcs.plane_elems(ny + 2, nx + 2, "f32")
     d_f = torch.empty(n, dtype=torch.float32, device="cuda")
     assert L.tcs_pack_f32(d_A.data_ptr(), ny, nx, pad, 0.0, d_f.data_ptr(), None) == 0
     d_o = torch.empty((ny, nx), dtype=torch.float32, device="cuda")
     assert L.tcs_unpack_f32(d_f.data_ptr(), ny, nx, pad, d_o.data_ptr(), None) == 0
     np.testing.assert_array_equal(d_o.cpu().numpy(), A)
+    padded32 = np.zeros((ny + 2, nx + 2), np.float32)
+    padded32[1:-1, 1:-1] = A
+    np.testing.assert_array_equal(d_f.cpu().numpy(), to_plane(padded32, cpp=4))
+    n = tcs.plane_elems(ny + 2, nx + 2, "split")
     d_h = torch.empty(n, dtype=torch.int16, device="cuda")
     d_l = torch.empty(n, dtype=torch.int16, device="cuda")
     import ctypes
@@ -85,8 +93,8 @@ def test_pack_unpack_f32_and_split(tcs, torch_cuda):
     padded = np.zeros((ny + 2, nx + 2), np.float64)
     padded[1:-1, 1:-1] = A
     hi, lo = oracle.split(padded, e)
-    np.testing.assert_array_equal(d_h.cpu().numpy().view(np.uint16), oracle.brick_2d(hi))
-    np.testing.assert_array_equal(d_l.cpu().numpy().view(np.uint16), oracle.brick_2d(lo))
+    np.testing.assert_array_equal(d_h.cpu().numpy().view(np.uint16), to_plane(hi))
+    np.testing.assert_array_equal(d_l.cpu().numpy().view(np.uint16), to_plane(lo))
     assert L.tcs_unpack_split(d_h.data_ptr(), d_l.data_ptr(), ny, nx, pad, e, d_o.data_ptr(), None) == 0
     back = d_o.cpu().numpy().astype(np.float64)
     assert np.max(np.abs(back - A)) <= 2.0 ** (e - 23)
