@@ -218,6 +218,35 @@ int tcs_sweep_host(const float *h_in, float *h_out, const tcs_problem *problem, 
 /* Frees the calling thread's cached plans. */
 void tcs_release_cache(void);
 
+/* ---------------------------------------------------------------- batches
+ * A batch advances many independent grids (any mix of sizes, stencils,
+ * coefficients, FP16 or split precision, and step counts) with ONE persistent
+ * tensor-core launch per run: every (grid, step, tile) is a work item, and a
+ * tile of step t starts once its grid's step t-1 is stored.  Each grid gets
+ * the same bits as a tcs_plan of the same problem run alone.  No reference
+ * counterpart: the reference runs one grid per process (main_1r.cu /
+ * main_2r.cu); batches serve many small problems at once.
+ *
+ * Use: tcs_batch_add every grid, then upload each, then tcs_batch_run (any
+ * number of times; each run advances every grid by its own step count), then
+ * download.  Grids are added only before the first upload or run. */
+typedef struct tcs_batch_s *tcs_batch;
+
+int tcs_batch_create(tcs_batch *out);
+int tcs_batch_destroy(tcs_batch batch);
+/* Adds a grid (engine must be TCS_ENGINE_TENSOR, precision F16 or SPLIT) that
+ * advances `steps` steps per run; *index receives its position. */
+int tcs_batch_add(tcs_batch batch, const tcs_problem *problem, int steps, int *index);
+/* Loads grid `index` from an ny x nx FP32 row-major array (host or device). */
+int tcs_batch_upload(tcs_batch batch, int index, const float *grid, int grid_on_host, void *stream);
+/* Writes grid `index`'s current state as an ny x nx FP32 row-major array. */
+int tcs_batch_download(tcs_batch batch, int index, float *grid, int grid_on_host, void *stream);
+/* One run: every grid advances by its step count.  use_graph != 0 replays a
+ * captured CUDA graph of the run. */
+int tcs_batch_run(tcs_batch batch, int use_graph, void *stream);
+/* Point updates per run, work items per run and the number of grids. */
+int tcs_batch_info(tcs_batch batch, long long *point_updates, int *items, int *grids);
+
 #ifdef __cplusplus
 }
 #endif

@@ -98,6 +98,14 @@ SIGNATURES = {
     "tcs_noalloc_scratch_bytes": (_SZ, []),
     "tcs_sweep_steps_noalloc": (_I, [ctypes.POINTER(StepArgs), _P, _P, _I, _P]),
     "tcs_release_cache": (None, []),
+    "tcs_batch_create": (_I, [ctypes.POINTER(_P)]),
+    "tcs_batch_destroy": (_I, [_P]),
+    "tcs_batch_add": (_I, [_P, ctypes.POINTER(Problem), _I, ctypes.POINTER(_I)]),
+    "tcs_batch_upload": (_I, [_P, _I, _P, _I, _P]),
+    "tcs_batch_download": (_I, [_P, _I, _P, _I, _P]),
+    "tcs_batch_run": (_I, [_P, _I, _P]),
+    "tcs_batch_info": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I),
+                            ctypes.POINTER(_I)]),
 }
 
 
@@ -286,6 +294,62 @@ class Plan:
     def set_coeffs(self, coeffs) -> None:
         self._c = _coeffs(coeffs, self.stencil)
         _check(lib().tcs_plan_set_coeffs(self._h, _ptr(self._c)))
+
+
+def _on_host(a) -> bool:
+    return isinstance(a, np.ndarray) or (hasattr(a, "is_cuda") and not a.is_cuda)
+
+
+class Batch:
+    """Many grids advanced by one persistent tensor-core launch per run
+    (tcs_batch_*).  Add every grid, upload each, then run and download."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        _check(lib().tcs_batch_create(ctypes.byref(h)))
+        self._h = h
+        self._coeffs = []
+        self.shapes = []
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().tcs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, ny: int, nx: int, stencil: str, coeffs, steps: int, precision: str = "f16",
+            rect=None) -> int:
+        c = _coeffs(coeffs, stencil)
+        y0, y1, x0, x1 = _rect(rect)
+        pr = Problem(ny, nx, STENCILS[stencil], ENGINES["tensor"], PRECISIONS[precision], y0, y1,
+                     x0, x1, c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        idx = ctypes.c_int(-1)
+        _check(lib().tcs_batch_add(self._h, ctypes.byref(pr), int(steps), ctypes.byref(idx)))
+        self._coeffs.append(c)
+        self.shapes.append((ny, nx))
+        return idx.value
+
+    def upload(self, index: int, grid, stream=None) -> None:
+        _check(lib().tcs_batch_upload(self._h, index, _ptr(grid), int(_on_host(grid)),
+                                      _stream(stream)))
+
+    def download(self, index: int, out, stream=None) -> None:
+        _check(lib().tcs_batch_download(self._h, index, _ptr(out), int(_on_host(out)),
+                                        _stream(stream)))
+
+    def run(self, use_graph: bool = True, stream=None) -> None:
+        _check(lib().tcs_batch_run(self._h, int(use_graph), _stream(stream)))
+
+    def info(self):
+        """(point updates per run, work items per run, grids)."""
+        pu, it, g = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().tcs_batch_info(self._h, ctypes.byref(pu), ctypes.byref(it), ctypes.byref(g)))
+        return pu.value, it.value, g.value
 
 
 def sweep_host(h_in: np.ndarray, steps: int, stencil: str, coeffs, engine: str = "tensor",

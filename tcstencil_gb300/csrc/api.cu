@@ -174,6 +174,10 @@ int tcs_device_error(int *code) {
     int c = 0;
     st = cuda_status(tc_take_error(&c), "reading the device error word");
     if (st) return st;
+    int cb = 0;
+    st = cuda_status(batch_take_error(&cb), "reading the batch error word");
+    if (st) return st;
+    if (!c) c = cb;
     if (code) *code = c;
     return c ? fail(TCS_ERR_TIMEOUT, "device wait timed out (code %d)", c) : TCS_OK;
 }

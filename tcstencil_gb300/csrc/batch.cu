@@ -1,0 +1,616 @@
+// Batched sweeps: many grids of different sizes, stencils, coefficients,
+// precisions (FP16 or split) and step counts advanced by ONE persistent
+// tensor-core launch.
+//
+// Work list.  Every (grid, step, tile) is one item; items are ordered step
+// major (all grids' first steps, then all second steps, ...), and CTA c takes
+// items c, c + G, c + 2G, ... (G = grid size <= SM count, one CTA per SM, all
+// co-resident).  An item of step t > 0 needs every tile of its grid's step
+// t - 1: the producer waits (bounded) on a per-(grid, step) completion counter
+// that the epilogue warps increment after their stores.  Those items come
+// earlier in the list, so a chain of waits always ends at an item whose inputs
+// are ready: the launch cannot deadlock.  The same counters also guard the
+// ping-pong's write-after-read hazard: step t+1 overwrites the plane step t-1
+// read, and starts only after all of step t, hence all of step t-1, finished.
+//
+// Per item the producer bulk-copies the tile's input panels AND the grid's
+// coefficient bands (prebuilt in global memory by build_bands_kernel) into the
+// stage, so the MMA issuer needs nothing else; stencil radius and precision
+// select one of four fully unrolled MMA sequences (tc_core.cuh), the same code
+// the single-grid kernel runs, so every grid gets the same bits alone and in
+// a batch.  The run ends with a tiny kernel that flips each grid's ping-pong
+// state, so a captured graph can be replayed to advance the batch again.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "tc_core.cuh"
+
+namespace tcs {
+
+namespace {
+
+using namespace tc;
+
+__device__ int g_batch_error = 0;
+
+constexpr int kStages = 2;
+constexpr int kMaxBandBytes = 4 * 5 * kBandBytes;  // split, radius 2
+constexpr int kStageBytes = 2 * kPlaneStage + kMaxBandBytes;
+constexpr int kAccStride = Mode<true>::ACC;        // TMEM columns per accumulator buffer
+constexpr int kTmemCols = 512;
+constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + 256;
+static_assert(kSmem <= 232448, "shared memory budget");
+static_assert(2 * kAccStride <= kTmemCols, "TMEM budget");
+
+struct BatchGrid {
+    uint16_t *plane[2][2];  // [ping-pong state][hi, lo]
+    PlaneGeom pg;
+    int y0, y1, x0, x1;
+    int tiles_x;
+    int n_tiles;
+    int r, box, split;
+    int steps;
+    int ctr_base;   // completion counter of step 0
+    int band_base;  // first band element in the band buffer
+    int state;      // which plane holds the current state (flipped after a run)
+};
+
+struct BatchItem {
+    int g, t, tile;
+};
+
+struct BatchParams {
+    const BatchGrid *grids;
+    const BatchItem *items;
+    int n_items;
+    unsigned *counters;
+    const uint16_t *bands;
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int sub_tiles(const BatchGrid &g) { return g.split ? 2 : 1; }
+
+__global__ void build_bands_kernel(BatchGrid *grids, const float *coefs, uint16_t *bands) {
+    const BatchGrid &g = grids[blockIdx.x];
+    build_bands(bands + g.band_base, coefs + 25 * blockIdx.x, g.r, g.box, g.split, threadIdx.x,
+                blockDim.x);
+}
+
+__global__ void flip_states_kernel(BatchGrid *grids, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) grids[i].state ^= grids[i].steps & 1;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                ~static_cast<uintptr_t>(1023));
+    uint8_t *stage_base = smem;  // [kStages][hi | lo | bands]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)kStages * kStageBytes);
+    uint64_t *full = bars;                         // [kStages]
+    uint64_t *empty = bars + kStages;              // [kStages]
+    uint64_t *acc_full = bars + 2 * kStages;       // [2]
+    uint64_t *acc_empty = bars + 2 * kStages + 2;  // [2]
+    uint64_t *drain = bars + 2 * kStages + 4;      // [1]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 5);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    volatile int *grid_error = &g_batch_error;
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], kEpiWarps);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 1) {
+        __syncwarp();
+        tmem_alloc(tmem_slot, kTmemCols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        // ------------------------------------------------------ producer ---
+        if (lane == 0) {
+            int i = 0;
+            int last_issued = -1;
+            for (int k = blockIdx.x; k < p.n_items; k += gridDim.x, i++) {
+                const BatchItem it = p.items[k];
+                const BatchGrid &g = p.grids[it.g];
+                const int s = i % kStages;
+                if (!mbar_wait(&empty[s], ((i / kStages) & 1) ^ 1, abort_flag)) {
+                    record_error(&g_batch_error, kErrWaitEmpty);
+                    *abort_flag = 1;
+                    break;
+                }
+                if (it.t > 0) {
+                    // every tile of the previous step of this grid is stored
+                    const unsigned target =
+                        (unsigned)(g.n_tiles * kEpiWarps * sub_tiles(g));
+                    const unsigned *ctr = p.counters + g.ctr_base + it.t - 1;
+                    if (ld_acquire(ctr) < target) {
+                        const uint64_t t0 = global_timer_ns();
+                        bool ok = true;
+                        while (ld_acquire(ctr) < target) {
+                            if (*grid_error || global_timer_ns() - t0 > kWaitLimitNs) {
+                                ok = false;
+                                break;
+                            }
+                            __nanosleep(64);
+                        }
+                        if (!ok) {
+                            record_error(&g_batch_error, kErrWaitDep);
+                            *abort_flag = 1;
+                            break;
+                        }
+                    }
+                    // the bulk copies below read what other SMs stored
+                    fence_proxy_async_global();
+                }
+                const int nplanes = g.split ? 2 : 1;
+                const int band_bytes = (g.split ? 4 : 1) * (2 * g.r + 1) * kBandBytes;
+                uint8_t *st = stage_base + (size_t)s * kStageBytes;
+                mbar_arrive_expect_tx(&full[s], nplanes * kPlaneStage + band_bytes);
+                const int in = (g.state + it.t) & 1;
+                load_tile(g.plane[in][0], g.plane[in][1], nplanes, g.pg,
+                          (it.tile / g.tiles_x) * kTile, (it.tile % g.tiles_x) * kTile, st,
+                          &full[s]);
+                bulk_load(st + 2 * kPlaneStage, p.bands + g.band_base, band_bytes, &full[s]);
+                last_issued = i;
+            }
+            for (int k = 0; k < kStages && last_issued - k >= 0; k++) {
+                const int ii = last_issued - k;
+                const uint64_t t0 = global_timer_ns();
+                while (!mbar_try_wait(&full[ii % kStages], (ii / kStages) & 1)) {
+                    if (global_timer_ns() - t0 > kWaitLimitNs) {
+                        record_error(&g_batch_error, kErrWaitDrain);
+                        break;
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------- MMA issuer ---
+        if (lane == 0) {
+            int i = 0;
+            int kacc = 0;  // accumulator buffer counter (sub-tiles issued)
+            bool issued_any = false;
+            bool stop = false;
+            for (int k = blockIdx.x; k < p.n_items && !stop; k += gridDim.x, i++) {
+                const BatchItem it = p.items[k];
+                const BatchGrid &g = p.grids[it.g];
+                const int s = i % kStages;
+                if (!mbar_wait(&full[s], (i / kStages) & 1, abort_flag)) {
+                    record_error(&g_batch_error, kErrWaitFull);
+                    *abort_flag = 1;
+                    break;
+                }
+                uint8_t *st = stage_base + (size_t)s * kStageBytes;
+                const uint64_t a_hi0 = smem_desc(smem_u32(st), kChunkBytes, 128);
+                const uint64_t b_desc0 = smem_desc(smem_u32(st + 2 * kPlaneStage), 512, 128);
+                const int nsub = sub_tiles(g);
+                for (int h = 0; h < nsub; h++, kacc++) {
+                    const int b = kacc & 1;
+                    if (!mbar_wait(&acc_empty[b], ((kacc >> 1) & 1) ^ 1, abort_flag)) {
+                        record_error(&g_batch_error, kErrWaitAccum);
+                        *abort_flag = 1;
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d = tmem_base + b * kAccStride;
+                    if (g.split) {
+                        if (g.r == 1) issue_subtile<1, true>(a_hi0, b_desc0, d, h);
+                        else issue_subtile<2, true>(a_hi0, b_desc0, d, h);
+                    } else {
+                        if (g.r == 1) issue_subtile<1, false>(a_hi0, b_desc0, d, h);
+                        else issue_subtile<2, false>(a_hi0, b_desc0, d, h);
+                    }
+                    umma_commit(&acc_full[b]);
+                    issued_any = true;
+                }
+                umma_commit(&empty[s]);
+            }
+            if (issued_any) {
+                umma_commit(drain);
+                const uint64_t t0 = global_timer_ns();
+                while (!mbar_try_wait(drain, 0)) {
+                    if (global_timer_ns() - t0 > kWaitLimitNs) {
+                        record_error(&g_batch_error, kErrWaitDrain);
+                        break;
+                    }
+                }
+            }
+        }
+    } else {
+        // ------------------------------------------------------ epilogue ---
+        const int q = warp & 3;
+        const int half = (warp - 2) >> 2;
+        const int m = q * 32 + lane;
+        int kacc = 0;
+        bool stop = false;
+        for (int k = blockIdx.x; k < p.n_items && !stop; k += gridDim.x) {
+            const BatchItem it = p.items[k];
+            const BatchGrid &g = p.grids[it.g];
+            const int in = (g.state + it.t) & 1;
+            TileOut o;
+            o.in_hi = g.plane[in][0];
+            o.in_lo = g.plane[in][1];
+            o.out_hi = g.plane[in ^ 1][0];
+            o.out_lo = g.plane[in ^ 1][1];
+            o.pg = g.pg;
+            o.y0 = g.y0; o.y1 = g.y1; o.x0 = g.x0; o.x1 = g.x1;
+            const int Y0 = (it.tile / g.tiles_x) * kTile;
+            const int X0 = (it.tile % g.tiles_x) * kTile;
+            const int nsub = sub_tiles(g);
+            for (int h = 0; h < nsub; h++, kacc++) {
+                const int b = kacc & 1;
+                bool ok = mbar_wait(&acc_full[b], (kacc >> 1) & 1, abort_flag);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) {
+                    if (lane == 0) {
+                        record_error(&g_batch_error, kErrWaitResult);
+                        *abort_flag = 1;
+                    }
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t lane_addr = tmem_base + ((uint32_t)(q * 32) << 16) + b * kAccStride + 16;
+                if (g.split) epilogue_subtile<true>(o, lane_addr, h, half, m, Y0, X0);
+                else epilogue_subtile<false>(o, lane_addr, h, half, m, Y0, X0);
+                tc_fence_before();
+                __threadfence();  // this warp's stores before the completion count
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(&acc_empty[b]);
+                    atomicAdd(p.counters + g.ctr_base + it.t, 1u);
+                }
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) {
+        __syncwarp();
+        tmem_dealloc(tmem_base, kTmemCols);
+    }
+}
+
+int g_sms = 0;
+
+}  // namespace
+
+cudaError_t batch_take_error(int *code) {
+    int zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(code, g_batch_error, sizeof(int));
+    if (e != cudaSuccess) return e;
+    return *code ? cudaMemcpyToSymbol(g_batch_error, &zero, sizeof(int)) : cudaSuccess;
+}
+
+}  // namespace tcs
+
+using namespace tcs;
+
+// ================================================================ C-ABI ==
+struct tcs_batch_s {
+    struct Entry {
+        tcs_problem prob;
+        float coeffs[25];
+        GridGeom g;
+        int steps;
+        int scale_exp;
+        size_t plane_elems;
+        size_t offset[2][2];  // element offsets of the planes in the pool
+    };
+    std::vector<Entry> entries;
+    uint16_t *pool = nullptr;
+    size_t pool_elems = 0;
+    BatchGrid *d_grids = nullptr;
+    BatchItem *d_items = nullptr;
+    unsigned *d_counters = nullptr;
+    uint16_t *d_bands = nullptr;
+    float *d_coefs = nullptr;
+    float *d_staging = nullptr;
+    size_t staging_elems = 0;
+    unsigned *d_max = nullptr;
+    int n_items = 0;
+    int n_counters = 0;
+    long long point_updates = 0;
+    bool built = false;
+    int runs = 0;  // completed runs (each flips states by steps & 1)
+    cudaStream_t capture_stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+
+    ~tcs_batch_s() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (capture_stream) cudaStreamDestroy(capture_stream);
+        for (void *p : {(void *)pool, (void *)d_grids, (void *)d_items, (void *)d_counters,
+                        (void *)d_bands, (void *)d_coefs, (void *)d_staging, (void *)d_max})
+            if (p) cudaFree(p);
+    }
+
+    int state_of(const Entry &e) const { return (runs * (e.steps & 1)) & 1; }
+};
+
+namespace {
+
+int batch_build(tcs_batch b) {
+    if (b->built) return TCS_OK;
+    if (b->entries.empty()) return fail(TCS_ERR_INVALID, "tcs_batch: no grids");
+    // device plane pool (zeroed: padding must be finite)
+    size_t total = 0;
+    for (auto &e : b->entries)
+        for (int s = 0; s < 2; s++)
+            for (int pl = 0; pl < 2; pl++) {
+                if (pl == 1 && e.prob.precision != TCS_PREC_SPLIT) {
+                    e.offset[s][pl] = 0;
+                    continue;
+                }
+                e.offset[s][pl] = total;
+                total += (e.plane_elems + 127) / 128 * 128;  // 256-byte aligned planes
+            }
+    int st = cuda_status(cudaMalloc(&b->pool, total * sizeof(uint16_t)), "cudaMalloc(batch planes)");
+    if (!st) st = cuda_status(cudaMemset(b->pool, 0, total * sizeof(uint16_t)), "cudaMemset(batch planes)");
+    if (st) return st;
+    b->pool_elems = total;
+    // descriptors, bands, counters, work list
+    std::vector<BatchGrid> grids(b->entries.size());
+    std::vector<float> coefs(25 * b->entries.size(), 0.0f);
+    int ctr = 0, band = 0, max_steps = 0;
+    for (size_t i = 0; i < b->entries.size(); i++) {
+        const auto &e = b->entries[i];
+        BatchGrid &G = grids[i];
+        const bool split = e.prob.precision == TCS_PREC_SPLIT;
+        for (int s = 0; s < 2; s++) {
+            G.plane[s][0] = b->pool + e.offset[s][0];
+            G.plane[s][1] = split ? b->pool + e.offset[s][1] : nullptr;
+        }
+        G.pg = e.g.p16;
+        G.y0 = e.g.y0; G.y1 = e.g.y1; G.x0 = e.g.x0; G.x1 = e.g.x1;
+        G.tiles_x = (e.g.nx + kTile - 1) / kTile;
+        G.n_tiles = G.tiles_x * ((e.g.ny + kTile - 1) / kTile);
+        G.r = stencil_r(e.prob.stencil);
+        G.box = stencil_box(e.prob.stencil);
+        G.split = split;
+        G.steps = e.steps;
+        G.ctr_base = ctr;
+        G.band_base = band;
+        G.state = 0;
+        ctr += std::max(e.steps, 1);
+        band += (split ? 4 : 1) * (2 * G.r + 1) * kBandElems;
+        max_steps = std::max(max_steps, e.steps);
+        std::memcpy(&coefs[25 * i], e.coeffs, sizeof(e.coeffs));
+        b->point_updates += (long long)(e.g.y1 - e.g.y0) * (e.g.x1 - e.g.x0) * e.steps;
+    }
+    std::vector<BatchItem> items;
+    for (int t = 0; t < max_steps; t++)
+        for (size_t i = 0; i < grids.size(); i++)
+            if (grids[i].steps > t)
+                for (int tile = 0; tile < grids[i].n_tiles; tile++)
+                    items.push_back(BatchItem{(int)i, t, tile});
+    b->n_items = (int)items.size();
+    b->n_counters = ctr;
+    st = cuda_status(cudaMalloc(&b->d_grids, grids.size() * sizeof(BatchGrid)), "cudaMalloc(grids)");
+    if (!st) st = cuda_status(cudaMalloc(&b->d_items, std::max<size_t>(1, items.size()) * sizeof(BatchItem)), "cudaMalloc(items)");
+    if (!st) st = cuda_status(cudaMalloc(&b->d_counters, ctr * sizeof(unsigned)), "cudaMalloc(counters)");
+    if (!st) st = cuda_status(cudaMalloc(&b->d_bands, std::max(band, 1) * sizeof(uint16_t)), "cudaMalloc(bands)");
+    if (!st) st = cuda_status(cudaMalloc(&b->d_coefs, coefs.size() * sizeof(float)), "cudaMalloc(coefs)");
+    if (!st) st = cuda_status(cudaMemcpy(b->d_grids, grids.data(), grids.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice), "grids copy");
+    if (!st && !items.empty()) st = cuda_status(cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice), "items copy");
+    if (!st) st = cuda_status(cudaMemcpy(b->d_coefs, coefs.data(), coefs.size() * sizeof(float), cudaMemcpyHostToDevice), "coefs copy");
+    if (st) return st;
+    build_bands_kernel<<<(unsigned)grids.size(), 256>>>(b->d_grids, b->d_coefs, b->d_bands);
+    st = cuda_status(cudaGetLastError(), "band build launch");
+    if (st) return st;
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+        st = cuda_status(cudaFuncSetAttribute(tc_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)kSmem), "batch kernel set-up");
+        if (st) return st;
+    }
+    b->built = true;
+    return TCS_OK;
+}
+
+int batch_enqueue(tcs_batch b, cudaStream_t s) {
+    int st = cuda_status(cudaMemsetAsync(b->d_counters, 0, b->n_counters * sizeof(unsigned), s),
+                         "counter reset");
+    if (st) return st;
+    if (b->n_items > 0) {
+        BatchParams p;
+        p.grids = b->d_grids;
+        p.items = b->d_items;
+        p.n_items = b->n_items;
+        p.counters = b->d_counters;
+        p.bands = b->d_bands;
+        const int grid = std::min(b->n_items, g_sms);
+        tc_batch_kernel<<<grid, kThreads, kSmem, s>>>(p);
+        st = cuda_status(cudaGetLastError(), "batch kernel launch");
+        if (st) return st;
+    }
+    const int n = (int)b->entries.size();
+    flip_states_kernel<<<(n + 255) / 256, 256, 0, s>>>(b->d_grids, n);
+    return cuda_status(cudaGetLastError(), "state flip launch");
+}
+
+int ensure_staging(tcs_batch b, size_t elems) {
+    if (b->staging_elems >= elems) return TCS_OK;
+    if (b->d_staging) cudaFree(b->d_staging);
+    b->d_staging = nullptr;
+    b->staging_elems = 0;
+    int st = cuda_status(cudaMalloc(&b->d_staging, elems * sizeof(float)), "cudaMalloc(staging)");
+    if (!st) b->staging_elems = elems;
+    return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tcs_batch_create(tcs_batch *out) {
+    if (!out) return fail(TCS_ERR_INVALID, "tcs_batch_create: null argument");
+    *out = new tcs_batch_s();
+    return TCS_OK;
+}
+
+int tcs_batch_destroy(tcs_batch b) {
+    delete b;
+    return TCS_OK;
+}
+
+int tcs_batch_add(tcs_batch b, const tcs_problem *pr, int steps, int *index) {
+    if (!b || !pr || !pr->coeffs || steps < 0) return fail(TCS_ERR_INVALID, "tcs_batch_add: bad arguments");
+    if (b->built) return fail(TCS_ERR_INVALID, "tcs_batch_add: the batch already ran; create a new one");
+    if (pr->engine != TCS_ENGINE_TENSOR || (pr->precision != TCS_PREC_F16 && pr->precision != TCS_PREC_SPLIT))
+        return fail(TCS_ERR_UNSUPPORTED, "batches run on the tensor engine, FP16 or split precision");
+    tcs_batch_s::Entry e;
+    e.prob = *pr;
+    int st = make_geom(pr->ny, pr->nx, pr->stencil, pr->y0, pr->y1, pr->x0, pr->x1, &e.g);
+    if (st) return st;
+    const int n = 2 * stencil_r(pr->stencil) + 1;
+    for (int k = 0; k < 25; k++) e.coeffs[k] = k < n * n ? pr->coeffs[k] : 0.0f;
+    e.prob.coeffs = nullptr;
+    if (pr->precision == TCS_PREC_SPLIT && !(tap_abs_sum(pr->stencil, e.coeffs) <= kSplitMaxAbsSum))
+        return fail(TCS_ERR_UNSUPPORTED, "split precision needs a non-expanding stencil (sum of |c| <= 1)");
+    e.steps = steps;
+    e.scale_exp = 0;
+    e.plane_elems = plane_elems(e.g.p16);
+    if (index) *index = (int)b->entries.size();
+    b->entries.push_back(e);
+    return TCS_OK;
+}
+
+int tcs_batch_upload(tcs_batch b, int index, const float *grid, int on_host, void *stream) {
+    if (!b || !grid || index < 0 || index >= (int)b->entries.size())
+        return fail(TCS_ERR_INVALID, "tcs_batch_upload: bad arguments");
+    int st = batch_build(b);
+    if (st) return st;
+    auto &e = b->entries[index];
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t cells = (size_t)e.g.ny * e.g.nx;
+    const float *src = grid;
+    if (on_host) {
+        st = ensure_staging(b, cells);
+        if (!st) st = cuda_status(cudaMemcpyAsync(b->d_staging, grid, cells * sizeof(float), cudaMemcpyHostToDevice, s), "upload copy");
+        if (st) return st;
+        src = b->d_staging;
+    }
+    const int cur = b->state_of(e);
+    uint16_t *hi = b->pool + e.offset[cur][0];
+    if (e.prob.precision == TCS_PREC_SPLIT) {
+        // scale so that max |x| 2^-E <= 1 (needs the maximum on the host)
+        if (!b->d_max) st = cuda_status(cudaMalloc(&b->d_max, sizeof(unsigned)), "cudaMalloc(max)");
+        if (!st) st = cuda_status(cudaMemsetAsync(b->d_max, 0, sizeof(unsigned), s), "memset(max)");
+        if (!st) st = cuda_status(launch_max_abs(src, cells, b->d_max, s), "max_abs launch");
+        unsigned bits = 0;
+        if (!st) st = cuda_status(cudaMemcpyAsync(&bits, b->d_max, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "max copy");
+        if (!st) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        if (st) return st;
+        float mx;
+        std::memcpy(&mx, &bits, sizeof(mx));
+        e.scale_exp = split_scale_exp(mx);
+        st = cuda_status(launch_pack_split(src, e.g.ny, e.g.nx, 0, 0.0f, e.scale_exp, hi,
+                                           b->pool + e.offset[cur][1], s), "pack launch");
+    } else {
+        st = cuda_status(launch_pack_f16(src, e.g.ny, e.g.nx, 0, 0.0f, hi, s), "pack launch");
+    }
+    if (st) return st;
+    return on_host ? cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize") : TCS_OK;
+}
+
+int tcs_batch_download(tcs_batch b, int index, float *grid, int on_host, void *stream) {
+    if (!b || !grid || index < 0 || index >= (int)b->entries.size() || !b->built)
+        return fail(TCS_ERR_INVALID, "tcs_batch_download: bad arguments");
+    auto &e = b->entries[index];
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t cells = (size_t)e.g.ny * e.g.nx;
+    float *dst = grid;
+    int st = TCS_OK;
+    if (on_host) {
+        st = ensure_staging(b, cells);
+        if (st) return st;
+        dst = b->d_staging;
+    }
+    const int cur = b->state_of(e);
+    if (e.prob.precision == TCS_PREC_SPLIT)
+        st = cuda_status(launch_unpack_split(b->pool + e.offset[cur][0], b->pool + e.offset[cur][1],
+                                             e.g.ny, e.g.nx, 0, e.scale_exp, dst, s), "unpack launch");
+    else
+        st = cuda_status(launch_unpack_f16(b->pool + e.offset[cur][0], e.g.ny, e.g.nx, 0, dst, s),
+                         "unpack launch");
+    if (st || !on_host) return st;
+    st = cuda_status(cudaMemcpyAsync(grid, b->d_staging, cells * sizeof(float), cudaMemcpyDeviceToHost, s), "download copy");
+    if (!st) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    return st;
+}
+
+int tcs_batch_run(tcs_batch b, int use_graph, void *stream) {
+    if (!b) return fail(TCS_ERR_INVALID, "tcs_batch_run: null batch");
+    int st = batch_build(b);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!use_graph) {
+        st = batch_enqueue(b, s);
+    } else {
+        if (!b->graph) {
+            if (!b->capture_stream) {
+                st = cuda_status(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+                if (st) return st;
+            }
+            st = cuda_status(cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+            if (st) return st;
+            const int est = batch_enqueue(b, b->capture_stream);
+            cudaGraph_t graph = nullptr;
+            st = cuda_status(cudaStreamEndCapture(b->capture_stream, &graph), "cudaStreamEndCapture");
+            if (est || st) {
+                if (graph) cudaGraphDestroy(graph);
+                return est ? est : st;
+            }
+            st = cuda_status(cudaGraphInstantiate(&b->graph, graph, 0), "cudaGraphInstantiate");
+            cudaGraphDestroy(graph);
+            if (st) return st;
+        }
+        st = cuda_status(cudaGraphLaunch(b->graph, s), "cudaGraphLaunch");
+    }
+    if (!st) b->runs++;
+    return st;
+}
+
+int tcs_batch_info(tcs_batch b, long long *point_updates, int *items, int *grids) {
+    if (!b) return fail(TCS_ERR_INVALID, "tcs_batch_info: null batch");
+    int st = batch_build(b);
+    if (st) return st;
+    if (point_updates) *point_updates = b->point_updates;
+    if (items) *items = b->n_items;
+    if (grids) *grids = (int)b->entries.size();
+    return TCS_OK;
+}
+
+}  // extern "C"

@@ -38,48 +38,35 @@
 // c3*hi, where cf*lo also carries the lo*(c - ch) term.  Both are combined in
 // FP32 with round-to-nearest in the epilogue.
 //
-// Pipeline (persistent, one CTA per SM, 6 warps):
+// Pipeline (persistent, one CTA per SM, 10 warps):
 //   warp 0      producer: bulk copies of each tile's panels into NS stages
 //   warp 1      TMEM allocator and single-thread MMA issuer
-//   warps 2..5  epilogue: TMEM -> registers -> FP16 (or hi/lo) -> global
+//   warps 2..9  epilogue (two warpgroups, one per column half):
+//               TMEM -> registers -> FP16 (or hi/lo) -> global
 // Two accumulator buffers let the epilogue of one (sub-)tile overlap the MMAs
 // of the next.  Every wait is bounded; on timeout the kernel records an error
 // word, stops, drains its own copies and MMAs, frees TMEM and returns.
-#include "tcs_device.cuh"
-#include "tcs_internal.h"
+#include "tc_core.cuh"
 
 namespace tcs {
 
 namespace {
 
-__device__ int g_tc_error = 0;
+using namespace tc;
 
-constexpr int kRowsStaged = kTile + 4;           // two halo rows above and below
-constexpr int kChunkBytes = kRowsStaged * 16;    // one panel of the stage
-constexpr int kSlots = kTile / 8 + 2;            // 16 panels + one each side
-constexpr int kPlaneStage = kSlots * kChunkBytes;
-constexpr int kBandBytes = 32 * 16 * 2;          // one 16(K) x 32(N) FP16 band
-constexpr int kEpiWarps = 8;                     // two warpgroups, one per column half
-constexpr int kThreads = 32 * (2 + kEpiWarps);
-constexpr uint32_t kIdesc = idesc_f16_f32(128, 32);
+__device__ int g_tc_error = 0;
 
 template <int S, bool SPLIT>
 struct Cfg {
+    using M = Mode<SPLIT>;
     static constexpr int R = stencil_r(S);
     static constexpr bool BOX = stencil_box(S);
-    static constexpr int NDY = 2 * R + 1;                 // coefficient rows
-    static constexpr int NSUB = SPLIT ? 2 : 1;            // sub-tiles per tile
-    static constexpr int SUB_BLOCKS = kTile / 16 / NSUB;  // 16-column output blocks per sub-tile
-    static constexpr int SUB_WIN = SUB_BLOCKS + 1;        // input windows per sub-tile
-    static constexpr int ACC_PLANE = 16 * (SUB_BLOCKS + 2);  // TMEM columns per accumulator
-    static constexpr int ACC = ACC_PLANE * (SPLIT ? 2 : 1);
+    static constexpr int NDY = 2 * R + 1;
     static constexpr int TMEM_COLS = 512;
-    static_assert(2 * ACC <= TMEM_COLS, "two accumulator buffers must fit in TMEM");
-    static constexpr int PLANES = SPLIT ? 2 : 1;          // hi (and lo) data planes
-    static constexpr int BAND_PLANES = SPLIT ? 4 : 1;     // ch (and cf, cl, c3)
+    static_assert(2 * M::ACC <= TMEM_COLS, "two accumulator buffers must fit in TMEM");
     static constexpr int STAGES = SPLIT ? 2 : 4;
-    static constexpr size_t SMEM = 1024 + (size_t)STAGES * PLANES * kPlaneStage +
-                                   (size_t)BAND_PLANES * NDY * kBandBytes + 256;
+    static constexpr size_t SMEM = 1024 + (size_t)STAGES * M::PLANES * kPlaneStage +
+                                   (size_t)M::BAND_PLANES * NDY * kBandBytes + 256;
     static_assert(SMEM <= 232448, "shared memory budget");
 };
 
@@ -91,29 +78,13 @@ struct TcParams {
     float coef[25];                 // n x n, row-major
 };
 
-__device__ __forceinline__ uint16_t h_bits(float v) {
-    __half h = __float2half_rn(v);
-    return *reinterpret_cast<uint16_t *>(&h);
-}
-__device__ __forceinline__ float h_val(uint16_t b) {
-    __half h = *reinterpret_cast<__half *>(&b);
-    return __half2float(h);
-}
-
-// Fixed-point split of a value v (|v| about 1 or below): hi = fp16 of
-// rint(v 2^11) 2^-11, lo = fp16((v - hi) 2^11).
-__device__ __forceinline__ void split_fixed(float v, uint16_t &hi, uint16_t &lo) {
-    hi = h_bits(rintf(v * 2048.0f) * (1.0f / 2048.0f));
-    lo = h_bits((v - h_val(hi)) * 2048.0f);
-}
-
 template <int S, bool SPLIT>
 __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p) {
     using C = Cfg<S, SPLIT>;
-    constexpr int R = C::R;
+    using M = Mode<SPLIT>;
     constexpr int NS = C::STAGES;
-    constexpr int NP = C::PLANES;
-    constexpr int NSUB = C::NSUB;
+    constexpr int NP = M::PLANES;
+    constexpr int NSUB = M::NSUB;
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -121,7 +92,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
     uint8_t *stage_base = smem;                                    // [NS][NP][stage]
     uint8_t *band_base = smem + (size_t)NS * NP * kPlaneStage;     // [BAND_PLANES][NDY]
     uint64_t *bars =
-        reinterpret_cast<uint64_t *>(band_base + C::BAND_PLANES * C::NDY * kBandBytes);
+        reinterpret_cast<uint64_t *>(band_base + M::BAND_PLANES * C::NDY * kBandBytes);
     uint64_t *full = bars;                    // [NS]
     uint64_t *empty = bars + NS;              // [NS]
     uint64_t *acc_full = bars + 2 * NS;       // [2]
@@ -153,30 +124,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
         tmem_alloc(tmem_slot, C::TMEM_COLS);
         tmem_relinquish();
     }
-    // Bands, K-major core-matrix layout: element (n, k) of the band of
-    // coefficient row dy at dy*512 + (k/8)*256 + n*8 + k%8.  Input column k of
-    // a window feeds output column n of its 32-column range with tap
-    // dx = 8 + k - n.
-    for (int idx = threadIdx.x; idx < C::NDY * 512; idx += kThreads) {
-        const int dy = idx >> 9, n = (idx >> 4) & 31, k = idx & 15;
-        const int dx = 8 + k - n;
-        const bool on_axis = C::BOX || dy == R || dx == 0;
-        float c = 0.0f;
-        if (dx >= -R && dx <= R && on_axis) c = p.coef[dy * (2 * R + 1) + dx + R];
-        const int off = dy * 512 + (k >> 3) * 256 + n * 8 + (k & 7);
-        uint16_t *band = reinterpret_cast<uint16_t *>(band_base);
-        if (!SPLIT) {
-            band[off] = h_bits(c);
-        } else {
-            const float ch = rintf(c * 2048.0f) * (1.0f / 2048.0f);
-            const float rem = (c - ch) * 2048.0f;  // exact
-            const uint16_t cl = h_bits(rem);
-            band[off] = h_bits(ch);                                  // ch: fixed point
-            band[C::NDY * 512 + off] = h_bits(c);                    // cf: fp16(c), multiplies lo
-            band[2 * C::NDY * 512 + off] = cl;                       // cl
-            band[3 * C::NDY * 512 + off] = h_bits(rem - h_val(cl));  // c3
-        }
-    }
+    build_bands(reinterpret_cast<uint16_t *>(band_base), p.coef, C::R, C::BOX, SPLIT, threadIdx.x,
+                kThreads);
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -199,20 +148,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
                     *abort_flag = 1;
                     break;
                 }
-                const int Y0 = (t / tiles_x) * kTile;
-                const int X0 = (t % tiles_x) * kTile;
                 mbar_arrive_expect_tx(&full[s], NP * kPlaneStage);
-                // rows Y0-2 .. Y0+129 of panels X0/8 - 1 .. X0/8 + 16
-                const size_t src0 = plane_index(pg, Y0 - 2, X0 - 8);
-#pragma unroll
-                for (int pl = 0; pl < NP; pl++) {
-                    const uint16_t *src = (pl ? p.in_lo : p.in_hi) + src0;
-                    uint8_t *st = stage_base + ((size_t)s * NP + pl) * kPlaneStage;
-#pragma unroll 1
-                    for (int c = 0; c < kSlots; c++)
-                        bulk_load(st + c * kChunkBytes, src + (size_t)c * pg.nyp * 8, kChunkBytes,
-                                  &full[s]);
-                }
+                load_tile(p.in_hi, p.in_lo, NP, pg, (t / tiles_x) * kTile, (t % tiles_x) * kTile,
+                          stage_base + (size_t)s * NP * kPlaneStage, &full[s]);
                 last_issued = i;
             }
             // Drain: every stage armed last must have landed before exit.
@@ -241,12 +179,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
                     *abort_flag = 1;
                     break;
                 }
-                // Descriptors: the start-address field holds (address >> 4)
-                // in its low bits, so a descriptor for base + offset is the
-                // base descriptor plus offset >> 4 (compile-time offsets).
-                const uint64_t a_hi0 =
-                    smem_desc(smem_u32(stage_base + ((size_t)s * NP) * kPlaneStage), kChunkBytes, 128);
-                const uint64_t a_lo0 = a_hi0 + (kPlaneStage >> 4);
+                const uint64_t a_hi0 = smem_desc(
+                    smem_u32(stage_base + (size_t)s * NP * kPlaneStage), kChunkBytes, 128);
 #pragma unroll
                 for (int h = 0; h < NSUB; h++) {
                     const int k = i * NSUB + h;  // sub-tile counter
@@ -258,32 +192,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t d_main = tmem_base + b * C::ACC;
-                    const uint32_t d_corr = d_main + C::ACC_PLANE;
-                    // even windows (disjoint outputs, initialise), then odd windows
-#pragma unroll
-                    for (int parity = 0; parity < 2; parity++) {
-#pragma unroll
-                        for (int dy = 0; dy < C::NDY; dy++) {
-                            const uint64_t b_ch = b_desc0 + (uint64_t)((dy * kBandBytes) >> 4);
-                            const uint32_t acc = (parity == 1 || dy > 0) ? 1u : 0u;
-#pragma unroll
-                            for (int w = parity; w < C::SUB_WIN; w += 2) {
-                                const int wg = h * C::SUB_BLOCKS + w;  // window in the tile
-                                const uint64_t a_off =
-                                    (uint64_t)((2 * wg * kChunkBytes + (2 - R + dy) * 16) >> 4);
-                                umma_f16(d_main + 16 * w, a_hi0 + a_off, b_ch, kIdesc, acc);
-                                if (SPLIT) {
-                                    const uint64_t b_cf = b_desc0 + (uint64_t)(((C::NDY + dy) * kBandBytes) >> 4);
-                                    const uint64_t b_cl = b_desc0 + (uint64_t)(((2 * C::NDY + dy) * kBandBytes) >> 4);
-                                    const uint64_t b_c3 = b_desc0 + (uint64_t)(((3 * C::NDY + dy) * kBandBytes) >> 4);
-                                    umma_f16(d_corr + 16 * w, a_lo0 + a_off, b_cf, kIdesc, acc);
-                                    umma_f16(d_corr + 16 * w, a_hi0 + a_off, b_cl, kIdesc, 1);
-                                    umma_f16(d_corr + 16 * w, a_hi0 + a_off, b_c3, kIdesc, 1);
-                                }
-                            }
-                        }
-                    }
+                    issue_subtile<C::R, SPLIT>(a_hi0, b_desc0, tmem_base + b * M::ACC, h);
                     umma_commit(&acc_full[b]);
                     issued_any = true;
                 }
@@ -302,18 +211,21 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
         }
     } else {
         // ------------------------------------------------------ epilogue ---
-        const int q = warp & 3;       // TMEM lane quarter of this warp
+        const int q = warp & 3;            // TMEM lane quarter of this warp
         const int half = (warp - 2) >> 2;  // which half of a sub-tile's column blocks
-        const int m = q * 32 + lane;  // output row within the tile
-        const GridGeom &g = p.g;
+        const int m = q * 32 + lane;       // output row within the tile
+        TileOut o;
+        o.in_hi = p.in_hi;
+        o.in_lo = p.in_lo;
+        o.out_hi = p.out_hi;
+        o.out_lo = p.out_lo;
+        o.pg = pg;
+        o.y0 = p.g.y0; o.y1 = p.g.y1; o.x0 = p.g.x0; o.x1 = p.g.x1;
         int i = 0;
         bool stop = false;
         for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
             const int Y0 = (t / tiles_x) * kTile;
             const int X0 = (t % tiles_x) * kTile;
-            const bool fast = Y0 >= g.y0 && Y0 + kTile <= g.y1 && X0 >= g.x0 && X0 + kTile <= g.x1;
-            const int y = Y0 + m;
-            const bool row_in = y >= g.y0 && y < g.y1;
 #pragma unroll 1
             for (int h = 0; h < NSUB; h++) {
                 const int k = i * NSUB + h;
@@ -330,86 +242,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
                 }
                 tc_fence_after();
                 // output block jl of the sub-tile is accumulator column 16(jl+1)
-                const uint32_t lane_addr =
-                    tmem_base + ((uint32_t)(q * 32) << 16) + b * C::ACC + 16;
-                // G blocks per TMEM round trip: all their loads are issued
-                // before one wait, so the load latency is paid once per group.
-                constexpr int G = C::SUB_BLOCKS / 2;  // this warp's blocks, one round trip
-                {
-                    const int j0 = half * G;
-                    uint32_t v[G][16];
-                    uint32_t w[SPLIT ? G : 1][16];
-#pragma unroll
-                    for (int gg = 0; gg < G; gg++) {
-                        tmem_ld_x16(lane_addr + 16 * (j0 + gg), v[gg]);
-                        if (SPLIT) tmem_ld_x16(lane_addr + C::ACC_PLANE + 16 * (j0 + gg), w[SPLIT ? gg : 0]);
-                    }
-                    tmem_ld_wait();
-#pragma unroll
-                    for (int gg = 0; gg < G; gg++) {
-                        const int xb = X0 + 16 * (h * C::SUB_BLOCKS + j0 + gg);
-                        const size_t off0 = plane_index(pg, y, xb);      // cells xb .. xb+7
-                        const size_t off1 = off0 + (size_t)pg.nyp * 8;   // cells xb+8 .. xb+15
-                        float f[16];
-#pragma unroll
-                        for (int c = 0; c < 16; c++) {
-                            f[c] = __uint_as_float(v[gg][c]);
-                            if (SPLIT) f[c] = fmaf(__uint_as_float(w[SPLIT ? gg : 0][c]), 1.0f / 2048.0f, f[c]);
-                        }
-                        uint32_t hw[8], lw[8];
-                        if (fast) {
-#pragma unroll
-                            for (int c = 0; c < 8; c++) {
-                                uint16_t h0, h1, l0 = 0, l1 = 0;
-                                if (SPLIT) {
-                                    split_fixed(f[2 * c], h0, l0);
-                                    split_fixed(f[2 * c + 1], h1, l1);
-                                } else {
-                                    h0 = h_bits(f[2 * c]);
-                                    h1 = h_bits(f[2 * c + 1]);
-                                }
-                                hw[c] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-                                lw[c] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-                            }
-                        } else {
-                            // Border tile: cells outside the update rectangle copy the input.
-                            const uint4 i0 = *reinterpret_cast<const uint4 *>(p.in_hi + off0);
-                            const uint4 i1 = *reinterpret_cast<const uint4 *>(p.in_hi + off1);
-                            const uint32_t iw[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
-                            uint32_t il[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                            if (SPLIT) {
-                                const uint4 l0 = *reinterpret_cast<const uint4 *>(p.in_lo + off0);
-                                const uint4 l1 = *reinterpret_cast<const uint4 *>(p.in_lo + off1);
-                                il[0] = l0.x; il[1] = l0.y; il[2] = l0.z; il[3] = l0.w;
-                                il[4] = l1.x; il[5] = l1.y; il[6] = l1.z; il[7] = l1.w;
-                            }
-#pragma unroll
-                            for (int c = 0; c < 8; c++) {
-                                uint16_t hh[2], ll[2];
-#pragma unroll
-                                for (int u = 0; u < 2; u++) {
-                                    const int x = xb + 2 * c + u;
-                                    const bool upd = row_in && x >= g.x0 && x < g.x1;
-                                    if (upd) {
-                                        if (SPLIT) split_fixed(f[2 * c + u], hh[u], ll[u]);
-                                        else { hh[u] = h_bits(f[2 * c + u]); ll[u] = 0; }
-                                    } else {
-                                        hh[u] = (uint16_t)(iw[c] >> (16 * u));
-                                        ll[u] = (uint16_t)(il[c] >> (16 * u));
-                                    }
-                                }
-                                hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
-                                lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
-                            }
-                        }
-                        *reinterpret_cast<uint4 *>(p.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                        *reinterpret_cast<uint4 *>(p.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
-                        if (SPLIT) {
-                            *reinterpret_cast<uint4 *>(p.out_lo + off0) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-                            *reinterpret_cast<uint4 *>(p.out_lo + off1) = make_uint4(lw[4], lw[5], lw[6], lw[7]);
-                        }
-                    }
-                }
+                const uint32_t lane_addr = tmem_base + ((uint32_t)(q * 32) << 16) + b * M::ACC + 16;
+                epilogue_subtile<SPLIT>(o, lane_addr, h, half, m, Y0, X0);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&acc_empty[b]);

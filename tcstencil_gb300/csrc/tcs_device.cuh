@@ -16,6 +16,7 @@ enum DeviceError : int {
     kErrWaitAccum = 3,    // MMA issuer waited too long for a free accumulator
     kErrWaitResult = 4,   // epilogue waited too long for an accumulator
     kErrWaitDrain = 5,    // final drain of in-flight copies / MMAs timed out
+    kErrWaitDep = 6,      // batched run: a step waited too long for its previous step
 };
 
 // Upper bound on any single in-kernel wait: the hardware finishes each awaited

@@ -112,6 +112,7 @@ cudaError_t launch_cc_f32(const GridGeom &g, int stencil, const TapCoeffs &c, co
 
 // Reads and clears the tensor kernels' device error word.
 cudaError_t tc_take_error(int *code);
+cudaError_t batch_take_error(int *code);
 // Configures the tensor kernel of (stencil, split) ahead of its first launch.
 cudaError_t tc_prepare(int stencil, bool split);
 

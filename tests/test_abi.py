@@ -118,3 +118,24 @@ def test_split_rejects_expanding_stencils(tcs):
         tcs.sweep_step(1 << 20, 2 << 20, 64, 64, "box2d1r", B, precision="split",
                        d_in_lo=3 << 20, d_out_lo=4 << 20)
     assert e.value.status == tcs.TCS_ERR_UNSUPPORTED
+
+
+def test_batch_add_validates_before_any_device_work(tcs):
+    """Batches take tensor-engine FP16/split grids; every check runs in
+    tcs_batch_add, before the batch touches the device."""
+    b = tcs.Batch()
+    c = np.full((3, 3), 1.0 / 9.0, np.float32)
+    assert b.add(64, 64, "box2d1r", c, 3) == 0
+    assert b.add(200, 31, "box2d1r", c, 0, "split") == 1
+    with pytest.raises(tcs.TcsError) as e:
+        b.add(64, 64, "box2d1r", np.full((3, 3), 0.2, np.float32), 1, "split")
+    assert e.value.status == tcs.TCS_ERR_UNSUPPORTED
+    with pytest.raises(tcs.TcsError) as e:
+        b.add(64, 64, "box2d1r", c, 1, "f32")
+    assert e.value.status == tcs.TCS_ERR_UNSUPPORTED
+    with pytest.raises(tcs.TcsError) as e:
+        b.add(2, 64, "box2d1r", c, 1)
+    assert e.value.status == tcs.TCS_ERR_INVALID
+    with pytest.raises(tcs.TcsError):
+        b.add(64, 64, "box2d1r", c, -1)
+    b.close()
