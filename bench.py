@@ -12,7 +12,7 @@ reference ships no datasets; its benchmark meshes are synthetic too).
 Prints one JSON line.  `value` is device-timed Gpts/s (point-updates per
 second) with the grid resident in HBM; `e2e` is the same metric through the
 public one-call C-ABI (tcs_sweep_host) with pinned host buffers, host<->device
-copies inside the timed region.  Each brick plane is 134 MB and a sweep
+copies inside the timed region.  Each panel plane is 139 MB and a sweep
 alternates two of them, so the working set (269 MB) exceeds the 129 MB L2.
 `--impl reference` times the CPU gold code (the oracle's restatement of
 common/gold_box2d2r.cpp) on the host cores.  With torchrun (N > 1) every rank
@@ -54,6 +54,12 @@ def parse():
     ap.add_argument("--interior", type=int, default=INTERIOR)
     ap.add_argument("--timesteps", type=int, default=TIMESTEPS)
     ap.add_argument("--no-extras", action="store_true", help="skip comparator and CPU legs")
+    ap.add_argument("--workload", choices=["sweep", "batch", "serve"], default="sweep",
+                    help="sweep: one grid (default); batch: 512 mixed grids in one "
+                         "persistent launch per run; serve: Poisson-arrival request serving")
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--batch-grids", type=int, default=512)
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: upload the grid, run --timesteps single-step "
                          "launches (no graph), exit; for ncu captures")
@@ -215,7 +221,80 @@ def workload_config(args):
             "engine": args.engine, "precision": args.precision,
             "storage": "f32" if args.precision == "f32" else "f16",
             "accumulate": "f32", "parallelism": "replicas",
-            "l2": "inputs larger than L2 (two 134 MB brick planes > 129 MB L2)"}
+            "l2": "inputs larger than L2 (two 139 MB panel planes > 129 MB L2)"}
+
+
+def build_batch(tcs, specs):
+    b = tcs.Batch()
+    for sp in specs:
+        b.add(sp.ny, sp.nx, sp.stencil, sp.coeffs, sp.steps, sp.precision)
+    return b
+
+
+def batch_leg(torch, tcs, K, W, stream, count=512):
+    """Batched mixed stencils (512 grids, sides log-uniform in [64, 2048], 1-64
+    steps, FP16 and split 50/50): one persistent launch per run, replayed as a
+    CUDA graph.  Returns device-timed and end-to-end figures."""
+    from tcstencil_gb300.workloads import mixed_batch
+
+    specs = mixed_batch(count)
+    grids = [torch.from_numpy(sp.grid()).pin_memory() for sp in specs]
+    outs = [torch.empty_like(g).pin_memory() for g in grids]
+    b = build_batch(tcs, specs)
+    for k, g in enumerate(grids):
+        b.upload(k, g.numpy(), stream=stream)
+    pu, items, ngrids = b.info()
+    byts = sum(sp.bytes for sp in specs)
+    for _ in range(W):
+        b.run(use_graph=True, stream=stream)
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(K):
+        b.run(use_graph=True, stream=stream)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    t = start.elapsed_time(stop) / 1e3 / K
+    assert tcs.device_error() == 0
+    # end to end: pinned host grids in, one run, host grids out, every run
+    Ke = max(2, K // 4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        for k, g in enumerate(grids):
+            b.upload(k, g.numpy(), stream=stream)
+        b.run(use_graph=True, stream=stream)
+        for k, o in enumerate(outs):
+            b.download(k, o.numpy(), stream=stream)
+        torch.cuda.synchronize()
+    te = (time.perf_counter() - t0) / Ke
+    b.close()
+    host_bytes = sum(g.numel() * 4 for g in grids)
+    return {"gpts": pu / t / 1e9, "ms_per_run": 1e3 * t, "point_updates_per_run": pu,
+            "items_per_run": items, "grids": ngrids, "algorithmic_bytes_per_run": byts,
+            "achieved_gbs": byts / t / 1e9, "e2e_gpts": pu / te / 1e9,
+            "e2e_h2d_bytes": host_bytes, "e2e_d2h_bytes": host_bytes}
+
+
+def serve_leg(tcs, seconds=10.0, rate=2000.0, budget_gb=120.0):
+    """Served stencil solves: Poisson arrivals at `rate`/s for `seconds`, sides
+    log-uniform in [128, 4096] per axis, random stencil and coefficients, 1-200
+    steps, FP16 or split; admission against a `budget_gb` HBM budget."""
+    from tcstencil_gb300.serving import InputPool, OutputRing, replay
+    from tcstencil_gb300.workloads import poisson_requests
+
+    reqs = poisson_requests(rate=rate, duration=seconds)
+    srv = tcs.Server(int(budget_gb * 2**30))
+    try:
+        res = replay(srv, reqs, InputPool(1 << 26), OutputRing(1 << 28))
+    finally:
+        srv.close()
+    res["algorithmic_bytes"] = sum(r.spec.bytes for r in reqs)
+    res["achieved_gbs"] = res["algorithmic_bytes"] / res["span_s"] / 1e9
+    res["offered_gpts"] = res["point_updates"] / seconds / 1e9
+    res["budget_gb"] = budget_gb
+    return res
 
 
 def timed_sweeps(torch, tcs, plan, K, W, timesteps, stream):
@@ -314,6 +393,12 @@ def run_ours(args):
                 t2 = timed_sweeps(torch, tcs, p2, max(5, args.steps // 4), 2, args.timesteps, stream)
                 p2.close()
                 extras[f"{st}/{eng}/f16"] = round(updates_per_step * max(5, args.steps // 4) / t2 / 1e9, 2)
+        r = batch_leg(torch, tcs, 10, 3, stream)
+        extras["batched_512_mixed"] = {k: round(v, 3) if isinstance(v, float) else v
+                                       for k, v in r.items()}
+        r = serve_leg(tcs, args.serve_seconds, args.serve_rate)
+        extras["served_poisson"] = {k: round(v, 3) if isinstance(v, float) else v
+                                    for k, v in r.items()}
     if ws > 1:
         torch.distributed.barrier()
     if rank != 0:
@@ -345,10 +430,116 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_batch(args):
+    """--workload batch: the batched mixed-stencil configuration as the line."""
+    import torch
+
+    import tcstencil_gb300 as tcs
+
+    rank, local_rank, ws = dist_env()
+    torch.cuda.set_device(local_rank)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    stream = torch.cuda.current_stream()
+    sampler = ClockSampler(local_rank) if rank == 0 else None
+    r = batch_leg(torch, tcs, args.steps, args.warmup, stream, args.batch_grids)
+    clocks = ClockSampler.summarize(sampler.stop()) if sampler else None
+    t = r["ms_per_run"] * args.steps / 1e3
+    te = r["point_updates_per_run"] / r["e2e_gpts"] / 1e9
+    if ws > 1:
+        tt = torch.tensor([t, te], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t, te = (float(v) for v in tt.tolist())
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+    peak, peak_kind = load_peaks()
+    pu = r["point_updates_per_run"]
+    line = {
+        "metric": "batched mixed-stencil Jacobi point-updates per second (Gpts/s)",
+        "value": round(ws * pu * args.steps / t / 1e9, 3), "unit": "Gpts/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * t / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16",
+        "data": "synthetic (seeded U[-1,1) grids, normalised U[0,1) coefficients)",
+        "config": {"workload": f"{r['grids']} grids, sides log-uniform in [64, 2048] per axis, "
+                               "stencil uniform over the four, 1-64 steps each, FP16 and split "
+                               "50/50; one persistent launch per run (CUDA graph)",
+                   "grids": r["grids"], "items_per_run": r["items_per_run"],
+                   "point_updates_per_run": pu, "parallelism": "replicas",
+                   "l2": "inputs larger than L2 (1.3 GB of planes > 129 MB L2)"},
+        "roofline": {"bound": "hbm", "achieved": round(r["achieved_gbs"], 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(r["achieved_gbs"] / peak, 4),
+                     "traffic": None, "peak_kind": peak_kind,
+                     "basis": "4 B (FP16) / 8 B (split) per point-update, summed over the batch, "
+                              "/ run time (CUDA events)"},
+        "e2e": {"value": round(ws * pu / te / 1e9, 3), "unit": "Gpts/s",
+                "h2d_bytes_per_step": r["e2e_h2d_bytes"], "d2h_bytes_per_step": r["e2e_d2h_bytes"],
+                "api": "tcs_batch_upload / tcs_batch_run / tcs_batch_download, pinned host grids"},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_serve(args):
+    """--workload serve: the served configuration as the line (rank 0 only
+    serves; a server is per GPU, so N GPUs are N independent replicas)."""
+    import torch
+
+    import tcstencil_gb300 as tcs
+
+    rank, local_rank, ws = dist_env()
+    torch.cuda.set_device(local_rank)
+    sampler = ClockSampler(local_rank) if rank == 0 else None
+    r = serve_leg(tcs, args.serve_seconds, args.serve_rate)
+    clocks = ClockSampler.summarize(sampler.stop()) if sampler else None
+    if rank != 0:
+        return
+    peak, peak_kind = load_peaks()
+    line = {
+        "metric": "served stencil solves: aggregate point-updates per second (Gpts/s), "
+                  "p50/p99 latency in 'latency'",
+        "value": round(r["gpts"], 3), "unit": "Gpts/s", "n_gpus": ws, "steps": r["requests"],
+        "warmup": 0, "ms_per_step": round(r["mean_ms"], 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16",
+        "data": "synthetic (Poisson arrivals; seeded U[-1,1) grids, normalised coefficients)",
+        "config": {"workload": f"Poisson arrivals at {args.serve_rate:g} req/s for "
+                               f"{args.serve_seconds:g} s, sides log-uniform in [128, 4096], "
+                               "random stencil, 1-200 steps, FP16 or split, 120 GB HBM budget",
+                   "requests": r["requests"], "parallelism": "replicas",
+                   "l2": "request state far larger than L2"},
+        "latency": {"p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "mean_ms": r["mean_ms"],
+                    "max_ms": r["max_ms"], "basis": "completion (result in host memory) minus "
+                                                    "scheduled arrival"},
+        "roofline": {"bound": "hbm", "achieved": round(r["achieved_gbs"], 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(r["achieved_gbs"] / peak, 4),
+                     "traffic": None, "peak_kind": peak_kind,
+                     "basis": "4 B (FP16) / 8 B (split) per point-update over the arrival-to-"
+                              "last-completion span"},
+        "e2e": {"value": round(r["gpts"], 3), "unit": "Gpts/s",
+                "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                "api": "tcs_server_submit with pinned host grids; every request's host grid "
+                       "goes in and its result comes back inside the span"},
+        "serving": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()},
+        "gpu_launches": r["rounds"],
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.profile:
         run_profile(args)
+    elif args.impl == "ours" and args.workload == "serve":
+        run_serve(args)
+    elif args.impl == "ours" and args.workload == "batch":
+        run_batch(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

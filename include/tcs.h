@@ -247,6 +247,59 @@ int tcs_batch_run(tcs_batch batch, int use_graph, void *stream);
 /* Point updates per run, work items per run and the number of grids. */
 int tcs_batch_info(tcs_batch batch, long long *point_updates, int *items, int *grids);
 
+/* ---------------------------------------------------------------- serving
+ * A request server does continuous batching of stencil solves on one GPU.
+ * No reference counterpart.  A native scheduler thread does the work:
+ *   - admits queued requests while the HBM budget has room for their state
+ *     (ping-pong planes plus an FP32 staging grid);
+ *   - uploads and packs each one on a copy stream;
+ *   - folds every resident request into the next round, which is ONE batched
+ *     persistent launch advancing each request by up to round_steps steps
+ *     (all of its remaining steps when round_steps is 0);
+ *   - unpacks and downloads finished requests while later rounds run, then
+ *     frees their memory.
+ * A request's state stays on the device between rounds.  A request that
+ * arrives while a round runs joins a following round.  Results are
+ * bit-identical to the same problem run alone (tcs_plan, tensor engine). */
+typedef struct tcs_server_s *tcs_server;
+
+typedef struct tcs_server_config {
+    size_t hbm_budget_bytes; /* device memory for request state (allocated once) */
+    int max_active;          /* resident requests at most (0 = 1024)            */
+    int round_steps;         /* steps per request per round (0 = all remaining)  */
+} tcs_server_config;
+
+typedef struct tcs_server_stats {
+    long long submitted, completed, failed;
+    long long rounds;
+    long long point_updates;   /* completed requests' interior point-updates */
+    long long algorithmic_bytes; /* 4 B (FP16) / 8 B (split) per point-update  */
+    double gpu_busy_s;         /* sum of round durations (CUDA events)       */
+    size_t budget_bytes, peak_bytes_in_use;
+    int active, queued;
+} tcs_server_stats;
+
+int tcs_server_create(const tcs_server_config *config, tcs_server *out);
+/* Waits for every submitted request, stops the scheduler, frees everything. */
+int tcs_server_destroy(tcs_server server);
+/* Queues a solve: `steps` steps of `problem` (tensor engine, F16 or SPLIT)
+ * from the ny x nx FP32 grid h_in into h_out.  Both are host buffers, ideally
+ * pinned.  They belong to the server until the ticket completes.  Fails with
+ * TCS_ERR_NOMEM when the request alone exceeds the budget. */
+int tcs_server_submit(tcs_server server, const tcs_problem *problem, int steps, const float *h_in,
+                      float *h_out, long long *ticket);
+/* Ticket state: 0 queued, 1 resident, 2 done, 3 failed; *status = its status. */
+int tcs_server_poll(tcs_server server, long long ticket, int *state, int *status);
+/* Blocks until the ticket is done or failed, or until timeout_s (< 0: no limit). */
+int tcs_server_wait(tcs_server server, long long ticket, double timeout_s);
+/* Seconds, on the server's clock, of the ticket's submission, admission and
+ * completion (its result in h_out). */
+int tcs_server_times(tcs_server server, long long ticket, double *submitted, double *admitted,
+                     double *completed);
+/* The server's clock (seconds since creation). */
+double tcs_server_clock(tcs_server server);
+int tcs_server_get_stats(tcs_server server, tcs_server_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,20 @@ class Problem(ctypes.Structure):
                 ("coeffs", ctypes.POINTER(ctypes.c_float))]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_active", ctypes.c_int),
+                ("round_steps", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong),
+                ("failed", ctypes.c_longlong), ("rounds", ctypes.c_longlong),
+                ("point_updates", ctypes.c_longlong), ("algorithmic_bytes", ctypes.c_longlong),
+                ("gpu_busy_s", ctypes.c_double), ("budget_bytes", ctypes.c_size_t),
+                ("peak_bytes_in_use", ctypes.c_size_t), ("active", ctypes.c_int),
+                ("queued", ctypes.c_int)]
+
+
 _lib = None
 
 # name -> (restype, argtypes) for every function include/tcs.h declares
@@ -106,6 +120,16 @@ SIGNATURES = {
     "tcs_batch_run": (_I, [_P, _I, _P]),
     "tcs_batch_info": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I),
                             ctypes.POINTER(_I)]),
+    "tcs_server_create": (_I, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
+    "tcs_server_destroy": (_I, [_P]),
+    "tcs_server_submit": (_I, [_P, ctypes.POINTER(Problem), _I, _P, _P,
+                               ctypes.POINTER(ctypes.c_longlong)]),
+    "tcs_server_poll": (_I, [_P, ctypes.c_longlong, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "tcs_server_wait": (_I, [_P, ctypes.c_longlong, ctypes.c_double]),
+    "tcs_server_times": (_I, [_P, ctypes.c_longlong, ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "tcs_server_clock": (ctypes.c_double, [_P]),
+    "tcs_server_get_stats": (_I, [_P, ctypes.POINTER(ServerStats)]),
 }
 
 
@@ -350,6 +374,73 @@ class Batch:
         pu, it, g = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
         _check(lib().tcs_batch_info(self._h, ctypes.byref(pu), ctypes.byref(it), ctypes.byref(g)))
         return pu.value, it.value, g.value
+
+
+class Server:
+    """Continuous-batching request server (tcs_server_*).  submit() hands the
+    host buffers to the server until the ticket completes; keep references to
+    them (this wrapper does) until then."""
+
+    def __init__(self, hbm_budget_bytes: int, max_active: int = 0, round_steps: int = 0):
+        cfg = ServerConfig(int(hbm_budget_bytes), int(max_active), int(round_steps))
+        h = ctypes.c_void_p()
+        _check(lib().tcs_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._held = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _check(lib().tcs_server_destroy(self._h))
+            self._h = None
+            self._held.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, grid: np.ndarray, out: np.ndarray, stencil: str, coeffs, steps: int,
+               precision: str = "f16", rect=None) -> int:
+        """Queues `steps` steps of a tensor-engine solve from `grid` into `out`
+        (both ny x nx float32 host arrays, ideally pinned); returns the ticket."""
+        assert grid.dtype == np.float32 and out.dtype == np.float32 and grid.shape == out.shape
+        assert grid.flags.c_contiguous and out.flags.c_contiguous
+        ny, nx = grid.shape
+        c = _coeffs(coeffs, stencil)
+        y0, y1, x0, x1 = _rect(rect)
+        pr = Problem(ny, nx, STENCILS[stencil], ENGINES["tensor"], PRECISIONS[precision], y0, y1,
+                     x0, x1, c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        t = ctypes.c_longlong()
+        _check(lib().tcs_server_submit(self._h, ctypes.byref(pr), int(steps), _ptr(grid),
+                                       _ptr(out), ctypes.byref(t)))
+        self._held[t.value] = (grid, out)
+        return t.value
+
+    def poll(self, ticket: int):
+        """(state, status): state 0 queued, 1 resident, 2 done, 3 failed."""
+        st, status = ctypes.c_int(), ctypes.c_int()
+        _check(lib().tcs_server_poll(self._h, ticket, ctypes.byref(st), ctypes.byref(status)))
+        return st.value, status.value
+
+    def wait(self, ticket: int, timeout: float = -1.0) -> None:
+        _check(lib().tcs_server_wait(self._h, ticket, float(timeout)))
+        self._held.pop(ticket, None)
+
+    def times(self, ticket: int):
+        """(submitted, admitted, completed) on the server clock, seconds."""
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(lib().tcs_server_times(self._h, ticket, ctypes.byref(a), ctypes.byref(b),
+                                      ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def clock(self) -> float:
+        return lib().tcs_server_clock(self._h)
+
+    def stats(self) -> dict:
+        o = ServerStats()
+        _check(lib().tcs_server_get_stats(self._h, ctypes.byref(o)))
+        return {k: getattr(o, k) for k, _ in ServerStats._fields_}
 
 
 def sweep_host(h_in: np.ndarray, steps: int, stencil: str, coeffs, engine: str = "tensor",

@@ -12,6 +12,7 @@
 #include <tuple>
 #include <vector>
 
+#include "batch.h"
 #include "tcs_internal.h"
 
 namespace tcs {

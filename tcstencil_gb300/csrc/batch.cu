@@ -5,7 +5,7 @@
 // Work list.  Every (grid, step, tile) is one item; items are ordered step
 // major (all grids' first steps, then all second steps, ...), and CTA c takes
 // items c, c + G, c + 2G, ... (G = grid size <= SM count, one CTA per SM, all
-// co-resident).  An item of step t > 0 needs every tile of its grid's step
+// co-resident: the launch is cooperative).  An item of step t > 0 needs every tile of its grid's step
 // t - 1: the producer waits (bounded) on a per-(grid, step) completion counter
 // that the epilogue warps increment after their stores.  Those items come
 // earlier in the list, so a chain of waits always ends at an item whose inputs
@@ -26,6 +26,7 @@
 #include <memory>
 #include <vector>
 
+#include "batch.h"
 #include "tc_core.cuh"
 
 namespace tcs {
@@ -45,31 +46,6 @@ constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + 256;
 static_assert(kSmem <= 232448, "shared memory budget");
 static_assert(2 * kAccStride <= kTmemCols, "TMEM budget");
 
-struct BatchGrid {
-    uint16_t *plane[2][2];  // [ping-pong state][hi, lo]
-    PlaneGeom pg;
-    int y0, y1, x0, x1;
-    int tiles_x;
-    int n_tiles;
-    int r, box, split;
-    int steps;
-    int ctr_base;   // completion counter of step 0
-    int band_base;  // first band element in the band buffer
-    int state;      // which plane holds the current state (flipped after a run)
-};
-
-struct BatchItem {
-    int g, t, tile;
-};
-
-struct BatchParams {
-    const BatchGrid *grids;
-    const BatchItem *items;
-    int n_items;
-    unsigned *counters;
-    const uint16_t *bands;
-};
-
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -82,6 +58,14 @@ __global__ void build_bands_kernel(BatchGrid *grids, const float *coefs, uint16_
     const BatchGrid &g = grids[blockIdx.x];
     build_bands(bands + g.band_base, coefs + 25 * blockIdx.x, g.r, g.box, g.split, threadIdx.x,
                 blockDim.x);
+}
+
+struct BandArgs {
+    float coef[25];
+};
+
+__global__ void build_one_band_kernel(const BandArgs a, int r, int box, int split, uint16_t *dst) {
+    build_bands(dst, a.coef, r, box, split, threadIdx.x, blockDim.x);
 }
 
 __global__ void flip_states_kernel(BatchGrid *grids, int n) {
@@ -304,6 +288,51 @@ int g_sms = 0;
 
 }  // namespace
 
+cudaError_t batch_prepare(int *num_sms) {
+    if (!g_sms) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tc_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kSmem);
+        if (e != cudaSuccess) {
+            g_sms = 0;
+            return e;
+        }
+        if (g_sms <= 0) g_sms = 1;
+    }
+    if (num_sms) *num_sms = g_sms;
+    return cudaSuccess;
+}
+
+// Cooperative launch: every CTA of the grid is resident at once (or the
+// launch waits until it can be), which the cross-CTA step waits rely on even
+// when other kernels share the GPU.
+cudaError_t launch_batch(const BatchParams &p, int num_sms, cudaStream_t s) {
+    if (p.n_items <= 0) return cudaSuccess;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(p.n_items < num_sms ? p.n_items : num_sms);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = kSmem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, tc_batch_kernel, p);
+}
+
+cudaError_t launch_build_bands(const float *coef, int r, bool box, bool split, uint16_t *dst,
+                               cudaStream_t s) {
+    BandArgs a;
+    const int n = 2 * r + 1;
+    for (int k = 0; k < 25; k++) a.coef[k] = k < n * n ? coef[k] : 0.0f;
+    build_one_band_kernel<<<1, 256, 0, s>>>(a, r, box, split, dst);
+    return cudaGetLastError();
+}
+
 cudaError_t batch_take_error(int *code) {
     int zero = 0;
     cudaError_t e = cudaMemcpyFromSymbol(code, g_batch_error, sizeof(int));
@@ -401,7 +430,7 @@ int batch_build(tcs_batch b) {
         G.band_base = band;
         G.state = 0;
         ctr += std::max(e.steps, 1);
-        band += (split ? 4 : 1) * (2 * G.r + 1) * kBandElems;
+        band += batch_band_elems(G.r, split);
         max_steps = std::max(max_steps, e.steps);
         std::memcpy(&coefs[25 * i], e.coeffs, sizeof(e.coeffs));
         b->point_updates += (long long)(e.g.y1 - e.g.y0) * (e.g.x1 - e.g.x0) * e.steps;
@@ -426,15 +455,8 @@ int batch_build(tcs_batch b) {
     build_bands_kernel<<<(unsigned)grids.size(), 256>>>(b->d_grids, b->d_coefs, b->d_bands);
     st = cuda_status(cudaGetLastError(), "band build launch");
     if (st) return st;
-    if (!g_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = 1;
-        st = cuda_status(cudaFuncSetAttribute(tc_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)kSmem), "batch kernel set-up");
-        if (st) return st;
-    }
+    st = cuda_status(batch_prepare(nullptr), "batch kernel set-up");
+    if (st) return st;
     b->built = true;
     return TCS_OK;
 }
@@ -443,18 +465,14 @@ int batch_enqueue(tcs_batch b, cudaStream_t s) {
     int st = cuda_status(cudaMemsetAsync(b->d_counters, 0, b->n_counters * sizeof(unsigned), s),
                          "counter reset");
     if (st) return st;
-    if (b->n_items > 0) {
-        BatchParams p;
-        p.grids = b->d_grids;
-        p.items = b->d_items;
-        p.n_items = b->n_items;
-        p.counters = b->d_counters;
-        p.bands = b->d_bands;
-        const int grid = std::min(b->n_items, g_sms);
-        tc_batch_kernel<<<grid, kThreads, kSmem, s>>>(p);
-        st = cuda_status(cudaGetLastError(), "batch kernel launch");
-        if (st) return st;
-    }
+    BatchParams p;
+    p.grids = b->d_grids;
+    p.items = b->d_items;
+    p.n_items = b->n_items;
+    p.counters = b->d_counters;
+    p.bands = b->d_bands;
+    st = cuda_status(launch_batch(p, g_sms, s), "batch kernel launch");
+    if (st) return st;
     const int n = (int)b->entries.size();
     flip_states_kernel<<<(n + 255) / 256, 256, 0, s>>>(b->d_grids, n);
     return cuda_status(cudaGetLastError(), "state flip launch");

@@ -118,10 +118,28 @@ __global__ void unpack_f32_kernel(const float *__restrict__ in, int ny, int nx, 
     }
 }
 
+// Scale exponent E of a grid whose max |x| has float bits `bits`: the
+// smallest E with max |x| < 2^E (frexp's exponent), 0 for an all-zero grid.
+__device__ __forceinline__ int scale_exp_of(unsigned bits) {
+    const float m = __uint_as_float(bits);
+    if (!(m > 0.0f) || !isfinite(m)) return 0;
+    int e = 0;
+    frexpf(m, &e);
+    return e;
+}
+
+// With max_bits set, the scale comes from the device-side maximum (and E is
+// written to exp_out), so that packing needs no host round trip.
 __global__ void pack_split_kernel(const float *__restrict__ in, int ny, int nx, int pad,
-                                  float pad_value, float scale, uint16_t *__restrict__ hi,
+                                  float pad_value, float scale, const unsigned *max_bits,
+                                  int *exp_out, uint16_t *__restrict__ hi,
                                   uint16_t *__restrict__ lo, PlaneGeom p, size_t n_rows) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (max_bits) {
+        const int e = scale_exp_of(*max_bits);
+        scale = ldexpf(1.0f, -e);
+        if (id == 0 && exp_out) *exp_out = e;
+    }
     if (id >= n_rows) return;
     const PanelRow r = panel_row(id, p);
     uint32_t wh[4], wl[4];
@@ -141,10 +159,11 @@ __global__ void pack_split_kernel(const float *__restrict__ in, int ny, int nx, 
 
 __global__ void unpack_split_kernel(const uint16_t *__restrict__ hi,
                                     const uint16_t *__restrict__ lo, int ny, int nx, int pad,
-                                    float scale, float *__restrict__ out, PlaneGeom p,
-                                    size_t n_rows) {
+                                    float scale, const int *exp_in, float *__restrict__ out,
+                                    PlaneGeom p, size_t n_rows) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_rows) return;
+    if (exp_in) scale = ldexpf(1.0f, *exp_in);
     const PanelRow r = panel_row(id, p);
     const int iy = r.Y - pad;
     if (iy < 0 || iy >= ny) return;
@@ -290,7 +309,16 @@ cudaError_t launch_pack_split(const float *in, int ny, int nx, int pad, float pa
                               int scale_exp, uint16_t *hi, uint16_t *lo, cudaStream_t s) {
     const PackShape ps = pack_shape(ny, nx, pad, 8);
     pack_split_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(
-        in, ny, nx, pad, pad_value, ldexpf(1.0f, -scale_exp), hi, lo, ps.p, ps.rows);
+        in, ny, nx, pad, pad_value, ldexpf(1.0f, -scale_exp), nullptr, nullptr, hi, lo, ps.p,
+        ps.rows);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_split_dev(const float *in, int ny, int nx, const unsigned *max_bits,
+                                  int *exp_out, uint16_t *hi, uint16_t *lo, cudaStream_t s) {
+    const PackShape ps = pack_shape(ny, nx, 0, 8);
+    pack_split_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(
+        in, ny, nx, 0, 0.0f, 1.0f, max_bits, exp_out, hi, lo, ps.p, ps.rows);
     return cudaGetLastError();
 }
 
@@ -298,7 +326,15 @@ cudaError_t launch_unpack_split(const uint16_t *hi, const uint16_t *lo, int ny, 
                                 int scale_exp, float *out, cudaStream_t s) {
     const PackShape ps = pack_shape(ny, nx, pad, 8);
     unpack_split_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(
-        hi, lo, ny, nx, pad, ldexpf(1.0f, scale_exp), out, ps.p, ps.rows);
+        hi, lo, ny, nx, pad, ldexpf(1.0f, scale_exp), nullptr, out, ps.p, ps.rows);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_split_dev(const uint16_t *hi, const uint16_t *lo, int ny, int nx,
+                                    const int *exp_in, float *out, cudaStream_t s) {
+    const PackShape ps = pack_shape(ny, nx, 0, 8);
+    unpack_split_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(hi, lo, ny, nx, 0, 1.0f, exp_in,
+                                                                 out, ps.p, ps.rows);
     return cudaGetLastError();
 }
 

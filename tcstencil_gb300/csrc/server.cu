@@ -1,0 +1,637 @@
+// Request server: continuous batching of stencil solves on one GPU
+// (tcs_server_*).  No reference counterpart: the reference runs one grid per
+// process; this serves many concurrent solves through the batched persistent
+// kernel (batch.cu).
+//
+// Threads and streams.  Callers submit from any thread into a FIFO queue.  One
+// scheduler thread owns everything on the device:
+//   admit   - while the budget has room: carve the request's block (ping-pong
+//             planes + FP32 staging grid) from one pre-allocated device region
+//             (first-fit, coalescing), then on the copy stream: H2D, max |x|
+//             (split), pack, coefficient bands; event `ready`.
+//   round   - every resident request with steps left, up to round_steps each,
+//             becomes one work list; on the compute stream: wait for the
+//             `ready` events of new requests, H2D of descriptors and items,
+//             counter reset, ONE cooperative batched launch.  Two rounds may
+//             be in flight (double-buffered descriptor memory), so the host
+//             builds round k+1 while round k runs.
+//   finish  - requests whose last step is in the round: on the copy stream,
+//             after the round's end event: unpack, D2H into the caller's
+//             buffer, host callback (completion time, wake waiters).
+//   reap    - completed requests return their block and band slot.
+// The split scale exponent is computed and consumed on the device, so no step
+// of a request needs a host round trip.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <iterator>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "batch.h"
+
+namespace tcs {
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+// First-fit allocator over the offsets of one device region; freed ranges
+// coalesce with their neighbours.
+class RangeAllocator {
+  public:
+    void reset(size_t capacity) {
+        free_.clear();
+        if (capacity) free_[0] = capacity;
+        used_ = peak_ = 0;
+    }
+    bool alloc(size_t bytes, size_t *off) {
+        bytes = align_up(bytes);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < bytes) continue;
+            *off = it->first;
+            const size_t rest = it->second - bytes, at = it->first + bytes;
+            free_.erase(it);
+            if (rest) free_[at] = rest;
+            used_ += bytes;
+            peak_ = std::max(peak_, used_);
+            return true;
+        }
+        return false;
+    }
+    void release(size_t off, size_t bytes) {
+        bytes = align_up(bytes);
+        used_ -= bytes;
+        auto next = free_.lower_bound(off);
+        if (next != free_.begin()) {
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == off) {
+                off = prev->first;
+                bytes += prev->second;
+                free_.erase(prev);
+            }
+        }
+        if (next != free_.end() && off + bytes == next->first) {
+            bytes += next->second;
+            free_.erase(next);
+        }
+        free_[off] = bytes;
+    }
+    size_t peak() const { return peak_; }
+
+  private:
+    std::map<size_t, size_t> free_;
+    size_t used_ = 0, peak_ = 0;
+};
+
+enum TicketState { kQueued = 0, kResident = 1, kDone = 2, kFailed = 3 };
+
+}  // namespace
+}  // namespace tcs
+
+using namespace tcs;
+
+struct tcs_server_s;
+
+namespace {
+
+struct Request {
+    long long ticket = 0;
+    tcs_server_s *srv = nullptr;
+    int stencil = 0, r = 0;
+    bool box = false, split = false;
+    float coeffs[25];
+    GridGeom g;
+    int steps = 0, done_steps = 0;
+    const float *h_in = nullptr;
+    float *h_out = nullptr;
+    size_t plane_bytes = 0, bytes = 0, off = 0;
+    int slot = -1;
+    bool waited = false;  // the compute stream already waits on `ready`
+    cudaEvent_t ready = nullptr;
+    int state = kQueued;  // guarded by the server mutex
+    int status = TCS_OK;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    long long updates() const {
+        return (long long)(g.y1 - g.y0) * (g.x1 - g.x0) * steps;
+    }
+};
+
+}  // namespace
+
+struct tcs_server_s {
+    tcs_server_config cfg{};
+    uint8_t *pool = nullptr;
+    RangeAllocator alloc;
+    int sms = 1;
+    cudaStream_t compute = nullptr, copy = nullptr;
+    uint16_t *d_bands = nullptr;
+    unsigned *d_maxbits = nullptr;
+    int *d_exp = nullptr;
+    std::vector<int> free_slots;
+
+    // double-buffered round descriptors
+    struct RoundBuf {
+        BatchGrid *h_grids = nullptr, *d_grids = nullptr;
+        BatchItem *h_items = nullptr, *d_items = nullptr;
+        unsigned *d_counters = nullptr;
+        size_t cap_hg = 0, cap_hi = 0, cap_dg = 0, cap_di = 0, cap_dc = 0;
+        cudaEvent_t start = nullptr, end = nullptr;
+        bool pending = false;
+    } rb[2];
+    long long round_idx = 0;
+
+    std::mutex mu;
+    std::condition_variable cv_sched, cv_done;
+    std::deque<Request *> queued;
+    std::vector<Request *> active;    // scheduler thread only
+    std::vector<Request *> finished;  // from host callbacks, guarded by mu
+    std::unordered_map<long long, std::unique_ptr<Request>> tickets;
+    long long next_ticket = 1;
+    bool stop = false;
+    bool new_work = false;
+    size_t peak_bytes = 0;
+    std::thread worker;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+
+    // stats, guarded by mu
+    long long submitted = 0, completed = 0, failed = 0, rounds = 0;
+    long long point_updates = 0, alg_bytes = 0;
+    double busy_s = 0.0;
+    int n_active = 0;
+
+    double now() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    uint16_t *plane(const Request *q, int s, int pl) const {
+        return reinterpret_cast<uint16_t *>(pool + q->off + (size_t)(2 * s + pl) * q->plane_bytes);
+    }
+    float *staging(const Request *q) const {
+        return reinterpret_cast<float *>(pool + q->off + 4 * q->plane_bytes);
+    }
+
+    void loop();
+    void reap(std::vector<Request *> &done);
+    void admit();
+    void poll_rounds();
+    bool launch_round();
+    void fail_request(Request *q, int status);
+};
+
+namespace {
+
+void CUDART_CB on_request_done(void *arg) {
+    Request *q = static_cast<Request *>(arg);
+    tcs_server_s *s = q->srv;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        q->t_done = s->now();
+        q->state = kDone;
+        s->finished.push_back(q);
+    }
+    s->cv_done.notify_all();
+    s->cv_sched.notify_one();
+}
+
+template <typename T>
+int grow_pinned(T **h, size_t *cap, size_t want) {
+    if (*cap >= want) return TCS_OK;
+    const size_t n = std::max(want, *cap * 2);
+    if (*h) cudaFreeHost(*h);
+    *h = nullptr;
+    *cap = 0;
+    int st = cuda_status(cudaMallocHost(reinterpret_cast<void **>(h), n * sizeof(T)), "cudaMallocHost(round)");
+    if (!st) *cap = n;
+    return st;
+}
+
+template <typename T>
+int grow_device(T **d, size_t *cap, size_t want) {
+    if (*cap >= want) return TCS_OK;
+    const size_t n = std::max(want, *cap * 2);
+    if (*d) cudaFree(*d);
+    *d = nullptr;
+    *cap = 0;
+    int st = cuda_status(cudaMalloc(reinterpret_cast<void **>(d), n * sizeof(T)), "cudaMalloc(round)");
+    if (!st) *cap = n;
+    return st;
+}
+
+}  // namespace
+
+void tcs_server_s::fail_request(Request *q, int status) {
+    std::lock_guard<std::mutex> lk(mu);
+    q->status = status;
+    q->state = kFailed;
+    q->t_done = now();
+    finished.push_back(q);
+    cv_done.notify_all();
+}
+
+void tcs_server_s::reap(std::vector<Request *> &done) {
+    for (Request *q : done) {
+        if (q->slot >= 0) {
+            alloc.release(q->off, q->bytes);
+            free_slots.push_back(q->slot);
+            q->slot = -1;
+        }
+        if (q->ready) {
+            cudaEventDestroy(q->ready);
+            q->ready = nullptr;
+        }
+        auto it = std::find(active.begin(), active.end(), q);
+        if (it != active.end()) active.erase(it);
+        std::lock_guard<std::mutex> lk(mu);
+        if (q->state == kDone) {
+            completed++;
+            point_updates += q->updates();
+            alg_bytes += (q->split ? 8 : 4) * q->updates();
+        } else {
+            failed++;
+        }
+        n_active = (int)active.size();
+    }
+    done.clear();
+}
+
+void tcs_server_s::admit() {
+    while (true) {
+        Request *q;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            if (queued.empty()) return;
+            q = queued.front();
+        }
+        if ((int)active.size() >= cfg.max_active || free_slots.empty()) return;
+        size_t off;
+        if (!alloc.alloc(q->bytes, &off)) return;  // head of line waits for memory
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            queued.pop_front();
+            q->state = kResident;
+            q->t_admit = now();
+        }
+        q->off = off;
+        q->slot = free_slots.back();
+        free_slots.pop_back();
+        active.push_back(q);
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            n_active = (int)active.size();
+            peak_bytes = alloc.peak();
+        }
+        const size_t cells = (size_t)q->g.ny * q->g.nx;
+        float *stg = staging(q);
+        unsigned *mx = d_maxbits + q->slot;
+        int st = cuda_status(cudaMemcpyAsync(stg, q->h_in, cells * sizeof(float), cudaMemcpyHostToDevice, copy), "request upload");
+        // state-1 planes: padding cells must be finite (pack writes all of state 0)
+        if (!st) st = cuda_status(cudaMemsetAsync(plane(q, 1, 0), 0, 2 * q->plane_bytes, copy), "plane clear");
+        if (!st && q->split) {
+            st = cuda_status(cudaMemsetAsync(mx, 0, sizeof(unsigned), copy), "max clear");
+            if (!st) st = cuda_status(launch_max_abs(stg, cells, mx, copy), "max_abs launch");
+            if (!st) st = cuda_status(launch_pack_split_dev(stg, q->g.ny, q->g.nx, mx, d_exp + q->slot, plane(q, 0, 0), plane(q, 0, 1), copy), "pack launch");
+        } else if (!st) {
+            st = cuda_status(launch_pack_f16(stg, q->g.ny, q->g.nx, 0, 0.0f, plane(q, 0, 0), copy), "pack launch");
+        }
+        if (!st) st = cuda_status(launch_build_bands(q->coeffs, q->r, q->box, q->split, d_bands + (size_t)q->slot * kBatchMaxBandElems, copy), "band build");
+        if (!st) st = cuda_status(cudaEventRecord(q->ready, copy), "cudaEventRecord");
+        if (st) {
+            fail_request(q, st);
+            continue;
+        }
+        if (q->steps == 0) {
+            // nothing to sweep: the result is the stored input
+            if (q->split) st = cuda_status(launch_unpack_split_dev(plane(q, 0, 0), plane(q, 0, 1), q->g.ny, q->g.nx, d_exp + q->slot, stg, copy), "unpack launch");
+            else st = cuda_status(launch_unpack_f16(plane(q, 0, 0), q->g.ny, q->g.nx, 0, stg, copy), "unpack launch");
+            if (!st) st = cuda_status(cudaMemcpyAsync(q->h_out, stg, cells * sizeof(float), cudaMemcpyDeviceToHost, copy), "request download");
+            if (!st) st = cuda_status(cudaLaunchHostFunc(copy, on_request_done, q), "cudaLaunchHostFunc");
+            if (st) fail_request(q, st);
+        }
+    }
+}
+
+void tcs_server_s::poll_rounds() {
+    for (auto &b : rb) {
+        if (!b.pending || cudaEventQuery(b.end) != cudaSuccess) continue;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, b.start, b.end);
+        b.pending = false;
+        std::lock_guard<std::mutex> lk(mu);
+        busy_s += ms * 1e-3;
+        rounds++;
+    }
+}
+
+// Builds and enqueues one round; false when there was nothing to run or no
+// free round buffer.
+bool tcs_server_s::launch_round() {
+    RoundBuf &b = rb[round_idx & 1];
+    if (b.pending) return false;  // its previous round still runs
+    std::vector<Request *> part;
+    for (Request *q : active)
+        if (q->state == kResident && q->done_steps < q->steps) part.push_back(q);
+    if (part.empty()) return false;
+
+    std::vector<int> run_steps(part.size());
+    size_t n_items = 0, n_ctr = 0;
+    int max_s = 0;
+    for (size_t i = 0; i < part.size(); i++) {
+        const Request *q = part[i];
+        const int rem = q->steps - q->done_steps;
+        run_steps[i] = cfg.round_steps > 0 ? std::min(rem, cfg.round_steps) : rem;
+        const size_t tiles = (size_t)((q->g.ny + kTile - 1) / kTile) * ((q->g.nx + kTile - 1) / kTile);
+        n_items += tiles * run_steps[i];
+        n_ctr += run_steps[i];
+        max_s = std::max(max_s, run_steps[i]);
+    }
+    // buffer b is idle (its last round completed), so it may be regrown
+    int st = grow_pinned(&b.h_grids, &b.cap_hg, part.size());
+    if (!st) st = grow_pinned(&b.h_items, &b.cap_hi, n_items);
+    if (!st) st = grow_device(&b.d_grids, &b.cap_dg, part.size());
+    if (!st) st = grow_device(&b.d_items, &b.cap_di, n_items);
+    if (!st) st = grow_device(&b.d_counters, &b.cap_dc, n_ctr);
+    if (st) {
+        for (Request *q : part) fail_request(q, st);
+        return true;
+    }
+    int ctr = 0;
+    for (size_t i = 0; i < part.size(); i++) {
+        Request *q = part[i];
+        BatchGrid &G = b.h_grids[i];
+        for (int s = 0; s < 2; s++) {
+            G.plane[s][0] = plane(q, s, 0);
+            G.plane[s][1] = q->split ? plane(q, s, 1) : nullptr;
+        }
+        G.pg = q->g.p16;
+        G.y0 = q->g.y0; G.y1 = q->g.y1; G.x0 = q->g.x0; G.x1 = q->g.x1;
+        G.tiles_x = (q->g.nx + kTile - 1) / kTile;
+        G.n_tiles = G.tiles_x * ((q->g.ny + kTile - 1) / kTile);
+        G.r = q->r;
+        G.box = q->box;
+        G.split = q->split;
+        G.steps = run_steps[i];
+        G.ctr_base = ctr;
+        G.band_base = q->slot * kBatchMaxBandElems;
+        G.state = q->done_steps & 1;
+        ctr += run_steps[i];
+    }
+    size_t k = 0;
+    for (int t = 0; t < max_s; t++)
+        for (size_t i = 0; i < part.size(); i++)
+            if (run_steps[i] > t)
+                for (int tile = 0; tile < b.h_grids[i].n_tiles; tile++)
+                    b.h_items[k++] = BatchItem{(int)i, t, tile};
+
+    for (Request *q : part)
+        if (!q->waited) {
+            if (!st) st = cuda_status(cudaStreamWaitEvent(compute, q->ready, 0), "cudaStreamWaitEvent");
+            q->waited = true;
+        }
+    if (!st) st = cuda_status(cudaMemcpyAsync(b.d_grids, b.h_grids, part.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice, compute), "round descriptors");
+    if (!st) st = cuda_status(cudaMemcpyAsync(b.d_items, b.h_items, n_items * sizeof(BatchItem), cudaMemcpyHostToDevice, compute), "round items");
+    if (!st) st = cuda_status(cudaMemsetAsync(b.d_counters, 0, n_ctr * sizeof(unsigned), compute), "round counters");
+    if (!st) st = cuda_status(cudaEventRecord(b.start, compute), "cudaEventRecord");
+    if (!st) {
+        BatchParams p;
+        p.grids = b.d_grids;
+        p.items = b.d_items;
+        p.n_items = (int)n_items;
+        p.counters = b.d_counters;
+        p.bands = d_bands;
+        st = cuda_status(launch_batch(p, sms, compute), "batch launch");
+    }
+    if (!st) st = cuda_status(cudaEventRecord(b.end, compute), "cudaEventRecord");
+    if (st) {
+        for (Request *q : part) fail_request(q, st);
+        return true;
+    }
+    b.pending = true;
+    round_idx++;
+    bool waited_round = false;
+    for (size_t i = 0; i < part.size(); i++) {
+        Request *q = part[i];
+        q->done_steps += run_steps[i];
+        if (q->done_steps < q->steps) continue;
+        // finished in this round: unpack and download behind it
+        const int cur = q->done_steps & 1;
+        const size_t cells = (size_t)q->g.ny * q->g.nx;
+        float *stg = staging(q);
+        int rs = TCS_OK;
+        if (!waited_round) {
+            rs = cuda_status(cudaStreamWaitEvent(copy, b.end, 0), "cudaStreamWaitEvent");
+            waited_round = true;
+        }
+        if (!rs) {
+            if (q->split) rs = cuda_status(launch_unpack_split_dev(plane(q, cur, 0), plane(q, cur, 1), q->g.ny, q->g.nx, d_exp + q->slot, stg, copy), "unpack launch");
+            else rs = cuda_status(launch_unpack_f16(plane(q, cur, 0), q->g.ny, q->g.nx, 0, stg, copy), "unpack launch");
+        }
+        if (!rs) rs = cuda_status(cudaMemcpyAsync(q->h_out, stg, cells * sizeof(float), cudaMemcpyDeviceToHost, copy), "request download");
+        if (!rs) rs = cuda_status(cudaLaunchHostFunc(copy, on_request_done, q), "cudaLaunchHostFunc");
+        if (rs) fail_request(q, rs);
+    }
+    return true;
+}
+
+void tcs_server_s::loop() {
+    std::vector<Request *> done;
+    bool progressed = true;
+    while (true) {
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            // Sleep unless the last pass made progress; submissions, completions
+            // and stop wake the thread, and rounds are polled every 50 us.
+            if (!progressed)
+                cv_sched.wait_for(lk, std::chrono::microseconds(50),
+                                  [&] { return stop || new_work || !finished.empty(); });
+            new_work = false;
+            done.swap(finished);
+            if (stop && queued.empty() && active.empty() && done.empty()) break;
+        }
+        const size_t before = active.size();
+        const bool reaped = !done.empty();
+        reap(done);
+        admit();
+        poll_rounds();
+        const bool launched = launch_round();
+        progressed = reaped || launched || active.size() != before;
+    }
+}
+
+// ================================================================ C-ABI ==
+extern "C" {
+
+int tcs_server_create(const tcs_server_config *config, tcs_server *out) {
+    if (!config || !out || config->hbm_budget_bytes == 0 || config->round_steps < 0 ||
+        config->max_active < 0)
+        return fail(TCS_ERR_INVALID, "tcs_server_create: bad configuration");
+    *out = nullptr;
+    std::unique_ptr<tcs_server_s> s(new tcs_server_s());
+    s->cfg = *config;
+    if (s->cfg.max_active == 0) s->cfg.max_active = 1024;
+    s->cfg.hbm_budget_bytes = align_up(s->cfg.hbm_budget_bytes);
+    int st = cuda_status(batch_prepare(&s->sms), "batch kernel set-up");
+    if (!st) st = cuda_status(cudaMalloc(&s->pool, s->cfg.hbm_budget_bytes), "cudaMalloc(server budget)");
+    if (st) {
+        if (st == TCS_ERR_CUDA) return fail(TCS_ERR_NOMEM, "cannot reserve %zu bytes of device memory", s->cfg.hbm_budget_bytes);
+        return st;
+    }
+    s->alloc.reset(s->cfg.hbm_budget_bytes);
+    const int slots = s->cfg.max_active;
+    if (!st) st = cuda_status(cudaMalloc(&s->d_bands, (size_t)slots * kBatchMaxBandElems * sizeof(uint16_t)), "cudaMalloc(bands)");
+    if (!st) st = cuda_status(cudaMalloc(&s->d_maxbits, slots * sizeof(unsigned)), "cudaMalloc(max)");
+    if (!st) st = cuda_status(cudaMalloc(&s->d_exp, slots * sizeof(int)), "cudaMalloc(exp)");
+    if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (auto &b : s->rb) {
+        if (!st) st = cuda_status(cudaEventCreate(&b.start), "cudaEventCreate");
+        if (!st) st = cuda_status(cudaEventCreate(&b.end), "cudaEventCreate");
+    }
+    if (st) {
+        tcs_server_destroy(s.release());
+        return st;
+    }
+    for (int i = slots - 1; i >= 0; i--) s->free_slots.push_back(i);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    tcs_server_s *raw = s.get();
+    s->worker = std::thread([raw, dev] {
+        cudaSetDevice(dev);
+        raw->loop();
+    });
+    *out = s.release();
+    return TCS_OK;
+}
+
+int tcs_server_destroy(tcs_server s) {
+    if (!s) return TCS_OK;
+    if (s->worker.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stop = true;
+        }
+        s->cv_sched.notify_one();
+        s->worker.join();
+    }
+    if (s->compute) cudaStreamSynchronize(s->compute);
+    if (s->copy) cudaStreamSynchronize(s->copy);
+    for (auto &b : s->rb) {
+        if (b.start) cudaEventDestroy(b.start);
+        if (b.end) cudaEventDestroy(b.end);
+        if (b.h_grids) cudaFreeHost(b.h_grids);
+        if (b.h_items) cudaFreeHost(b.h_items);
+        for (void *p : {(void *)b.d_grids, (void *)b.d_items, (void *)b.d_counters})
+            if (p) cudaFree(p);
+    }
+    for (auto &kv : s->tickets)
+        if (kv.second->ready) cudaEventDestroy(kv.second->ready);
+    for (void *p : {(void *)s->pool, (void *)s->d_bands, (void *)s->d_maxbits, (void *)s->d_exp})
+        if (p) cudaFree(p);
+    if (s->compute) cudaStreamDestroy(s->compute);
+    if (s->copy) cudaStreamDestroy(s->copy);
+    delete s;
+    return TCS_OK;
+}
+
+int tcs_server_submit(tcs_server s, const tcs_problem *pr, int steps, const float *h_in,
+                      float *h_out, long long *ticket) {
+    if (!s || !pr || !pr->coeffs || !h_in || !h_out || steps < 0)
+        return fail(TCS_ERR_INVALID, "tcs_server_submit: bad arguments");
+    if (pr->engine != TCS_ENGINE_TENSOR || (pr->precision != TCS_PREC_F16 && pr->precision != TCS_PREC_SPLIT))
+        return fail(TCS_ERR_UNSUPPORTED, "the server runs the tensor engine, FP16 or split precision");
+    std::unique_ptr<Request> q(new Request());
+    int st = make_geom(pr->ny, pr->nx, pr->stencil, pr->y0, pr->y1, pr->x0, pr->x1, &q->g);
+    if (st) return st;
+    q->stencil = pr->stencil;
+    q->r = stencil_r(pr->stencil);
+    q->box = stencil_box(pr->stencil);
+    q->split = pr->precision == TCS_PREC_SPLIT;
+    const int n = 2 * q->r + 1;
+    for (int k = 0; k < 25; k++) q->coeffs[k] = k < n * n ? pr->coeffs[k] : 0.0f;
+    if (q->split && !(tap_abs_sum(pr->stencil, q->coeffs) <= kSplitMaxAbsSum))
+        return fail(TCS_ERR_UNSUPPORTED, "split precision needs a non-expanding stencil (sum of |c| <= 1)");
+    q->steps = steps;
+    q->h_in = h_in;
+    q->h_out = h_out;
+    q->srv = s;
+    q->plane_bytes = align_up(plane_elems(q->g.p16) * sizeof(uint16_t));
+    q->bytes = 4 * q->plane_bytes + align_up((size_t)q->g.ny * q->g.nx * sizeof(float));
+    if (q->bytes > s->cfg.hbm_budget_bytes)
+        return fail(TCS_ERR_NOMEM, "request needs %zu bytes, the server budget is %zu", q->bytes, s->cfg.hbm_budget_bytes);
+    st = cuda_status(cudaEventCreateWithFlags(&q->ready, cudaEventDisableTiming), "cudaEventCreate");
+    if (st) return st;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        q->ticket = s->next_ticket++;
+        q->t_submit = s->now();
+        if (ticket) *ticket = q->ticket;
+        s->queued.push_back(q.get());
+        s->submitted++;
+        s->new_work = true;
+        s->tickets.emplace(q->ticket, std::move(q));
+    }
+    s->cv_sched.notify_one();
+    return TCS_OK;
+}
+
+int tcs_server_poll(tcs_server s, long long ticket, int *state, int *status) {
+    if (!s) return fail(TCS_ERR_INVALID, "tcs_server_poll: null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return fail(TCS_ERR_INVALID, "unknown ticket %lld", ticket);
+    if (state) *state = it->second->state;
+    if (status) *status = it->second->status;
+    return TCS_OK;
+}
+
+int tcs_server_wait(tcs_server s, long long ticket, double timeout_s) {
+    if (!s) return fail(TCS_ERR_INVALID, "tcs_server_wait: null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return fail(TCS_ERR_INVALID, "unknown ticket %lld", ticket);
+    Request *q = it->second.get();
+    auto finished = [&] { return q->state == kDone || q->state == kFailed; };
+    if (timeout_s < 0) s->cv_done.wait(lk, finished);
+    else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), finished))
+        return fail(TCS_ERR_TIMEOUT, "ticket %lld not finished after %.3f s", ticket, timeout_s);
+    return q->state == kDone ? TCS_OK : q->status;
+}
+
+int tcs_server_times(tcs_server s, long long ticket, double *submitted, double *admitted,
+                     double *completed) {
+    if (!s) return fail(TCS_ERR_INVALID, "tcs_server_times: null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return fail(TCS_ERR_INVALID, "unknown ticket %lld", ticket);
+    if (submitted) *submitted = it->second->t_submit;
+    if (admitted) *admitted = it->second->t_admit;
+    if (completed) *completed = it->second->t_done;
+    return TCS_OK;
+}
+
+double tcs_server_clock(tcs_server s) { return s ? s->now() : 0.0; }
+
+int tcs_server_get_stats(tcs_server s, tcs_server_stats *o) {
+    if (!s || !o) return fail(TCS_ERR_INVALID, "tcs_server_get_stats: null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    o->submitted = s->submitted;
+    o->completed = s->completed;
+    o->failed = s->failed;
+    o->rounds = s->rounds;
+    o->point_updates = s->point_updates;
+    o->algorithmic_bytes = s->alg_bytes;
+    o->gpu_busy_s = s->busy_s;
+    o->budget_bytes = s->cfg.hbm_budget_bytes;
+    o->peak_bytes_in_use = s->peak_bytes;
+    o->active = s->n_active;
+    o->queued = (int)s->queued.size();
+    return TCS_OK;
+}
+
+}  // extern "C"

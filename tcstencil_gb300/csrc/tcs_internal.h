@@ -112,7 +112,6 @@ cudaError_t launch_cc_f32(const GridGeom &g, int stencil, const TapCoeffs &c, co
 
 // Reads and clears the tensor kernels' device error word.
 cudaError_t tc_take_error(int *code);
-cudaError_t batch_take_error(int *code);
 // Configures the tensor kernel of (stencil, split) ahead of its first launch.
 cudaError_t tc_prepare(int stencil, bool split);
 
@@ -139,6 +138,12 @@ cudaError_t launch_pack_split(const float *in, int ny, int nx, int pad, float pa
 cudaError_t launch_unpack_split(const uint16_t *hi, const uint16_t *lo, int ny, int nx, int pad,
                                 int scale_exp, float *out, cudaStream_t s);
 // max |x| over n floats into *out_bits (float bits; *out_bits must start at 0)
+// Split pack/unpack (pad 0) with the scale exponent kept in device memory:
+// pack derives E from the max-|x| bits that launch_max_abs left and stores it.
+cudaError_t launch_pack_split_dev(const float *in, int ny, int nx, const unsigned *max_bits,
+                                  int *exp_out, uint16_t *hi, uint16_t *lo, cudaStream_t s);
+cudaError_t launch_unpack_split_dev(const uint16_t *hi, const uint16_t *lo, int ny, int nx,
+                                    const int *exp_in, float *out, cudaStream_t s);
 cudaError_t launch_max_abs(const float *in, size_t n, unsigned *out_bits, cudaStream_t s);
 // the reference's layout16 transforms (bricks of 16 x 16, row-major inside)
 cudaError_t launch_padding_2d(const uint16_t *in, uint16_t *out, int size, int halo,

@@ -139,3 +139,12 @@ def test_batch_add_validates_before_any_device_work(tcs):
     with pytest.raises(tcs.TcsError):
         b.add(64, 64, "box2d1r", c, -1)
     b.close()
+
+
+def test_server_config_is_validated_before_any_device_work(tcs):
+    import ctypes
+
+    h = ctypes.c_void_p()
+    for cfg in [tcs.ServerConfig(0, 0, 0), tcs.ServerConfig(1 << 20, -1, 0),
+                tcs.ServerConfig(1 << 20, 0, -2)]:
+        assert tcs.lib().tcs_server_create(ctypes.byref(cfg), ctypes.byref(h)) == tcs.TCS_ERR_INVALID
