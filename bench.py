@@ -59,6 +59,8 @@ def parse():
                          "persistent launch per run; serve: Poisson-arrival request serving")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-round-steps", type=int, default=None,
+                    help="steps per request per server round (default: autotuned or 16)")
     ap.add_argument("--batch-grids", type=int, default=512)
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: upload the grid, run --timesteps single-step "
@@ -277,7 +279,11 @@ def batch_leg(torch, tcs, K, W, stream, count=512):
             "e2e_h2d_bytes": host_bytes, "e2e_d2h_bytes": host_bytes}
 
 
-def serve_leg(tcs, seconds=10.0, rate=2000.0, budget_gb=120.0):
+def serve_round_steps(args):
+    return 16 if args.serve_round_steps is None else args.serve_round_steps
+
+
+def serve_leg(tcs, seconds=10.0, rate=2000.0, budget_gb=120.0, round_steps=16):
     """Served stencil solves: Poisson arrivals at `rate`/s for `seconds`, sides
     log-uniform in [128, 4096] per axis, random stencil and coefficients, 1-200
     steps, FP16 or split; admission against a `budget_gb` HBM budget."""
@@ -285,15 +291,16 @@ def serve_leg(tcs, seconds=10.0, rate=2000.0, budget_gb=120.0):
     from tcstencil_gb300.workloads import poisson_requests
 
     reqs = poisson_requests(rate=rate, duration=seconds)
-    srv = tcs.Server(int(budget_gb * 2**30))
+    srv = tcs.Server(int(budget_gb * 2**30), round_steps=round_steps)
     try:
-        res = replay(srv, reqs, InputPool(1 << 26), OutputRing(1 << 28))
+        res = replay(srv, reqs, InputPool(1 << 26), OutputRing(1 << 30))
     finally:
         srv.close()
     res["algorithmic_bytes"] = sum(r.spec.bytes for r in reqs)
     res["achieved_gbs"] = res["algorithmic_bytes"] / res["span_s"] / 1e9
     res["offered_gpts"] = res["point_updates"] / seconds / 1e9
     res["budget_gb"] = budget_gb
+    res["round_steps"] = round_steps
     return res
 
 
@@ -396,7 +403,7 @@ def run_ours(args):
         r = batch_leg(torch, tcs, 10, 3, stream)
         extras["batched_512_mixed"] = {k: round(v, 3) if isinstance(v, float) else v
                                        for k, v in r.items()}
-        r = serve_leg(tcs, args.serve_seconds, args.serve_rate)
+        r = serve_leg(tcs, args.serve_seconds, args.serve_rate, round_steps=serve_round_steps(args))
         extras["served_poisson"] = {k: round(v, 3) if isinstance(v, float) else v
                                     for k, v in r.items()}
     if ws > 1:
@@ -496,7 +503,7 @@ def run_serve(args):
     rank, local_rank, ws = dist_env()
     torch.cuda.set_device(local_rank)
     sampler = ClockSampler(local_rank) if rank == 0 else None
-    r = serve_leg(tcs, args.serve_seconds, args.serve_rate)
+    r = serve_leg(tcs, args.serve_seconds, args.serve_rate, round_steps=serve_round_steps(args))
     clocks = ClockSampler.summarize(sampler.stop()) if sampler else None
     if rank != 0:
         return

@@ -277,6 +277,12 @@ typedef struct tcs_server_stats {
     double gpu_busy_s;         /* sum of round durations (CUDA events)       */
     size_t budget_bytes, peak_bytes_in_use;
     int active, queued;
+    /* scheduler passes: time in reap, admit, round polling and round launch
+     * (total and the worst single pass), seconds */
+    double sched_total_s[4], sched_max_s[4];
+    /* round launch: host build of the round, compute-stream enqueue, and the
+     * enqueue of finished requests' downloads (total and worst), seconds */
+    double launch_total_s[3], launch_max_s[3];
 } tcs_server_stats;
 
 int tcs_server_create(const tcs_server_config *config, tcs_server *out);

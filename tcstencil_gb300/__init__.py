@@ -66,7 +66,9 @@ class ServerStats(ctypes.Structure):
                 ("point_updates", ctypes.c_longlong), ("algorithmic_bytes", ctypes.c_longlong),
                 ("gpu_busy_s", ctypes.c_double), ("budget_bytes", ctypes.c_size_t),
                 ("peak_bytes_in_use", ctypes.c_size_t), ("active", ctypes.c_int),
-                ("queued", ctypes.c_int)]
+                ("queued", ctypes.c_int), ("sched_total_s", ctypes.c_double * 4),
+                ("sched_max_s", ctypes.c_double * 4), ("launch_total_s", ctypes.c_double * 3),
+                ("launch_max_s", ctypes.c_double * 3)]
 
 
 _lib = None
@@ -440,7 +442,8 @@ class Server:
     def stats(self) -> dict:
         o = ServerStats()
         _check(lib().tcs_server_get_stats(self._h, ctypes.byref(o)))
-        return {k: getattr(o, k) for k, _ in ServerStats._fields_}
+        return {k: (list(getattr(o, k)) if k.startswith(("sched_", "launch_")) else getattr(o, k))
+                for k, _ in ServerStats._fields_}
 
 
 def sweep_host(h_in: np.ndarray, steps: int, stencil: str, coeffs, engine: str = "tensor",

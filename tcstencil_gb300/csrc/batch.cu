@@ -3,15 +3,19 @@
 // tensor-core launch.
 //
 // Work list.  Every (grid, step, tile) is one item; items are ordered step
-// major (all grids' first steps, then all second steps, ...), and CTA c takes
-// items c, c + G, c + 2G, ... (G = grid size <= SM count, one CTA per SM, all
-// co-resident: the launch is cooperative).  An item of step t > 0 needs every tile of its grid's step
-// t - 1: the producer waits (bounded) on a per-(grid, step) completion counter
-// that the epilogue warps increment after their stores.  Those items come
-// earlier in the list, so a chain of waits always ends at an item whose inputs
-// are ready: the launch cannot deadlock.  The same counters also guard the
-// ping-pong's write-after-read hazard: step t+1 overwrites the plane step t-1
-// read, and starts only after all of step t, hence all of step t-1, finished.
+// major (all grids' first steps, then all second steps, ...) and decoded from
+// their index on the device (BatchParams), so a run's description is a few
+// small tables however many items it has.  Each CTA (one per SM) takes the
+// next index from a global counter, so items are taken in order, and only by
+// running CTAs.  An item of step t > 0 needs every
+// tile of its grid's step t - 1: the producer waits (bounded) on a
+// per-(grid, step) completion counter that the epilogue warps increment after
+// their stores.  Those items come earlier in the list and so were taken by
+// running CTAs; the earliest unfinished item always has its inputs ready, so
+// the launch cannot deadlock, whatever else shares the GPU.
+// The same counters also guard the ping-pong's write-after-read hazard: step
+// t+1 overwrites the plane step t-1 read, and starts only after all of step t,
+// hence all of step t-1, finished.
 //
 // Per item the producer bulk-copies the tile's input panels AND the grid's
 // coefficient bands (prebuilt in global memory by build_bands_kernel) into the
@@ -42,7 +46,10 @@ constexpr int kMaxBandBytes = 4 * 5 * kBandBytes;  // split, radius 2
 constexpr int kStageBytes = 2 * kPlaneStage + kMaxBandBytes;
 constexpr int kAccStride = Mode<true>::ACC;        // TMEM columns per accumulator buffer
 constexpr int kTmemCols = 512;
-constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + 256;
+constexpr int kRing = 8;  // published work items in flight (> kStages + 2)
+constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + 512;
+static_assert(kRing > kStages + 2, "a ring slot is reused only after its item's epilogue");
+static_assert((2 * kStages + 5 + kRing) * 8 + kRing * 12 + 8 <= 512, "barrier area");
 static_assert(kSmem <= 232448, "shared memory budget");
 static_assert(2 * kAccStride <= kTmemCols, "TMEM budget");
 
@@ -53,6 +60,31 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 }
 
 __device__ __forceinline__ int sub_tiles(const BatchGrid &g) { return g.split ? 2 : 1; }
+
+// A bounded wait gave up: record the code in the launch's error word (which
+// every CTA polls to stop early) and in the unit's word tcs_device_error reads.
+__device__ __forceinline__ void batch_fail(const BatchParams &p, int code) {
+    record_error(p.error, code);
+    batch_fail(p, code);
+}
+
+// Work index k -> (grid, step, tile); see BatchParams.
+__device__ __forceinline__ BatchItem decode_item(const BatchParams &p, int k) {
+    int lo = 0, hi = p.n_steps;  // step_off[lo] <= k < step_off[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(p.step_off + mid) <= k) lo = mid;
+        else hi = mid;
+    }
+    const int local = k - __ldg(p.step_off + lo);
+    int a = 0, b = p.n_grids;  // tile_prefix[a] <= local < tile_prefix[b]
+    while (b - a > 1) {
+        const int mid = (a + b) >> 1;
+        if (__ldg(p.tile_prefix + mid) <= local) a = mid;
+        else b = mid;
+    }
+    return BatchItem{a, lo, local - __ldg(p.tile_prefix + a)};
+}
 
 __global__ void build_bands_kernel(BatchGrid *grids, const float *coefs, uint16_t *bands) {
     const BatchGrid &g = grids[blockIdx.x];
@@ -79,14 +111,16 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                                                 ~static_cast<uintptr_t>(1023));
     uint8_t *stage_base = smem;  // [kStages][hi | lo | bands]
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)kStages * kStageBytes);
-    uint64_t *full = bars;                         // [kStages]
-    uint64_t *empty = bars + kStages;              // [kStages]
-    uint64_t *acc_full = bars + 2 * kStages;       // [2]
-    uint64_t *acc_empty = bars + 2 * kStages + 2;  // [2]
-    uint64_t *drain = bars + 2 * kStages + 4;      // [1]
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 5);
+    uint64_t *full = bars;                          // [kStages]
+    uint64_t *empty = bars + kStages;               // [kStages]
+    uint64_t *acc_full = bars + 2 * kStages;        // [2]
+    uint64_t *acc_empty = bars + 2 * kStages + 2;   // [2]
+    uint64_t *drain = bars + 2 * kStages + 4;       // [1]
+    uint64_t *item_ready = bars + 2 * kStages + 5;  // [kRing]
+    BatchItem *ring = reinterpret_cast<BatchItem *>(bars + 2 * kStages + 5 + kRing);  // [kRing]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(ring + kRing);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-    volatile int *grid_error = &g_batch_error;
+    volatile int *grid_error = p.error;
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -101,6 +135,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
             mbar_init(&acc_empty[b], kEpiWarps);
         }
         mbar_init(drain, 1);
+        for (int j = 0; j < kRing; j++) mbar_init(&item_ready[j], 1);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -116,18 +151,28 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
 
     if (warp == 0) {
         // ------------------------------------------------------ producer ---
+        // Takes work indices in increasing order from the global counter,
+        // decodes each once and publishes it in ring slot i % kRing; an index
+        // past the end is published as the stop sentinel (g = -1).
         if (lane == 0) {
-            int i = 0;
             int last_issued = -1;
-            for (int k = blockIdx.x; k < p.n_items; k += gridDim.x, i++) {
-                const BatchItem it = p.items[k];
-                const BatchGrid &g = p.grids[it.g];
-                const int s = i % kStages;
+            for (int i = 0;; i++) {
+                const int s = i % kStages, j = i % kRing;
                 if (!mbar_wait(&empty[s], ((i / kStages) & 1) ^ 1, abort_flag)) {
-                    record_error(&g_batch_error, kErrWaitEmpty);
+                    batch_fail(p, kErrWaitEmpty);
                     *abort_flag = 1;
                     break;
                 }
+                const int k = (int)atomicAdd(p.work_counter, 1u);
+                if (k >= p.n_items) {
+                    ring[j] = BatchItem{-1, 0, 0};
+                    mbar_arrive(&item_ready[j]);
+                    break;
+                }
+                const BatchItem it = decode_item(p, k);
+                ring[j] = it;
+                mbar_arrive(&item_ready[j]);
+                const BatchGrid &g = p.grids[it.g];
                 if (it.t > 0) {
                     // every tile of the previous step of this grid is stored
                     const unsigned target =
@@ -144,7 +189,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                             __nanosleep(64);
                         }
                         if (!ok) {
-                            record_error(&g_batch_error, kErrWaitDep);
+                            batch_fail(p, kErrWaitDep);
                             *abort_flag = 1;
                             break;
                         }
@@ -153,7 +198,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                     fence_proxy_async_global();
                 }
                 const int nplanes = g.split ? 2 : 1;
-                const int band_bytes = (g.split ? 4 : 1) * (2 * g.r + 1) * kBandBytes;
+                const int band_bytes = batch_band_elems(g.r, g.split) * 2;
                 uint8_t *st = stage_base + (size_t)s * kStageBytes;
                 mbar_arrive_expect_tx(&full[s], nplanes * kPlaneStage + band_bytes);
                 const int in = (g.state + it.t) & 1;
@@ -168,7 +213,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                 const uint64_t t0 = global_timer_ns();
                 while (!mbar_try_wait(&full[ii % kStages], (ii / kStages) & 1)) {
                     if (global_timer_ns() - t0 > kWaitLimitNs) {
-                        record_error(&g_batch_error, kErrWaitDrain);
+                        batch_fail(p, kErrWaitDrain);
                         break;
                     }
                 }
@@ -177,19 +222,24 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
     } else if (warp == 1) {
         // ---------------------------------------------------- MMA issuer ---
         if (lane == 0) {
-            int i = 0;
             int kacc = 0;  // accumulator buffer counter (sub-tiles issued)
             bool issued_any = false;
             bool stop = false;
-            for (int k = blockIdx.x; k < p.n_items && !stop; k += gridDim.x, i++) {
-                const BatchItem it = p.items[k];
-                const BatchGrid &g = p.grids[it.g];
+            for (int i = 0; !stop; i++) {
                 const int s = i % kStages;
-                if (!mbar_wait(&full[s], (i / kStages) & 1, abort_flag)) {
-                    record_error(&g_batch_error, kErrWaitFull);
+                if (!mbar_wait(&item_ready[i % kRing], (i / kRing) & 1, abort_flag)) {
+                    batch_fail(p, kErrWaitFull);
                     *abort_flag = 1;
                     break;
                 }
+                const BatchItem it = ring[i % kRing];
+                if (it.g < 0) break;
+                if (!mbar_wait(&full[s], (i / kStages) & 1, abort_flag)) {
+                    batch_fail(p, kErrWaitFull);
+                    *abort_flag = 1;
+                    break;
+                }
+                const BatchGrid &g = p.grids[it.g];
                 uint8_t *st = stage_base + (size_t)s * kStageBytes;
                 const uint64_t a_hi0 = smem_desc(smem_u32(st), kChunkBytes, 128);
                 const uint64_t b_desc0 = smem_desc(smem_u32(st + 2 * kPlaneStage), 512, 128);
@@ -197,7 +247,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                 for (int h = 0; h < nsub; h++, kacc++) {
                     const int b = kacc & 1;
                     if (!mbar_wait(&acc_empty[b], ((kacc >> 1) & 1) ^ 1, abort_flag)) {
-                        record_error(&g_batch_error, kErrWaitAccum);
+                        batch_fail(p, kErrWaitAccum);
                         *abort_flag = 1;
                         stop = true;
                         break;
@@ -221,7 +271,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                 const uint64_t t0 = global_timer_ns();
                 while (!mbar_try_wait(drain, 0)) {
                     if (global_timer_ns() - t0 > kWaitLimitNs) {
-                        record_error(&g_batch_error, kErrWaitDrain);
+                        batch_fail(p, kErrWaitDrain);
                         break;
                     }
                 }
@@ -234,8 +284,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
         const int m = q * 32 + lane;
         int kacc = 0;
         bool stop = false;
-        for (int k = blockIdx.x; k < p.n_items && !stop; k += gridDim.x) {
-            const BatchItem it = p.items[k];
+        for (int i = 0; !stop; i++) {
+            const int j = i % kRing;
+            bool ok = mbar_wait(&item_ready[j], (i / kRing) & 1, abort_flag);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) {
+                if (lane == 0) {
+                    batch_fail(p, kErrWaitResult);
+                    *abort_flag = 1;
+                }
+                break;
+            }
+            const BatchItem it = ring[j];
+            if (it.g < 0) break;
             const BatchGrid &g = p.grids[it.g];
             const int in = (g.state + it.t) & 1;
             TileOut o;
@@ -250,11 +311,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
             const int nsub = sub_tiles(g);
             for (int h = 0; h < nsub; h++, kacc++) {
                 const int b = kacc & 1;
-                bool ok = mbar_wait(&acc_full[b], (kacc >> 1) & 1, abort_flag);
+                ok = mbar_wait(&acc_full[b], (kacc >> 1) & 1, abort_flag);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) {
                     if (lane == 0) {
-                        record_error(&g_batch_error, kErrWaitResult);
+                        batch_fail(p, kErrWaitResult);
                         *abort_flag = 1;
                     }
                     stop = true;
@@ -306,22 +367,14 @@ cudaError_t batch_prepare(int *num_sms) {
     return cudaSuccess;
 }
 
-// Cooperative launch: every CTA of the grid is resident at once (or the
-// launch waits until it can be), which the cross-CTA step waits rely on even
-// when other kernels share the GPU.
+// One CTA per SM.  Work is taken dynamically in index order, so a CTA waits
+// only on items already taken by running CTAs: progress needs no guarantee
+// that all CTAs are resident at once.
 cudaError_t launch_batch(const BatchParams &p, int num_sms, cudaStream_t s) {
     if (p.n_items <= 0) return cudaSuccess;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(p.n_items < num_sms ? p.n_items : num_sms);
-    cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = kSmem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, tc_batch_kernel, p);
+    const int grid = p.n_items < num_sms ? p.n_items : num_sms;
+    tc_batch_kernel<<<grid, kThreads, kSmem, s>>>(p);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_build_bands(const float *coef, int r, bool box, bool split, uint16_t *dst,
@@ -358,15 +411,15 @@ struct tcs_batch_s {
     std::vector<Entry> entries;
     uint16_t *pool = nullptr;
     size_t pool_elems = 0;
-    BatchGrid *d_grids = nullptr;
-    BatchItem *d_items = nullptr;
+    BatchGrid *d_grids = nullptr;  // sorted by steps, descending
+    int *d_layout = nullptr;       // step_off then tile_prefix
     unsigned *d_counters = nullptr;
     uint16_t *d_bands = nullptr;
     float *d_coefs = nullptr;
     float *d_staging = nullptr;
     size_t staging_elems = 0;
     unsigned *d_max = nullptr;
-    int n_items = 0;
+    int n_items = 0, n_steps = 0;
     int n_counters = 0;
     long long point_updates = 0;
     bool built = false;
@@ -377,7 +430,7 @@ struct tcs_batch_s {
     ~tcs_batch_s() {
         if (graph) cudaGraphExecDestroy(graph);
         if (capture_stream) cudaStreamDestroy(capture_stream);
-        for (void *p : {(void *)pool, (void *)d_grids, (void *)d_items, (void *)d_counters,
+        for (void *p : {(void *)pool, (void *)d_grids, (void *)d_layout, (void *)d_counters,
                         (void *)d_bands, (void *)d_coefs, (void *)d_staging, (void *)d_max})
             if (p) cudaFree(p);
     }
@@ -406,12 +459,18 @@ int batch_build(tcs_batch b) {
     if (!st) st = cuda_status(cudaMemset(b->pool, 0, total * sizeof(uint16_t)), "cudaMemset(batch planes)");
     if (st) return st;
     b->pool_elems = total;
-    // descriptors, bands, counters, work list
-    std::vector<BatchGrid> grids(b->entries.size());
-    std::vector<float> coefs(25 * b->entries.size(), 0.0f);
-    int ctr = 0, band = 0, max_steps = 0;
-    for (size_t i = 0; i < b->entries.size(); i++) {
-        const auto &e = b->entries[i];
+    // descriptors (sorted by steps, descending), bands, counters, work layout
+    const int n = (int)b->entries.size();
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return b->entries[x].steps > b->entries[y].steps; });
+    std::vector<BatchGrid> grids(n);
+    std::vector<float> coefs(25 * (size_t)n, 0.0f);
+    std::vector<int> steps(n), tiles(n);
+    int ctr = 0, band = 0;
+    for (int i = 0; i < n; i++) {
+        const auto &e = b->entries[order[i]];
         BatchGrid &G = grids[i];
         const bool split = e.prob.precision == TCS_PREC_SPLIT;
         for (int s = 0; s < 2; s++) {
@@ -429,27 +488,27 @@ int batch_build(tcs_batch b) {
         G.ctr_base = ctr;
         G.band_base = band;
         G.state = 0;
+        steps[i] = e.steps;
+        tiles[i] = G.n_tiles;
         ctr += std::max(e.steps, 1);
         band += batch_band_elems(G.r, split);
-        max_steps = std::max(max_steps, e.steps);
-        std::memcpy(&coefs[25 * i], e.coeffs, sizeof(e.coeffs));
+        std::memcpy(&coefs[25 * (size_t)i], e.coeffs, sizeof(e.coeffs));
         b->point_updates += (long long)(e.g.y1 - e.g.y0) * (e.g.x1 - e.g.x0) * e.steps;
     }
-    std::vector<BatchItem> items;
-    for (int t = 0; t < max_steps; t++)
-        for (size_t i = 0; i < grids.size(); i++)
-            if (grids[i].steps > t)
-                for (int tile = 0; tile < grids[i].n_tiles; tile++)
-                    items.push_back(BatchItem{(int)i, t, tile});
-    b->n_items = (int)items.size();
+    b->n_steps = n ? steps[0] : 0;
+    std::vector<int> layout(b->n_steps + 1 + n + 1);
+    const long long n_items = batch_layout(steps.data(), tiles.data(), n, layout.data(),
+                                           layout.data() + b->n_steps + 1);
+    if (n_items < 0) return fail(TCS_ERR_INVALID, "tcs_batch: more than 2^31 work items per run");
+    b->n_items = (int)n_items;
     b->n_counters = ctr;
     st = cuda_status(cudaMalloc(&b->d_grids, grids.size() * sizeof(BatchGrid)), "cudaMalloc(grids)");
-    if (!st) st = cuda_status(cudaMalloc(&b->d_items, std::max<size_t>(1, items.size()) * sizeof(BatchItem)), "cudaMalloc(items)");
-    if (!st) st = cuda_status(cudaMalloc(&b->d_counters, ctr * sizeof(unsigned)), "cudaMalloc(counters)");
+    if (!st) st = cuda_status(cudaMalloc(&b->d_layout, layout.size() * sizeof(int)), "cudaMalloc(layout)");
+    if (!st) st = cuda_status(cudaMalloc(&b->d_counters, (ctr + 2) * sizeof(unsigned)), "cudaMalloc(counters)");
     if (!st) st = cuda_status(cudaMalloc(&b->d_bands, std::max(band, 1) * sizeof(uint16_t)), "cudaMalloc(bands)");
     if (!st) st = cuda_status(cudaMalloc(&b->d_coefs, coefs.size() * sizeof(float)), "cudaMalloc(coefs)");
     if (!st) st = cuda_status(cudaMemcpy(b->d_grids, grids.data(), grids.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice), "grids copy");
-    if (!st && !items.empty()) st = cuda_status(cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice), "items copy");
+    if (!st) st = cuda_status(cudaMemcpy(b->d_layout, layout.data(), layout.size() * sizeof(int), cudaMemcpyHostToDevice), "layout copy");
     if (!st) st = cuda_status(cudaMemcpy(b->d_coefs, coefs.data(), coefs.size() * sizeof(float), cudaMemcpyHostToDevice), "coefs copy");
     if (st) return st;
     build_bands_kernel<<<(unsigned)grids.size(), 256>>>(b->d_grids, b->d_coefs, b->d_bands);
@@ -462,14 +521,19 @@ int batch_build(tcs_batch b) {
 }
 
 int batch_enqueue(tcs_batch b, cudaStream_t s) {
-    int st = cuda_status(cudaMemsetAsync(b->d_counters, 0, b->n_counters * sizeof(unsigned), s),
+    int st = cuda_status(cudaMemsetAsync(b->d_counters, 0, (b->n_counters + 2) * sizeof(unsigned), s),
                          "counter reset");
     if (st) return st;
     BatchParams p;
     p.grids = b->d_grids;
-    p.items = b->d_items;
+    p.step_off = b->d_layout;
+    p.tile_prefix = b->d_layout + b->n_steps + 1;
+    p.n_steps = b->n_steps;
+    p.n_grids = (int)b->entries.size();
     p.n_items = b->n_items;
     p.counters = b->d_counters;
+    p.work_counter = b->d_counters + b->n_counters;
+    p.error = reinterpret_cast<int *>(b->d_counters + b->n_counters + 1);
     p.bands = b->d_bands;
     st = cuda_status(launch_batch(p, g_sms, s), "batch kernel launch");
     if (st) return st;

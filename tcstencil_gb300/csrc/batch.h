@@ -26,22 +26,50 @@ struct BatchItem {
     int g, t, tile;  // grid, step within the run, tile
 };
 
+// One run's work: items are ordered step major and, within a step, by grid
+// then tile.  Grids are sorted by step count (descending), so the grids still
+// running at step t are a prefix of the array: step t holds the first
+// tile_prefix[G_t] tiles of the concatenated grids, and work index k decodes
+// with two binary searches (step_off, then tile_prefix).
 struct BatchParams {
-    const BatchGrid *grids;
-    const BatchItem *items;
-    int n_items;
-    unsigned *counters;  // one per (grid, step), zero at launch
+    const BatchGrid *grids;  // [n_grids], steps descending
+    const int *step_off;     // [n_steps + 1]: first work index of each step
+    const int *tile_prefix;  // [n_grids + 1]: first tile of each grid within a step
+    int n_steps, n_grids, n_items;
+    unsigned *counters;      // one per (grid, step), zero at launch
+    unsigned *work_counter;  // next work index, zero at launch
+    int *error;              // first failed wait of this launch (0 = none)
     const uint16_t *bands;
 };
 
+// Fills step_off and tile_prefix for grids whose run steps (descending) and
+// tile counts are given; returns the number of work items, or -1 when it
+// would not fit an int.
+inline long long batch_layout(const int *steps, const int *tiles, int n_grids, int *step_off,
+                              int *tile_prefix) {
+    tile_prefix[0] = 0;
+    for (int i = 0; i < n_grids; i++) tile_prefix[i + 1] = tile_prefix[i] + tiles[i];
+    const int n_steps = n_grids ? steps[0] : 0;
+    long long off = 0;
+    int g = n_grids;  // grids with steps > t
+    step_off[0] = 0;
+    for (int t = 0; t < n_steps; t++) {
+        while (g > 0 && steps[g - 1] <= t) g--;
+        off += tile_prefix[g];
+        if (off > 0x7fffffffLL) return -1;
+        step_off[t + 1] = static_cast<int>(off);
+    }
+    return off;
+}
+
 // Band bytes of one grid's stencil in the band buffer (FP16 or four split
 // pieces, 2r+1 coefficient rows).
-inline int batch_band_elems(int r, bool split) { return (split ? 4 : 1) * (2 * r + 1) * 512; }
+__host__ __device__ inline int batch_band_elems(int r, bool split) { return (split ? 4 : 1) * (2 * r + 1) * 512; }
 constexpr int kBatchMaxBandElems = 4 * 5 * 512;
 
 // Sets the kernel attributes and returns the SM count (the launch grid).
 cudaError_t batch_prepare(int *num_sms);
-// One persistent launch over p's work list; grid = min(items, SMs).
+// One persistent launch over p's work; grid = min(items, SMs).
 cudaError_t launch_batch(const BatchParams &p, int num_sms, cudaStream_t s);
 // Bands of one stencil (coefficients n x n row-major, n = 2r+1) into dst.
 cudaError_t launch_build_bands(const float *coef, int r, bool box, bool split, uint16_t *dst,

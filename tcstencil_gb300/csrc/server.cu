@@ -11,13 +11,14 @@
 //             (split), pack, coefficient bands; event `ready`.
 //   round   - every resident request with steps left, up to round_steps each,
 //             becomes one work list; on the compute stream: wait for the
-//             `ready` events of new requests, H2D of descriptors and items,
-//             counter reset, ONE cooperative batched launch.  Two rounds may
+//             `ready` events of new requests, H2D of descriptors and work layout,
+//             counter reset, ONE batched persistent launch.  Two rounds may
 //             be in flight (double-buffered descriptor memory), so the host
 //             builds round k+1 while round k runs.
 //   finish  - requests whose last step is in the round: on the copy stream,
 //             after the round's end event: unpack, D2H into the caller's
-//             buffer, host callback (completion time, wake waiters).
+//             buffer, completion event, which the scheduler polls (completion
+//             time, wake waiters).
 //   reap    - completed requests return their block and band slot.
 // The split scale exponent is computed and consumed on the device, so no step
 // of a request needs a host round trip.
@@ -93,6 +94,10 @@ class RangeAllocator {
 
 enum TicketState { kQueued = 0, kResident = 1, kDone = 2, kFailed = 3 };
 
+struct Retired {
+    std::vector<void *> host, dev;
+};
+
 }  // namespace
 }  // namespace tcs
 
@@ -115,7 +120,8 @@ struct Request {
     size_t plane_bytes = 0, bytes = 0, off = 0;
     int slot = -1;
     bool waited = false;  // the compute stream already waits on `ready`
-    cudaEvent_t ready = nullptr;
+    cudaEvent_t ready = nullptr;  // upload and pack done
+    cudaEvent_t done = nullptr;   // result and error word in host memory
     int state = kQueued;  // guarded by the server mutex
     int status = TCS_OK;
     double t_submit = 0, t_admit = 0, t_done = 0;
@@ -135,14 +141,26 @@ struct tcs_server_s {
     uint16_t *d_bands = nullptr;
     unsigned *d_maxbits = nullptr;
     int *d_exp = nullptr;
+    int *d_err = nullptr;       // sticky: the first failed wait of any round
+    int *h_slot_err = nullptr;  // pinned, per slot: d_err as seen at completion
     std::vector<int> free_slots;
+    std::vector<cudaEvent_t> event_pool;  // scheduler thread only
+    Retired retired;
+    // scheduler phase timing: total and worst pass, seconds
+    double phase_total[4] = {0, 0, 0, 0}, phase_max[4] = {0, 0, 0, 0};
+    // round launch sub-steps: build, compute-stream enqueue, finish enqueue
+    double launch_total[3] = {0, 0, 0}, launch_max[3] = {0, 0, 0};
+    void note_launch(int i, double dt) {
+        launch_total[i] += dt;
+        launch_max[i] = std::max(launch_max[i], dt);
+    }
 
     // double-buffered round descriptors
     struct RoundBuf {
         BatchGrid *h_grids = nullptr, *d_grids = nullptr;
-        BatchItem *h_items = nullptr, *d_items = nullptr;
+        int *h_layout = nullptr, *d_layout = nullptr;  // step_off then tile_prefix
         unsigned *d_counters = nullptr;
-        size_t cap_hg = 0, cap_hi = 0, cap_dg = 0, cap_di = 0, cap_dc = 0;
+        size_t cap_hg = 0, cap_hl = 0, cap_dg = 0, cap_dl = 0, cap_dc = 0;
         cudaEvent_t start = nullptr, end = nullptr;
         bool pending = false;
     } rb[2];
@@ -151,8 +169,9 @@ struct tcs_server_s {
     std::mutex mu;
     std::condition_variable cv_sched, cv_done;
     std::deque<Request *> queued;
-    std::vector<Request *> active;    // scheduler thread only
-    std::vector<Request *> finished;  // from host callbacks, guarded by mu
+    std::vector<Request *> active;       // scheduler thread only
+    std::vector<Request *> downloading;  // scheduler thread only: `done` recorded
+    std::vector<Request *> finished;     // guarded by mu
     std::unordered_map<long long, std::unique_ptr<Request>> tickets;
     long long next_ticket = 1;
     bool stop = false;
@@ -181,50 +200,112 @@ struct tcs_server_s {
     void reap(std::vector<Request *> &done);
     void admit();
     void poll_rounds();
+    bool poll_downloads();
     bool launch_round();
+    cudaEvent_t take_event();
+    int finish(Request *q, int cur, bool wait_round, cudaEvent_t round_end);
     void fail_request(Request *q, int status);
 };
 
 namespace {
 
-void CUDART_CB on_request_done(void *arg) {
-    Request *q = static_cast<Request *>(arg);
-    tcs_server_s *s = q->srv;
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        q->t_done = s->now();
-        q->state = kDone;
-        s->finished.push_back(q);
-    }
-    s->cv_done.notify_all();
-    s->cv_sched.notify_one();
+// Round buffers grow by allocating anew; the old buffer is retired, not freed,
+// until the server is destroyed: cudaFree / cudaFreeHost would wait for the
+// device, stalling admission behind a running round.
+template <typename T>
+int grow_pinned(T **h, size_t *cap, size_t want, Retired &ret) {
+    if (*cap >= want) return TCS_OK;
+    const size_t n = std::max(want, *cap * 2);
+    T *p = nullptr;
+    int st = cuda_status(cudaMallocHost(reinterpret_cast<void **>(&p), n * sizeof(T)), "cudaMallocHost(round)");
+    if (st) return st;
+    if (*h) ret.host.push_back(*h);
+    *h = p;
+    *cap = n;
+    return TCS_OK;
 }
 
 template <typename T>
-int grow_pinned(T **h, size_t *cap, size_t want) {
+int grow_device(T **d, size_t *cap, size_t want, Retired &ret) {
     if (*cap >= want) return TCS_OK;
     const size_t n = std::max(want, *cap * 2);
-    if (*h) cudaFreeHost(*h);
-    *h = nullptr;
-    *cap = 0;
-    int st = cuda_status(cudaMallocHost(reinterpret_cast<void **>(h), n * sizeof(T)), "cudaMallocHost(round)");
-    if (!st) *cap = n;
-    return st;
-}
-
-template <typename T>
-int grow_device(T **d, size_t *cap, size_t want) {
-    if (*cap >= want) return TCS_OK;
-    const size_t n = std::max(want, *cap * 2);
-    if (*d) cudaFree(*d);
-    *d = nullptr;
-    *cap = 0;
-    int st = cuda_status(cudaMalloc(reinterpret_cast<void **>(d), n * sizeof(T)), "cudaMalloc(round)");
-    if (!st) *cap = n;
-    return st;
+    T *p = nullptr;
+    int st = cuda_status(cudaMalloc(reinterpret_cast<void **>(&p), n * sizeof(T)), "cudaMalloc(round)");
+    if (st) return st;
+    if (*d) ret.dev.push_back(*d);
+    *d = p;
+    *cap = n;
+    return TCS_OK;
 }
 
 }  // namespace
+
+cudaEvent_t tcs_server_s::take_event() {
+    if (event_pool.empty()) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        return e;
+    }
+    cudaEvent_t e = event_pool.back();
+    event_pool.pop_back();
+    return e;
+}
+
+// Enqueues the download of a finished request's state `cur` on the copy
+// stream (behind round_end when given): unpack, D2H of the grid and of the
+// sticky error word, completion event.
+int tcs_server_s::finish(Request *q, int cur, bool wait_round, cudaEvent_t round_end) {
+    const size_t cells = (size_t)q->g.ny * q->g.nx;
+    float *stg = staging(q);
+    int st = TCS_OK;
+    if (wait_round) st = cuda_status(cudaStreamWaitEvent(copy, round_end, 0), "cudaStreamWaitEvent");
+    if (!st) {
+        if (q->split) st = cuda_status(launch_unpack_split_dev(plane(q, cur, 0), plane(q, cur, 1), q->g.ny, q->g.nx, d_exp + q->slot, stg, copy), "unpack launch");
+        else st = cuda_status(launch_unpack_f16(plane(q, cur, 0), q->g.ny, q->g.nx, 0, stg, copy), "unpack launch");
+    }
+    if (!st) st = cuda_status(cudaMemcpyAsync(q->h_out, stg, cells * sizeof(float), cudaMemcpyDeviceToHost, copy), "request download");
+    if (!st) st = cuda_status(cudaMemcpyAsync(h_slot_err + q->slot, d_err, sizeof(int), cudaMemcpyDeviceToHost, copy), "error word copy");
+    if (!st && !q->done) {
+        q->done = take_event();
+        if (!q->done) st = fail(TCS_ERR_CUDA, "cudaEventCreate failed");
+    }
+    if (!st) st = cuda_status(cudaEventRecord(q->done, copy), "cudaEventRecord");
+    if (!st) downloading.push_back(q);
+    return st;
+}
+
+// Completes requests whose downloads have landed; true when any did.
+bool tcs_server_s::poll_downloads() {
+    bool any = false;
+    for (size_t i = 0; i < downloading.size();) {
+        Request *q = downloading[i];
+        if (cudaEventQuery(q->done) != cudaSuccess) {
+            i++;
+            continue;
+        }
+        downloading[i] = downloading.back();
+        downloading.pop_back();
+        any = true;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            q->t_done = now();
+            finished.push_back(q);
+            if (h_slot_err[q->slot] != 0) {
+                // a round this request ran in (or a later one) gave up a wait
+                q->state = kFailed;
+                q->status = TCS_ERR_TIMEOUT;
+                failed++;
+            } else {
+                q->state = kDone;
+                completed++;
+                point_updates += q->updates();
+                alg_bytes += (q->split ? 8 : 4) * q->updates();
+            }
+        }
+    }
+    if (any) cv_done.notify_all();
+    return any;
+}
 
 void tcs_server_s::fail_request(Request *q, int status) {
     std::lock_guard<std::mutex> lk(mu);
@@ -232,6 +313,7 @@ void tcs_server_s::fail_request(Request *q, int status) {
     q->state = kFailed;
     q->t_done = now();
     finished.push_back(q);
+    failed++;
     cv_done.notify_all();
 }
 
@@ -242,20 +324,14 @@ void tcs_server_s::reap(std::vector<Request *> &done) {
             free_slots.push_back(q->slot);
             q->slot = -1;
         }
-        if (q->ready) {
-            cudaEventDestroy(q->ready);
-            q->ready = nullptr;
-        }
+        for (cudaEvent_t *e : {&q->ready, &q->done})
+            if (*e) {
+                event_pool.push_back(*e);
+                *e = nullptr;
+            }
         auto it = std::find(active.begin(), active.end(), q);
         if (it != active.end()) active.erase(it);
         std::lock_guard<std::mutex> lk(mu);
-        if (q->state == kDone) {
-            completed++;
-            point_updates += q->updates();
-            alg_bytes += (q->split ? 8 : 4) * q->updates();
-        } else {
-            failed++;
-        }
         n_active = (int)active.size();
     }
     done.clear();
@@ -277,6 +353,14 @@ void tcs_server_s::admit() {
             queued.pop_front();
             q->state = kResident;
             q->t_admit = now();
+        }
+        q->ready = take_event();
+        if (!q->ready) {
+            alloc.release(off, q->bytes);
+            std::lock_guard<std::mutex> lk(mu);
+            queued.push_front(q);
+            q->state = kQueued;
+            return;
         }
         q->off = off;
         q->slot = free_slots.back();
@@ -308,10 +392,7 @@ void tcs_server_s::admit() {
         }
         if (q->steps == 0) {
             // nothing to sweep: the result is the stored input
-            if (q->split) st = cuda_status(launch_unpack_split_dev(plane(q, 0, 0), plane(q, 0, 1), q->g.ny, q->g.nx, d_exp + q->slot, stg, copy), "unpack launch");
-            else st = cuda_status(launch_unpack_f16(plane(q, 0, 0), q->g.ny, q->g.nx, 0, stg, copy), "unpack launch");
-            if (!st) st = cuda_status(cudaMemcpyAsync(q->h_out, stg, cells * sizeof(float), cudaMemcpyDeviceToHost, copy), "request download");
-            if (!st) st = cuda_status(cudaLaunchHostFunc(copy, on_request_done, q), "cudaLaunchHostFunc");
+            st = finish(q, 0, false, nullptr);
             if (st) fail_request(q, st);
         }
     }
@@ -332,6 +413,7 @@ void tcs_server_s::poll_rounds() {
 // Builds and enqueues one round; false when there was nothing to run or no
 // free round buffer.
 bool tcs_server_s::launch_round() {
+    const double t_begin = now();
     RoundBuf &b = rb[round_idx & 1];
     if (b.pending) return false;  // its previous round still runs
     std::vector<Request *> part;
@@ -339,30 +421,51 @@ bool tcs_server_s::launch_round() {
         if (q->state == kResident && q->done_steps < q->steps) part.push_back(q);
     if (part.empty()) return false;
 
+    // grids sorted by this round's steps, descending (stable: admission order)
     std::vector<int> run_steps(part.size());
-    size_t n_items = 0, n_ctr = 0;
-    int max_s = 0;
     for (size_t i = 0; i < part.size(); i++) {
-        const Request *q = part[i];
-        const int rem = q->steps - q->done_steps;
+        const int rem = part[i]->steps - part[i]->done_steps;
         run_steps[i] = cfg.round_steps > 0 ? std::min(rem, cfg.round_steps) : rem;
-        const size_t tiles = (size_t)((q->g.ny + kTile - 1) / kTile) * ((q->g.nx + kTile - 1) / kTile);
-        n_items += tiles * run_steps[i];
-        n_ctr += run_steps[i];
-        max_s = std::max(max_s, run_steps[i]);
     }
+    std::vector<size_t> order(part.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t x, size_t y) { return run_steps[x] > run_steps[y]; });
+    {
+        std::vector<Request *> p2(part.size());
+        std::vector<int> s2(part.size());
+        for (size_t i = 0; i < order.size(); i++) {
+            p2[i] = part[order[i]];
+            s2[i] = run_steps[order[i]];
+        }
+        part.swap(p2);
+        run_steps.swap(s2);
+    }
+    const int n = (int)part.size();
+    const int max_s = run_steps[0];
+    size_t n_ctr = 0;
+    std::vector<int> tiles(n);
+    for (int i = 0; i < n; i++) {
+        const Request *q = part[i];
+        tiles[i] = ((q->g.ny + kTile - 1) / kTile) * ((q->g.nx + kTile - 1) / kTile);
+        n_ctr += run_steps[i];
+    }
+    const size_t n_layout = (size_t)max_s + 1 + n + 1;
     // buffer b is idle (its last round completed), so it may be regrown
-    int st = grow_pinned(&b.h_grids, &b.cap_hg, part.size());
-    if (!st) st = grow_pinned(&b.h_items, &b.cap_hi, n_items);
-    if (!st) st = grow_device(&b.d_grids, &b.cap_dg, part.size());
-    if (!st) st = grow_device(&b.d_items, &b.cap_di, n_items);
-    if (!st) st = grow_device(&b.d_counters, &b.cap_dc, n_ctr);
+    int st = grow_pinned(&b.h_grids, &b.cap_hg, part.size(), retired);
+    if (!st) st = grow_pinned(&b.h_layout, &b.cap_hl, n_layout, retired);
+    if (!st) st = grow_device(&b.d_grids, &b.cap_dg, part.size(), retired);
+    if (!st) st = grow_device(&b.d_layout, &b.cap_dl, n_layout, retired);
+    if (!st) st = grow_device(&b.d_counters, &b.cap_dc, n_ctr + 1, retired);
+    const long long n_items =
+        st ? 0 : batch_layout(run_steps.data(), tiles.data(), n, b.h_layout, b.h_layout + max_s + 1);
+    if (!st && n_items < 0) st = fail(TCS_ERR_INVALID, "round of more than 2^31 work items");
     if (st) {
         for (Request *q : part) fail_request(q, st);
         return true;
     }
     int ctr = 0;
-    for (size_t i = 0; i < part.size(); i++) {
+    for (int i = 0; i < n; i++) {
         Request *q = part[i];
         BatchGrid &G = b.h_grids[i];
         for (int s = 0; s < 2; s++) {
@@ -372,7 +475,7 @@ bool tcs_server_s::launch_round() {
         G.pg = q->g.p16;
         G.y0 = q->g.y0; G.y1 = q->g.y1; G.x0 = q->g.x0; G.x1 = q->g.x1;
         G.tiles_x = (q->g.nx + kTile - 1) / kTile;
-        G.n_tiles = G.tiles_x * ((q->g.ny + kTile - 1) / kTile);
+        G.n_tiles = tiles[i];
         G.r = q->r;
         G.box = q->box;
         G.split = q->split;
@@ -382,28 +485,28 @@ bool tcs_server_s::launch_round() {
         G.state = q->done_steps & 1;
         ctr += run_steps[i];
     }
-    size_t k = 0;
-    for (int t = 0; t < max_s; t++)
-        for (size_t i = 0; i < part.size(); i++)
-            if (run_steps[i] > t)
-                for (int tile = 0; tile < b.h_grids[i].n_tiles; tile++)
-                    b.h_items[k++] = BatchItem{(int)i, t, tile};
 
+    const double t_built = now();
     for (Request *q : part)
         if (!q->waited) {
             if (!st) st = cuda_status(cudaStreamWaitEvent(compute, q->ready, 0), "cudaStreamWaitEvent");
             q->waited = true;
         }
     if (!st) st = cuda_status(cudaMemcpyAsync(b.d_grids, b.h_grids, part.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice, compute), "round descriptors");
-    if (!st) st = cuda_status(cudaMemcpyAsync(b.d_items, b.h_items, n_items * sizeof(BatchItem), cudaMemcpyHostToDevice, compute), "round items");
-    if (!st) st = cuda_status(cudaMemsetAsync(b.d_counters, 0, n_ctr * sizeof(unsigned), compute), "round counters");
+    if (!st) st = cuda_status(cudaMemcpyAsync(b.d_layout, b.h_layout, n_layout * sizeof(int), cudaMemcpyHostToDevice, compute), "round layout");
+    if (!st) st = cuda_status(cudaMemsetAsync(b.d_counters, 0, (n_ctr + 1) * sizeof(unsigned), compute), "round counters");
     if (!st) st = cuda_status(cudaEventRecord(b.start, compute), "cudaEventRecord");
     if (!st) {
         BatchParams p;
         p.grids = b.d_grids;
-        p.items = b.d_items;
+        p.step_off = b.d_layout;
+        p.tile_prefix = b.d_layout + max_s + 1;
+        p.n_steps = max_s;
+        p.n_grids = n;
         p.n_items = (int)n_items;
         p.counters = b.d_counters;
+        p.work_counter = b.d_counters + n_ctr;
+        p.error = d_err;
         p.bands = d_bands;
         st = cuda_status(launch_batch(p, sms, compute), "batch launch");
     }
@@ -414,27 +517,23 @@ bool tcs_server_s::launch_round() {
     }
     b.pending = true;
     round_idx++;
+    const double t_enq = now();
     bool waited_round = false;
     for (size_t i = 0; i < part.size(); i++) {
         Request *q = part[i];
         q->done_steps += run_steps[i];
         if (q->done_steps < q->steps) continue;
         // finished in this round: unpack and download behind it
-        const int cur = q->done_steps & 1;
-        const size_t cells = (size_t)q->g.ny * q->g.nx;
-        float *stg = staging(q);
-        int rs = TCS_OK;
-        if (!waited_round) {
-            rs = cuda_status(cudaStreamWaitEvent(copy, b.end, 0), "cudaStreamWaitEvent");
-            waited_round = true;
-        }
-        if (!rs) {
-            if (q->split) rs = cuda_status(launch_unpack_split_dev(plane(q, cur, 0), plane(q, cur, 1), q->g.ny, q->g.nx, d_exp + q->slot, stg, copy), "unpack launch");
-            else rs = cuda_status(launch_unpack_f16(plane(q, cur, 0), q->g.ny, q->g.nx, 0, stg, copy), "unpack launch");
-        }
-        if (!rs) rs = cuda_status(cudaMemcpyAsync(q->h_out, stg, cells * sizeof(float), cudaMemcpyDeviceToHost, copy), "request download");
-        if (!rs) rs = cuda_status(cudaLaunchHostFunc(copy, on_request_done, q), "cudaLaunchHostFunc");
+        const int rs = finish(q, q->done_steps & 1, !waited_round, b.end);
+        waited_round = true;
         if (rs) fail_request(q, rs);
+    }
+    const double t_fin = now();
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        note_launch(0, t_built - t_begin);
+        note_launch(1, t_enq - t_built);
+        note_launch(2, t_fin - t_enq);
     }
     return true;
 }
@@ -456,11 +555,25 @@ void tcs_server_s::loop() {
         }
         const size_t before = active.size();
         const bool reaped = !done.empty();
+        double t[5];
+        t[0] = now();
         reap(done);
+        t[1] = now();
         admit();
+        t[2] = now();
         poll_rounds();
+        const bool landed = poll_downloads();
+        t[3] = now();
         const bool launched = launch_round();
-        progressed = reaped || launched || active.size() != before;
+        t[4] = now();
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            for (int i = 0; i < 4; i++) {
+                phase_total[i] += t[i + 1] - t[i];
+                phase_max[i] = std::max(phase_max[i], t[i + 1] - t[i]);
+            }
+        }
+        progressed = reaped || landed || launched || active.size() != before;
     }
 }
 
@@ -487,11 +600,25 @@ int tcs_server_create(const tcs_server_config *config, tcs_server *out) {
     if (!st) st = cuda_status(cudaMalloc(&s->d_bands, (size_t)slots * kBatchMaxBandElems * sizeof(uint16_t)), "cudaMalloc(bands)");
     if (!st) st = cuda_status(cudaMalloc(&s->d_maxbits, slots * sizeof(unsigned)), "cudaMalloc(max)");
     if (!st) st = cuda_status(cudaMalloc(&s->d_exp, slots * sizeof(int)), "cudaMalloc(exp)");
+    if (!st) st = cuda_status(cudaMalloc(&s->d_err, sizeof(int)), "cudaMalloc(error)");
+    if (!st) st = cuda_status(cudaMemset(s->d_err, 0, sizeof(int)), "cudaMemset(error)");
+    if (!st) st = cuda_status(cudaMallocHost(&s->h_slot_err, slots * sizeof(int)), "cudaMallocHost(errors)");
     if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking), "cudaStreamCreate");
     if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking), "cudaStreamCreate");
     for (auto &b : s->rb) {
         if (!st) st = cuda_status(cudaEventCreate(&b.start), "cudaEventCreate");
         if (!st) st = cuda_status(cudaEventCreate(&b.end), "cudaEventCreate");
+    }
+    if (st) {
+        tcs_server_destroy(s.release());
+        return st;
+    }
+    for (auto &b : s->rb) {
+        if (!st) st = grow_pinned(&b.h_grids, &b.cap_hg, (size_t)slots, s->retired);
+        if (!st) st = grow_pinned(&b.h_layout, &b.cap_hl, (size_t)slots + 1024, s->retired);
+        if (!st) st = grow_device(&b.d_grids, &b.cap_dg, (size_t)slots, s->retired);
+        if (!st) st = grow_device(&b.d_layout, &b.cap_dl, (size_t)slots + 1024, s->retired);
+        if (!st) st = grow_device(&b.d_counters, &b.cap_dc, (size_t)1 << 16, s->retired);
     }
     if (st) {
         tcs_server_destroy(s.release());
@@ -525,14 +652,20 @@ int tcs_server_destroy(tcs_server s) {
         if (b.start) cudaEventDestroy(b.start);
         if (b.end) cudaEventDestroy(b.end);
         if (b.h_grids) cudaFreeHost(b.h_grids);
-        if (b.h_items) cudaFreeHost(b.h_items);
-        for (void *p : {(void *)b.d_grids, (void *)b.d_items, (void *)b.d_counters})
+        if (b.h_layout) cudaFreeHost(b.h_layout);
+        for (void *p : {(void *)b.d_grids, (void *)b.d_layout, (void *)b.d_counters})
             if (p) cudaFree(p);
     }
     for (auto &kv : s->tickets)
-        if (kv.second->ready) cudaEventDestroy(kv.second->ready);
-    for (void *p : {(void *)s->pool, (void *)s->d_bands, (void *)s->d_maxbits, (void *)s->d_exp})
+        for (cudaEvent_t e : {kv.second->ready, kv.second->done})
+            if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
+    for (void *p : s->retired.host) cudaFreeHost(p);
+    for (void *p : s->retired.dev) cudaFree(p);
+    for (void *p : {(void *)s->pool, (void *)s->d_bands, (void *)s->d_maxbits, (void *)s->d_exp,
+                    (void *)s->d_err})
         if (p) cudaFree(p);
+    if (s->h_slot_err) cudaFreeHost(s->h_slot_err);
     if (s->compute) cudaStreamDestroy(s->compute);
     if (s->copy) cudaStreamDestroy(s->copy);
     delete s;
@@ -564,8 +697,6 @@ int tcs_server_submit(tcs_server s, const tcs_problem *pr, int steps, const floa
     q->bytes = 4 * q->plane_bytes + align_up((size_t)q->g.ny * q->g.nx * sizeof(float));
     if (q->bytes > s->cfg.hbm_budget_bytes)
         return fail(TCS_ERR_NOMEM, "request needs %zu bytes, the server budget is %zu", q->bytes, s->cfg.hbm_budget_bytes);
-    st = cuda_status(cudaEventCreateWithFlags(&q->ready, cudaEventDisableTiming), "cudaEventCreate");
-    if (st) return st;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         q->ticket = s->next_ticket++;
@@ -631,6 +762,14 @@ int tcs_server_get_stats(tcs_server s, tcs_server_stats *o) {
     o->peak_bytes_in_use = s->peak_bytes;
     o->active = s->n_active;
     o->queued = (int)s->queued.size();
+    for (int i = 0; i < 4; i++) {
+        o->sched_total_s[i] = s->phase_total[i];
+        o->sched_max_s[i] = s->phase_max[i];
+    }
+    for (int i = 0; i < 3; i++) {
+        o->launch_total_s[i] = s->launch_total[i];
+        o->launch_max_s[i] = s->launch_max[i];
+    }
     return TCS_OK;
 }
 

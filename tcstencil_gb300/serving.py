@@ -66,7 +66,7 @@ class OutputRing:
 
 
 def replay(server, requests: list[Request], inputs: InputPool, outputs: OutputRing | None = None,
-           keep_outputs: bool = False, spin_s: float = 2e-4) -> dict:
+           keep_outputs: bool = False, spin_s: float = 2e-4, timeout_s: float = 120.0) -> dict:
     """Submits every request at its arrival time on the server clock (open
     loop), waits for all, and returns per-request latencies (completion minus
     scheduled arrival, seconds) with p50/p99 and aggregate Gpts/s."""
@@ -87,13 +87,13 @@ def replay(server, requests: list[Request], inputs: InputPool, outputs: OutputRi
             t = server.submit(g, out, sp.stencil, sp.coeffs, sp.steps, sp.precision)
             kept[rq.rid] = (g, out)
         else:
-            out, s0, e0 = outputs.take(sp.ny, sp.nx, server.wait)
+            out, s0, e0 = outputs.take(sp.ny, sp.nx, lambda t: server.wait(t, timeout_s))
             t = server.submit(g, out, sp.stencil, sp.coeffs, sp.steps, sp.precision)
             outputs.hold(t, s0, e0)
         lag.append(server.clock() - target)
         tickets.append((t, target, rq))
     for t, _, _ in tickets:
-        server.wait(t)
+        server.wait(t, timeout_s)
     lat, queue_wait, updates = [], [], 0
     first = tickets[0][1] if tickets else 0.0
     last_done = first
@@ -121,6 +121,10 @@ def replay(server, requests: list[Request], inputs: InputPool, outputs: OutputRi
         "rounds": st["rounds"],
         "peak_bytes_in_use": st["peak_bytes_in_use"],
         "failed": st["failed"],
+        "sched_max_ms": [round(v * 1e3, 3) for v in st["sched_max_s"]],
+        "sched_total_s": [round(v, 3) for v in st["sched_total_s"]],
+        "launch_max_ms": [round(v * 1e3, 3) for v in st["launch_max_s"]],
+        "launch_total_s": [round(v, 3) for v in st["launch_total_s"]],
     }
     if keep_outputs:
         res["outputs"] = kept
