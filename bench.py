@@ -280,7 +280,11 @@ def batch_leg(torch, tcs, K, W, stream, count=512):
 
 
 def serve_round_steps(args):
-    return 16 if args.serve_round_steps is None else args.serve_round_steps
+    if args.serve_round_steps is not None:
+        return args.serve_round_steps
+    from tcstencil_gb300.autotune import best_round_steps
+
+    return best_round_steps(args.serve_rate)
 
 
 def serve_leg(tcs, seconds=10.0, rate=2000.0, budget_gb=120.0, round_steps=16):

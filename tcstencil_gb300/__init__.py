@@ -273,6 +273,11 @@ class Plan:
 
     def __init__(self, ny: int, nx: int, stencil: str, coeffs, engine: str = "tensor",
                  precision: str = "f16", rect=None):
+        """engine "auto" takes the autotuner's choice for this problem class."""
+        if engine == "auto":
+            from .autotune import best_engine
+
+            engine = best_engine(stencil, precision, ny, nx)
         self._c = _coeffs(coeffs, stencil)
         y0, y1, x0, x1 = _rect(rect)
         self.ny, self.nx, self.stencil, self.engine, self.precision = ny, nx, stencil, engine, precision

@@ -7,7 +7,7 @@
 // scheduler thread owns everything on the device:
 //   admit   - while the budget has room: carve the request's block (ping-pong
 //             planes + FP32 staging grid) from one pre-allocated device region
-//             (first-fit, coalescing), then on the copy stream: H2D, max |x|
+//             (first-fit, coalescing), then on the upload stream: H2D, max |x|
 //             (split), pack, coefficient bands; event `ready`.
 //   round   - every resident request with steps left, up to round_steps each,
 //             becomes one work list; on the compute stream: wait for the
@@ -15,7 +15,7 @@
 //             counter reset, ONE batched persistent launch.  Two rounds may
 //             be in flight (double-buffered descriptor memory), so the host
 //             builds round k+1 while round k runs.
-//   finish  - requests whose last step is in the round: on the copy stream,
+//   finish  - requests whose last step is in the round: on the download stream,
 //             after the round's end event: unpack, D2H into the caller's
 //             buffer, completion event, which the scheduler polls (completion
 //             time, wake waiters).
@@ -137,7 +137,9 @@ struct tcs_server_s {
     uint8_t *pool = nullptr;
     RangeAllocator alloc;
     int sms = 1;
-    cudaStream_t compute = nullptr, copy = nullptr;
+    // upload: admission (never waits on a round); download: finished requests
+    // (each behind its round's end); compute: rounds
+    cudaStream_t compute = nullptr, upload = nullptr, download = nullptr;
     uint16_t *d_bands = nullptr;
     unsigned *d_maxbits = nullptr;
     int *d_exp = nullptr;
@@ -251,25 +253,25 @@ cudaEvent_t tcs_server_s::take_event() {
     return e;
 }
 
-// Enqueues the download of a finished request's state `cur` on the copy
+// Enqueues the download of a finished request's state `cur` on the download
 // stream (behind round_end when given): unpack, D2H of the grid and of the
 // sticky error word, completion event.
 int tcs_server_s::finish(Request *q, int cur, bool wait_round, cudaEvent_t round_end) {
     const size_t cells = (size_t)q->g.ny * q->g.nx;
     float *stg = staging(q);
     int st = TCS_OK;
-    if (wait_round) st = cuda_status(cudaStreamWaitEvent(copy, round_end, 0), "cudaStreamWaitEvent");
+    if (wait_round) st = cuda_status(cudaStreamWaitEvent(download, round_end, 0), "cudaStreamWaitEvent");
     if (!st) {
-        if (q->split) st = cuda_status(launch_unpack_split_dev(plane(q, cur, 0), plane(q, cur, 1), q->g.ny, q->g.nx, d_exp + q->slot, stg, copy), "unpack launch");
-        else st = cuda_status(launch_unpack_f16(plane(q, cur, 0), q->g.ny, q->g.nx, 0, stg, copy), "unpack launch");
+        if (q->split) st = cuda_status(launch_unpack_split_dev(plane(q, cur, 0), plane(q, cur, 1), q->g.ny, q->g.nx, d_exp + q->slot, stg, download), "unpack launch");
+        else st = cuda_status(launch_unpack_f16(plane(q, cur, 0), q->g.ny, q->g.nx, 0, stg, download), "unpack launch");
     }
-    if (!st) st = cuda_status(cudaMemcpyAsync(q->h_out, stg, cells * sizeof(float), cudaMemcpyDeviceToHost, copy), "request download");
-    if (!st) st = cuda_status(cudaMemcpyAsync(h_slot_err + q->slot, d_err, sizeof(int), cudaMemcpyDeviceToHost, copy), "error word copy");
+    if (!st) st = cuda_status(cudaMemcpyAsync(q->h_out, stg, cells * sizeof(float), cudaMemcpyDeviceToHost, download), "request download");
+    if (!st) st = cuda_status(cudaMemcpyAsync(h_slot_err + q->slot, d_err, sizeof(int), cudaMemcpyDeviceToHost, download), "error word copy");
     if (!st && !q->done) {
         q->done = take_event();
         if (!q->done) st = fail(TCS_ERR_CUDA, "cudaEventCreate failed");
     }
-    if (!st) st = cuda_status(cudaEventRecord(q->done, copy), "cudaEventRecord");
+    if (!st) st = cuda_status(cudaEventRecord(q->done, download), "cudaEventRecord");
     if (!st) downloading.push_back(q);
     return st;
 }
@@ -374,25 +376,26 @@ void tcs_server_s::admit() {
         const size_t cells = (size_t)q->g.ny * q->g.nx;
         float *stg = staging(q);
         unsigned *mx = d_maxbits + q->slot;
-        int st = cuda_status(cudaMemcpyAsync(stg, q->h_in, cells * sizeof(float), cudaMemcpyHostToDevice, copy), "request upload");
+        int st = cuda_status(cudaMemcpyAsync(stg, q->h_in, cells * sizeof(float), cudaMemcpyHostToDevice, upload), "request upload");
         // state-1 planes: padding cells must be finite (pack writes all of state 0)
-        if (!st) st = cuda_status(cudaMemsetAsync(plane(q, 1, 0), 0, 2 * q->plane_bytes, copy), "plane clear");
+        if (!st) st = cuda_status(cudaMemsetAsync(plane(q, 1, 0), 0, 2 * q->plane_bytes, upload), "plane clear");
         if (!st && q->split) {
-            st = cuda_status(cudaMemsetAsync(mx, 0, sizeof(unsigned), copy), "max clear");
-            if (!st) st = cuda_status(launch_max_abs(stg, cells, mx, copy), "max_abs launch");
-            if (!st) st = cuda_status(launch_pack_split_dev(stg, q->g.ny, q->g.nx, mx, d_exp + q->slot, plane(q, 0, 0), plane(q, 0, 1), copy), "pack launch");
+            st = cuda_status(cudaMemsetAsync(mx, 0, sizeof(unsigned), upload), "max clear");
+            if (!st) st = cuda_status(launch_max_abs(stg, cells, mx, upload), "max_abs launch");
+            if (!st) st = cuda_status(launch_pack_split_dev(stg, q->g.ny, q->g.nx, mx, d_exp + q->slot, plane(q, 0, 0), plane(q, 0, 1), upload), "pack launch");
         } else if (!st) {
-            st = cuda_status(launch_pack_f16(stg, q->g.ny, q->g.nx, 0, 0.0f, plane(q, 0, 0), copy), "pack launch");
+            st = cuda_status(launch_pack_f16(stg, q->g.ny, q->g.nx, 0, 0.0f, plane(q, 0, 0), upload), "pack launch");
         }
-        if (!st) st = cuda_status(launch_build_bands(q->coeffs, q->r, q->box, q->split, d_bands + (size_t)q->slot * kBatchMaxBandElems, copy), "band build");
-        if (!st) st = cuda_status(cudaEventRecord(q->ready, copy), "cudaEventRecord");
+        if (!st) st = cuda_status(launch_build_bands(q->coeffs, q->r, q->box, q->split, d_bands + (size_t)q->slot * kBatchMaxBandElems, upload), "band build");
+        if (!st) st = cuda_status(cudaEventRecord(q->ready, upload), "cudaEventRecord");
         if (st) {
             fail_request(q, st);
             continue;
         }
         if (q->steps == 0) {
             // nothing to sweep: the result is the stored input
-            st = finish(q, 0, false, nullptr);
+            st = cuda_status(cudaStreamWaitEvent(download, q->ready, 0), "cudaStreamWaitEvent");
+            if (!st) st = finish(q, 0, false, nullptr);
             if (st) fail_request(q, st);
         }
     }
@@ -604,7 +607,8 @@ int tcs_server_create(const tcs_server_config *config, tcs_server *out) {
     if (!st) st = cuda_status(cudaMemset(s->d_err, 0, sizeof(int)), "cudaMemset(error)");
     if (!st) st = cuda_status(cudaMallocHost(&s->h_slot_err, slots * sizeof(int)), "cudaMallocHost(errors)");
     if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking), "cudaStreamCreate");
-    if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->upload, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->download, cudaStreamNonBlocking), "cudaStreamCreate");
     for (auto &b : s->rb) {
         if (!st) st = cuda_status(cudaEventCreate(&b.start), "cudaEventCreate");
         if (!st) st = cuda_status(cudaEventCreate(&b.end), "cudaEventCreate");
@@ -647,7 +651,8 @@ int tcs_server_destroy(tcs_server s) {
         s->worker.join();
     }
     if (s->compute) cudaStreamSynchronize(s->compute);
-    if (s->copy) cudaStreamSynchronize(s->copy);
+    if (s->upload) cudaStreamSynchronize(s->upload);
+    if (s->download) cudaStreamSynchronize(s->download);
     for (auto &b : s->rb) {
         if (b.start) cudaEventDestroy(b.start);
         if (b.end) cudaEventDestroy(b.end);
@@ -667,7 +672,8 @@ int tcs_server_destroy(tcs_server s) {
         if (p) cudaFree(p);
     if (s->h_slot_err) cudaFreeHost(s->h_slot_err);
     if (s->compute) cudaStreamDestroy(s->compute);
-    if (s->copy) cudaStreamDestroy(s->copy);
+    if (s->upload) cudaStreamDestroy(s->upload);
+    if (s->download) cudaStreamDestroy(s->download);
     delete s;
     return TCS_OK;
 }

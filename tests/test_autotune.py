@@ -1,0 +1,79 @@
+"""Autotuner: choice rules and the persistent cache (CPU, with injected
+timings), and one real tuning pass on the device."""
+import json
+
+import numpy as np
+import pytest
+
+from tcstencil_gb300 import autotune
+
+
+def test_sweep_choice_is_persisted_per_class(tmp_path):
+    path = str(tmp_path / "tune.json")
+    fake = {"tensor": 2e-5, "cudacore": 1e-5}
+    cache = autotune.Cache(path, shipped=None)
+    e = autotune.tune_sweep("star2d1r", "f16", 300, 300, cache=cache,
+                            timer=lambda eng, *a: fake[eng])
+    assert e["engine"] == "cudacore"
+    # a fresh reader sees it, for any grid of the same size class only
+    c2 = autotune.Cache(path, shipped=None)
+    assert autotune.best_engine("star2d1r", "f16", 500, 270, cache=c2) == "cudacore"
+    assert autotune.best_engine("star2d1r", "f16", 600, 300, cache=c2) == "tensor"
+    assert autotune.best_engine("box2d2r", "f16", 300, 300, cache=c2) == "tensor"
+    assert autotune.best_engine("box2d2r", "f32", 300, 300, cache=c2) == "cudacore"
+    data = json.load(open(path))
+    assert list(data.values())[0]["sweep"]["star2d1r/f16/9x9"]["engine"] == "cudacore"
+
+
+def test_shipped_results_back_up_an_empty_cache(tmp_path):
+    shipped = tmp_path / "shipped.json"
+    dev = autotune.device_key()
+    shipped.write_text(json.dumps({dev: {"sweep": {"box2d1r/f16/8x8": {"engine": "cudacore"}},
+                                         "serve": {"poisson/2000": {"round_steps": 4}}}}))
+    c = autotune.Cache(str(tmp_path / "user.json"), shipped=str(shipped))
+    assert autotune.best_engine("box2d1r", "f16", 200, 256, cache=c) == "cudacore"
+    assert autotune.best_round_steps(2000.0, cache=c) == 4
+    c.section("serve")["poisson/2000"] = {"round_steps": 8}  # the user's own result wins
+    assert autotune.best_round_steps(2000.0, cache=c) == 8
+
+
+def test_split_only_tries_the_tensor_engine(tmp_path):
+    seen = []
+    autotune.tune_sweep("box2d1r", "split", 64, 64, cache=autotune.Cache(str(tmp_path / "t.json")),
+                        timer=lambda eng, *a: seen.append(eng) or 1.0)
+    assert seen == ["tensor"]
+
+
+def test_serve_choice_prefers_low_p99_among_those_keeping_up(tmp_path):
+    runs = {0: {"gpts": 260.0, "p50_ms": 20.0, "p99_ms": 58.0},
+            4: {"gpts": 265.0, "p50_ms": 6.0, "p99_ms": 66.0},
+            16: {"gpts": 265.0, "p50_ms": 7.0, "p99_ms": 63.0},
+            32: {"gpts": 200.0, "p50_ms": 5.0, "p99_ms": 10.0}}  # fell behind
+    cache = autotune.Cache(str(tmp_path / "t.json"), shipped=None)
+    e = autotune.tune_serve(2000.0, candidates=tuple(runs), cache=cache,
+                            runner=lambda rate, sec, rs, b: runs[rs])
+    assert e["round_steps"] == 0  # 260 is within 2 % of 265, and its p99 is lowest
+    assert autotune.best_round_steps(2000.0, cache=autotune.Cache(cache.path, shipped=None)) == 0
+    assert autotune.best_round_steps(1000.0, cache=cache) == autotune.DEFAULT_ROUND_STEPS
+
+
+@pytest.mark.gpu
+def test_real_tuning_pass_and_auto_engine(tcs, torch_cuda, tmp_path, monkeypatch):
+    monkeypatch.setenv("TCS_AUTOTUNE_CACHE", str(tmp_path / "t.json"))
+    e = autotune.tune_sweep("star2d2r", "f16", 512, 512, steps=5)
+    assert e["engine"] in ("tensor", "cudacore")
+    assert all(t > 0 for t in e["s_per_step"].values())
+    p = tcs.Plan(512, 512, "star2d2r", np.full((5, 5), 0.04, np.float32), engine="auto")
+    g = np.random.default_rng(0).uniform(-1, 1, (512, 512)).astype(np.float32)
+    p.upload(g)
+    p.run(3)
+    out = np.empty_like(g)
+    p.download(out)
+    torch_cuda.cuda.synchronize()
+    ref = tcs.Plan(512, 512, "star2d2r", np.full((5, 5), 0.04, np.float32), engine=e["engine"])
+    ref.upload(g)
+    ref.run(3)
+    out2 = np.empty_like(g)
+    ref.download(out2)
+    torch_cuda.cuda.synchronize()
+    np.testing.assert_array_equal(out, out2)
