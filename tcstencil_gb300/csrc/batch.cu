@@ -44,14 +44,11 @@ __device__ int g_batch_error = 0;
 constexpr int kStages = 2;
 constexpr int kMaxBandBytes = 4 * 5 * kBandBytes;  // split, radius 2
 constexpr int kStageBytes = 2 * kPlaneStage + kMaxBandBytes;
-constexpr int kAccStride = Mode<true>::ACC;        // TMEM columns per accumulator buffer
-constexpr int kTmemCols = 512;
 constexpr int kRing = 8;  // published work items in flight (> kStages + 2)
 constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + 512;
 static_assert(kRing > kStages + 2, "a ring slot is reused only after its item's epilogue");
 static_assert((2 * kStages + 5 + kRing) * 8 + kRing * 12 + 8 <= 512, "barrier area");
 static_assert(kSmem <= 232448, "shared memory budget");
-static_assert(2 * kAccStride <= kTmemCols, "TMEM budget");
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     unsigned v;
@@ -222,7 +219,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
     } else if (warp == 1) {
         // ---------------------------------------------------- MMA issuer ---
         if (lane == 0) {
-            int kacc = 0;  // accumulator buffer counter (sub-tiles issued)
+            AccSlots slots;
             bool issued_any = false;
             bool stop = false;
             for (int i = 0; !stop; i++) {
@@ -242,26 +239,28 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                 const BatchGrid &g = p.grids[it.g];
                 uint8_t *st = stage_base + (size_t)s * kStageBytes;
                 const uint64_t a_hi0 = smem_desc(smem_u32(st), kChunkBytes, 128);
-                const uint64_t b_desc0 = smem_desc(smem_u32(st + 2 * kPlaneStage), 512, 128);
+                const uint32_t band = smem_u32(st + 2 * kPlaneStage);
                 const int nsub = sub_tiles(g);
-                for (int h = 0; h < nsub; h++, kacc++) {
-                    const int b = kacc & 1;
-                    if (!mbar_wait(&acc_empty[b], ((kacc >> 1) & 1) ^ 1, abort_flag)) {
+                for (int h = 0; h < nsub; h++) {
+                    uint32_t col;
+                    const uint32_t mask = slots.take(g.split, col);
+                    if (!slots.acquire(acc_empty, mask, abort_flag)) {
                         batch_fail(p, kErrWaitAccum);
                         *abort_flag = 1;
                         stop = true;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t d = tmem_base + b * kAccStride;
+                    const uint32_t d = tmem_base + col;
                     if (g.split) {
-                        if (g.r == 1) issue_subtile<1, true>(a_hi0, b_desc0, d, h);
-                        else issue_subtile<2, true>(a_hi0, b_desc0, d, h);
+                        if (g.r == 1) issue_subtile<1, true>(a_hi0, band, d, h);
+                        else issue_subtile<2, true>(a_hi0, band, d, h);
                     } else {
-                        if (g.r == 1) issue_subtile<1, false>(a_hi0, b_desc0, d, h);
-                        else issue_subtile<2, false>(a_hi0, b_desc0, d, h);
+                        if (g.r == 1) issue_subtile<1, false>(a_hi0, band, d, h);
+                        else issue_subtile<2, false>(a_hi0, band, d, h);
                     }
-                    umma_commit(&acc_full[b]);
+                    slots.commit(acc_full, mask);
+                    slots.used(mask);
                     issued_any = true;
                 }
                 umma_commit(&empty[s]);
@@ -282,7 +281,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
         const int q = warp & 3;
         const int half = (warp - 2) >> 2;
         const int m = q * 32 + lane;
-        int kacc = 0;
+        AccSlots slots;
+        const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
         bool stop = false;
         for (int i = 0; !stop; i++) {
             const int j = i % kRing;
@@ -309,9 +309,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
             const int Y0 = (it.tile / g.tiles_x) * kTile;
             const int X0 = (it.tile % g.tiles_x) * kTile;
             const int nsub = sub_tiles(g);
-            for (int h = 0; h < nsub; h++, kacc++) {
-                const int b = kacc & 1;
-                ok = mbar_wait(&acc_full[b], (kacc >> 1) & 1, abort_flag);
+            for (int h = 0; h < nsub; h++) {
+                uint32_t col;
+                const uint32_t mask = slots.take(g.split, col);
+                ok = slots.ready(acc_full, mask, abort_flag);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) {
                     if (lane == 0) {
@@ -322,16 +323,25 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                     break;
                 }
                 tc_fence_after();
-                const uint32_t lane_addr = tmem_base + ((uint32_t)(q * 32) << 16) + b * kAccStride + 16;
-                if (g.split) epilogue_subtile<true>(o, lane_addr, h, half, m, Y0, X0);
-                else epilogue_subtile<false>(o, lane_addr, h, half, m, Y0, X0);
-                tc_fence_before();
+                if (g.split) {
+                    float f[Mode<true>::SUB_BLOCKS / 2][16];
+                    epilogue_load<true>(lane_base + col, half, f);
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) slots.release(acc_empty, mask);
+                    epilogue_store<true>(o, f, h, half, m, Y0, X0);
+                } else {
+                    float f[Mode<false>::SUB_BLOCKS / 2][16];
+                    epilogue_load<false>(lane_base + col, half, f);
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) slots.release(acc_empty, mask);
+                    epilogue_store<false>(o, f, h, half, m, Y0, X0);
+                }
+                slots.used(mask);
                 __threadfence();  // this warp's stores before the completion count
                 __syncwarp();
-                if (lane == 0) {
-                    mbar_arrive(&acc_empty[b]);
-                    atomicAdd(p.counters + g.ctr_base + it.t, 1u);
-                }
+                if (lane == 0) atomicAdd(p.counters + g.ctr_base + it.t, 1u);
             }
         }
     }

@@ -62,8 +62,6 @@ struct Cfg {
     static constexpr int R = stencil_r(S);
     static constexpr bool BOX = stencil_box(S);
     static constexpr int NDY = 2 * R + 1;
-    static constexpr int TMEM_COLS = 512;
-    static_assert(2 * M::ACC <= TMEM_COLS, "two accumulator buffers must fit in TMEM");
     static constexpr int STAGES = SPLIT ? 2 : 4;
     static constexpr size_t SMEM = 1024 + (size_t)STAGES * M::PLANES * kPlaneStage +
                                    (size_t)M::BAND_PLANES * NDY * kBandBytes + 256;
@@ -121,7 +119,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
     }
     if (warp == 1) {
         __syncwarp();
-        tmem_alloc(tmem_slot, C::TMEM_COLS);
+        tmem_alloc(tmem_slot, kTmemCols);
         tmem_relinquish();
     }
     build_bands(reinterpret_cast<uint16_t *>(band_base), p.coef, C::R, C::BOX, SPLIT, threadIdx.x,
@@ -171,7 +169,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
             int i = 0;
             bool issued_any = false;
             bool stop = false;
-            const uint64_t b_desc0 = smem_desc(smem_u32(band_base), 512, 128);
+            AccSlots slots;
+            const uint32_t band = smem_u32(band_base);
             for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
                 const int s = i % NS;
                 if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
@@ -183,17 +182,18 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
                     smem_u32(stage_base + (size_t)s * NP * kPlaneStage), kChunkBytes, 128);
 #pragma unroll
                 for (int h = 0; h < NSUB; h++) {
-                    const int k = i * NSUB + h;  // sub-tile counter
-                    const int b = k & 1;
-                    if (!mbar_wait(&acc_empty[b], ((k >> 1) & 1) ^ 1, abort_flag)) {
+                    uint32_t col;
+                    const uint32_t mask = slots.take(SPLIT, col);
+                    if (!slots.acquire(acc_empty, mask, abort_flag)) {
                         record_error(&g_tc_error, kErrWaitAccum);
                         *abort_flag = 1;
                         stop = true;
                         break;
                     }
                     tc_fence_after();
-                    issue_subtile<C::R, SPLIT>(a_hi0, b_desc0, tmem_base + b * M::ACC, h);
-                    umma_commit(&acc_full[b]);
+                    issue_subtile<C::R, SPLIT>(a_hi0, band, tmem_base + col, h);
+                    slots.commit(acc_full, mask);
+                    slots.used(mask);
                     issued_any = true;
                 }
                 umma_commit(&empty[s]);
@@ -221,16 +221,17 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
         o.out_lo = p.out_lo;
         o.pg = pg;
         o.y0 = p.g.y0; o.y1 = p.g.y1; o.x0 = p.g.x0; o.x1 = p.g.x1;
-        int i = 0;
         bool stop = false;
-        for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
+        AccSlots slots;
+        const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
+        for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x) {
             const int Y0 = (t / tiles_x) * kTile;
             const int X0 = (t % tiles_x) * kTile;
 #pragma unroll 1
             for (int h = 0; h < NSUB; h++) {
-                const int k = i * NSUB + h;
-                const int b = k & 1;
-                bool ok = mbar_wait(&acc_full[b], (k >> 1) & 1, abort_flag);
+                uint32_t col;
+                const uint32_t mask = slots.take(SPLIT, col);
+                bool ok = slots.ready(acc_full, mask, abort_flag);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) {
                     if (lane == 0) {
@@ -241,12 +242,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
                     break;
                 }
                 tc_fence_after();
-                // output block jl of the sub-tile is accumulator column 16(jl+1)
-                const uint32_t lane_addr = tmem_base + ((uint32_t)(q * 32) << 16) + b * M::ACC + 16;
-                epilogue_subtile<SPLIT>(o, lane_addr, h, half, m, Y0, X0);
+                float f[M::SUB_BLOCKS / 2][16];
+                epilogue_load<SPLIT>(lane_base + col, half, f);
+                // accumulators read: the issuer may refill them while we store
                 tc_fence_before();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&acc_empty[b]);
+                if (lane == 0) slots.release(acc_empty, mask);
+                slots.used(mask);
+                epilogue_store<SPLIT>(o, f, h, half, m, Y0, X0);
             }
         }
     }
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
     tc_fence_after();
     if (warp == 1) {
         __syncwarp();
-        tmem_dealloc(tmem_base, C::TMEM_COLS);
+        tmem_dealloc(tmem_base, kTmemCols);
     }
 }
 

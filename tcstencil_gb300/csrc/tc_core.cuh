@@ -18,17 +18,88 @@ constexpr int kBandElems = 32 * 16;             // one 16(K) x 32(N) FP16 band
 constexpr int kBandBytes = kBandElems * 2;
 constexpr int kEpiWarps = 8;                    // two warpgroups, one per column half
 constexpr int kThreads = 32 * (2 + kEpiWarps);  // producer, MMA issuer, epilogue
+constexpr int kTmemCols = 512;                  // two accumulator slots of 256 columns
+constexpr int kSlotCols = 256;
 constexpr uint32_t kIdesc = idesc_f16_f32(128, 32);
+constexpr uint32_t kIdescStack = idesc_f16_f32(128, 96);
 
+// Accumulator layout.
+//  plain: one 128-column tile; window w adds into columns [16w, 16w+32) of a
+//    160-column accumulator (overlapping windows accumulate in place); it
+//    occupies one slot, so two sub-tiles double-buffer.
+//  split: 64-column sub-tiles of five windows.  Each window has its own
+//    96-column region [ch.hi | cl.hi + cf.lo | c3.hi] (three products of the
+//    stacked band in one N=96 MMA, the lo product accumulated into the middle
+//    part), even windows at 96e, odd windows at 288 + 96o: 480 columns, both
+//    slots.  Neighbouring windows then never share columns, and an output
+//    block sums the second half of window j with the first half of window j+1.
 template <bool SPLIT>
 struct Mode {
     static constexpr int NSUB = SPLIT ? 2 : 1;            // sub-tiles per tile
     static constexpr int SUB_BLOCKS = kTile / 16 / NSUB;  // 16-column blocks per sub-tile
     static constexpr int SUB_WIN = SUB_BLOCKS + 1;        // input windows per sub-tile
-    static constexpr int ACC_PLANE = 16 * (SUB_BLOCKS + 2);  // TMEM columns per accumulator
-    static constexpr int ACC = ACC_PLANE * (SPLIT ? 2 : 1);
+    static constexpr int ACC = SPLIT ? 480 : 16 * (SUB_BLOCKS + 2);  // TMEM columns used
     static constexpr int PLANES = SPLIT ? 2 : 1;          // hi (and lo) data planes
-    static constexpr int BAND_PLANES = SPLIT ? 4 : 1;     // ch (and cf, cl, c3)
+    static constexpr int BAND_PLANES = SPLIT ? 4 : 1;     // band bytes per row, in kBandBytes
+};
+static_assert(Mode<false>::ACC <= kSlotCols && Mode<true>::ACC <= kTmemCols, "TMEM layout");
+
+// First TMEM column of split window w's region.
+__host__ __device__ constexpr int split_region(int w) { return (w & 1) ? 288 + 96 * (w >> 1) : 96 * (w >> 1); }
+
+// Which accumulator slots a sub-tile holds: plain sub-tiles alternate between
+// the two slots, a split sub-tile takes both.  The MMA issuer and the
+// epilogue walk the same sequence, so both see the same slots, and each slot
+// counts its own uses for the barrier parities.
+struct AccSlots {
+    uint32_t uses[2] = {0, 0};
+    int next = 0;
+    // Returns the slot mask (bit s = slot s) and the first column.
+    __device__ __forceinline__ uint32_t take(bool split, uint32_t &col) {
+        if (split) {
+            next = 0;
+            col = 0;
+            return 3u;
+        }
+        const int s = next;
+        next ^= 1;
+        col = (uint32_t)(s * kSlotCols);
+        return 1u << s;
+    }
+    __device__ __forceinline__ void used(uint32_t mask) {
+        if (mask & 1u) uses[0]++;
+        if (mask & 2u) uses[1]++;
+    }
+    // MMA issuer: waits until every slot of the mask is free (bounded).
+    __device__ __forceinline__ bool acquire(uint64_t *acc_empty, uint32_t mask,
+                                            const volatile int *abort) const {
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+            if ((mask >> s) & 1u)
+                if (!mbar_wait(&acc_empty[s], (uses[s] & 1u) ^ 1u, abort)) return false;
+        return true;
+    }
+    // MMA issuer: the slots' accumulators are complete when the MMAs are.
+    __device__ __forceinline__ void commit(uint64_t *acc_full, uint32_t mask) const {
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+            if ((mask >> s) & 1u) umma_commit(&acc_full[s]);
+    }
+    // Epilogue: waits until the slots' accumulators are complete (bounded).
+    __device__ __forceinline__ bool ready(uint64_t *acc_full, uint32_t mask,
+                                          const volatile int *abort) const {
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+            if ((mask >> s) & 1u)
+                if (!mbar_wait(&acc_full[s], uses[s] & 1u, abort)) return false;
+        return true;
+    }
+    // Epilogue (one lane per warp): this warp is done reading the slots.
+    __device__ __forceinline__ void release(uint64_t *acc_empty, uint32_t mask) const {
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+            if ((mask >> s) & 1u) mbar_arrive(&acc_empty[s]);
+    }
 };
 
 __device__ __forceinline__ uint16_t h_bits(float v) {
@@ -69,23 +140,33 @@ __device__ __forceinline__ uint16_t band_element(const float *coef, int R, bool 
     }
 }
 
-// Element offset of (n, k) in band (piece, dy), K-major core-matrix layout:
-// (piece*NDY + dy)*512 + (k/8)*256 + n*8 + k%8.
-__device__ __forceinline__ int band_offset(int ndy, int piece, int dy, int n, int k) {
-    return (piece * ndy + dy) * kBandElems + (k >> 3) * 256 + n * 8 + (k & 7);
+// Band memory of a stencil, K-major core-matrix layout (8 N-rows x 16 bytes,
+// SBO = 128 B between 8-row groups, LBO between the two K halves):
+//  plain: per coefficient row dy, a 32(N) x 16(K) band of fp16(c) at dy*512
+//    elements, LBO 512 B;
+//  split: per dy, the stacked 96 x 16 band [ch | cl | c3] at dy*1536, LBO
+//    1536 B; then per dy the 32 x 16 cf band at NDY*1536 + dy*512, LBO 512 B.
+// Both take BAND_PLANES * NDY * kBandBytes bytes.
+__device__ __forceinline__ int band_offset(int ndy, bool split, int part, int dy, int n, int k) {
+    if (!split) return dy * kBandElems + (k >> 3) * 256 + n * 8 + (k & 7);
+    if (part < 3) return dy * 1536 + (k >> 3) * 768 + (part * 32 + n) * 8 + (k & 7);
+    return ndy * 1536 + dy * kBandElems + (k >> 3) * 256 + n * 8 + (k & 7);
 }
 
 // Fills `band` (shared or global memory) with all bands of a stencil, using
-// threads [tid, .., nthreads).
+// threads [tid, .., nthreads).  Split parts 0..3 are ch, cl, c3 (stacked)
+// and cf.
 __device__ __forceinline__ void build_bands(uint16_t *band, const float *coef, int R, bool box,
                                             bool split, int tid, int nthreads) {
     const int ndy = 2 * R + 1;
-    const int pieces = split ? 4 : 1;
-    for (int idx = tid; idx < pieces * ndy * kBandElems; idx += nthreads) {
-        const int piece = idx / (ndy * kBandElems);
+    const int parts = split ? 4 : 1;
+    for (int idx = tid; idx < parts * ndy * kBandElems; idx += nthreads) {
+        const int part = idx / (ndy * kBandElems);
         const int rem = idx % (ndy * kBandElems);
         const int dy = rem / kBandElems, n = (rem >> 4) & 31, k = rem & 15;
-        band[band_offset(ndy, piece, dy, n, k)] =
+        // band_element pieces: 0 ch, 1 cf, 2 cl, 3 c3
+        const int piece = !split ? 0 : (part == 0 ? 0 : part == 1 ? 2 : part == 2 ? 3 : 1);
+        band[band_offset(ndy, split, part, dy, n, k)] =
             band_element(coef, R, box, split, piece, dy, n, k);
     }
 }
@@ -105,38 +186,98 @@ __device__ __forceinline__ void load_tile(const uint16_t *hi, const uint16_t *lo
     }
 }
 
-// MMAs of sub-tile h of a staged tile.  a_hi0 is the descriptor of the
-// stage's hi plane; b_desc0 of the first band.  Descriptors for base + offset
-// are the base descriptor plus offset >> 4 (the start-address field holds
-// address >> 4 in its low bits).  Even windows (disjoint outputs, the first
-// of them initialising) are issued before odd windows.
+// MMAs of sub-tile h of a staged tile into accumulator columns from d.
+// a_hi0 is the descriptor of the stage's hi plane (lo follows at
+// +kPlaneStage); band is the shared-memory address of the stencil's bands.
+// Descriptors for base + offset are the base descriptor plus offset >> 4 (the
+// start-address field holds address >> 4 in its low bits).
+//  plain: even windows (disjoint outputs, the first of them initialising)
+//    before odd windows, which add into the overlaps.
+//  split: per window and coefficient row, one N=96 MMA of hi with the stacked
+//    band (initialising its region on the first row) and one N=32 MMA of lo
+//    with cf into the region's middle part.
 template <int R, bool SPLIT>
-__device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint64_t b_desc0, uint32_t d_main,
-                                              int h) {
+__device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint32_t band, uint32_t d, int h) {
     using M = Mode<SPLIT>;
     constexpr int NDY = 2 * R + 1;
-    const uint64_t a_lo0 = a_hi0 + (kPlaneStage >> 4);
-    const uint32_t d_corr = d_main + M::ACC_PLANE;
+    if (!SPLIT) {
+        const uint64_t b0 = smem_desc(band, 512, 128);
 #pragma unroll
-    for (int parity = 0; parity < 2; parity++) {
+        for (int parity = 0; parity < 2; parity++) {
+#pragma unroll
+            for (int dy = 0; dy < NDY; dy++) {
+                const uint64_t b = b0 + (uint64_t)((dy * kBandBytes) >> 4);
+                const uint32_t acc = (parity == 1 || dy > 0) ? 1u : 0u;
+#pragma unroll
+                for (int w = parity; w < M::SUB_WIN; w += 2) {
+                    const int wg = h * M::SUB_BLOCKS + w;  // window in the tile
+                    const uint64_t a_off = (uint64_t)((2 * wg * kChunkBytes + (2 - R + dy) * 16) >> 4);
+                    umma_f16(d + 16 * w, a_hi0 + a_off, b, kIdesc, acc);
+                }
+            }
+        }
+    } else {
+        const uint64_t a_lo0 = a_hi0 + (kPlaneStage >> 4);
+        const uint64_t bs0 = smem_desc(band, 1536, 128);
+        const uint64_t bf0 = smem_desc(band + NDY * 3072, 512, 128);
 #pragma unroll
         for (int dy = 0; dy < NDY; dy++) {
-            const uint64_t b_ch = b_desc0 + (uint64_t)((dy * kBandBytes) >> 4);
-            const uint32_t acc = (parity == 1 || dy > 0) ? 1u : 0u;
+            const uint64_t bs = bs0 + (uint64_t)((dy * 3072) >> 4);
+            const uint64_t bf = bf0 + (uint64_t)((dy * kBandBytes) >> 4);
 #pragma unroll
-            for (int w = parity; w < M::SUB_WIN; w += 2) {
-                const int wg = h * M::SUB_BLOCKS + w;  // window in the tile
+            for (int w = 0; w < M::SUB_WIN; w++) {
+                const int wg = h * M::SUB_BLOCKS + w;
                 const uint64_t a_off = (uint64_t)((2 * wg * kChunkBytes + (2 - R + dy) * 16) >> 4);
-                umma_f16(d_main + 16 * w, a_hi0 + a_off, b_ch, kIdesc, acc);
-                if (SPLIT) {
-                    // correction accumulator, units 2^-11: cf*lo + cl*hi + c3*hi
-                    const uint64_t b_cf = b_desc0 + (uint64_t)(((NDY + dy) * kBandBytes) >> 4);
-                    const uint64_t b_cl = b_desc0 + (uint64_t)(((2 * NDY + dy) * kBandBytes) >> 4);
-                    const uint64_t b_c3 = b_desc0 + (uint64_t)(((3 * NDY + dy) * kBandBytes) >> 4);
-                    umma_f16(d_corr + 16 * w, a_lo0 + a_off, b_cf, kIdesc, acc);
-                    umma_f16(d_corr + 16 * w, a_hi0 + a_off, b_cl, kIdesc, 1);
-                    umma_f16(d_corr + 16 * w, a_hi0 + a_off, b_c3, kIdesc, 1);
-                }
+                const uint32_t dw = d + split_region(w);
+                umma_f16(dw, a_hi0 + a_off, bs, kIdescStack, dy > 0 ? 1u : 0u);
+                umma_f16(dw + 32, a_lo0 + a_off, bf, kIdesc, 1u);
+            }
+        }
+    }
+}
+
+// Epilogue, first half: this warp's accumulators of a sub-tile into
+// registers, one FP32 value per output (lanes = tile rows of the warp's lane
+// quarter, `half` = which half of the sub-tile's column blocks).  lane_col is
+// the TMEM address of the warp's lane quarter at the sub-tile's first column.
+// After it returns the accumulator may be reused.
+template <bool SPLIT>
+__device__ __forceinline__ void epilogue_load(uint32_t lane_col, int half,
+                                              float (&f)[Mode<SPLIT>::SUB_BLOCKS / 2][16]) {
+    using M = Mode<SPLIT>;
+    constexpr int G = M::SUB_BLOCKS / 2;
+    const int j0 = half * G;
+    if (!SPLIT) {
+        // output block jl is accumulator columns 16(jl+1) .. 16(jl+1)+15
+        uint32_t v[G][16];
+#pragma unroll
+        for (int gg = 0; gg < G; gg++) tmem_ld_x16(lane_col + 16 * (j0 + gg + 1), v[gg]);
+        tmem_ld_wait();
+#pragma unroll
+        for (int gg = 0; gg < G; gg++)
+#pragma unroll
+            for (int c = 0; c < 16; c++) f[gg][c] = __uint_as_float(v[gg][c]);
+    } else {
+        // block jl = second half of window jl + first half of window jl+1
+#pragma unroll
+        for (int gg = 0; gg < G; gg++) {
+            const int jl = j0 + gg;
+            const uint32_t ca = lane_col + split_region(jl) + 16;
+            const uint32_t cb = lane_col + split_region(jl + 1);
+            uint32_t v[6][16];
+#pragma unroll
+            for (int part = 0; part < 3; part++) {
+                tmem_ld_x16(ca + 32 * part, v[2 * part]);
+                tmem_ld_x16(cb + 32 * part, v[2 * part + 1]);
+            }
+            tmem_ld_wait();
+#pragma unroll
+            for (int c = 0; c < 16; c++) {
+                // main (exact sum of ch.hi), correction in units of 2^-11
+                const float main = __uint_as_float(v[0][c]) + __uint_as_float(v[1][c]);
+                const float corr = (__uint_as_float(v[2][c]) + __uint_as_float(v[3][c])) +
+                                   (__uint_as_float(v[4][c]) + __uint_as_float(v[5][c]));
+                f[gg][c] = fmaf(corr, 1.0f / 2048.0f, main);
             }
         }
     }
@@ -150,49 +291,34 @@ struct TileOut {
     int y0, y1, x0, x1;
 };
 
-// Epilogue of sub-tile h for one warp: TMEM rows of lane quarter q (tile row
-// m = 32q + lane), column blocks of `half`.  lane_addr addresses the
-// accumulator's first output block for this warp's lanes.  Cells outside the
-// update rectangle copy the input.
+// Epilogue, second half: converts and stores this warp's outputs of sub-tile
+// h (tile row m).  Cells outside the update rectangle copy the input.
 template <bool SPLIT>
-__device__ __forceinline__ void epilogue_subtile(const TileOut &o, uint32_t lane_addr, int h,
-                                                 int half, int m, int Y0, int X0) {
+__device__ __forceinline__ void epilogue_store(const TileOut &o,
+                                               const float (&f)[Mode<SPLIT>::SUB_BLOCKS / 2][16],
+                                               int h, int half, int m, int Y0, int X0) {
     using M = Mode<SPLIT>;
-    constexpr int G = M::SUB_BLOCKS / 2;  // this warp's blocks, one TMEM round trip
+    constexpr int G = M::SUB_BLOCKS / 2;
     const int j0 = half * G;
     const int y = Y0 + m;
     const bool fast = Y0 >= o.y0 && Y0 + kTile <= o.y1 && X0 >= o.x0 && X0 + kTile <= o.x1;
     const bool row_in = y >= o.y0 && y < o.y1;
-    uint32_t v[G][16];
-    uint32_t w[SPLIT ? G : 1][16];
-#pragma unroll
-    for (int gg = 0; gg < G; gg++) {
-        tmem_ld_x16(lane_addr + 16 * (j0 + gg), v[gg]);
-        if (SPLIT) tmem_ld_x16(lane_addr + M::ACC_PLANE + 16 * (j0 + gg), w[SPLIT ? gg : 0]);
-    }
-    tmem_ld_wait();
 #pragma unroll
     for (int gg = 0; gg < G; gg++) {
         const int xb = X0 + 16 * (h * M::SUB_BLOCKS + j0 + gg);
         const size_t off0 = plane_index(o.pg, y, xb);     // cells xb .. xb+7
         const size_t off1 = off0 + (size_t)o.pg.nyp * 8;  // cells xb+8 .. xb+15
-        float f[16];
-#pragma unroll
-        for (int c = 0; c < 16; c++) {
-            f[c] = __uint_as_float(v[gg][c]);
-            if (SPLIT) f[c] = fmaf(__uint_as_float(w[SPLIT ? gg : 0][c]), 1.0f / 2048.0f, f[c]);
-        }
         uint32_t hw[8], lw[8];
         if (fast) {
 #pragma unroll
             for (int c = 0; c < 8; c++) {
                 uint16_t h0, h1, l0 = 0, l1 = 0;
                 if (SPLIT) {
-                    split_fixed(f[2 * c], h0, l0);
-                    split_fixed(f[2 * c + 1], h1, l1);
+                    split_fixed(f[gg][2 * c], h0, l0);
+                    split_fixed(f[gg][2 * c + 1], h1, l1);
                 } else {
-                    h0 = h_bits(f[2 * c]);
-                    h1 = h_bits(f[2 * c + 1]);
+                    h0 = h_bits(f[gg][2 * c]);
+                    h1 = h_bits(f[gg][2 * c + 1]);
                 }
                 hw[c] = (uint32_t)h0 | ((uint32_t)h1 << 16);
                 lw[c] = (uint32_t)l0 | ((uint32_t)l1 << 16);
@@ -216,8 +342,8 @@ __device__ __forceinline__ void epilogue_subtile(const TileOut &o, uint32_t lane
                     const int x = xb + 2 * c + u;
                     const bool upd = row_in && x >= o.x0 && x < o.x1;
                     if (upd) {
-                        if (SPLIT) split_fixed(f[2 * c + u], hh[u], ll[u]);
-                        else { hh[u] = h_bits(f[2 * c + u]); ll[u] = 0; }
+                        if (SPLIT) split_fixed(f[gg][2 * c + u], hh[u], ll[u]);
+                        else { hh[u] = h_bits(f[gg][2 * c + u]); ll[u] = 0; }
                     } else {
                         hh[u] = (uint16_t)(iw[c] >> (16 * u));
                         ll[u] = (uint16_t)(il[c] >> (16 * u));
