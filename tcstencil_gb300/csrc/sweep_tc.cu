@@ -264,6 +264,228 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
     }
 }
 
+// Split form, single grid: a streaming window ring.  The nine 16-column
+// windows of a tile (kTile / 16 + 1) are computed once each, in order, into a
+// ring of kRingSlots 96-column TMEM regions (slot = global window index mod
+// kRingSlots), and output block j is read from windows j and j+1 as soon as
+// both are complete.  The MMA issuer can so run ahead of the epilogue by a
+// few windows, instead of the two alternating with the whole accumulator.
+// Epilogue group g (warps 2-5, 6-9) takes the blocks of parity g, so each
+// group reads each window once (window 0 only group 0, window 8 only group 1;
+// the other group releases those without reading).  A slot is free again when
+// all eight epilogue warps have released its window; every warp releases a
+// window only after seeing it complete, so releases always count toward the
+// window they belong to.
+constexpr int kRingSlots = 5;
+constexpr int kRegionCols = 96;
+constexpr int kTileWindows = kTile / 16 + 1;
+static_assert(kRingSlots * kRegionCols <= kTmemCols, "window ring fits TMEM");
+
+template <int S>
+__global__ void __launch_bounds__(kThreads, 1) tc_split_ring_kernel(const TcParams p) {
+    using C = Cfg<S, true>;
+    using M = Mode<true>;
+    constexpr int NS = C::STAGES;
+    constexpr int NP = M::PLANES;
+
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                ~static_cast<uintptr_t>(1023));
+    uint8_t *stage_base = smem;                                 // [NS][NP][stage]
+    uint8_t *band_base = smem + (size_t)NS * NP * kPlaneStage;  // NDY * 4 KB
+    uint64_t *bars =
+        reinterpret_cast<uint64_t *>(band_base + M::BAND_PLANES * C::NDY * kBandBytes);
+    uint64_t *full = bars;                                    // [NS]
+    uint64_t *empty = bars + NS;                              // [NS]
+    uint64_t *win_full = bars + 2 * NS;                       // [kRingSlots]
+    uint64_t *win_empty = bars + 2 * NS + kRingSlots;         // [kRingSlots]
+    uint64_t *drain = bars + 2 * NS + 2 * kRingSlots;         // [1]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    static_assert((2 * NS + 2 * kRingSlots + 1) * 8 + 8 <= 256, "barrier area");
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const PlaneGeom pg = p.g.p16;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int r = 0; r < kRingSlots; r++) {
+            mbar_init(&win_full[r], 1);
+            mbar_init(&win_empty[r], kEpiWarps);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 1) {
+        __syncwarp();
+        tmem_alloc(tmem_slot, kTmemCols);
+        tmem_relinquish();
+    }
+    build_bands(reinterpret_cast<uint16_t *>(band_base), p.coef, C::R, C::BOX, true, threadIdx.x,
+                kThreads);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    const int tiles_x = p.tiles_x;
+    const int n_tiles = p.n_tiles;
+
+    if (warp == 0) {
+        // ------------------------------------------------------ producer ---
+        if (lane == 0) {
+            int i = 0;
+            int last_issued = -1;
+            for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, i++) {
+                const int s = i % NS;
+                if (!mbar_wait(&empty[s], ((i / NS) & 1) ^ 1, abort_flag)) {
+                    record_error(&g_tc_error, kErrWaitEmpty);
+                    *abort_flag = 1;
+                    break;
+                }
+                mbar_arrive_expect_tx(&full[s], NP * kPlaneStage);
+                load_tile(p.in_hi, p.in_lo, NP, pg, (t / tiles_x) * kTile, (t % tiles_x) * kTile,
+                          stage_base + (size_t)s * NP * kPlaneStage, &full[s]);
+                last_issued = i;
+            }
+            for (int k = 0; k < NS && last_issued - k >= 0; k++) {
+                const int ii = last_issued - k;
+                const uint64_t t0 = global_timer_ns();
+                while (!mbar_try_wait(&full[ii % NS], (ii / NS) & 1)) {
+                    if (global_timer_ns() - t0 > kWaitLimitNs) {
+                        record_error(&g_tc_error, kErrWaitDrain);
+                        break;
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------- MMA issuer ---
+        if (lane == 0) {
+            int i = 0, G = 0;  // tiles, global windows
+            bool issued_any = false;
+            bool stop = false;
+            const uint32_t band = smem_u32(band_base);
+            for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
+                const int s = i % NS;
+                if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
+                    record_error(&g_tc_error, kErrWaitFull);
+                    *abort_flag = 1;
+                    break;
+                }
+                const uint64_t a_hi0 = smem_desc(
+                    smem_u32(stage_base + (size_t)s * NP * kPlaneStage), kChunkBytes, 128);
+#pragma unroll 1
+                for (int wg = 0; wg < kTileWindows; wg++, G++) {
+                    const int r = G % kRingSlots;
+                    if (!mbar_wait(&win_empty[r], ((G / kRingSlots) & 1) ^ 1, abort_flag)) {
+                        record_error(&g_tc_error, kErrWaitAccum);
+                        *abort_flag = 1;
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    issue_split_window<C::R>(a_hi0, band, tmem_base + r * kRegionCols, wg);
+                    umma_commit(&win_full[r]);
+                    issued_any = true;
+                }
+                umma_commit(&empty[s]);
+            }
+            if (issued_any) {
+                umma_commit(drain);
+                const uint64_t t0 = global_timer_ns();
+                while (!mbar_try_wait(drain, 0)) {
+                    if (global_timer_ns() - t0 > kWaitLimitNs) {
+                        record_error(&g_tc_error, kErrWaitDrain);
+                        break;
+                    }
+                }
+            }
+        }
+    } else {
+        // ------------------------------------------------------ epilogue ---
+        const int q = warp & 3;           // TMEM lane quarter
+        const int grp = (warp - 2) >> 2;  // block parity of this group
+        const int m = q * 32 + lane;
+        const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
+        TileOut o;
+        o.in_hi = p.in_hi;
+        o.in_lo = p.in_lo;
+        o.out_hi = p.out_hi;
+        o.out_lo = p.out_lo;
+        o.pg = pg;
+        o.y0 = p.g.y0; o.y1 = p.g.y1; o.x0 = p.g.x0; o.x1 = p.g.x1;
+        // waits (bounded) until global window Gw is complete
+        auto window_ready = [&](int Gw) {
+            bool ok = mbar_wait(&win_full[Gw % kRingSlots], (Gw / kRingSlots) & 1, abort_flag);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok && lane == 0) {
+                record_error(&g_tc_error, kErrWaitResult);
+                *abort_flag = 1;
+            }
+            return ok;
+        };
+        bool stop = false;
+        int G0 = 0;  // first global window of the tile
+        for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, G0 += kTileWindows) {
+            const int Y0 = (t / tiles_x) * kTile;
+            const int X0 = (t % tiles_x) * kTile;
+            const int y = Y0 + m;
+            const bool fast = tile_inside(o, Y0, X0);
+            const bool row_in = y >= o.y0 && y < o.y1;
+            if (grp == 1) {
+                // window 0 is read by group 0 only
+                if (!window_ready(G0)) break;
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&win_empty[G0 % kRingSlots]);
+            }
+#pragma unroll 1
+            for (int j = grp; j < kTileWindows - 1; j += 2) {
+                const int Ga = G0 + j, Gb = Ga + 1;
+                if (!window_ready(Ga) || !window_ready(Gb)) {
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                float f[16];
+                split_block_load(lane_base + (Ga % kRingSlots) * kRegionCols,
+                                 lane_base + (Gb % kRingSlots) * kRegionCols, f);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(&win_empty[Ga % kRingSlots]);
+                    mbar_arrive(&win_empty[Gb % kRingSlots]);
+                }
+                store_block<true>(o, f, y, X0 + 16 * j, fast, row_in);
+            }
+            if (stop) break;
+            if (grp == 0) {
+                // the last window is read by group 1 only
+                const int Gl = G0 + kTileWindows - 1;
+                if (!window_ready(Gl)) break;
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&win_empty[Gl % kRingSlots]);
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) {
+        __syncwarp();
+        tmem_dealloc(tmem_base, kTmemCols);
+    }
+}
+
 int g_num_sms = 0;
 
 // Sets the kernel's shared-memory limit and reads the SM count; called before
@@ -272,9 +494,15 @@ template <int S, bool SPLIT>
 cudaError_t prepare_tc() {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(tc_sweep_kernel<S, SPLIT>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(Cfg<S, SPLIT>::SMEM));
+        cudaError_t e;
+        if constexpr (SPLIT)
+            e = cudaFuncSetAttribute(tc_split_ring_kernel<S>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(Cfg<S, SPLIT>::SMEM));
+        else
+            e = cudaFuncSetAttribute(tc_sweep_kernel<S, SPLIT>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(Cfg<S, SPLIT>::SMEM));
         if (e != cudaSuccess) return e;
         configured = true;
     }
@@ -305,7 +533,8 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     for (int k = 0; k < 25; k++) p.coef[k] = 0.0f;
     for (int k = 0; k < C::NDY * C::NDY; k++) p.coef[k] = B[k];
     const int grid = p.n_tiles < g_num_sms ? p.n_tiles : g_num_sms;
-    tc_sweep_kernel<S, SPLIT><<<grid, kThreads, C::SMEM, s>>>(p);
+    if constexpr (SPLIT) tc_split_ring_kernel<S><<<grid, kThreads, C::SMEM, s>>>(p);
+    else tc_sweep_kernel<S, SPLIT><<<grid, kThreads, C::SMEM, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -118,6 +118,36 @@ __device__ __forceinline__ void split_fixed(float v, uint16_t &hi, uint16_t &lo)
     lo = h_bits((v - h_val(hi)) * 2048.0f);
 }
 
+// Two FP32 values as packed FP16 (round to nearest even), v0 in the low half.
+__device__ __forceinline__ uint32_t pack_h2(float v0, float v1) {
+    const __half2 h = __floats2half2_rn(v0, v1);
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// split_fixed of two values into packed hi and lo words, with the same bits
+// and less conversion work: u = v 2^11 is exact, t = rint(u) is formed by the
+// add-and-subtract of 1.5 * 2^23 (round to nearest even for |u| < 2^22; the
+// sign copy keeps rint's -0 for small negative u).  While |t| <= 2^11, hi =
+// t 2^-11 is exact in FP16 and lo = u - t = (v - hi) 2^11 is exact; past that
+// (|v| slightly above 1, or NaN) hi rounds in FP16 and split_fixed's rule is
+// taken.
+__device__ __forceinline__ void split_pair(float v0, float v1, uint32_t &hw, uint32_t &lw) {
+    constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
+    const float u0 = v0 * 2048.0f, u1 = v1 * 2048.0f;
+    const float t0 = copysignf(__fsub_rn(__fadd_rn(u0, kRound), kRound), u0);
+    const float t1 = copysignf(__fsub_rn(__fadd_rn(u1, kRound), kRound), u1);
+    if (fabsf(t0) <= 2048.0f && fabsf(t1) <= 2048.0f) {
+        hw = pack_h2(t0 * (1.0f / 2048.0f), t1 * (1.0f / 2048.0f));
+        lw = pack_h2(__fsub_rn(u0, t0), __fsub_rn(u1, t1));
+    } else {
+        uint16_t h0, l0, h1, l1;
+        split_fixed(v0, h0, l0);
+        split_fixed(v1, h1, l1);
+        hw = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        lw = (uint32_t)l0 | ((uint32_t)l1 << 16);
+    }
+}
+
 // Band element (n, k) of coefficient row dy: input column k of a 16-column
 // window feeds output column n of its 32-column range with tap dx = 8 + k - n.
 // Pieces: plain -> fp16(c); split -> 0: ch = rint(c 2^11) 2^-11, 1: cf =
@@ -186,6 +216,48 @@ __device__ __forceinline__ void load_tile(const uint16_t *hi, const uint16_t *lo
     }
 }
 
+// One 16-column output block of the split form from the regions of its two
+// windows (TMEM addresses of this warp's lane quarter at each region): the
+// second half of window a plus the first half of window b, per part.
+__device__ __forceinline__ void split_block_load(uint32_t region_a, uint32_t region_b,
+                                                 float (&f)[16]) {
+    uint32_t v[6][16];
+#pragma unroll
+    for (int part = 0; part < 3; part++) {
+        tmem_ld_x16(region_a + 16 + 32 * part, v[2 * part]);
+        tmem_ld_x16(region_b + 32 * part, v[2 * part + 1]);
+    }
+    tmem_ld_wait();
+#pragma unroll
+    for (int c = 0; c < 16; c++) {
+        // main (exact sum of ch.hi), correction in units of 2^-11
+        const float main = __uint_as_float(v[0][c]) + __uint_as_float(v[1][c]);
+        const float corr = (__uint_as_float(v[2][c]) + __uint_as_float(v[3][c])) +
+                           (__uint_as_float(v[4][c]) + __uint_as_float(v[5][c]));
+        f[c] = fmaf(corr, 1.0f / 2048.0f, main);
+    }
+}
+
+// MMAs of one split window (global window index wg of a staged tile) into
+// the 96-column region at d: per coefficient row, the stacked hi MMA (which
+// initialises the region on the first row) and the lo MMA into its middle
+// part.
+template <int R>
+__device__ __forceinline__ void issue_split_window(uint64_t a_hi0, uint32_t band, uint32_t d,
+                                                   int wg) {
+    constexpr int NDY = 2 * R + 1;
+    const uint64_t a_lo0 = a_hi0 + (kPlaneStage >> 4);
+    const uint64_t bs0 = smem_desc(band, 1536, 128);
+    const uint64_t bf0 = smem_desc(band + NDY * 3072, 512, 128);
+#pragma unroll
+    for (int dy = 0; dy < NDY; dy++) {
+        const uint64_t a_off = (uint64_t)((2 * wg * kChunkBytes + (2 - R + dy) * 16) >> 4);
+        umma_f16(d, a_hi0 + a_off, bs0 + (uint64_t)((dy * 3072) >> 4), kIdescStack,
+                 dy > 0 ? 1u : 0u);
+        umma_f16(d + 32, a_lo0 + a_off, bf0 + (uint64_t)((dy * kBandBytes) >> 4), kIdesc, 1u);
+    }
+}
+
 // MMAs of sub-tile h of a staged tile into accumulator columns from d.
 // a_hi0 is the descriptor of the stage's hi plane (lo follows at
 // +kPlaneStage); band is the shared-memory address of the stencil's bands.
@@ -217,22 +289,9 @@ __device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint32_t band, uin
             }
         }
     } else {
-        const uint64_t a_lo0 = a_hi0 + (kPlaneStage >> 4);
-        const uint64_t bs0 = smem_desc(band, 1536, 128);
-        const uint64_t bf0 = smem_desc(band + NDY * 3072, 512, 128);
 #pragma unroll
-        for (int dy = 0; dy < NDY; dy++) {
-            const uint64_t bs = bs0 + (uint64_t)((dy * 3072) >> 4);
-            const uint64_t bf = bf0 + (uint64_t)((dy * kBandBytes) >> 4);
-#pragma unroll
-            for (int w = 0; w < M::SUB_WIN; w++) {
-                const int wg = h * M::SUB_BLOCKS + w;
-                const uint64_t a_off = (uint64_t)((2 * wg * kChunkBytes + (2 - R + dy) * 16) >> 4);
-                const uint32_t dw = d + split_region(w);
-                umma_f16(dw, a_hi0 + a_off, bs, kIdescStack, dy > 0 ? 1u : 0u);
-                umma_f16(dw + 32, a_lo0 + a_off, bf, kIdesc, 1u);
-            }
-        }
+        for (int w = 0; w < M::SUB_WIN; w++)
+            issue_split_window<R>(a_hi0, band, d + split_region(w), h * M::SUB_BLOCKS + w);
     }
 }
 
@@ -262,23 +321,7 @@ __device__ __forceinline__ void epilogue_load(uint32_t lane_col, int half,
 #pragma unroll
         for (int gg = 0; gg < G; gg++) {
             const int jl = j0 + gg;
-            const uint32_t ca = lane_col + split_region(jl) + 16;
-            const uint32_t cb = lane_col + split_region(jl + 1);
-            uint32_t v[6][16];
-#pragma unroll
-            for (int part = 0; part < 3; part++) {
-                tmem_ld_x16(ca + 32 * part, v[2 * part]);
-                tmem_ld_x16(cb + 32 * part, v[2 * part + 1]);
-            }
-            tmem_ld_wait();
-#pragma unroll
-            for (int c = 0; c < 16; c++) {
-                // main (exact sum of ch.hi), correction in units of 2^-11
-                const float main = __uint_as_float(v[0][c]) + __uint_as_float(v[1][c]);
-                const float corr = (__uint_as_float(v[2][c]) + __uint_as_float(v[3][c])) +
-                                   (__uint_as_float(v[4][c]) + __uint_as_float(v[5][c]));
-                f[gg][c] = fmaf(corr, 1.0f / 2048.0f, main);
-            }
+            split_block_load(lane_col + split_region(jl), lane_col + split_region(jl + 1), f[gg]);
         }
     }
 }
@@ -291,8 +334,69 @@ struct TileOut {
     int y0, y1, x0, x1;
 };
 
+// Converts and stores one 16-column output block of tile row y (cells xb ..
+// xb+15).  fast: the whole tile is inside the update rectangle; otherwise
+// cells outside it copy the input.
+template <bool SPLIT>
+__device__ __forceinline__ void store_block(const TileOut &o, const float (&f)[16], int y, int xb,
+                                            bool fast, bool row_in) {
+    const size_t off0 = plane_index(o.pg, y, xb);     // cells xb .. xb+7
+    const size_t off1 = off0 + (size_t)o.pg.nyp * 8;  // cells xb+8 .. xb+15
+    uint32_t hw[8], lw[8];
+    if (fast) {
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            if (SPLIT) {
+                split_pair(f[2 * c], f[2 * c + 1], hw[c], lw[c]);
+            } else {
+                hw[c] = pack_h2(f[2 * c], f[2 * c + 1]);
+                lw[c] = 0;
+            }
+        }
+    } else {
+        const uint4 i0 = *reinterpret_cast<const uint4 *>(o.in_hi + off0);
+        const uint4 i1 = *reinterpret_cast<const uint4 *>(o.in_hi + off1);
+        const uint32_t iw[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
+        uint32_t il[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (SPLIT) {
+            const uint4 l0 = *reinterpret_cast<const uint4 *>(o.in_lo + off0);
+            const uint4 l1 = *reinterpret_cast<const uint4 *>(o.in_lo + off1);
+            il[0] = l0.x; il[1] = l0.y; il[2] = l0.z; il[3] = l0.w;
+            il[4] = l1.x; il[5] = l1.y; il[6] = l1.z; il[7] = l1.w;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            uint16_t hh[2], ll[2];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int x = xb + 2 * c + u;
+                const bool upd = row_in && x >= o.x0 && x < o.x1;
+                if (upd) {
+                    if (SPLIT) split_fixed(f[2 * c + u], hh[u], ll[u]);
+                    else { hh[u] = h_bits(f[2 * c + u]); ll[u] = 0; }
+                } else {
+                    hh[u] = (uint16_t)(iw[c] >> (16 * u));
+                    ll[u] = (uint16_t)(il[c] >> (16 * u));
+                }
+            }
+            hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
+            lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
+        }
+    }
+    *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+    if (SPLIT) {
+        *reinterpret_cast<uint4 *>(o.out_lo + off0) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        *reinterpret_cast<uint4 *>(o.out_lo + off1) = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+    }
+}
+
+__device__ __forceinline__ bool tile_inside(const TileOut &o, int Y0, int X0) {
+    return Y0 >= o.y0 && Y0 + kTile <= o.y1 && X0 >= o.x0 && X0 + kTile <= o.x1;
+}
+
 // Epilogue, second half: converts and stores this warp's outputs of sub-tile
-// h (tile row m).  Cells outside the update rectangle copy the input.
+// h (tile row m).
 template <bool SPLIT>
 __device__ __forceinline__ void epilogue_store(const TileOut &o,
                                                const float (&f)[Mode<SPLIT>::SUB_BLOCKS / 2][16],
@@ -301,65 +405,11 @@ __device__ __forceinline__ void epilogue_store(const TileOut &o,
     constexpr int G = M::SUB_BLOCKS / 2;
     const int j0 = half * G;
     const int y = Y0 + m;
-    const bool fast = Y0 >= o.y0 && Y0 + kTile <= o.y1 && X0 >= o.x0 && X0 + kTile <= o.x1;
+    const bool fast = tile_inside(o, Y0, X0);
     const bool row_in = y >= o.y0 && y < o.y1;
 #pragma unroll
-    for (int gg = 0; gg < G; gg++) {
-        const int xb = X0 + 16 * (h * M::SUB_BLOCKS + j0 + gg);
-        const size_t off0 = plane_index(o.pg, y, xb);     // cells xb .. xb+7
-        const size_t off1 = off0 + (size_t)o.pg.nyp * 8;  // cells xb+8 .. xb+15
-        uint32_t hw[8], lw[8];
-        if (fast) {
-#pragma unroll
-            for (int c = 0; c < 8; c++) {
-                uint16_t h0, h1, l0 = 0, l1 = 0;
-                if (SPLIT) {
-                    split_fixed(f[gg][2 * c], h0, l0);
-                    split_fixed(f[gg][2 * c + 1], h1, l1);
-                } else {
-                    h0 = h_bits(f[gg][2 * c]);
-                    h1 = h_bits(f[gg][2 * c + 1]);
-                }
-                hw[c] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-                lw[c] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-            }
-        } else {
-            const uint4 i0 = *reinterpret_cast<const uint4 *>(o.in_hi + off0);
-            const uint4 i1 = *reinterpret_cast<const uint4 *>(o.in_hi + off1);
-            const uint32_t iw[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
-            uint32_t il[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            if (SPLIT) {
-                const uint4 l0 = *reinterpret_cast<const uint4 *>(o.in_lo + off0);
-                const uint4 l1 = *reinterpret_cast<const uint4 *>(o.in_lo + off1);
-                il[0] = l0.x; il[1] = l0.y; il[2] = l0.z; il[3] = l0.w;
-                il[4] = l1.x; il[5] = l1.y; il[6] = l1.z; il[7] = l1.w;
-            }
-#pragma unroll
-            for (int c = 0; c < 8; c++) {
-                uint16_t hh[2], ll[2];
-#pragma unroll
-                for (int u = 0; u < 2; u++) {
-                    const int x = xb + 2 * c + u;
-                    const bool upd = row_in && x >= o.x0 && x < o.x1;
-                    if (upd) {
-                        if (SPLIT) split_fixed(f[gg][2 * c + u], hh[u], ll[u]);
-                        else { hh[u] = h_bits(f[gg][2 * c + u]); ll[u] = 0; }
-                    } else {
-                        hh[u] = (uint16_t)(iw[c] >> (16 * u));
-                        ll[u] = (uint16_t)(il[c] >> (16 * u));
-                    }
-                }
-                hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
-                lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
-            }
-        }
-        *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-        *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
-        if (SPLIT) {
-            *reinterpret_cast<uint4 *>(o.out_lo + off0) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-            *reinterpret_cast<uint4 *>(o.out_lo + off1) = make_uint4(lw[4], lw[5], lw[6], lw[7]);
-        }
-    }
+    for (int gg = 0; gg < G; gg++)
+        store_block<SPLIT>(o, f[gg], y, X0 + 16 * (h * M::SUB_BLOCKS + j0 + gg), fast, row_in);
 }
 
 }  // namespace tc
