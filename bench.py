@@ -73,6 +73,20 @@ def run_profile(args):
 
     import tcstencil_gb300 as tcs
 
+    if args.workload == "batch":
+        from tcstencil_gb300.workloads import mixed_batch
+
+        specs = mixed_batch(args.batch_grids)
+        b = build_batch(tcs, specs)
+        for k, sp in enumerate(specs):
+            b.upload(k, sp.grid())
+        b.run(use_graph=False)
+        b.run(use_graph=False)
+        torch.cuda.synchronize()
+        assert tcs.device_error() == 0
+        print(f"profile run: batch of {args.batch_grids} mixed grids x 2 runs {b.info()}")
+        b.close()
+        return
     n = args.interior + 2 * HALO
     A, B = make_inputs(n, args.stencil, 1000)
     plan = tcs.Plan(n, n, args.stencil, B, engine=args.engine, precision=args.precision)
