@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--precision", default="f16")
     ap.add_argument("--interior", type=int, default=INTERIOR)
     ap.add_argument("--timesteps", type=int, default=TIMESTEPS)
+    ap.add_argument("--temporal-depth", type=int, default=1,
+                    help="2: split sweeps in temporally blocked pairs")
     ap.add_argument("--no-extras", action="store_true", help="skip comparator and CPU legs")
     ap.add_argument("--workload", choices=["sweep", "batch", "serve"], default="sweep",
                     help="sweep: one grid (default); batch: 512 mixed grids in one "
@@ -89,7 +91,8 @@ def run_profile(args):
         return
     n = args.interior + 2 * HALO
     A, B = make_inputs(n, args.stencil, 1000)
-    plan = tcs.Plan(n, n, args.stencil, B, engine=args.engine, precision=args.precision)
+    plan = tcs.Plan(n, n, args.stencil, B, engine=args.engine, precision=args.precision,
+                    temporal_depth=args.temporal_depth)
     plan.upload(A)
     plan.run(args.timesteps, use_graph=False)
     torch.cuda.synchronize()
@@ -350,7 +353,8 @@ def run_ours(args):
     n = args.interior + 2 * HALO
     A, B = make_inputs(n, args.stencil, 1000 + rank)
     stream = torch.cuda.current_stream()
-    plan = tcs.Plan(n, n, args.stencil, B, engine=args.engine, precision=args.precision)
+    plan = tcs.Plan(n, n, args.stencil, B, engine=args.engine, precision=args.precision,
+                    temporal_depth=args.temporal_depth)
     plan.upload(A)
     torch.cuda.synchronize()
     updates_per_step = args.interior * args.interior * args.timesteps

@@ -210,6 +210,10 @@ int tcs_plan_state(tcs_plan plan, void **hi, void **lo, size_t *plane_bytes);
 int tcs_plan_scale_exp(tcs_plan plan, int *scale_exp);
 /* Replaces the coefficients (host n*n). */
 int tcs_plan_set_coeffs(tcs_plan plan, const float *coeffs);
+/* Temporal blocking depth: 1 (one launch per step, the default) or 2 (two
+ * steps per launch, intermediate kept on chip; split precision on the tensor
+ * engine).  Results are bit-identical either way; the autotuner picks. */
+int tcs_plan_set_temporal_depth(tcs_plan plan, int depth);
 
 /* One-call form: host FP32 grid in, `steps` steps, host FP32 grid out.  Device
  * state is kept in a per-thread cache keyed by shape and mode, so repeated

@@ -110,6 +110,7 @@ SIGNATURES = {
     "tcs_plan_run": (_I, [_P, _I, _I, _P]),
     "tcs_plan_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_SZ)]),
     "tcs_plan_set_coeffs": (_I, [_P, _P]),
+    "tcs_plan_set_temporal_depth": (_I, [_P, _I]),
     "tcs_sweep_host": (_I, [_P, _P, ctypes.POINTER(Problem), _I]),
     "tcs_noalloc_scratch_bytes": (_SZ, []),
     "tcs_sweep_steps_noalloc": (_I, [ctypes.POINTER(StepArgs), _P, _P, _I, _P]),
@@ -272,12 +273,16 @@ class Plan:
     """Device-resident sweep of one grid (tcs_plan_*)."""
 
     def __init__(self, ny: int, nx: int, stencil: str, coeffs, engine: str = "tensor",
-                 precision: str = "f16", rect=None):
-        """engine "auto" takes the autotuner's choice for this problem class."""
+                 precision: str = "f16", rect=None, temporal_depth: int | None = None):
+        """engine "auto" takes the autotuner's choice for this problem class
+        (engine and temporal depth); temporal_depth 2 runs steps in blocked
+        pairs (split precision, tensor engine)."""
         if engine == "auto":
-            from .autotune import best_engine
+            from .autotune import best_config
 
-            engine = best_engine(stencil, precision, ny, nx)
+            engine, tuned_depth = best_config(stencil, precision, ny, nx)
+            if temporal_depth is None:
+                temporal_depth = tuned_depth
         self._c = _coeffs(coeffs, stencil)
         y0, y1, x0, x1 = _rect(rect)
         self.ny, self.nx, self.stencil, self.engine, self.precision = ny, nx, stencil, engine, precision
@@ -286,6 +291,11 @@ class Plan:
         h = ctypes.c_void_p()
         _check(lib().tcs_plan_create(ctypes.byref(pr), ctypes.byref(h)))
         self._h = h
+        if temporal_depth and temporal_depth != 1:
+            self.set_temporal_depth(temporal_depth)
+
+    def set_temporal_depth(self, depth: int) -> None:
+        _check(lib().tcs_plan_set_temporal_depth(self._h, int(depth)))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

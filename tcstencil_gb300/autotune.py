@@ -7,6 +7,7 @@ script/process_data.py:29-43).  Here the candidates are run-time choices of
 one library, timed with CUDA events:
 
   sweep  (stencil, precision, size class) -> engine ("tensor" | "cudacore")
+                                             and temporal depth (1 | 2)
   serve  (offered load)                   -> round_steps of the request server
 
 Size classes are powers of two of each side, so one entry covers grids of
@@ -31,6 +32,10 @@ import numpy as np
 from .workloads import RADIUS, normalized_coeffs
 
 ENGINES_FOR = {"f16": ("tensor", "cudacore"), "split": ("tensor",), "f32": ("cudacore",)}
+# (engine, temporal depth) candidates per precision
+CANDIDATES = {"f16": (("tensor", 1), ("cudacore", 1)),
+              "split": (("tensor", 1), ("tensor", 2)),
+              "f32": (("cudacore", 1),)}
 DEFAULT_ROUND_STEPS = 16
 
 
@@ -102,8 +107,8 @@ def pick_fastest(timings: dict) -> str:
     return min(timings, key=lambda k: (timings[k], list(timings).index(k)))
 
 
-def time_sweep(engine: str, stencil: str, precision: str, ny: int, nx: int, steps: int,
-               reps: int = 3) -> float:
+def time_sweep(engine: str, depth: int, stencil: str, precision: str, ny: int, nx: int,
+               steps: int, reps: int = 3) -> float:
     """Seconds per step of a plan on the device (CUDA-graph runs, CUDA events)."""
     import torch
 
@@ -112,7 +117,7 @@ def time_sweep(engine: str, stencil: str, precision: str, ny: int, nx: int, step
     rng = np.random.default_rng(7)
     g = rng.uniform(-1, 1, (ny, nx)).astype(np.float32)
     p = tcs.Plan(ny, nx, stencil, normalized_coeffs(rng, stencil), engine=engine,
-                 precision=precision)
+                 precision=precision, temporal_depth=depth)
     try:
         p.upload(g)
         p.run(steps, use_graph=True)
@@ -133,25 +138,34 @@ def time_sweep(engine: str, stencil: str, precision: str, ny: int, nx: int, step
 
 def tune_sweep(stencil: str, precision: str, ny: int, nx: int, steps: int = 20,
                cache: Cache | None = None, timer=time_sweep) -> dict:
-    """Times every engine that supports the precision; stores and returns
-    {"engine": best, "s_per_step": {engine: seconds}}."""
+    """Times every (engine, temporal depth) that supports the precision; stores
+    and returns {"engine", "temporal_depth", "s_per_step": {"engine/depth": s}}."""
     cache = cache or Cache()
-    timings = {e: timer(e, stencil, precision, ny, nx, steps) for e in ENGINES_FOR[precision]}
-    entry = {"engine": pick_fastest(timings), "s_per_step": timings,
+    timings = {f"{e}/{d}": timer(e, d, stencil, precision, ny, nx, steps)
+               for e, d in CANDIDATES[precision]}
+    best = pick_fastest(timings)
+    engine, depth = best.split("/")
+    entry = {"engine": engine, "temporal_depth": int(depth), "s_per_step": timings,
              "measured_on": [ny, nx], "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
     cache.section("sweep")[sweep_key(stencil, precision, ny, nx)] = entry
     cache.save()
     return entry
 
 
-def best_engine(stencil: str, precision: str, ny: int, nx: int, cache: Cache | None = None) -> str:
-    """The tuned engine for this problem class, else the tensor engine (the
-    CUDA-core engine for FP32, the only one that has it)."""
+def best_config(stencil: str, precision: str, ny: int, nx: int,
+                cache: Cache | None = None) -> tuple:
+    """The tuned (engine, temporal depth) for this problem class, else the
+    tensor engine at depth 1 (the CUDA-core engine for FP32, the only one
+    that has it)."""
     cache = cache or Cache()
     e = cache.lookup("sweep", sweep_key(stencil, precision, ny, nx))
     if e:
-        return e["engine"]
-    return ENGINES_FOR[precision][0]
+        return e["engine"], int(e.get("temporal_depth", 1))
+    return CANDIDATES[precision][0]
+
+
+def best_engine(stencil: str, precision: str, ny: int, nx: int, cache: Cache | None = None) -> str:
+    return best_config(stencil, precision, ny, nx, cache)[0]
 
 
 def serve_key(rate: float) -> str:

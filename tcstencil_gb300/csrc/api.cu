@@ -179,6 +179,9 @@ int tcs_device_error(int *code) {
     st = cuda_status(batch_take_error(&cb), "reading the batch error word");
     if (st) return st;
     if (!c) c = cb;
+    st = cuda_status(tb_take_error(&cb), "reading the blocked-sweep error word");
+    if (st) return st;
+    if (!c) c = cb;
     if (code) *code = c;
     return c ? fail(TCS_ERR_TIMEOUT, "device wait timed out (code %d)", c) : TCS_OK;
 }
@@ -356,6 +359,40 @@ struct tcs_plan_s {
         return run_step(g, prob.stencil, prob.engine, prob.precision, coeffs, buf[from][0],
                         buf[from][1], buf[1 - from][0], buf[1 - from][1], s);
     }
+
+    // Temporal depth 2 (split precision on the tensor engine): steps run in
+    // blocked pairs, with the same bits as single steps.
+    int temporal_depth = 1;
+    bool pairs() const { return temporal_depth == 2; }
+    int step2(int from, cudaStream_t s) {
+        return cuda_status(
+            launch_tc_split2(g, prob.stencil, coeffs, static_cast<const uint16_t *>(buf[from][0]),
+                             static_cast<const uint16_t *>(buf[from][1]),
+                             static_cast<uint16_t *>(buf[1 - from][0]),
+                             static_cast<uint16_t *>(buf[1 - from][1]), s),
+            "blocked sweep launch");
+    }
+    // The state `steps` steps from `from` ends in: one flip per launch.
+    int final_state(int steps, int from) const {
+        const int launches = pairs() ? steps / 2 + steps % 2 : steps;
+        return from ^ (launches & 1);
+    }
+    // Enqueues `steps` steps from state `from`; returns the final state in *to.
+    int enqueue(int steps, int from, cudaStream_t s, int *to) {
+        int st = TCS_OK;
+        for (int t = 0; t < steps && !st;) {
+            if (pairs() && steps - t >= 2) {
+                st = step2(from, s);
+                t += 2;
+            } else {
+                st = step(from, s);
+                t += 1;
+            }
+            from ^= 1;
+        }
+        *to = from;
+        return st;
+    }
 };
 
 namespace {
@@ -480,6 +517,17 @@ int tcs_plan_download(tcs_plan p, float *grid, int on_host, void *stream) {
                                        cudaMemcpyDeviceToHost, s), "download copy");
 }
 
+int tcs_plan_set_temporal_depth(tcs_plan p, int depth) {
+    if (!p || depth < 1 || depth > 2) return fail(TCS_ERR_INVALID, "tcs_plan_set_temporal_depth: depth is 1 or 2");
+    if (depth == 2 && !(p->prob.engine == TCS_ENGINE_TENSOR && p->prob.precision == TCS_PREC_SPLIT))
+        return fail(TCS_ERR_UNSUPPORTED, "temporal depth 2 is built for split precision on the tensor engine");
+    if (depth != p->temporal_depth) {
+        p->temporal_depth = depth;
+        p->drop_graphs();  // graphs hold the launch sequence
+    }
+    return TCS_OK;
+}
+
 int tcs_plan_state(tcs_plan p, void **hi, void **lo, size_t *plane_bytes) {
     if (!p) return fail(TCS_ERR_INVALID, "tcs_plan_state: null plan");
     if (hi) *hi = p->buf[p->cur][0];
@@ -498,12 +546,10 @@ int tcs_plan_run(tcs_plan p, int steps, int use_graph, void *stream) {
     if (!p || steps < 0) return fail(TCS_ERR_INVALID, "tcs_plan_run: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
     if (!use_graph || steps <= 1) {
-        for (int t = 0; t < steps; t++) {
-            int st = p->step(p->cur, s);
-            if (st) return st;
-            p->cur ^= 1;
-        }
-        return TCS_OK;
+        int to = p->cur;
+        const int st = p->enqueue(steps, p->cur, s, &to);
+        if (!st) p->cur = to;
+        return st;
     }
     const auto key = std::make_pair(steps, p->cur);
     auto it = p->graphs.find(key);
@@ -516,12 +562,8 @@ int tcs_plan_run(tcs_plan p, int steps, int use_graph, void *stream) {
         int st = cuda_status(cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal),
                              "cudaStreamBeginCapture");
         if (st) return st;
-        int from = p->cur;
-        int launch_st = TCS_OK;
-        for (int t = 0; t < steps && !launch_st; t++) {
-            launch_st = p->step(from, p->capture_stream);
-            from ^= 1;
-        }
+        int to = p->cur;
+        const int launch_st = p->enqueue(steps, p->cur, p->capture_stream, &to);
         cudaGraph_t graph = nullptr;
         st = cuda_status(cudaStreamEndCapture(p->capture_stream, &graph), "cudaStreamEndCapture");
         if (launch_st || st) {
@@ -536,7 +578,7 @@ int tcs_plan_run(tcs_plan p, int steps, int use_graph, void *stream) {
     }
     int st = cuda_status(cudaGraphLaunch(it->second, s), "cudaGraphLaunch");
     if (st) return st;
-    p->cur ^= (steps & 1);
+    p->cur = p->final_state(steps, p->cur);
     return TCS_OK;
 }
 

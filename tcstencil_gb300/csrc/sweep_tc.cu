@@ -270,19 +270,22 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
 // kRingSlots), and output block j is read from windows j and j+1 as soon as
 // both are complete.  The MMA issuer can so run ahead of the epilogue by a
 // few windows, instead of the two alternating with the whole accumulator.
-// Epilogue group g (warps 2-5, 6-9) takes the blocks of parity g, so each
-// group reads each window once (window 0 only group 0, window 8 only group 1;
-// the other group releases those without reading).  A slot is free again when
-// all eight epilogue warps have released its window; every warp releases a
+// Twelve epilogue warps in three block groups (a lane quarter each) take
+// blocks j with j mod 3 = group; a window is read by the groups of its two
+// blocks and released unread by the third.  A slot is free again when all
+// twelve epilogue warps have released its window; every warp releases a
 // window only after seeing it complete, so releases always count toward the
 // window they belong to.
 constexpr int kRingSlots = 5;
 constexpr int kRegionCols = 96;
+constexpr int kRingGroups = 3;                     // epilogue block groups
+constexpr int kRingEpiWarps = 4 * kRingGroups;     // a lane quarter each
+constexpr int kRingThreads = 32 * (2 + kRingEpiWarps);
 constexpr int kTileWindows = kTile / 16 + 1;
 static_assert(kRingSlots * kRegionCols <= kTmemCols, "window ring fits TMEM");
 
 template <int S>
-__global__ void __launch_bounds__(kThreads, 1) tc_split_ring_kernel(const TcParams p) {
+__global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const TcParams p) {
     using C = Cfg<S, true>;
     using M = Mode<true>;
     constexpr int NS = C::STAGES;
@@ -315,7 +318,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_split_ring_kernel(const TcPara
         }
         for (int r = 0; r < kRingSlots; r++) {
             mbar_init(&win_full[r], 1);
-            mbar_init(&win_empty[r], kEpiWarps);
+            mbar_init(&win_empty[r], kRingEpiWarps);
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -327,7 +330,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_split_ring_kernel(const TcPara
         tmem_relinquish();
     }
     build_bands(reinterpret_cast<uint16_t *>(band_base), p.coef, C::R, C::BOX, true, threadIdx.x,
-                kThreads);
+                kRingThreads);
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -410,8 +413,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_split_ring_kernel(const TcPara
         }
     } else {
         // ------------------------------------------------------ epilogue ---
-        const int q = warp & 3;           // TMEM lane quarter
-        const int grp = (warp - 2) >> 2;  // block parity of this group
+        const int q = warp & 3;             // TMEM lane quarter
+        const int grp = (warp - 2) >> 2;    // block group: blocks j with j % 3 == grp
         const int m = q * 32 + lane;
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
         TileOut o;
@@ -421,8 +424,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_split_ring_kernel(const TcPara
         o.out_lo = p.out_lo;
         o.pg = pg;
         o.y0 = p.g.y0; o.y1 = p.g.y1; o.x0 = p.g.x0; o.x1 = p.g.x1;
-        // waits (bounded) until global window Gw is complete
-        auto window_ready = [&](int Gw) {
+        int G0 = 0;  // first global window of the tile
+        // bounded wait for window w of the tile
+        auto ready = [&](int w) {
+            const int Gw = G0 + w;
             bool ok = mbar_wait(&win_full[Gw % kRingSlots], (Gw / kRingSlots) & 1, abort_flag);
             ok = __all_sync(0xffffffffu, ok);
             if (!ok && lane == 0) {
@@ -431,28 +436,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_split_ring_kernel(const TcPara
             }
             return ok;
         };
-        bool stop = false;
-        int G0 = 0;  // first global window of the tile
-        for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, G0 += kTileWindows) {
+        auto release = [&](int w) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&win_empty[(G0 + w) % kRingSlots]);
+        };
+        for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, G0 += kTileWindows) {
             const int Y0 = (t / tiles_x) * kTile;
             const int X0 = (t % tiles_x) * kTile;
             const int y = Y0 + m;
             const bool fast = tile_inside(o, Y0, X0);
             const bool row_in = y >= o.y0 && y < o.y1;
-            if (grp == 1) {
-                // window 0 is read by group 0 only
-                if (!window_ready(G0)) break;
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&win_empty[G0 % kRingSlots]);
-            }
-#pragma unroll 1
-            for (int j = grp; j < kTileWindows - 1; j += 2) {
+            const bool ok = walk_windows(grp, kRingGroups, kTileWindows, ready, release, [&](int j) {
                 const int Ga = G0 + j, Gb = Ga + 1;
-                if (!window_ready(Ga) || !window_ready(Gb)) {
-                    stop = true;
-                    break;
-                }
                 tc_fence_after();
                 float f[16];
                 split_block_load(lane_base + (Ga % kRingSlots) * kRegionCols,
@@ -464,16 +460,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_split_ring_kernel(const TcPara
                     mbar_arrive(&win_empty[Gb % kRingSlots]);
                 }
                 store_block<true>(o, f, y, X0 + 16 * j, fast, row_in);
-            }
-            if (stop) break;
-            if (grp == 0) {
-                // the last window is read by group 1 only
-                const int Gl = G0 + kTileWindows - 1;
-                if (!window_ready(Gl)) break;
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&win_empty[Gl % kRingSlots]);
-            }
+            });
+            if (!ok) break;
         }
     }
 
@@ -533,7 +521,7 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     for (int k = 0; k < 25; k++) p.coef[k] = 0.0f;
     for (int k = 0; k < C::NDY * C::NDY; k++) p.coef[k] = B[k];
     const int grid = p.n_tiles < g_num_sms ? p.n_tiles : g_num_sms;
-    if constexpr (SPLIT) tc_split_ring_kernel<S><<<grid, kThreads, C::SMEM, s>>>(p);
+    if constexpr (SPLIT) tc_split_ring_kernel<S><<<grid, kRingThreads, C::SMEM, s>>>(p);
     else tc_sweep_kernel<S, SPLIT><<<grid, kThreads, C::SMEM, s>>>(p);
     return cudaGetLastError();
 }

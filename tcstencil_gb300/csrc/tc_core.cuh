@@ -238,24 +238,32 @@ __device__ __forceinline__ void split_block_load(uint32_t region_a, uint32_t reg
     }
 }
 
-// MMAs of one split window (global window index wg of a staged tile) into
-// the 96-column region at d: per coefficient row, the stacked hi MMA (which
+// MMAs of one split window, whose K panels are stage slots `slot` and
+// `slot`+1 (the lo image lo_bytes after the hi image), into the 96-column
+// region at d: per coefficient row, the stacked hi MMA (which
 // initialises the region on the first row) and the lo MMA into its middle
 // part.
 template <int R>
-__device__ __forceinline__ void issue_split_window(uint64_t a_hi0, uint32_t band, uint32_t d,
-                                                   int wg) {
+__device__ __forceinline__ void issue_split_window_at(uint64_t a_hi0, uint32_t band, uint32_t d,
+                                                      int slot, int lo_bytes = kPlaneStage) {
     constexpr int NDY = 2 * R + 1;
-    const uint64_t a_lo0 = a_hi0 + (kPlaneStage >> 4);
+    const uint64_t a_lo0 = a_hi0 + (uint64_t)(lo_bytes >> 4);
     const uint64_t bs0 = smem_desc(band, 1536, 128);
     const uint64_t bf0 = smem_desc(band + NDY * 3072, 512, 128);
 #pragma unroll
     for (int dy = 0; dy < NDY; dy++) {
-        const uint64_t a_off = (uint64_t)((2 * wg * kChunkBytes + (2 - R + dy) * 16) >> 4);
+        const uint64_t a_off = (uint64_t)((slot * kChunkBytes + (2 - R + dy) * 16) >> 4);
         umma_f16(d, a_hi0 + a_off, bs0 + (uint64_t)((dy * 3072) >> 4), kIdescStack,
                  dy > 0 ? 1u : 0u);
         umma_f16(d + 32, a_lo0 + a_off, bf0 + (uint64_t)((dy * kBandBytes) >> 4), kIdesc, 1u);
     }
+}
+
+// The same for window wg of a staged tile (its panels 2wg, 2wg+1).
+template <int R>
+__device__ __forceinline__ void issue_split_window(uint64_t a_hi0, uint32_t band, uint32_t d,
+                                                   int wg) {
+    issue_split_window_at<R>(a_hi0, band, d, 2 * wg);
 }
 
 // MMAs of sub-tile h of a staged tile into accumulator columns from d.
@@ -333,6 +341,32 @@ struct TileOut {
     PlaneGeom pg;
     int y0, y1, x0, x1;
 };
+
+// Epilogue walk over one step of split windows for block group g of ng
+// groups: block j (windows j and j+1) belongs to group j mod ng.  Every
+// window is released exactly once per group, in increasing order, whether
+// the group reads it or not; ready(w) is the bounded wait for window w,
+// release(w) gives it back, block(j) loads block j, releases its two
+// windows and stores.  Returns false when a wait gave up.
+template <typename Ready, typename Release, typename Block>
+__device__ __forceinline__ bool walk_windows(int g, int ng, int nwin, Ready &&ready,
+                                             Release &&release, Block &&block) {
+    int w = 0;
+    for (int j = g; j < nwin - 1; j += ng) {
+        for (; w < j; w++) {
+            if (!ready(w)) return false;
+            release(w);
+        }
+        if (!ready(j) || !ready(j + 1)) return false;
+        block(j);
+        w = j + 2;
+    }
+    for (; w < nwin; w++) {
+        if (!ready(w)) return false;
+        release(w);
+    }
+    return true;
+}
 
 // Converts and stores one 16-column output block of tile row y (cells xb ..
 // xb+15).  fast: the whole tile is inside the update rectangle; otherwise

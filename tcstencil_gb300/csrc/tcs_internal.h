@@ -112,6 +112,11 @@ cudaError_t launch_cc_f32(const GridGeom &g, int stencil, const TapCoeffs &c, co
 
 // Reads and clears the tensor kernels' device error word.
 cudaError_t tc_take_error(int *code);
+// Two steps of the split form in one launch (temporal blocking), in -> out.
+cudaError_t launch_tc_split2(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
+                             const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
+                             cudaStream_t s);
+cudaError_t tb_take_error(int *code);
 // Configures the tensor kernel of (stencil, split) ahead of its first launch.
 cudaError_t tc_prepare(int stencil, bool split);
 

@@ -13,8 +13,8 @@ def test_sweep_choice_is_persisted_per_class(tmp_path):
     fake = {"tensor": 2e-5, "cudacore": 1e-5}
     cache = autotune.Cache(path, shipped=None)
     e = autotune.tune_sweep("star2d1r", "f16", 300, 300, cache=cache,
-                            timer=lambda eng, *a: fake[eng])
-    assert e["engine"] == "cudacore"
+                            timer=lambda eng, depth, *a: fake[eng])
+    assert e["engine"] == "cudacore" and e["temporal_depth"] == 1
     # a fresh reader sees it, for any grid of the same size class only
     c2 = autotune.Cache(path, shipped=None)
     assert autotune.best_engine("star2d1r", "f16", 500, 270, cache=c2) == "cudacore"
@@ -37,11 +37,15 @@ def test_shipped_results_back_up_an_empty_cache(tmp_path):
     assert autotune.best_round_steps(2000.0, cache=c) == 8
 
 
-def test_split_only_tries_the_tensor_engine(tmp_path):
+def test_split_tries_both_temporal_depths(tmp_path):
     seen = []
-    autotune.tune_sweep("box2d1r", "split", 64, 64, cache=autotune.Cache(str(tmp_path / "t.json")),
-                        timer=lambda eng, *a: seen.append(eng) or 1.0)
-    assert seen == ["tensor"]
+    cache = autotune.Cache(str(tmp_path / "t.json"), shipped=None)
+    e = autotune.tune_sweep("box2d1r", "split", 64, 64, cache=cache,
+                            timer=lambda eng, depth, *a: seen.append((eng, depth)) or 1.0 / depth)
+    assert seen == [("tensor", 1), ("tensor", 2)]
+    assert e["engine"] == "tensor" and e["temporal_depth"] == 2
+    assert autotune.best_config("box2d1r", "split", 60, 33, cache=cache) == ("tensor", 2)
+    assert autotune.best_config("box2d2r", "split", 60, 33, cache=cache) == ("tensor", 1)
 
 
 def test_serve_choice_prefers_low_p99_among_those_keeping_up(tmp_path):
@@ -63,6 +67,8 @@ def test_real_tuning_pass_and_auto_engine(tcs, torch_cuda, tmp_path, monkeypatch
     e = autotune.tune_sweep("star2d2r", "f16", 512, 512, steps=5)
     assert e["engine"] in ("tensor", "cudacore")
     assert all(t > 0 for t in e["s_per_step"].values())
+    s = autotune.tune_sweep("star2d2r", "split", 512, 512, steps=6)
+    assert set(s["s_per_step"]) == {"tensor/1", "tensor/2"}
     p = tcs.Plan(512, 512, "star2d2r", np.full((5, 5), 0.04, np.float32), engine="auto")
     g = np.random.default_rng(0).uniform(-1, 1, (512, 512)).astype(np.float32)
     p.upload(g)
