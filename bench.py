@@ -325,6 +325,65 @@ def serve_leg(tcs, seconds=10.0, rate=2000.0, budget_gb=120.0, round_steps=16):
     return res
 
 
+def split_config_leg(torch, tcs, stream, interior=16384, steps=200, check_every=50,
+                     stencil="box2d1r"):
+    """Split-precision configuration: box2d1r on a 16384^2 interior + 1-cell
+    zero halo, input U[-1,1) + sin(2 pi x) sin(2 pi y), 200 steps.  Times the
+    200 steps (CUDA events, graph replay), then replays them one by one beside
+    the FP64 shadow (tcs_drift) and reports the error after every step, with
+    the drift checks every 50 steps called out."""
+    from tcstencil_gb300.autotune import best_config
+    from tcstencil_gb300.workloads import normalized_coeffs
+
+    r = 1 if stencil in ("star2d1r", "box2d1r") else 2
+    n = interior + 2 * r
+    rng = np.random.default_rng(3000)
+    yy, xx = np.meshgrid(np.arange(interior) / interior, np.arange(interior) / interior,
+                         indexing="ij")
+    A = np.zeros((n, n), np.float32)
+    A[r:-r, r:-r] = (rng.uniform(-1, 1, (interior, interior)) +
+                     np.sin(2 * np.pi * xx) * np.sin(2 * np.pi * yy))
+    del xx, yy
+    B = normalized_coeffs(rng, stencil)
+    _, depth = best_config(stencil, "split", n, n)
+    plan = tcs.Plan(n, n, stencil, B, engine="tensor", precision="split", temporal_depth=depth)
+    plan.upload(A)
+    plan.run(10, use_graph=True, stream=stream)
+    torch.cuda.synchronize()
+    plan.upload(A)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    plan.run(steps, use_graph=True, stream=stream)
+    b.record(stream)
+    torch.cuda.synchronize()
+    t = a.elapsed_time(b) / 1e3
+    assert tcs.device_error() == 0
+    pts = interior * interior * steps
+    # error vs FP64 after every step (not timed)
+    drift = tcs.Drift(n, n, stencil, B)
+    plan.upload(A)
+    drift.upload(A)
+    out = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    errs = []
+    for k in range(steps):
+        plan.run(1, use_graph=False, stream=stream)
+        drift.run(1)
+        plan.download(out, stream=stream)
+        errs.append(drift.compare(out, stream=stream)[0])
+    drift.close()
+    plan.close()
+    peak, _ = load_peaks()
+    return {"workload": f"{stencil} split precision, {interior}^2 interior + {r}-cell zero halo, "
+                        f"{steps} steps, U[-1,1) + sin(2 pi x) sin(2 pi y)",
+            "gpts": pts / t / 1e9, "ms_per_step": 1e3 * t / steps,
+            "roofline_frac": 8 * pts / t / 1e9 / peak, "temporal_depth": depth,
+            "rel_l2_vs_fp64_max": max(errs),
+            "drift_checks": {str(s): errs[s - 1] for s in range(check_every, steps + 1, check_every)},
+            "rel_l2_vs_fp64_every_10_steps": [round(e, 10) for e in errs[9::10]]}
+
+
 def timed_sweeps(torch, tcs, plan, K, W, timesteps, stream):
     for _ in range(W):
         plan.run(timesteps, use_graph=True, stream=stream)
@@ -422,6 +481,9 @@ def run_ours(args):
                 t2 = timed_sweeps(torch, tcs, p2, max(5, args.steps // 4), 2, args.timesteps, stream)
                 p2.close()
                 extras[f"{st}/{eng}/f16"] = round(updates_per_step * max(5, args.steps // 4) / t2 / 1e9, 2)
+        r = split_config_leg(torch, tcs, stream)
+        extras["split_16384_box2d1r"] = {k: (round(v, 10) if isinstance(v, float) else v)
+                                         for k, v in r.items()}
         r = batch_leg(torch, tcs, 10, 3, stream)
         extras["batched_512_mixed"] = {k: round(v, 3) if isinstance(v, float) else v
                                        for k, v in r.items()}

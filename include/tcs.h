@@ -251,6 +251,28 @@ int tcs_batch_run(tcs_batch batch, int use_graph, void *stream);
 /* Point updates per run, work items per run and the number of grids. */
 int tcs_batch_info(tcs_batch batch, long long *point_updates, int *items, int *grids);
 
+/* ------------------------------------------------------- FP64 drift check
+ * An FP64 shadow of a problem on the device, stepped with gold's tap order
+ * and separately rounded multiply and add (the oracle's FP64 restatement of
+ * common/gold_*.cpp, bit for bit), and a comparison of any FP32 grid with it.
+ * FP64 appears only here, never in the sweep kernels.  Step it beside a plan
+ * and compare every k steps to watch the error of the FP16 or split form. */
+typedef struct tcs_drift_s *tcs_drift;
+
+int tcs_drift_create(const tcs_problem *problem, tcs_drift *out);
+int tcs_drift_destroy(tcs_drift drift);
+/* Loads the ny x nx FP32 starting grid (host or device), widened to FP64. */
+int tcs_drift_upload(tcs_drift drift, const float *grid, int grid_on_host, void *stream);
+int tcs_drift_run(tcs_drift drift, int steps, void *stream);
+/* Relative L2 (||a - ref|| / ||ref||) and max |a - ref| of the device FP32
+ * grid a (ny x nx row-major) against the shadow's state.  Synchronises. */
+int tcs_drift_compare(tcs_drift drift, const float *d_grid, double *rel_l2, double *max_abs,
+                      void *stream);
+/* Copies the shadow's FP64 state to host memory (ny x nx).  Synchronises. */
+int tcs_drift_download(tcs_drift drift, double *h_grid, void *stream);
+/* Device pointer of the shadow's current FP64 state (ny x nx row-major). */
+int tcs_drift_state(tcs_drift drift, const double **d_grid);
+
 /* ---------------------------------------------------------------- serving
  * A request server does continuous batching of stencil solves on one GPU.
  * No reference counterpart.  A native scheduler thread does the work:

@@ -123,6 +123,14 @@ SIGNATURES = {
     "tcs_batch_run": (_I, [_P, _I, _P]),
     "tcs_batch_info": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I),
                             ctypes.POINTER(_I)]),
+    "tcs_drift_create": (_I, [ctypes.POINTER(Problem), ctypes.POINTER(_P)]),
+    "tcs_drift_destroy": (_I, [_P]),
+    "tcs_drift_upload": (_I, [_P, _P, _I, _P]),
+    "tcs_drift_run": (_I, [_P, _I, _P]),
+    "tcs_drift_compare": (_I, [_P, _P, ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double), _P]),
+    "tcs_drift_state": (_I, [_P, ctypes.POINTER(_P)]),
+    "tcs_drift_download": (_I, [_P, _P, _P]),
     "tcs_server_create": (_I, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
     "tcs_server_destroy": (_I, [_P]),
     "tcs_server_submit": (_I, [_P, ctypes.POINTER(Problem), _I, _P, _P,
@@ -391,6 +399,54 @@ class Batch:
         pu, it, g = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
         _check(lib().tcs_batch_info(self._h, ctypes.byref(pu), ctypes.byref(it), ctypes.byref(g)))
         return pu.value, it.value, g.value
+
+
+class Drift:
+    """FP64 shadow of a stencil problem on the device (tcs_drift_*)."""
+
+    def __init__(self, ny: int, nx: int, stencil: str, coeffs, rect=None):
+        self._c = _coeffs(coeffs, stencil)
+        y0, y1, x0, x1 = _rect(rect)
+        pr = Problem(ny, nx, STENCILS[stencil], ENGINES["tensor"], PRECISIONS["f16"], y0, y1, x0,
+                     x1, self._c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        h = ctypes.c_void_p()
+        _check(lib().tcs_drift_create(ctypes.byref(pr), ctypes.byref(h)))
+        self._h = h
+        self.shape = (ny, nx)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().tcs_drift_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, grid, stream=None) -> None:
+        _check(lib().tcs_drift_upload(self._h, _ptr(grid), int(_on_host(grid)), _stream(stream)))
+
+    def run(self, steps: int, stream=None) -> None:
+        _check(lib().tcs_drift_run(self._h, int(steps), _stream(stream)))
+
+    def compare(self, d_grid, stream=None):
+        """(relative L2, max abs) of a device FP32 grid against the shadow."""
+        rel, mx = ctypes.c_double(), ctypes.c_double()
+        _check(lib().tcs_drift_compare(self._h, _ptr(d_grid), ctypes.byref(rel),
+                                       ctypes.byref(mx), _stream(stream)))
+        return rel.value, mx.value
+
+    def state(self) -> int:
+        p = ctypes.c_void_p()
+        _check(lib().tcs_drift_state(self._h, ctypes.byref(p)))
+        return p.value
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.shape, np.float64)
+        _check(lib().tcs_drift_download(self._h, _ptr(out), None))
+        return out
 
 
 class Server:
