@@ -62,7 +62,7 @@ __device__ __forceinline__ int sub_tiles(const BatchGrid &g) { return g.split ? 
 // every CTA polls to stop early) and in the unit's word tcs_device_error reads.
 __device__ __forceinline__ void batch_fail(const BatchParams &p, int code) {
     record_error(p.error, code);
-    batch_fail(p, code);
+    record_error(&g_batch_error, code);
 }
 
 // Work index k -> (grid, step, tile); see BatchParams.
