@@ -41,14 +41,28 @@ using namespace tc;
 
 __device__ int g_batch_error = 0;
 
-constexpr int kStages = 2;
-constexpr int kMaxBandBytes = 4 * 5 * kBandBytes;  // split, radius 2
-constexpr int kStageBytes = 2 * kPlaneStage + kMaxBandBytes;
-constexpr int kRing = 8;  // published work items in flight (> kStages + 2)
-constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + 512;
-static_assert(kRing > kStages + 2, "a ring slot is reused only after its item's epilogue");
-static_assert((2 * kStages + 5 + kRing) * 8 + kRing * 12 + 8 <= 512, "barrier area");
-static_assert(kSmem <= 232448, "shared memory budget");
+// Per-precision launch shapes.  FP16 items: three stages of one plane plus
+// bands, two accumulator slots, eight epilogue warps (the single-grid plain
+// kernel's shape).  Split items: two stages of hi+lo plus bands, the window
+// ring of the single-grid split kernel, twelve epilogue warps in three groups.
+constexpr int kRing = 8;  // published work items in flight
+template <bool SPLIT>
+struct BatchCfg {
+    static constexpr int STAGES = SPLIT ? 2 : 3;
+    static constexpr int PLANES = SPLIT ? 2 : 1;
+    static constexpr int BAND_BYTES = (SPLIT ? 4 : 1) * 5 * kBandBytes;  // radius 2
+    static constexpr int STAGE_BYTES = PLANES * kPlaneStage + BAND_BYTES;
+    static constexpr int GROUPS = SPLIT ? 3 : 2;
+    static constexpr int EPI_WARPS = 4 * GROUPS;
+    static constexpr int THREADS = 32 * (2 + EPI_WARPS);
+    static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 512;
+    static_assert(kRing > STAGES + 2, "a ring slot is reused only after its item's epilogue");
+    static_assert(SMEM <= 232448, "shared memory budget");
+    static_assert(STAGE_BYTES % 16 == 0, "bulk copy alignment");
+};
+constexpr int kBatchRingSlots = 5;  // split window regions in TMEM
+constexpr int kBatchRegion = 96;
+constexpr int kBatchWindows = kTile / 16 + 1;
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     unsigned v;
@@ -56,7 +70,6 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     return v;
 }
 
-__device__ __forceinline__ int sub_tiles(const BatchGrid &g) { return g.split ? 2 : 1; }
 
 // A bounded wait gave up: record the code in the launch's error word (which
 // every CTA polls to stop early) and in the unit's word tcs_device_error reads.
@@ -102,34 +115,40 @@ __global__ void flip_states_kernel(BatchGrid *grids, int n) {
     if (i < n) grids[i].state ^= grids[i].steps & 1;
 }
 
-__global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams p) {
+template <bool SPLIT>
+__global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(const BatchParams p) {
+    using C = BatchCfg<SPLIT>;
+    constexpr int NS = C::STAGES;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                 ~static_cast<uintptr_t>(1023));
-    uint8_t *stage_base = smem;  // [kStages][hi | lo | bands]
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)kStages * kStageBytes);
-    uint64_t *full = bars;                          // [kStages]
-    uint64_t *empty = bars + kStages;               // [kStages]
-    uint64_t *acc_full = bars + 2 * kStages;        // [2]
-    uint64_t *acc_empty = bars + 2 * kStages + 2;   // [2]
-    uint64_t *drain = bars + 2 * kStages + 4;       // [1]
-    uint64_t *item_ready = bars + 2 * kStages + 5;  // [kRing]
-    BatchItem *ring = reinterpret_cast<BatchItem *>(bars + 2 * kStages + 5 + kRing);  // [kRing]
+    uint8_t *stage_base = smem;  // [NS][planes | bands]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)NS * C::STAGE_BYTES);
+    // accumulator barriers: plain [2] slots, split [kBatchRingSlots] windows
+    constexpr int NACC = SPLIT ? kBatchRingSlots : 2;
+    uint64_t *full = bars;                        // [NS]
+    uint64_t *empty = bars + NS;                  // [NS]
+    uint64_t *acc_full = bars + 2 * NS;           // [NACC]
+    uint64_t *acc_empty = acc_full + NACC;        // [NACC]
+    uint64_t *drain = acc_empty + NACC;           // [1]
+    uint64_t *item_ready = drain + 1;             // [kRing]
+    BatchItem *ring = reinterpret_cast<BatchItem *>(item_ready + kRing);  // [kRing]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(ring + kRing);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     volatile int *grid_error = p.error;
+    static_assert((2 * NS + 2 * NACC + 1 + kRing) * 8 + kRing * 12 + 8 <= 512, "barrier area");
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; s++) {
+        for (int s = 0; s < NS; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; b++) {
+        for (int b = 0; b < NACC; b++) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], kEpiWarps);
+            mbar_init(&acc_empty[b], C::EPI_WARPS);
         }
         mbar_init(drain, 1);
         for (int j = 0; j < kRing; j++) mbar_init(&item_ready[j], 1);
@@ -154,8 +173,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
         if (lane == 0) {
             int last_issued = -1;
             for (int i = 0;; i++) {
-                const int s = i % kStages, j = i % kRing;
-                if (!mbar_wait(&empty[s], ((i / kStages) & 1) ^ 1, abort_flag)) {
+                const int s = i % NS, j = i % kRing;
+                if (!mbar_wait(&empty[s], ((i / NS) & 1) ^ 1, abort_flag)) {
                     batch_fail(p, kErrWaitEmpty);
                     *abort_flag = 1;
                     break;
@@ -172,8 +191,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                 const BatchGrid &g = p.grids[it.g];
                 if (it.t > 0) {
                     // every tile of the previous step of this grid is stored
-                    const unsigned target =
-                        (unsigned)(g.n_tiles * kEpiWarps * sub_tiles(g));
+                    const unsigned target = (unsigned)(g.n_tiles * C::EPI_WARPS);
                     const unsigned *ctr = p.counters + g.ctr_base + it.t - 1;
                     if (ld_acquire(ctr) < target) {
                         const uint64_t t0 = global_timer_ns();
@@ -194,21 +212,20 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                     // the bulk copies below read what other SMs stored
                     fence_proxy_async_global();
                 }
-                const int nplanes = g.split ? 2 : 1;
-                const int band_bytes = batch_band_elems(g.r, g.split) * 2;
-                uint8_t *st = stage_base + (size_t)s * kStageBytes;
-                mbar_arrive_expect_tx(&full[s], nplanes * kPlaneStage + band_bytes);
+                const int band_bytes = batch_band_elems(g.r, SPLIT) * 2;
+                uint8_t *st = stage_base + (size_t)s * C::STAGE_BYTES;
+                mbar_arrive_expect_tx(&full[s], C::PLANES * kPlaneStage + band_bytes);
                 const int in = (g.state + it.t) & 1;
-                load_tile(g.plane[in][0], g.plane[in][1], nplanes, g.pg,
+                load_tile(g.plane[in][0], g.plane[in][1], C::PLANES, g.pg,
                           (it.tile / g.tiles_x) * kTile, (it.tile % g.tiles_x) * kTile, st,
                           &full[s]);
-                bulk_load(st + 2 * kPlaneStage, p.bands + g.band_base, band_bytes, &full[s]);
+                bulk_load(st + C::PLANES * kPlaneStage, p.bands + g.band_base, band_bytes, &full[s]);
                 last_issued = i;
             }
-            for (int k = 0; k < kStages && last_issued - k >= 0; k++) {
+            for (int k = 0; k < NS && last_issued - k >= 0; k++) {
                 const int ii = last_issued - k;
                 const uint64_t t0 = global_timer_ns();
-                while (!mbar_try_wait(&full[ii % kStages], (ii / kStages) & 1)) {
+                while (!mbar_try_wait(&full[ii % NS], (ii / NS) & 1)) {
                     if (global_timer_ns() - t0 > kWaitLimitNs) {
                         batch_fail(p, kErrWaitDrain);
                         break;
@@ -219,11 +236,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
     } else if (warp == 1) {
         // ---------------------------------------------------- MMA issuer ---
         if (lane == 0) {
-            AccSlots slots;
+            AccSlots slots;  // plain
+            int G = 0;       // split: global window counter of the ring
             bool issued_any = false;
             bool stop = false;
             for (int i = 0; !stop; i++) {
-                const int s = i % kStages;
+                const int s = i % NS;
                 if (!mbar_wait(&item_ready[i % kRing], (i / kRing) & 1, abort_flag)) {
                     batch_fail(p, kErrWaitFull);
                     *abort_flag = 1;
@@ -231,39 +249,50 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
                 }
                 const BatchItem it = ring[i % kRing];
                 if (it.g < 0) break;
-                if (!mbar_wait(&full[s], (i / kStages) & 1, abort_flag)) {
+                if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
                     batch_fail(p, kErrWaitFull);
                     *abort_flag = 1;
                     break;
                 }
                 const BatchGrid &g = p.grids[it.g];
-                uint8_t *st = stage_base + (size_t)s * kStageBytes;
+                uint8_t *st = stage_base + (size_t)s * C::STAGE_BYTES;
                 const uint64_t a_hi0 = smem_desc(smem_u32(st), kChunkBytes, 128);
-                const uint32_t band = smem_u32(st + 2 * kPlaneStage);
-                const int nsub = sub_tiles(g);
-                for (int h = 0; h < nsub; h++) {
+                const uint32_t band = smem_u32(st + C::PLANES * kPlaneStage);
+                if constexpr (SPLIT) {
+#pragma unroll 1
+                    for (int w = 0; w < kBatchWindows; w++, G++) {
+                        const int r = G % kBatchRingSlots;
+                        if (!mbar_wait(&acc_empty[r], ((G / kBatchRingSlots) & 1) ^ 1, abort_flag)) {
+                            batch_fail(p, kErrWaitAccum);
+                            *abort_flag = 1;
+                            stop = true;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t d = tmem_base + r * kBatchRegion;
+                        if (g.r == 1) issue_split_window<1>(a_hi0, band, d, w);
+                        else issue_split_window<2>(a_hi0, band, d, w);
+                        umma_commit(&acc_full[r]);
+                        issued_any = true;
+                    }
+                } else {
                     uint32_t col;
-                    const uint32_t mask = slots.take(g.split, col);
+                    const uint32_t mask = slots.take(false, col);
                     if (!slots.acquire(acc_empty, mask, abort_flag)) {
                         batch_fail(p, kErrWaitAccum);
                         *abort_flag = 1;
                         stop = true;
-                        break;
-                    }
-                    tc_fence_after();
-                    const uint32_t d = tmem_base + col;
-                    if (g.split) {
-                        if (g.r == 1) issue_subtile<1, true>(a_hi0, band, d, h);
-                        else issue_subtile<2, true>(a_hi0, band, d, h);
                     } else {
-                        if (g.r == 1) issue_subtile<1, false>(a_hi0, band, d, h);
-                        else issue_subtile<2, false>(a_hi0, band, d, h);
+                        tc_fence_after();
+                        const uint32_t d = tmem_base + col;
+                        if (g.r == 1) issue_subtile<1, false>(a_hi0, band, d, 0);
+                        else issue_subtile<2, false>(a_hi0, band, d, 0);
+                        slots.commit(acc_full, mask);
+                        slots.used(mask);
+                        issued_any = true;
                     }
-                    slots.commit(acc_full, mask);
-                    slots.used(mask);
-                    issued_any = true;
                 }
-                umma_commit(&empty[s]);
+                if (!stop) umma_commit(&empty[s]);
             }
             if (issued_any) {
                 umma_commit(drain);
@@ -279,20 +308,24 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;
-        const int half = (warp - 2) >> 2;
+        const int grp = (warp - 2) >> 2;  // plain: column half; split: block group
         const int m = q * 32 + lane;
         AccSlots slots;
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
+        int G0 = 0;  // split: first ring window of the item
         bool stop = false;
+        auto fail_result = [&]() {
+            if (lane == 0) {
+                batch_fail(p, kErrWaitResult);
+                *abort_flag = 1;
+            }
+        };
         for (int i = 0; !stop; i++) {
             const int j = i % kRing;
             bool ok = mbar_wait(&item_ready[j], (i / kRing) & 1, abort_flag);
             ok = __all_sync(0xffffffffu, ok);
             if (!ok) {
-                if (lane == 0) {
-                    batch_fail(p, kErrWaitResult);
-                    *abort_flag = 1;
-                }
+                fail_result();
                 break;
             }
             const BatchItem it = ring[j];
@@ -308,41 +341,64 @@ __global__ void __launch_bounds__(kThreads, 1) tc_batch_kernel(const BatchParams
             o.y0 = g.y0; o.y1 = g.y1; o.x0 = g.x0; o.x1 = g.x1;
             const int Y0 = (it.tile / g.tiles_x) * kTile;
             const int X0 = (it.tile % g.tiles_x) * kTile;
-            const int nsub = sub_tiles(g);
-            for (int h = 0; h < nsub; h++) {
+            if constexpr (SPLIT) {
+                const int y = Y0 + m;
+                const bool fast = tile_inside(o, Y0, X0);
+                const bool row_in = y >= o.y0 && y < o.y1;
+                auto ready = [&](int w) {
+                    const int Gw = G0 + w;
+                    bool okw = mbar_wait(&acc_full[Gw % kBatchRingSlots],
+                                         (Gw / kBatchRingSlots) & 1, abort_flag);
+                    okw = __all_sync(0xffffffffu, okw);
+                    if (!okw) fail_result();
+                    return okw;
+                };
+                auto release = [&](int w) {
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&acc_empty[(G0 + w) % kBatchRingSlots]);
+                };
+                ok = walk_windows(grp, C::GROUPS, kBatchWindows, ready, release, [&](int jb) {
+                    const int Ga = G0 + jb, Gb = Ga + 1;
+                    tc_fence_after();
+                    float f[16];
+                    split_block_load(lane_base + (Ga % kBatchRingSlots) * kBatchRegion,
+                                     lane_base + (Gb % kBatchRingSlots) * kBatchRegion, f);
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) {
+                        mbar_arrive(&acc_empty[Ga % kBatchRingSlots]);
+                        mbar_arrive(&acc_empty[Gb % kBatchRingSlots]);
+                    }
+                    store_block<true>(o, f, y, X0 + 16 * jb, fast, row_in);
+                });
+                G0 += kBatchWindows;
+                if (!ok) {
+                    stop = true;
+                    break;
+                }
+            } else {
                 uint32_t col;
-                const uint32_t mask = slots.take(g.split, col);
+                const uint32_t mask = slots.take(false, col);
                 ok = slots.ready(acc_full, mask, abort_flag);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) {
-                    if (lane == 0) {
-                        batch_fail(p, kErrWaitResult);
-                        *abort_flag = 1;
-                    }
+                    fail_result();
                     stop = true;
                     break;
                 }
                 tc_fence_after();
-                if (g.split) {
-                    float f[Mode<true>::SUB_BLOCKS / 2][16];
-                    epilogue_load<true>(lane_base + col, half, f);
-                    tc_fence_before();
-                    __syncwarp();
-                    if (lane == 0) slots.release(acc_empty, mask);
-                    epilogue_store<true>(o, f, h, half, m, Y0, X0);
-                } else {
-                    float f[Mode<false>::SUB_BLOCKS / 2][16];
-                    epilogue_load<false>(lane_base + col, half, f);
-                    tc_fence_before();
-                    __syncwarp();
-                    if (lane == 0) slots.release(acc_empty, mask);
-                    epilogue_store<false>(o, f, h, half, m, Y0, X0);
-                }
-                slots.used(mask);
-                __threadfence();  // this warp's stores before the completion count
+                float f[Mode<false>::SUB_BLOCKS / 2][16];
+                epilogue_load<false>(lane_base + col, grp, f);
+                tc_fence_before();
                 __syncwarp();
-                if (lane == 0) atomicAdd(p.counters + g.ctr_base + it.t, 1u);
+                if (lane == 0) slots.release(acc_empty, mask);
+                epilogue_store<false>(o, f, 0, grp, m, Y0, X0);
+                slots.used(mask);
             }
+            __threadfence();  // this warp's stores before the completion count
+            __syncwarp();
+            if (lane == 0) atomicAdd(p.counters + g.ctr_base + it.t, 1u);
         }
     }
 
@@ -365,8 +421,13 @@ cudaError_t batch_prepare(int *num_sms) {
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(tc_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kSmem);
+            e = cudaFuncSetAttribute(tc_batch_kernel<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)BatchCfg<false>::SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tc_batch_kernel<true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)BatchCfg<true>::SMEM);
         if (e != cudaSuccess) {
             g_sms = 0;
             return e;
@@ -380,10 +441,13 @@ cudaError_t batch_prepare(int *num_sms) {
 // One CTA per SM.  Work is taken dynamically in index order, so a CTA waits
 // only on items already taken by running CTAs: progress needs no guarantee
 // that all CTAs are resident at once.
-cudaError_t launch_batch(const BatchParams &p, int num_sms, cudaStream_t s) {
+cudaError_t launch_batch(const BatchParams &p, bool split, int num_sms, cudaStream_t s) {
     if (p.n_items <= 0) return cudaSuccess;
     const int grid = p.n_items < num_sms ? p.n_items : num_sms;
-    tc_batch_kernel<<<grid, kThreads, kSmem, s>>>(p);
+    if (split)
+        tc_batch_kernel<true><<<grid, BatchCfg<true>::THREADS, BatchCfg<true>::SMEM, s>>>(p);
+    else
+        tc_batch_kernel<false><<<grid, BatchCfg<false>::THREADS, BatchCfg<false>::SMEM, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -421,16 +485,21 @@ struct tcs_batch_s {
     std::vector<Entry> entries;
     uint16_t *pool = nullptr;
     size_t pool_elems = 0;
-    BatchGrid *d_grids = nullptr;  // sorted by steps, descending
-    int *d_layout = nullptr;       // step_off then tile_prefix
-    unsigned *d_counters = nullptr;
+    // all grids, FP16 ones first then split ones, each part sorted by steps
+    // (descending); one launch per part
+    BatchGrid *d_grids = nullptr;
+    int n_grids = 0;
+    struct Part {
+        int first = 0, n_grids = 0;
+        int *d_layout = nullptr;        // step_off then tile_prefix
+        unsigned *d_counters = nullptr; // per (grid, step), then work counter, error word
+        int n_items = 0, n_steps = 0, n_counters = 0;
+    } part[2];                          // [FP16, split]
     uint16_t *d_bands = nullptr;
     float *d_coefs = nullptr;
     float *d_staging = nullptr;
     size_t staging_elems = 0;
     unsigned *d_max = nullptr;
-    int n_items = 0, n_steps = 0;
-    int n_counters = 0;
     long long point_updates = 0;
     bool built = false;
     int runs = 0;  // completed runs (each flips states by steps & 1)
@@ -440,8 +509,10 @@ struct tcs_batch_s {
     ~tcs_batch_s() {
         if (graph) cudaGraphExecDestroy(graph);
         if (capture_stream) cudaStreamDestroy(capture_stream);
-        for (void *p : {(void *)pool, (void *)d_grids, (void *)d_layout, (void *)d_counters,
-                        (void *)d_bands, (void *)d_coefs, (void *)d_staging, (void *)d_max})
+        for (void *p : {(void *)pool, (void *)d_grids, (void *)part[0].d_layout,
+                        (void *)part[0].d_counters, (void *)part[1].d_layout,
+                        (void *)part[1].d_counters, (void *)d_bands, (void *)d_coefs,
+                        (void *)d_staging, (void *)d_max})
             if (p) cudaFree(p);
     }
 
@@ -469,16 +540,21 @@ int batch_build(tcs_batch b) {
     if (!st) st = cuda_status(cudaMemset(b->pool, 0, total * sizeof(uint16_t)), "cudaMemset(batch planes)");
     if (st) return st;
     b->pool_elems = total;
-    // descriptors (sorted by steps, descending), bands, counters, work layout
+    // descriptors (FP16 grids then split grids, each sorted by steps,
+    // descending), bands, per-part counters and work layouts
     const int n = (int)b->entries.size();
     std::vector<int> order(n);
     for (int i = 0; i < n; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int x, int y) { return b->entries[x].steps > b->entries[y].steps; });
+    auto is_split = [&](int i) { return b->entries[i].prob.precision == TCS_PREC_SPLIT; };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        if (is_split(x) != is_split(y)) return !is_split(x);
+        return b->entries[x].steps > b->entries[y].steps;
+    });
     std::vector<BatchGrid> grids(n);
     std::vector<float> coefs(25 * (size_t)n, 0.0f);
     std::vector<int> steps(n), tiles(n);
-    int ctr = 0, band = 0;
+    int band = 0;
+    int ctr[2] = {0, 0};
     for (int i = 0; i < n; i++) {
         const auto &e = b->entries[order[i]];
         BatchGrid &G = grids[i];
@@ -495,30 +571,42 @@ int batch_build(tcs_batch b) {
         G.box = stencil_box(e.prob.stencil);
         G.split = split;
         G.steps = e.steps;
-        G.ctr_base = ctr;
+        G.ctr_base = ctr[split];
         G.band_base = band;
         G.state = 0;
         steps[i] = e.steps;
         tiles[i] = G.n_tiles;
-        ctr += std::max(e.steps, 1);
+        ctr[split] += std::max(e.steps, 1);
         band += batch_band_elems(G.r, split);
         std::memcpy(&coefs[25 * (size_t)i], e.coeffs, sizeof(e.coeffs));
         b->point_updates += (long long)(e.g.y1 - e.g.y0) * (e.g.x1 - e.g.x0) * e.steps;
     }
-    b->n_steps = n ? steps[0] : 0;
-    std::vector<int> layout(b->n_steps + 1 + n + 1);
-    const long long n_items = batch_layout(steps.data(), tiles.data(), n, layout.data(),
-                                           layout.data() + b->n_steps + 1);
-    if (n_items < 0) return fail(TCS_ERR_INVALID, "tcs_batch: more than 2^31 work items per run");
-    b->n_items = (int)n_items;
-    b->n_counters = ctr;
+    b->n_grids = n;
+    int first = 0;
+    for (int k = 0; k < 2; k++) {
+        auto &P = b->part[k];
+        P.first = first;
+        P.n_grids = 0;
+        while (first + P.n_grids < n && (int)grids[first + P.n_grids].split == k) P.n_grids++;
+        first += P.n_grids;
+        P.n_steps = P.n_grids ? steps[P.first] : 0;
+        P.n_counters = ctr[k];
+        if (!P.n_grids) continue;
+        std::vector<int> layout(P.n_steps + 1 + P.n_grids + 1);
+        const long long n_items = batch_layout(steps.data() + P.first, tiles.data() + P.first,
+                                               P.n_grids, layout.data(),
+                                               layout.data() + P.n_steps + 1);
+        if (n_items < 0) return fail(TCS_ERR_INVALID, "tcs_batch: more than 2^31 work items per run");
+        P.n_items = (int)n_items;
+        st = cuda_status(cudaMalloc(&P.d_layout, layout.size() * sizeof(int)), "cudaMalloc(layout)");
+        if (!st) st = cuda_status(cudaMalloc(&P.d_counters, (P.n_counters + 2) * sizeof(unsigned)), "cudaMalloc(counters)");
+        if (!st) st = cuda_status(cudaMemcpy(P.d_layout, layout.data(), layout.size() * sizeof(int), cudaMemcpyHostToDevice), "layout copy");
+        if (st) return st;
+    }
     st = cuda_status(cudaMalloc(&b->d_grids, grids.size() * sizeof(BatchGrid)), "cudaMalloc(grids)");
-    if (!st) st = cuda_status(cudaMalloc(&b->d_layout, layout.size() * sizeof(int)), "cudaMalloc(layout)");
-    if (!st) st = cuda_status(cudaMalloc(&b->d_counters, (ctr + 2) * sizeof(unsigned)), "cudaMalloc(counters)");
     if (!st) st = cuda_status(cudaMalloc(&b->d_bands, std::max(band, 1) * sizeof(uint16_t)), "cudaMalloc(bands)");
     if (!st) st = cuda_status(cudaMalloc(&b->d_coefs, coefs.size() * sizeof(float)), "cudaMalloc(coefs)");
     if (!st) st = cuda_status(cudaMemcpy(b->d_grids, grids.data(), grids.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice), "grids copy");
-    if (!st) st = cuda_status(cudaMemcpy(b->d_layout, layout.data(), layout.size() * sizeof(int), cudaMemcpyHostToDevice), "layout copy");
     if (!st) st = cuda_status(cudaMemcpy(b->d_coefs, coefs.data(), coefs.size() * sizeof(float), cudaMemcpyHostToDevice), "coefs copy");
     if (st) return st;
     build_bands_kernel<<<(unsigned)grids.size(), 256>>>(b->d_grids, b->d_coefs, b->d_bands);
@@ -531,23 +619,27 @@ int batch_build(tcs_batch b) {
 }
 
 int batch_enqueue(tcs_batch b, cudaStream_t s) {
-    int st = cuda_status(cudaMemsetAsync(b->d_counters, 0, (b->n_counters + 2) * sizeof(unsigned), s),
-                         "counter reset");
-    if (st) return st;
-    BatchParams p;
-    p.grids = b->d_grids;
-    p.step_off = b->d_layout;
-    p.tile_prefix = b->d_layout + b->n_steps + 1;
-    p.n_steps = b->n_steps;
-    p.n_grids = (int)b->entries.size();
-    p.n_items = b->n_items;
-    p.counters = b->d_counters;
-    p.work_counter = b->d_counters + b->n_counters;
-    p.error = reinterpret_cast<int *>(b->d_counters + b->n_counters + 1);
-    p.bands = b->d_bands;
-    st = cuda_status(launch_batch(p, g_sms, s), "batch kernel launch");
-    if (st) return st;
-    const int n = (int)b->entries.size();
+    for (int k = 0; k < 2; k++) {
+        auto &P = b->part[k];
+        if (!P.n_grids) continue;
+        int st = cuda_status(cudaMemsetAsync(P.d_counters, 0, (P.n_counters + 2) * sizeof(unsigned), s),
+                             "counter reset");
+        if (st) return st;
+        BatchParams p;
+        p.grids = b->d_grids + P.first;
+        p.step_off = P.d_layout;
+        p.tile_prefix = P.d_layout + P.n_steps + 1;
+        p.n_steps = P.n_steps;
+        p.n_grids = P.n_grids;
+        p.n_items = P.n_items;
+        p.counters = P.d_counters;
+        p.work_counter = P.d_counters + P.n_counters;
+        p.error = reinterpret_cast<int *>(P.d_counters + P.n_counters + 1);
+        p.bands = b->d_bands;
+        st = cuda_status(launch_batch(p, k == 1, g_sms, s), "batch kernel launch");
+        if (st) return st;
+    }
+    const int n = b->n_grids;
     flip_states_kernel<<<(n + 255) / 256, 256, 0, s>>>(b->d_grids, n);
     return cuda_status(cudaGetLastError(), "state flip launch");
 }
@@ -700,7 +792,7 @@ int tcs_batch_info(tcs_batch b, long long *point_updates, int *items, int *grids
     int st = batch_build(b);
     if (st) return st;
     if (point_updates) *point_updates = b->point_updates;
-    if (items) *items = b->n_items;
+    if (items) *items = b->part[0].n_items + b->part[1].n_items;
     if (grids) *grids = (int)b->entries.size();
     return TCS_OK;
 }

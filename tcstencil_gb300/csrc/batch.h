@@ -69,8 +69,9 @@ constexpr int kBatchMaxBandElems = 4 * 5 * 512;
 
 // Sets the kernel attributes and returns the SM count (the launch grid).
 cudaError_t batch_prepare(int *num_sms);
-// One persistent launch over p's work; grid = min(items, SMs).
-cudaError_t launch_batch(const BatchParams &p, int num_sms, cudaStream_t s);
+// One persistent launch over p's work (all grids of one precision: split or
+// FP16); grid = min(items, SMs).  A run launches one per precision present.
+cudaError_t launch_batch(const BatchParams &p, bool split, int num_sms, cudaStream_t s);
 // Bands of one stencil (coefficients n x n row-major, n = 2r+1) into dst.
 cudaError_t launch_build_bands(const float *coef, int r, bool box, bool split, uint16_t *dst,
                                cudaStream_t s);

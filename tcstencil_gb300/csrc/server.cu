@@ -424,7 +424,8 @@ bool tcs_server_s::launch_round() {
         if (q->state == kResident && q->done_steps < q->steps) part.push_back(q);
     if (part.empty()) return false;
 
-    // grids sorted by this round's steps, descending (stable: admission order)
+    // FP16 grids first, then split grids (one batched launch each), each part
+    // sorted by this round's steps, descending (stable: admission order)
     std::vector<int> run_steps(part.size());
     for (size_t i = 0; i < part.size(); i++) {
         const int rem = part[i]->steps - part[i]->done_steps;
@@ -432,8 +433,10 @@ bool tcs_server_s::launch_round() {
     }
     std::vector<size_t> order(part.size());
     for (size_t i = 0; i < order.size(); i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](size_t x, size_t y) { return run_steps[x] > run_steps[y]; });
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+        if (part[x]->split != part[y]->split) return !part[x]->split;
+        return run_steps[x] > run_steps[y];
+    });
     {
         std::vector<Request *> p2(part.size());
         std::vector<int> s2(part.size());
@@ -445,7 +448,9 @@ bool tcs_server_s::launch_round() {
         run_steps.swap(s2);
     }
     const int n = (int)part.size();
-    const int max_s = run_steps[0];
+    int first[2] = {0, 0}, count[2] = {0, 0};
+    for (int i = 0; i < n; i++) count[part[i]->split]++;
+    first[1] = count[0];
     size_t n_ctr = 0;
     std::vector<int> tiles(n);
     for (int i = 0; i < n; i++) {
@@ -453,16 +458,26 @@ bool tcs_server_s::launch_round() {
         tiles[i] = ((q->g.ny + kTile - 1) / kTile) * ((q->g.nx + kTile - 1) / kTile);
         n_ctr += run_steps[i];
     }
-    const size_t n_layout = (size_t)max_s + 1 + n + 1;
+    // layouts: part k's step_off then tile_prefix at lay_off[k]
+    size_t lay_off[2], n_layout = 0;
+    for (int k = 0; k < 2; k++) {
+        lay_off[k] = n_layout;
+        if (count[k]) n_layout += (size_t)run_steps[first[k]] + 1 + count[k] + 1;
+    }
     // buffer b is idle (its last round completed), so it may be regrown
     int st = grow_pinned(&b.h_grids, &b.cap_hg, part.size(), retired);
     if (!st) st = grow_pinned(&b.h_layout, &b.cap_hl, n_layout, retired);
     if (!st) st = grow_device(&b.d_grids, &b.cap_dg, part.size(), retired);
     if (!st) st = grow_device(&b.d_layout, &b.cap_dl, n_layout, retired);
-    if (!st) st = grow_device(&b.d_counters, &b.cap_dc, n_ctr + 1, retired);
-    const long long n_items =
-        st ? 0 : batch_layout(run_steps.data(), tiles.data(), n, b.h_layout, b.h_layout + max_s + 1);
-    if (!st && n_items < 0) st = fail(TCS_ERR_INVALID, "round of more than 2^31 work items");
+    if (!st) st = grow_device(&b.d_counters, &b.cap_dc, n_ctr + 2, retired);
+    long long n_items[2] = {0, 0};
+    for (int k = 0; k < 2 && !st; k++) {
+        if (!count[k]) continue;
+        const int ms = run_steps[first[k]];
+        n_items[k] = batch_layout(run_steps.data() + first[k], tiles.data() + first[k], count[k],
+                                  b.h_layout + lay_off[k], b.h_layout + lay_off[k] + ms + 1);
+        if (n_items[k] < 0) st = fail(TCS_ERR_INVALID, "round of more than 2^31 work items");
+    }
     if (st) {
         for (Request *q : part) fail_request(q, st);
         return true;
@@ -497,21 +512,23 @@ bool tcs_server_s::launch_round() {
         }
     if (!st) st = cuda_status(cudaMemcpyAsync(b.d_grids, b.h_grids, part.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice, compute), "round descriptors");
     if (!st) st = cuda_status(cudaMemcpyAsync(b.d_layout, b.h_layout, n_layout * sizeof(int), cudaMemcpyHostToDevice, compute), "round layout");
-    if (!st) st = cuda_status(cudaMemsetAsync(b.d_counters, 0, (n_ctr + 1) * sizeof(unsigned), compute), "round counters");
+    if (!st) st = cuda_status(cudaMemsetAsync(b.d_counters, 0, (n_ctr + 2) * sizeof(unsigned), compute), "round counters");
     if (!st) st = cuda_status(cudaEventRecord(b.start, compute), "cudaEventRecord");
-    if (!st) {
+    for (int k = 0; k < 2 && !st; k++) {
+        if (!count[k]) continue;
+        const int ms = run_steps[first[k]];
         BatchParams p;
-        p.grids = b.d_grids;
-        p.step_off = b.d_layout;
-        p.tile_prefix = b.d_layout + max_s + 1;
-        p.n_steps = max_s;
-        p.n_grids = n;
-        p.n_items = (int)n_items;
-        p.counters = b.d_counters;
-        p.work_counter = b.d_counters + n_ctr;
+        p.grids = b.d_grids + first[k];
+        p.step_off = b.d_layout + lay_off[k];
+        p.tile_prefix = b.d_layout + lay_off[k] + ms + 1;
+        p.n_steps = ms;
+        p.n_grids = count[k];
+        p.n_items = (int)n_items[k];
+        p.counters = b.d_counters;  // ctr_base is absolute across both parts
+        p.work_counter = b.d_counters + n_ctr + k;
         p.error = d_err;
         p.bands = d_bands;
-        st = cuda_status(launch_batch(p, sms, compute), "batch launch");
+        st = cuda_status(launch_batch(p, k == 1, sms, compute), "batch launch");
     }
     if (!st) st = cuda_status(cudaEventRecord(b.end, compute), "cudaEventRecord");
     if (st) {
