@@ -10,7 +10,8 @@
 // running CTAs.  An item of step t > 0 needs every
 // tile of its grid's step t - 1: the producer waits (bounded) on a
 // per-(grid, step) completion counter that the epilogue warps increment after
-// their stores.  Those items come earlier in the list and so were taken by
+// their stores (a release reduction; the producer polls with acquire loads).
+// Those items come earlier in the list and so were taken by
 // running CTAs; the earliest unfinished item always has its inputs ready, so
 // the launch cannot deadlock, whatever else shares the GPU.
 // The same counters also guard the ping-pong's write-after-read hazard: step
@@ -46,6 +47,9 @@ __device__ int g_batch_error = 0;
 // kernel's shape).  Split items: two stages of hi+lo plus bands, the window
 // ring of the single-grid split kernel, twelve epilogue warps in three groups.
 constexpr int kRing = 8;  // published work items in flight
+// The work layout (step offsets, tile prefix) is copied into shared memory
+// when it fits, so decoding an item costs no global round trip.
+constexpr int kTableInts = 2048;
 template <bool SPLIT>
 struct BatchCfg {
     static constexpr int STAGES = SPLIT ? 2 : 3;
@@ -55,7 +59,7 @@ struct BatchCfg {
     static constexpr int GROUPS = SPLIT ? 3 : 2;
     static constexpr int EPI_WARPS = 4 * GROUPS;
     static constexpr int THREADS = 32 * (2 + EPI_WARPS);
-    static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 512;
+    static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 512 + kTableInts * 4;
     static_assert(kRing > STAGES + 2, "a ring slot is reused only after its item's epilogue");
     static_assert(SMEM <= 232448, "shared memory budget");
     static_assert(STAGE_BYTES % 16 == 0, "bulk copy alignment");
@@ -70,6 +74,13 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     return v;
 }
 
+// Completion count with release semantics: the warp's stores (ordered before
+// this lane's by the preceding __syncwarp) are visible at GPU scope before
+// the count, for the consumer's acquire load of it.
+__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 
 // A bounded wait gave up: record the code in the launch's error word (which
 // every CTA polls to stop early) and in the unit's word tcs_device_error reads.
@@ -78,22 +89,24 @@ __device__ __forceinline__ void batch_fail(const BatchParams &p, int code) {
     record_error(&g_batch_error, code);
 }
 
-// Work index k -> (grid, step, tile); see BatchParams.
-__device__ __forceinline__ BatchItem decode_item(const BatchParams &p, int k) {
-    int lo = 0, hi = p.n_steps;  // step_off[lo] <= k < step_off[hi]
+// Work index k -> (grid, step, tile) from the step offsets and tile prefix
+// (shared or global memory); see BatchParams.
+__device__ __forceinline__ BatchItem decode_item(const int *step_off, const int *tile_prefix,
+                                                 int n_steps, int n_grids, int k) {
+    int lo = 0, hi = n_steps;  // step_off[lo] <= k < step_off[hi]
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
-        if (__ldg(p.step_off + mid) <= k) lo = mid;
+        if (step_off[mid] <= k) lo = mid;
         else hi = mid;
     }
-    const int local = k - __ldg(p.step_off + lo);
-    int a = 0, b = p.n_grids;  // tile_prefix[a] <= local < tile_prefix[b]
+    const int local = k - step_off[lo];
+    int a = 0, b = n_grids;  // tile_prefix[a] <= local < tile_prefix[b]
     while (b - a > 1) {
         const int mid = (a + b) >> 1;
-        if (__ldg(p.tile_prefix + mid) <= local) a = mid;
+        if (tile_prefix[mid] <= local) a = mid;
         else b = mid;
     }
-    return BatchItem{a, lo, local - __ldg(p.tile_prefix + a)};
+    return BatchItem{a, lo, local - tile_prefix[a]};
 }
 
 __global__ void build_bands_kernel(BatchGrid *grids, const float *coefs, uint16_t *bands) {
@@ -137,6 +150,9 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     volatile int *grid_error = p.error;
     static_assert((2 * NS + 2 * NACC + 1 + kRing) * 8 + kRing * 12 + 8 <= 512, "barrier area");
+    int *tables = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(bars) + 512);
+    const int n_table = p.n_steps + 1 + p.n_grids + 1;
+    const bool tables_in_smem = n_table <= kTableInts;
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -160,6 +176,11 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
         tmem_alloc(tmem_slot, kTmemCols);
         tmem_relinquish();
     }
+    if (tables_in_smem) {
+        for (int i = threadIdx.x; i <= p.n_steps; i += blockDim.x) tables[i] = p.step_off[i];
+        for (int i = threadIdx.x; i <= p.n_grids; i += blockDim.x)
+            tables[p.n_steps + 1 + i] = p.tile_prefix[i];
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -167,25 +188,30 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
 
     if (warp == 0) {
         // ------------------------------------------------------ producer ---
-        // Takes work indices in increasing order from the global counter,
-        // decodes each once and publishes it in ring slot i % kRing; an index
-        // past the end is published as the stop sentinel (g = -1).
+        // Takes work indices in increasing order from the global counter (the
+        // next one is requested while the current one is loaded, to hide the
+        // atomic's latency), decodes each once and publishes it in ring slot
+        // i % kRing; an index past the end is published as the stop sentinel.
         if (lane == 0) {
+            const int *step_off = tables_in_smem ? tables : p.step_off;
+            const int *tile_prefix = tables_in_smem ? tables + p.n_steps + 1 : p.tile_prefix;
             int last_issued = -1;
+            int k_next = (int)atomicAdd(p.work_counter, 1u);
             for (int i = 0;; i++) {
                 const int s = i % NS, j = i % kRing;
+                const int k = k_next;
+                if (k < p.n_items) k_next = (int)atomicAdd(p.work_counter, 1u);
                 if (!mbar_wait(&empty[s], ((i / NS) & 1) ^ 1, abort_flag)) {
                     batch_fail(p, kErrWaitEmpty);
                     *abort_flag = 1;
                     break;
                 }
-                const int k = (int)atomicAdd(p.work_counter, 1u);
                 if (k >= p.n_items) {
                     ring[j] = BatchItem{-1, 0, 0};
                     mbar_arrive(&item_ready[j]);
                     break;
                 }
-                const BatchItem it = decode_item(p, k);
+                const BatchItem it = decode_item(step_off, tile_prefix, p.n_steps, p.n_grids, k);
                 ring[j] = it;
                 mbar_arrive(&item_ready[j]);
                 const BatchGrid &g = p.grids[it.g];
@@ -396,9 +422,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 epilogue_store<false>(o, f, 0, grp, m, Y0, X0);
                 slots.used(mask);
             }
-            __threadfence();  // this warp's stores before the completion count
             __syncwarp();
-            if (lane == 0) atomicAdd(p.counters + g.ctr_base + it.t, 1u);
+            if (lane == 0) red_release_add(p.counters + g.ctr_base + it.t, 1u);
         }
     }
 
