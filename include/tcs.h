@@ -250,6 +250,15 @@ int tcs_batch_download(tcs_batch batch, int index, float *grid, int grid_on_host
 int tcs_batch_run(tcs_batch batch, int use_graph, void *stream);
 /* Point updates per run, work items per run and the number of grids. */
 int tcs_batch_info(tcs_batch batch, long long *point_updates, int *items, int *grids);
+/* External gate: grid `index` starts its first step only once the device
+ * word *d_flag is >= value (written by another stream, kernel or copy), so a
+ * batch can consume what a producer elsewhere writes without a host round
+ * trip.  Set before the first upload or run. */
+int tcs_batch_set_gate(tcs_batch batch, int index, const unsigned *d_flag, unsigned value);
+/* Limit of the in-kernel dependency and gate waits (default 1 s).  A wait
+ * that runs out stops the launch cleanly and tcs_device_error reports
+ * TCS_ERR_TIMEOUT (code 6). */
+int tcs_batch_set_wait_limit(tcs_batch batch, double seconds);
 
 /* ------------------------------------------------------- FP64 drift check
  * An FP64 shadow of a problem on the device, stepped with gold's tap order

@@ -123,6 +123,8 @@ SIGNATURES = {
     "tcs_batch_run": (_I, [_P, _I, _P]),
     "tcs_batch_info": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I),
                             ctypes.POINTER(_I)]),
+    "tcs_batch_set_gate": (_I, [_P, _I, _P, ctypes.c_uint]),
+    "tcs_batch_set_wait_limit": (_I, [_P, ctypes.c_double]),
     "tcs_drift_create": (_I, [ctypes.POINTER(Problem), ctypes.POINTER(_P)]),
     "tcs_drift_destroy": (_I, [_P]),
     "tcs_drift_upload": (_I, [_P, _P, _I, _P]),
@@ -393,6 +395,13 @@ class Batch:
 
     def run(self, use_graph: bool = True, stream=None) -> None:
         _check(lib().tcs_batch_run(self._h, int(use_graph), _stream(stream)))
+
+    def set_gate(self, index: int, d_flag, value: int) -> None:
+        """Grid `index` starts once the device word at d_flag is >= value."""
+        _check(lib().tcs_batch_set_gate(self._h, index, _ptr(d_flag), int(value)))
+
+    def set_wait_limit(self, seconds: float) -> None:
+        _check(lib().tcs_batch_set_wait_limit(self._h, float(seconds)))
 
     def info(self):
         """(point updates per run, work items per run, grids)."""

@@ -215,15 +215,23 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 ring[j] = it;
                 mbar_arrive(&item_ready[j]);
                 const BatchGrid &g = p.grids[it.g];
+                // step t > 0: every tile of the grid's previous step is stored;
+                // step 0 of a gated grid: the external gate is open
+                const unsigned *ctr = nullptr;
+                unsigned target = 0;
                 if (it.t > 0) {
-                    // every tile of the previous step of this grid is stored
-                    const unsigned target = (unsigned)(g.n_tiles * C::EPI_WARPS);
-                    const unsigned *ctr = p.counters + g.ctr_base + it.t - 1;
+                    ctr = p.counters + g.ctr_base + it.t - 1;
+                    target = (unsigned)(g.n_tiles * C::EPI_WARPS);
+                } else if (g.gate) {
+                    ctr = g.gate;
+                    target = g.gate_value;
+                }
+                if (ctr) {
                     if (ld_acquire(ctr) < target) {
                         const uint64_t t0 = global_timer_ns();
                         bool ok = true;
                         while (ld_acquire(ctr) < target) {
-                            if (*grid_error || global_timer_ns() - t0 > kWaitLimitNs) {
+                            if (*grid_error || global_timer_ns() - t0 > p.wait_ns) {
                                 ok = false;
                                 break;
                             }
@@ -506,7 +514,10 @@ struct tcs_batch_s {
         int scale_exp;
         size_t plane_elems;
         size_t offset[2][2];  // element offsets of the planes in the pool
+        const unsigned *gate = nullptr;
+        unsigned gate_value = 0;
     };
+    unsigned long long wait_ns = kBatchWaitNs;
     std::vector<Entry> entries;
     uint16_t *pool = nullptr;
     size_t pool_elems = 0;
@@ -599,6 +610,8 @@ int batch_build(tcs_batch b) {
         G.ctr_base = ctr[split];
         G.band_base = band;
         G.state = 0;
+        G.gate = e.gate;
+        G.gate_value = e.gate_value;
         steps[i] = e.steps;
         tiles[i] = G.n_tiles;
         ctr[split] += std::max(e.steps, 1);
@@ -661,6 +674,7 @@ int batch_enqueue(tcs_batch b, cudaStream_t s) {
         p.work_counter = P.d_counters + P.n_counters;
         p.error = reinterpret_cast<int *>(P.d_counters + P.n_counters + 1);
         p.bands = b->d_bands;
+        p.wait_ns = b->wait_ns;
         st = cuda_status(launch_batch(p, k == 1, g_sms, s), "batch kernel launch");
         if (st) return st;
     }
@@ -810,6 +824,26 @@ int tcs_batch_run(tcs_batch b, int use_graph, void *stream) {
     }
     if (!st) b->runs++;
     return st;
+}
+
+int tcs_batch_set_gate(tcs_batch b, int index, const unsigned *d_flag, unsigned value) {
+    if (!b || index < 0 || index >= (int)b->entries.size())
+        return fail(TCS_ERR_INVALID, "tcs_batch_set_gate: bad arguments");
+    if (b->built) return fail(TCS_ERR_INVALID, "tcs_batch_set_gate: set gates before the first upload or run");
+    b->entries[index].gate = d_flag;
+    b->entries[index].gate_value = value;
+    return TCS_OK;
+}
+
+int tcs_batch_set_wait_limit(tcs_batch b, double seconds) {
+    if (!b || !(seconds > 0.0) || seconds > 3600.0)
+        return fail(TCS_ERR_INVALID, "tcs_batch_set_wait_limit: bad limit");
+    b->wait_ns = (unsigned long long)(seconds * 1e9);
+    if (b->graph) {  // the limit is a launch parameter
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return TCS_OK;
 }
 
 int tcs_batch_info(tcs_batch b, long long *point_updates, int *items, int *grids) {

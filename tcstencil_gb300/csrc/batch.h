@@ -20,6 +20,9 @@ struct BatchGrid {
     int ctr_base;   // completion counter of step 0 of the run
     int band_base;  // first band element in the band buffer
     int state;      // which plane holds the current state
+    // external gate: step 0 starts once *gate >= gate_value (null: no gate)
+    const unsigned *gate;
+    unsigned gate_value;
 };
 
 struct BatchItem {
@@ -40,7 +43,11 @@ struct BatchParams {
     unsigned *work_counter;  // next work index, zero at launch
     int *error;              // first failed wait of this launch (0 = none)
     const uint16_t *bands;
+    unsigned long long wait_ns;  // limit of the dependency and gate waits
 };
+
+// Default limit of a batched run's dependency and gate waits: one second.
+constexpr unsigned long long kBatchWaitNs = 1000000000ull;
 
 // Fills step_off and tile_prefix for grids whose run steps (descending) and
 // tile counts are given; returns the number of work items, or -1 when it

@@ -501,6 +501,8 @@ bool tcs_server_s::launch_round() {
         G.ctr_base = ctr;
         G.band_base = q->slot * kBatchMaxBandElems;
         G.state = q->done_steps & 1;
+        G.gate = nullptr;
+        G.gate_value = 0;
         ctr += run_steps[i];
     }
 
@@ -528,6 +530,7 @@ bool tcs_server_s::launch_round() {
         p.work_counter = b.d_counters + n_ctr + k;
         p.error = d_err;
         p.bands = d_bands;
+        p.wait_ns = kBatchWaitNs;
         st = cuda_status(launch_batch(p, k == 1, sms, compute), "batch launch");
     }
     if (!st) st = cuda_status(cudaEventRecord(b.end, compute), "cudaEventRecord");

@@ -138,6 +138,15 @@ def test_batch_add_validates_before_any_device_work(tcs):
     assert e.value.status == tcs.TCS_ERR_INVALID
     with pytest.raises(tcs.TcsError):
         b.add(64, 64, "box2d1r", c, -1)
+    for bad in [lambda: b.set_gate(2, 0x1000, 1), lambda: b.set_gate(-1, 0x1000, 1),
+                lambda: b.set_wait_limit(0.0), lambda: b.set_wait_limit(-1.0),
+                lambda: b.set_wait_limit(float("nan"))]:
+        with pytest.raises(tcs.TcsError) as e:
+            bad()
+        assert e.value.status == tcs.TCS_ERR_INVALID
+    b.set_gate(0, 0x1000, 1)
+    b.set_gate(0, None, 0)
+    b.set_wait_limit(0.25)
     b.close()
 
 

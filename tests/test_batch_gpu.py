@@ -140,3 +140,80 @@ def test_batch_device_buffers(tcs, torch_cuda):
     torch.cuda.synchronize()
     np.testing.assert_array_equal(d_out.cpu().numpy(), _solo(tcs, g0, "star2d2r", c, 4, "split"))
     b.close()
+
+
+def _gated_batch(tcs, rng, flag, limit=None):
+    """A gated FP16 grid and an ungated one (same launch) plus an ungated split
+    grid (its own launch)."""
+    cases = [("box2d1r", "f16", 300, 260, 3), ("star2d2r", "f16", 180, 210, 2),
+             ("box2d2r", "split", 200, 140, 2)]
+    b = tcs.Batch()
+    inputs, coeffs = [], []
+    for k, (stencil, precision, ny, nx, steps) in enumerate(cases):
+        c = normalized_coeffs(rng, stencil)
+        b.add(ny, nx, stencil, c, steps, precision)
+        coeffs.append(c)
+        inputs.append(grid(rng, ny, nx))
+    b.set_gate(0, flag, 1)
+    if limit is not None:
+        b.set_wait_limit(limit)
+    for k, g0 in enumerate(inputs):
+        b.upload(k, g0)
+    return b, cases, inputs, coeffs
+
+
+def test_gate_that_never_opens_times_out_cleanly(tcs, torch_cuda):
+    """A bounded wait runs out on a flag nothing sets: the launch stops, the
+    host reads TCS_ERR_TIMEOUT with the dependency-wait code 6, the split
+    launch after it is unaffected, and the context stays usable."""
+    torch = torch_cuda
+    rng = np.random.default_rng(47)
+    flag = torch.zeros(4, dtype=torch.int32, device="cuda")
+    b, cases, inputs, coeffs = _gated_batch(tcs, rng, flag, limit=0.05)
+    b.run(use_graph=False)
+    torch.cuda.synchronize()
+    with pytest.raises(tcs.TcsError) as e:
+        tcs.device_error()
+    assert e.value.status == tcs.TCS_ERR_TIMEOUT and "code 6" in str(e.value)
+    assert tcs.device_error() == 0  # the word was cleared
+    out = np.empty_like(inputs[2])
+    b.download(2, out)
+    stencil, precision, _, _, steps = cases[2]
+    np.testing.assert_array_equal(out, _solo(tcs, inputs[2], stencil, coeffs[2], steps, precision))
+    b.close()
+    # the same batch with its gate open runs to the plans' results
+    flag.fill_(1)
+    b, cases, inputs, coeffs = _gated_batch(tcs, np.random.default_rng(47), flag, limit=0.05)
+    b.run(use_graph=True)
+    for k, (stencil, precision, _, _, steps) in enumerate(cases):
+        out = np.empty_like(inputs[k])
+        b.download(k, out)
+        np.testing.assert_array_equal(out, _solo(tcs, inputs[k], stencil, coeffs[k], steps, precision))
+    torch.cuda.synchronize()
+    assert tcs.device_error() == 0
+    b.close()
+
+
+def test_gate_opened_by_a_copy_on_another_stream(tcs, torch_cuda):
+    """The batch waits in the kernel for a word another stream writes (a copy
+    engine transfer, no kernel), then runs to the plans' results."""
+    import time
+
+    torch = torch_cuda
+    rng = np.random.default_rng(48)
+    flag = torch.zeros(4, dtype=torch.int32, device="cuda")
+    one = torch.ones(4, dtype=torch.int32).pin_memory()
+    b, cases, inputs, coeffs = _gated_batch(tcs, rng, flag)
+    torch.cuda.synchronize()
+    s_run, s_copy = torch.cuda.Stream(), torch.cuda.Stream()
+    b.run(use_graph=False, stream=s_run)
+    time.sleep(0.02)
+    with torch.cuda.stream(s_copy):
+        flag.copy_(one, non_blocking=True)
+    torch.cuda.synchronize()
+    assert tcs.device_error() == 0
+    for k, (stencil, precision, _, _, steps) in enumerate(cases):
+        out = np.empty_like(inputs[k])
+        b.download(k, out)
+        np.testing.assert_array_equal(out, _solo(tcs, inputs[k], stencil, coeffs[k], steps, precision))
+    b.close()
