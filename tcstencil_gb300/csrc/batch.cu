@@ -10,8 +10,10 @@
 // running CTAs.  An item of step t > 0 needs every
 // tile of its grid's step t - 1: the producer waits (bounded) on a
 // per-(grid, step) completion counter that the epilogue warps increment after
-// their stores (a release reduction; the producer polls with acquire loads).
-// Those items come earlier in the list and so were taken by
+// their stores (release reductions, one per run of consecutive items of the
+// same grid and step; the producer polls with acquire loads, once per run of
+// items of the same grid and step).  Those items come earlier in the list and
+// so were taken by
 // running CTAs; the earliest unfinished item always has its inputs ready, so
 // the launch cannot deadlock, whatever else shares the GPU.
 // The same counters also guard the ping-pong's write-after-read hazard: step
@@ -58,7 +60,8 @@ struct BatchCfg {
     static constexpr int STAGE_BYTES = PLANES * kPlaneStage + BAND_BYTES;
     static constexpr int GROUPS = SPLIT ? 3 : 2;
     static constexpr int EPI_WARPS = 4 * GROUPS;
-    static constexpr int THREADS = 32 * (2 + EPI_WARPS);
+    static constexpr int SIGNAL_WARP = 2 + EPI_WARPS;
+    static constexpr int THREADS = 32 * (3 + EPI_WARPS);
     static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 512 + kTableInts * 4;
     static_assert(kRing > STAGES + 2, "a ring slot is reused only after its item's epilogue");
     static_assert(SMEM <= 232448, "shared memory budget");
@@ -145,17 +148,21 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
     uint64_t *acc_empty = acc_full + NACC;        // [NACC]
     uint64_t *drain = acc_empty + NACC;           // [1]
     uint64_t *item_ready = drain + 1;             // [kRing]
-    BatchItem *ring = reinterpret_cast<BatchItem *>(item_ready + kRing);  // [kRing]
+    uint64_t *item_done = item_ready + kRing;     // [kRing] epilogue stores issued
+    uint64_t *ring_free = item_done + kRing;      // [kRing] signal warp done with the slot
+    BatchItem *ring = reinterpret_cast<BatchItem *>(ring_free + kRing);  // [kRing]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(ring + kRing);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     volatile int *grid_error = p.error;
-    static_assert((2 * NS + 2 * NACC + 1 + kRing) * 8 + kRing * 12 + 8 <= 512, "barrier area");
+    static_assert((2 * NS + 2 * NACC + 1 + 3 * kRing) * 8 + kRing * 12 + 8 <= 512, "barrier area");
     int *tables = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(bars) + 512);
     const int n_table = p.n_steps + 1 + p.n_grids + 1;
     const bool tables_in_smem = n_table <= kTableInts;
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
+    // a wait on another role may span the producer's dependency or gate wait
+    const uint64_t wait_lim = p.wait_ns + kWaitLimitNs;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; s++) {
@@ -167,7 +174,11 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             mbar_init(&acc_empty[b], C::EPI_WARPS);
         }
         mbar_init(drain, 1);
-        for (int j = 0; j < kRing; j++) mbar_init(&item_ready[j], 1);
+        for (int j = 0; j < kRing; j++) {
+            mbar_init(&item_ready[j], 1);
+            mbar_init(&item_done[j], C::EPI_WARPS);
+            mbar_init(&ring_free[j], 1);
+        }
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -196,12 +207,16 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             const int *step_off = tables_in_smem ? tables : p.step_off;
             const int *tile_prefix = tables_in_smem ? tables + p.n_steps + 1 : p.tile_prefix;
             int last_issued = -1;
+            // (grid, step) whose dependency this thread has already seen met;
+            // later items of the same pair need no further poll or fence
+            int met_g = -1, met_t = -1;
             int k_next = (int)atomicAdd(p.work_counter, 1u);
             for (int i = 0;; i++) {
                 const int s = i % NS, j = i % kRing;
                 const int k = k_next;
                 if (k < p.n_items) k_next = (int)atomicAdd(p.work_counter, 1u);
-                if (!mbar_wait(&empty[s], ((i / NS) & 1) ^ 1, abort_flag)) {
+                if (!mbar_wait(&empty[s], ((i / NS) & 1) ^ 1, abort_flag, wait_lim) ||
+                    !mbar_wait(&ring_free[j], ((i / kRing) & 1) ^ 1, abort_flag, wait_lim)) {
                     batch_fail(p, kErrWaitEmpty);
                     *abort_flag = 1;
                     break;
@@ -219,7 +234,9 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 // step 0 of a gated grid: the external gate is open
                 const unsigned *ctr = nullptr;
                 unsigned target = 0;
-                if (it.t > 0) {
+                if (it.g == met_g && it.t == met_t) {
+                    // met before, and the proxy fence after that poll still orders the copies below
+                } else if (it.t > 0) {
                     ctr = p.counters + g.ctr_base + it.t - 1;
                     target = (unsigned)(g.n_tiles * C::EPI_WARPS);
                 } else if (g.gate) {
@@ -245,6 +262,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     }
                     // the bulk copies below read what other SMs stored
                     fence_proxy_async_global();
+                    met_g = it.g;
+                    met_t = it.t;
                 }
                 const int band_bytes = batch_band_elems(g.r, SPLIT) * 2;
                 uint8_t *st = stage_base + (size_t)s * C::STAGE_BYTES;
@@ -276,14 +295,14 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             bool stop = false;
             for (int i = 0; !stop; i++) {
                 const int s = i % NS;
-                if (!mbar_wait(&item_ready[i % kRing], (i / kRing) & 1, abort_flag)) {
+                if (!mbar_wait(&item_ready[i % kRing], (i / kRing) & 1, abort_flag, wait_lim)) {
                     batch_fail(p, kErrWaitFull);
                     *abort_flag = 1;
                     break;
                 }
                 const BatchItem it = ring[i % kRing];
                 if (it.g < 0) break;
-                if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
+                if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag, wait_lim)) {
                     batch_fail(p, kErrWaitFull);
                     *abort_flag = 1;
                     break;
@@ -296,7 +315,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
 #pragma unroll 1
                     for (int w = 0; w < kBatchWindows; w++, G++) {
                         const int r = G % kBatchRingSlots;
-                        if (!mbar_wait(&acc_empty[r], ((G / kBatchRingSlots) & 1) ^ 1, abort_flag)) {
+                        if (!mbar_wait(&acc_empty[r], ((G / kBatchRingSlots) & 1) ^ 1, abort_flag, wait_lim)) {
                             batch_fail(p, kErrWaitAccum);
                             *abort_flag = 1;
                             stop = true;
@@ -312,7 +331,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 } else {
                     uint32_t col;
                     const uint32_t mask = slots.take(false, col);
-                    if (!slots.acquire(acc_empty, mask, abort_flag)) {
+                    if (!slots.acquire(acc_empty, mask, abort_flag, wait_lim)) {
                         batch_fail(p, kErrWaitAccum);
                         *abort_flag = 1;
                         stop = true;
@@ -339,6 +358,47 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 }
             }
         }
+    } else if (warp == C::SIGNAL_WARP) {
+        // -------------------------------------------------------- signal ---
+        // Publishes completed items to the other SMs, off the epilogue
+        // warps' path: once all epilogue warps have issued an item's stores
+        // (item_done, release at CTA scope), one release reduction at GPU
+        // scope makes them visible before the count (release is cumulative).
+        // Counts are held while consecutive items share a (grid, step) and
+        // released when the next item differs or the run ends; the items
+        // that wait on them belong to a later step, which the producer
+        // publishes in the ring before it waits, so the release comes first.
+        if (lane == 0) {
+            unsigned *pend = nullptr;
+            unsigned n_pend = 0;
+            auto give_up = [&]() {
+                batch_fail(p, kErrWaitResult);
+                *abort_flag = 1;
+            };
+            for (int i = 0;; i++) {
+                const int j = i % kRing;
+                if (!mbar_wait(&item_ready[j], (i / kRing) & 1, abort_flag, wait_lim)) {
+                    give_up();
+                    break;
+                }
+                const BatchItem it = ring[j];
+                unsigned *ctr = nullptr;
+                if (it.g >= 0) ctr = p.counters + p.grids[it.g].ctr_base + it.t;
+                if (n_pend && ctr != pend) {
+                    red_release_add(pend, n_pend);
+                    n_pend = 0;
+                }
+                if (it.g < 0) break;
+                if (!mbar_wait(&item_done[j], (i / kRing) & 1, abort_flag, wait_lim)) {
+                    give_up();
+                    break;
+                }
+                mbar_arrive(&ring_free[j]);
+                pend = ctr;
+                n_pend += C::EPI_WARPS;
+            }
+            if (n_pend) red_release_add(pend, n_pend);
+        }
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;
@@ -356,7 +416,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
         };
         for (int i = 0; !stop; i++) {
             const int j = i % kRing;
-            bool ok = mbar_wait(&item_ready[j], (i / kRing) & 1, abort_flag);
+            bool ok = mbar_wait(&item_ready[j], (i / kRing) & 1, abort_flag, wait_lim);
             ok = __all_sync(0xffffffffu, ok);
             if (!ok) {
                 fail_result();
@@ -382,7 +442,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 auto ready = [&](int w) {
                     const int Gw = G0 + w;
                     bool okw = mbar_wait(&acc_full[Gw % kBatchRingSlots],
-                                         (Gw / kBatchRingSlots) & 1, abort_flag);
+                                         (Gw / kBatchRingSlots) & 1, abort_flag, wait_lim);
                     okw = __all_sync(0xffffffffu, okw);
                     if (!okw) fail_result();
                     return okw;
@@ -414,7 +474,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             } else {
                 uint32_t col;
                 const uint32_t mask = slots.take(false, col);
-                ok = slots.ready(acc_full, mask, abort_flag);
+                ok = slots.ready(acc_full, mask, abort_flag, wait_lim);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) {
                     fail_result();
@@ -430,8 +490,9 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 epilogue_store<false>(o, f, 0, grp, m, Y0, X0);
                 slots.used(mask);
             }
+            // this warp's stores are issued: the signal warp publishes them
             __syncwarp();
-            if (lane == 0) red_release_add(p.counters + g.ctr_base + it.t, 1u);
+            if (lane == 0) mbar_arrive(&item_done[j]);
         }
     }
 

@@ -284,11 +284,20 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
 // twelve epilogue warps have released its window; every warp releases a
 // window only after seeing it complete, so releases always count toward the
 // window they belong to.
+//
+// Two MMA issuers (warps 1 and 2) take the even and the odd windows.  Each
+// window costs its issuer a region wait and a commit; the tensor pipe takes
+// only a few MMAs ahead of the issuing thread, so with one issuer those
+// latencies would leave it idle for about 40 % of a window.  With two, one
+// issues while the other waits.  A region is reused five windows later, by
+// the other issuer, only after all twelve epilogue warps have released it;
+// a tile's stage is free when both issuers' commits for it have completed.
 constexpr int kRingSlots = 5;
 constexpr int kRegionCols = 96;
 constexpr int kRingGroups = 3;                     // epilogue block groups
 constexpr int kRingEpiWarps = 4 * kRingGroups;     // a lane quarter each
-constexpr int kRingThreads = 32 * (2 + kRingEpiWarps);
+constexpr int kRingIssuers = 2;                    // MMA issuer warps 1 and 2
+constexpr int kRingThreads = 32 * (1 + kRingIssuers + kRingEpiWarps);
 constexpr int kTileWindows = kTile / 16 + 1;
 static_assert(kRingSlots * kRegionCols <= kTmemCols, "window ring fits TMEM");
 
@@ -322,13 +331,13 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const Tc
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
+            mbar_init(&empty[s], kRingIssuers);
         }
         for (int r = 0; r < kRingSlots; r++) {
             mbar_init(&win_full[r], 1);
             mbar_init(&win_empty[r], kRingEpiWarps);
         }
-        mbar_init(drain, 1);
+        mbar_init(drain, kRingIssuers);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -376,11 +385,11 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const Tc
                 }
             }
         }
-    } else if (warp == 1) {
-        // ---------------------------------------------------- MMA issuer ---
+    } else if (warp <= kRingIssuers) {
+        // --------------------------------------------------- MMA issuers ---
         if (lane == 0) {
-            int i = 0, G = 0;  // tiles, global windows
-            bool issued_any = false;
+            const int id = warp - 1;  // takes the windows G with G % 2 == id
+            int i = 0, G = 0;         // tiles, global windows
             bool stop = false;
             const uint32_t band = smem_u32(band_base);
             for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
@@ -394,6 +403,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const Tc
                     smem_u32(stage_base + (size_t)s * NP * kPlaneStage), kChunkBytes, 128);
 #pragma unroll 1
                 for (int wg = 0; wg < kTileWindows; wg++, G++) {
+                    if ((G & 1) != id) continue;
                     const int r = G % kRingSlots;
                     if (!mbar_wait(&win_empty[r], ((G / kRingSlots) & 1) ^ 1, abort_flag)) {
                         record_error(&g_tc_error, kErrWaitAccum);
@@ -404,25 +414,24 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const Tc
                     tc_fence_after();
                     issue_split_window<C::R>(a_hi0, band, tmem_base + r * kRegionCols, wg);
                     umma_commit(&win_full[r]);
-                    issued_any = true;
                 }
-                umma_commit(&empty[s]);
+                if (!stop) umma_commit(&empty[s]);
             }
-            if (issued_any) {
-                umma_commit(drain);
-                const uint64_t t0 = global_timer_ns();
-                while (!mbar_try_wait(drain, 0)) {
-                    if (global_timer_ns() - t0 > kWaitLimitNs) {
-                        record_error(&g_tc_error, kErrWaitDrain);
-                        break;
-                    }
+            // both issuers commit (an issuer with nothing in flight completes
+            // its commit at once), so the drain phase always completes
+            umma_commit(drain);
+            const uint64_t t0 = global_timer_ns();
+            while (!mbar_try_wait(drain, 0)) {
+                if (global_timer_ns() - t0 > kWaitLimitNs) {
+                    record_error(&g_tc_error, kErrWaitDrain);
+                    break;
                 }
             }
         }
     } else {
         // ------------------------------------------------------ epilogue ---
-        const int q = warp & 3;             // TMEM lane quarter
-        const int grp = (warp - 2) >> 2;    // block group: blocks j with j % 3 == grp
+        const int q = warp & 3;                          // TMEM lane quarter
+        const int grp = (warp - 1 - kRingIssuers) >> 2;  // block group: blocks j with j % 3 == grp
         const int m = q * 32 + lane;
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
         TileOut o;

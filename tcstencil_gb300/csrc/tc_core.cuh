@@ -72,11 +72,12 @@ struct AccSlots {
     }
     // MMA issuer: waits until every slot of the mask is free (bounded).
     __device__ __forceinline__ bool acquire(uint64_t *acc_empty, uint32_t mask,
-                                            const volatile int *abort) const {
+                                            const volatile int *abort,
+                                            uint64_t limit_ns = kWaitLimitNs) const {
 #pragma unroll
         for (int s = 0; s < 2; s++)
             if ((mask >> s) & 1u)
-                if (!mbar_wait(&acc_empty[s], (uses[s] & 1u) ^ 1u, abort)) return false;
+                if (!mbar_wait(&acc_empty[s], (uses[s] & 1u) ^ 1u, abort, limit_ns)) return false;
         return true;
     }
     // MMA issuer: the slots' accumulators are complete when the MMAs are.
@@ -87,11 +88,12 @@ struct AccSlots {
     }
     // Epilogue: waits until the slots' accumulators are complete (bounded).
     __device__ __forceinline__ bool ready(uint64_t *acc_full, uint32_t mask,
-                                          const volatile int *abort) const {
+                                          const volatile int *abort,
+                                          uint64_t limit_ns = kWaitLimitNs) const {
 #pragma unroll
         for (int s = 0; s < 2; s++)
             if ((mask >> s) & 1u)
-                if (!mbar_wait(&acc_full[s], uses[s] & 1u, abort)) return false;
+                if (!mbar_wait(&acc_full[s], uses[s] & 1u, abort, limit_ns)) return false;
         return true;
     }
     // Epilogue (one lane per warp): this warp is done reading the slots.
