@@ -60,8 +60,12 @@ struct BatchCfg {
     static constexpr int STAGE_BYTES = PLANES * kPlaneStage + BAND_BYTES;
     static constexpr int GROUPS = SPLIT ? 3 : 2;
     static constexpr int EPI_WARPS = 4 * GROUPS;
-    static constexpr int SIGNAL_WARP = 2 + EPI_WARPS;
-    static constexpr int THREADS = 32 * (3 + EPI_WARPS);
+    // MMA issuer warps 1 .. ISSUERS: split items alternate windows between two
+    // (one issues while the other waits on a region or commits)
+    static constexpr int ISSUERS = SPLIT ? 2 : 1;
+    static constexpr int EPI_WARP0 = 1 + ISSUERS;
+    static constexpr int SIGNAL_WARP = EPI_WARP0 + EPI_WARPS;
+    static constexpr int THREADS = 32 * (SIGNAL_WARP + 1);
     static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 512 + kTableInts * 4;
     static_assert(kRing > STAGES + 2, "a ring slot is reused only after its item's epilogue");
     static_assert(SMEM <= 232448, "shared memory budget");
@@ -167,13 +171,13 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
+            mbar_init(&empty[s], C::ISSUERS);
         }
         for (int b = 0; b < NACC; b++) {
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], C::EPI_WARPS);
         }
-        mbar_init(drain, 1);
+        mbar_init(drain, C::ISSUERS);
         for (int j = 0; j < kRing; j++) {
             mbar_init(&item_ready[j], 1);
             mbar_init(&item_done[j], C::EPI_WARPS);
@@ -286,12 +290,12 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 }
             }
         }
-    } else if (warp == 1) {
-        // ---------------------------------------------------- MMA issuer ---
+    } else if (warp <= C::ISSUERS) {
+        // --------------------------------------------------- MMA issuers ---
         if (lane == 0) {
+            const int id = warp - 1;  // split: takes the windows G with G % 2 == id
             AccSlots slots;  // plain
             int G = 0;       // split: global window counter of the ring
-            bool issued_any = false;
             bool stop = false;
             for (int i = 0; !stop; i++) {
                 const int s = i % NS;
@@ -314,6 +318,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 if constexpr (SPLIT) {
 #pragma unroll 1
                     for (int w = 0; w < kBatchWindows; w++, G++) {
+                        if ((G & 1) != id) continue;
                         const int r = G % kBatchRingSlots;
                         if (!mbar_wait(&acc_empty[r], ((G / kBatchRingSlots) & 1) ^ 1, abort_flag, wait_lim)) {
                             batch_fail(p, kErrWaitAccum);
@@ -326,7 +331,6 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                         if (g.r == 1) issue_split_window<1>(a_hi0, band, d, w);
                         else issue_split_window<2>(a_hi0, band, d, w);
                         umma_commit(&acc_full[r]);
-                        issued_any = true;
                     }
                 } else {
                     uint32_t col;
@@ -342,19 +346,18 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                         else issue_subtile<2, false>(a_hi0, band, d, 0);
                         slots.commit(acc_full, mask);
                         slots.used(mask);
-                        issued_any = true;
                     }
                 }
                 if (!stop) umma_commit(&empty[s]);
             }
-            if (issued_any) {
-                umma_commit(drain);
-                const uint64_t t0 = global_timer_ns();
-                while (!mbar_try_wait(drain, 0)) {
-                    if (global_timer_ns() - t0 > kWaitLimitNs) {
-                        batch_fail(p, kErrWaitDrain);
-                        break;
-                    }
+            // every issuer commits (one with nothing in flight completes at
+            // once), so the drain phase always completes
+            umma_commit(drain);
+            const uint64_t t0 = global_timer_ns();
+            while (!mbar_try_wait(drain, 0)) {
+                if (global_timer_ns() - t0 > kWaitLimitNs) {
+                    batch_fail(p, kErrWaitDrain);
+                    break;
                 }
             }
         }
@@ -402,7 +405,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;
-        const int grp = (warp - 2) >> 2;  // plain: column half; split: block group
+        const int grp = (warp - C::EPI_WARP0) >> 2;  // plain: column half; split: block group
         const int m = q * 32 + lane;
         AccSlots slots;
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
