@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 const BatchItem it = decode_item(step_off, tile_prefix, p.n_steps, p.n_grids, k);
                 ring[j] = it;
                 mbar_arrive(&item_ready[j]);
-                const BatchGrid &g = p.grids[it.g];
+                const BatchGrid g = p.grids[it.g];  // one batch of loads, before any barrier
                 // step t > 0: every tile of the grid's previous step is stored;
                 // step 0 of a gated grid: the external gate is open
                 const unsigned *ctr = nullptr;
@@ -273,7 +273,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 uint8_t *st = stage_base + (size_t)s * C::STAGE_BYTES;
                 mbar_arrive_expect_tx(&full[s], C::PLANES * kPlaneStage + band_bytes);
                 const int in = (g.state + it.t) & 1;
-                load_tile(g.plane[in][0], g.plane[in][1], C::PLANES, g.pg,
+                load_tile(in ? g.plane[1][0] : g.plane[0][0], in ? g.plane[1][1] : g.plane[0][1],
+                          C::PLANES, g.pg,
                           (it.tile / g.tiles_x) * kTile, (it.tile % g.tiles_x) * kTile, st,
                           &full[s]);
                 bulk_load(st + C::PLANES * kPlaneStage, p.bands + g.band_base, band_bytes, &full[s]);
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     *abort_flag = 1;
                     break;
                 }
-                const BatchGrid &g = p.grids[it.g];
+                const BatchGrid g = p.grids[it.g];  // one batch of loads, before any barrier
                 uint8_t *st = stage_base + (size_t)s * C::STAGE_BYTES;
                 const uint64_t a_hi0 = smem_desc(smem_u32(st), kChunkBytes, 128);
                 const uint32_t band = smem_u32(st + C::PLANES * kPlaneStage);
@@ -427,13 +428,14 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             }
             const BatchItem it = ring[j];
             if (it.g < 0) break;
-            const BatchGrid &g = p.grids[it.g];
+            const BatchGrid g = p.grids[it.g];  // one batch of loads, before any barrier
             const int in = (g.state + it.t) & 1;
             TileOut o;
-            o.in_hi = g.plane[in][0];
-            o.in_lo = g.plane[in][1];
-            o.out_hi = g.plane[in ^ 1][0];
-            o.out_lo = g.plane[in ^ 1][1];
+            // (selects, not a runtime index, keep the descriptor in registers)
+            o.in_hi = in ? g.plane[1][0] : g.plane[0][0];
+            o.in_lo = in ? g.plane[1][1] : g.plane[0][1];
+            o.out_hi = in ? g.plane[0][0] : g.plane[1][0];
+            o.out_lo = in ? g.plane[0][1] : g.plane[1][1];
             o.pg = g.pg;
             o.y0 = g.y0; o.y1 = g.y1; o.x0 = g.x0; o.x1 = g.x1;
             const int Y0 = (it.tile / g.tiles_x) * kTile;
