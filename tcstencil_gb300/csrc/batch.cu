@@ -41,6 +41,7 @@ namespace tcs {
 namespace {
 
 using namespace tc;
+using SG = StageLines;  // line-aligned staging, as the single-grid kernels
 
 __device__ int g_batch_error = 0;
 
@@ -57,7 +58,7 @@ struct BatchCfg {
     static constexpr int STAGES = SPLIT ? 2 : 3;
     static constexpr int PLANES = SPLIT ? 2 : 1;
     static constexpr int BAND_BYTES = (SPLIT ? 4 : 1) * 5 * kBandBytes;  // radius 2
-    static constexpr int STAGE_BYTES = PLANES * kPlaneStage + BAND_BYTES;
+    static constexpr int STAGE_BYTES = PLANES * SG::PLANE + BAND_BYTES;
     static constexpr int GROUPS = SPLIT ? 3 : 2;
     static constexpr int EPI_WARPS = 4 * GROUPS;
     // MMA issuer warps 1 .. ISSUERS: split items alternate windows between two
@@ -203,10 +204,13 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
 
     if (warp == 0) {
         // ------------------------------------------------------ producer ---
-        // Takes work indices in increasing order from the global counter (the
-        // next one is requested while the current one is loaded, to hide the
-        // atomic's latency), decodes each once and publishes it in ring slot
-        // i % kRing; an index past the end is published as the stop sentinel.
+        // Takes work indices in increasing order from the global counter,
+        // decodes each once and publishes it in ring slot i % kRing; an index
+        // past the end is published as the stop sentinel.  Software
+        // pipelined: once an item's copies are issued, the next item (whose
+        // index was requested an item earlier) is decoded and its grid
+        // descriptor loaded, and the index after it is requested, so those
+        // latencies overlap the stage and ring waits of the next iteration.
         if (lane == 0) {
             const int *step_off = tables_in_smem ? tables : p.step_off;
             const int *tile_prefix = tables_in_smem ? tables + p.n_steps + 1 : p.tile_prefix;
@@ -214,11 +218,17 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             // (grid, step) whose dependency this thread has already seen met;
             // later items of the same pair need no further poll or fence
             int met_g = -1, met_t = -1;
-            int k_next = (int)atomicAdd(p.work_counter, 1u);
+            int k = (int)atomicAdd(p.work_counter, 1u);  // the item of this iteration
+            int k_next = k;                               // the index after it
+            BatchItem it{};
+            BatchGrid g{};
+            if (k < p.n_items) {
+                it = decode_item(step_off, tile_prefix, p.n_steps, p.n_grids, k);
+                g = p.grids[it.g];
+                k_next = (int)atomicAdd(p.work_counter, 1u);
+            }
             for (int i = 0;; i++) {
                 const int s = i % NS, j = i % kRing;
-                const int k = k_next;
-                if (k < p.n_items) k_next = (int)atomicAdd(p.work_counter, 1u);
                 if (!mbar_wait(&empty[s], ((i / NS) & 1) ^ 1, abort_flag, wait_lim) ||
                     !mbar_wait(&ring_free[j], ((i / kRing) & 1) ^ 1, abort_flag, wait_lim)) {
                     batch_fail(p, kErrWaitEmpty);
@@ -230,10 +240,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     mbar_arrive(&item_ready[j]);
                     break;
                 }
-                const BatchItem it = decode_item(step_off, tile_prefix, p.n_steps, p.n_grids, k);
                 ring[j] = it;
                 mbar_arrive(&item_ready[j]);
-                const BatchGrid g = p.grids[it.g];  // one batch of loads, before any barrier
                 // step t > 0: every tile of the grid's previous step is stored;
                 // step 0 of a gated grid: the external gate is open
                 const unsigned *ctr = nullptr;
@@ -271,14 +279,21 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 }
                 const int band_bytes = batch_band_elems(g.r, SPLIT) * 2;
                 uint8_t *st = stage_base + (size_t)s * C::STAGE_BYTES;
-                mbar_arrive_expect_tx(&full[s], C::PLANES * kPlaneStage + band_bytes);
+                mbar_arrive_expect_tx(&full[s], C::PLANES * SG::PLANE + band_bytes);
                 const int in = (g.state + it.t) & 1;
-                load_tile(in ? g.plane[1][0] : g.plane[0][0], in ? g.plane[1][1] : g.plane[0][1],
+                load_tile<SG>(in ? g.plane[1][0] : g.plane[0][0], in ? g.plane[1][1] : g.plane[0][1],
                           C::PLANES, g.pg,
                           (it.tile / g.tiles_x) * kTile, (it.tile % g.tiles_x) * kTile, st,
                           &full[s]);
-                bulk_load(st + C::PLANES * kPlaneStage, p.bands + g.band_base, band_bytes, &full[s]);
+                bulk_load(st + C::PLANES * SG::PLANE, p.bands + g.band_base, band_bytes, &full[s]);
                 last_issued = i;
+                // the next item: decoded, its descriptor loads in flight
+                k = k_next;
+                if (k < p.n_items) {
+                    it = decode_item(step_off, tile_prefix, p.n_steps, p.n_grids, k);
+                    g = p.grids[it.g];
+                    k_next = (int)atomicAdd(p.work_counter, 1u);
+                }
             }
             for (int k = 0; k < NS && last_issued - k >= 0; k++) {
                 const int ii = last_issued - k;
@@ -314,8 +329,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 }
                 const BatchGrid g = p.grids[it.g];  // one batch of loads, before any barrier
                 uint8_t *st = stage_base + (size_t)s * C::STAGE_BYTES;
-                const uint64_t a_hi0 = smem_desc(smem_u32(st), kChunkBytes, 128);
-                const uint32_t band = smem_u32(st + C::PLANES * kPlaneStage);
+                const uint64_t a_hi0 = smem_desc(smem_u32(st), SG::CHUNK, 128);
+                const uint32_t band = smem_u32(st + C::PLANES * SG::PLANE);
                 if constexpr (SPLIT) {
 #pragma unroll 1
                     for (int w = 0; w < kBatchWindows; w++, G++) {
@@ -329,8 +344,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                         }
                         tc_fence_after();
                         const uint32_t d = tmem_base + r * kBatchRegion;
-                        if (g.r == 1) issue_split_window<1>(a_hi0, band, d, w);
-                        else issue_split_window<2>(a_hi0, band, d, w);
+                        if (g.r == 1) issue_split_window<1, SG>(a_hi0, band, d, w);
+                        else issue_split_window<2, SG>(a_hi0, band, d, w);
                         umma_commit(&acc_full[r]);
                     }
                 } else {
@@ -343,8 +358,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     } else {
                         tc_fence_after();
                         const uint32_t d = tmem_base + col;
-                        if (g.r == 1) issue_subtile<1, false>(a_hi0, band, d, 0);
-                        else issue_subtile<2, false>(a_hi0, band, d, 0);
+                        if (g.r == 1) issue_subtile<1, false, SG>(a_hi0, band, d, 0);
+                        else issue_subtile<2, false, SG>(a_hi0, band, d, 0);
                         slots.commit(acc_full, mask);
                         slots.used(mask);
                     }

@@ -273,6 +273,46 @@ inline PackShape pack_shape(int ny, int nx, int pad, int cpp) {
 
 }  // namespace
 
+namespace {
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// The driver's cuTensorMapEncodeTiled, found through the runtime (no link
+// against the driver library).
+EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+}  // namespace
+
+cudaError_t encode_panel_map(const uint16_t *plane, const PlaneGeom &pg, CUtensorMap *map) {
+    const EncodeTiledFn enc = encode_tiled();
+    if (!enc) return cudaErrorNotSupported;
+    if (reinterpret_cast<uintptr_t>(plane) % 16 || pg.nyp % 8 || pg.cpp != 8)
+        return cudaErrorInvalidValue;
+    const cuuint64_t dims[3] = {16, (cuuint64_t)pg.nyp / 8, (cuuint64_t)pg.npan};
+    const cuuint64_t strides[2] = {128, (cuuint64_t)pg.nyp * 16};  // bytes, dims 1 and 2
+    const cuuint32_t box[3] = {16, (kTile + 8) / 8, kTile / 8 + 2};
+    const cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<uint16_t *>(plane),
+                           dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 cudaError_t launch_pack_f16(const float *in, int ny, int nx, int pad, float pad_value,
                             uint16_t *plane, cudaStream_t s) {
     const PackShape ps = pack_shape(ny, nx, pad, 8);

@@ -53,6 +53,7 @@ namespace tcs {
 namespace {
 
 using namespace tc;
+using SG = StageLines;  // line-aligned staging of the sweep kernels
 
 __device__ int g_tc_error = 0;
 
@@ -71,12 +72,13 @@ struct Cfg {
     static constexpr bool BOX = stencil_box(S);
     static constexpr int NDY = 2 * R + 1;
     static constexpr int STAGES = SPLIT ? 2 : TCS_PLAIN_STAGES;
-    static constexpr size_t SMEM = 1024 + (size_t)STAGES * M::PLANES * kPlaneStage +
+    static constexpr size_t SMEM = 1024 + (size_t)STAGES * M::PLANES * SG::PLANE +
                                    (size_t)M::BAND_PLANES * NDY * kBandBytes + 256;
     static_assert(SMEM <= 232448, "shared memory budget");
 };
 
 struct TcParams {
+    CUtensorMap map_hi, map_lo;     // input planes (encode_panel_map)
     GridGeom g;
     int tiles_x, n_tiles;
     const uint16_t *in_hi, *in_lo;  // input planes
@@ -85,7 +87,7 @@ struct TcParams {
 };
 
 template <int S, bool SPLIT>
-__global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p) {
+__global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const __grid_constant__ TcParams p) {
     using C = Cfg<S, SPLIT>;
     using M = Mode<SPLIT>;
     constexpr int NS = C::STAGES;
@@ -96,7 +98,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                 ~static_cast<uintptr_t>(1023));
     uint8_t *stage_base = smem;                                    // [NS][NP][stage]
-    uint8_t *band_base = smem + (size_t)NS * NP * kPlaneStage;     // [BAND_PLANES][NDY]
+    uint8_t *band_base = smem + (size_t)NS * NP * SG::PLANE;     // [BAND_PLANES][NDY]
     uint64_t *bars =
         reinterpret_cast<uint64_t *>(band_base + M::BAND_PLANES * C::NDY * kBandBytes);
     uint64_t *full = bars;                    // [NS]
@@ -154,9 +156,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
                     *abort_flag = 1;
                     break;
                 }
-                mbar_arrive_expect_tx(&full[s], NP * kPlaneStage);
-                load_tile(p.in_hi, p.in_lo, NP, pg, (t / tiles_x) * kTile, (t % tiles_x) * kTile,
-                          stage_base + (size_t)s * NP * kPlaneStage, &full[s]);
+                mbar_arrive_expect_tx(&full[s], NP * SG::PLANE);
+                load_tile_map(&p.map_hi, &p.map_lo, NP, (t / tiles_x) * kTile,
+                              (t % tiles_x) * kTile, stage_base + (size_t)s * NP * SG::PLANE,
+                              &full[s]);
                 last_issued = i;
             }
             // Drain: every stage armed last must have landed before exit.
@@ -187,7 +190,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
                     break;
                 }
                 const uint64_t a_hi0 = smem_desc(
-                    smem_u32(stage_base + (size_t)s * NP * kPlaneStage), kChunkBytes, 128);
+                    smem_u32(stage_base + (size_t)s * NP * SG::PLANE), SG::CHUNK, 128);
 #pragma unroll
                 for (int h = 0; h < NSUB; h++) {
                     uint32_t col;
@@ -199,7 +202,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const TcParams p)
                         break;
                     }
                     tc_fence_after();
-                    issue_subtile<C::R, SPLIT>(a_hi0, band, tmem_base + col, h);
+                    issue_subtile<C::R, SPLIT, SG>(a_hi0, band, tmem_base + col, h);
                     slots.commit(acc_full, mask);
                     slots.used(mask);
                     issued_any = true;
@@ -302,7 +305,7 @@ constexpr int kTileWindows = kTile / 16 + 1;
 static_assert(kRingSlots * kRegionCols <= kTmemCols, "window ring fits TMEM");
 
 template <int S>
-__global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const TcParams p) {
+__global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __grid_constant__ TcParams p) {
     using C = Cfg<S, true>;
     using M = Mode<true>;
     constexpr int NS = C::STAGES;
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const Tc
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                 ~static_cast<uintptr_t>(1023));
     uint8_t *stage_base = smem;                                 // [NS][NP][stage]
-    uint8_t *band_base = smem + (size_t)NS * NP * kPlaneStage;  // NDY * 4 KB
+    uint8_t *band_base = smem + (size_t)NS * NP * SG::PLANE;  // NDY * 4 KB
     uint64_t *bars =
         reinterpret_cast<uint64_t *>(band_base + M::BAND_PLANES * C::NDY * kBandBytes);
     uint64_t *full = bars;                                    // [NS]
@@ -369,9 +372,10 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const Tc
                     *abort_flag = 1;
                     break;
                 }
-                mbar_arrive_expect_tx(&full[s], NP * kPlaneStage);
-                load_tile(p.in_hi, p.in_lo, NP, pg, (t / tiles_x) * kTile, (t % tiles_x) * kTile,
-                          stage_base + (size_t)s * NP * kPlaneStage, &full[s]);
+                mbar_arrive_expect_tx(&full[s], NP * SG::PLANE);
+                load_tile_map(&p.map_hi, &p.map_lo, NP, (t / tiles_x) * kTile,
+                              (t % tiles_x) * kTile, stage_base + (size_t)s * NP * SG::PLANE,
+                              &full[s]);
                 last_issued = i;
             }
             for (int k = 0; k < NS && last_issued - k >= 0; k++) {
@@ -400,7 +404,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const Tc
                     break;
                 }
                 const uint64_t a_hi0 = smem_desc(
-                    smem_u32(stage_base + (size_t)s * NP * kPlaneStage), kChunkBytes, 128);
+                    smem_u32(stage_base + (size_t)s * NP * SG::PLANE), SG::CHUNK, 128);
 #pragma unroll 1
                 for (int wg = 0; wg < kTileWindows; wg++, G++) {
                     if ((G & 1) != id) continue;
@@ -412,7 +416,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const Tc
                         break;
                     }
                     tc_fence_after();
-                    issue_split_window<C::R>(a_hi0, band, tmem_base + r * kRegionCols, wg);
+                    issue_split_window<C::R, SG>(a_hi0, band, tmem_base + r * kRegionCols, wg);
                     umma_commit(&win_full[r]);
                 }
                 if (!stop) umma_commit(&empty[s]);
@@ -533,6 +537,9 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     p.n_tiles = tiles_y * p.tiles_x;
     p.in_hi = in_hi;
     p.in_lo = in_lo;
+    cudaError_t me = encode_panel_map(in_hi, g.p16, &p.map_hi);
+    if (me == cudaSuccess) me = encode_panel_map(SPLIT ? in_lo : in_hi, g.p16, &p.map_lo);
+    if (me != cudaSuccess) return me;
     p.out_hi = out_hi;
     p.out_lo = out_lo;
     for (int k = 0; k < 25; k++) p.coef[k] = 0.0f;

@@ -14,6 +14,21 @@ constexpr int kRowsStaged = kTile + 4;          // two halo rows above and below
 constexpr int kChunkBytes = kRowsStaged * 16;   // one panel of a stage
 constexpr int kSlots = kTile / 8 + 2;           // 16 panels + one each side
 constexpr int kPlaneStage = kSlots * kChunkBytes;
+
+// Staged-panel geometry: CHUNK bytes per panel (rows at a 16-byte stride),
+// TOP rows staged above the tile, PLANE bytes per staged plane.
+template <int CHUNK_, int TOP_>
+struct Staging {
+    static constexpr int CHUNK = CHUNK_;
+    static constexpr int TOP = TOP_;
+    static constexpr int PLANE = kSlots * CHUNK_;
+};
+// 132 rows from Y0 - 2: the two halo rows each side a radius-2 stencil needs.
+using StageHalo2 = Staging<kChunkBytes, 2>;
+// 136 rows from Y0 - 4: every panel run starts on a 128-byte line (tile rows
+// are multiples of 128 and the plane's top padding is 4 rows), so a tile's
+// copies move 17 whole lines per panel instead of 17 partial ones.
+using StageLines = Staging<(kTile + 8) * 16, 4>;
 constexpr int kBandElems = 32 * 16;             // one 16(K) x 32(N) FP16 band
 constexpr int kBandBytes = kBandElems * 2;
 constexpr int kEpiWarps = 8;                    // two warpgroups, one per column half
@@ -205,17 +220,29 @@ __device__ __forceinline__ void build_bands(uint16_t *band, const float *coef, i
 
 // Producer: bulk copies of rows Y0-2 .. Y0+129 of panels X0/8 - 1 .. X0/8 + 16
 // of each input plane into a stage (plane pl at stage + pl*kPlaneStage).
+template <class SG = StageHalo2>
 __device__ __forceinline__ void load_tile(const uint16_t *hi, const uint16_t *lo, int planes,
                                           const PlaneGeom &pg, int Y0, int X0, uint8_t *stage,
                                           uint64_t *bar) {
-    const size_t src0 = plane_index(pg, Y0 - 2, X0 - 8);
+    const size_t src0 = plane_index(pg, Y0 - SG::TOP, X0 - 8);
     for (int pl = 0; pl < planes; pl++) {
         const uint16_t *src = (pl ? lo : hi) + src0;
-        uint8_t *st = stage + (size_t)pl * kPlaneStage;
+        uint8_t *st = stage + (size_t)pl * SG::PLANE;
 #pragma unroll 1
         for (int c = 0; c < kSlots; c++)
-            bulk_load(st + c * kChunkBytes, src + (size_t)c * pg.nyp * 8, kChunkBytes, bar);
+            bulk_load(st + c * SG::CHUNK, src + (size_t)c * pg.nyp * 8, SG::CHUNK, bar);
     }
+}
+
+// The same tile in the line-aligned staging with one tensor-map load per
+// plane (maps from encode_panel_map): box origin (word 0, row group Y0 / 8 =
+// row Y0 - 4 + the plane's 4 top padding rows, panel of X0 - 8).
+__device__ __forceinline__ void load_tile_map(const CUtensorMap *hi, const CUtensorMap *lo,
+                                              int planes, int Y0, int X0, uint8_t *stage,
+                                              uint64_t *bar) {
+    static_assert(StageLines::TOP == kPadTop && StageLines::CHUNK == 17 * 128, "map box");
+    tma_load_3d(stage, hi, bar, 0, Y0 / 8, X0 / 8);
+    if (planes > 1) tma_load_3d(stage + StageLines::PLANE, lo, bar, 0, Y0 / 8, X0 / 8);
 }
 
 // One 16-column output block of the split form from the regions of its two
@@ -245,16 +272,16 @@ __device__ __forceinline__ void split_block_load(uint32_t region_a, uint32_t reg
 // region at d: per coefficient row, the stacked hi MMA (which
 // initialises the region on the first row) and the lo MMA into its middle
 // part.
-template <int R>
+template <int R, class SG = StageHalo2>
 __device__ __forceinline__ void issue_split_window_at(uint64_t a_hi0, uint32_t band, uint32_t d,
-                                                      int slot, int lo_bytes = kPlaneStage) {
+                                                      int slot, int lo_bytes = SG::PLANE) {
     constexpr int NDY = 2 * R + 1;
     const uint64_t a_lo0 = a_hi0 + (uint64_t)(lo_bytes >> 4);
     const uint64_t bs0 = smem_desc(band, 1536, 128);
     const uint64_t bf0 = smem_desc(band + NDY * 3072, 512, 128);
 #pragma unroll
     for (int dy = 0; dy < NDY; dy++) {
-        const uint64_t a_off = (uint64_t)((slot * kChunkBytes + (2 - R + dy) * 16) >> 4);
+        const uint64_t a_off = (uint64_t)((slot * SG::CHUNK + (SG::TOP - R + dy) * 16) >> 4);
         umma_f16(d, a_hi0 + a_off, bs0 + (uint64_t)((dy * 3072) >> 4), kIdescStack,
                  dy > 0 ? 1u : 0u);
         umma_f16(d + 32, a_lo0 + a_off, bf0 + (uint64_t)((dy * kBandBytes) >> 4), kIdesc, 1u);
@@ -262,10 +289,10 @@ __device__ __forceinline__ void issue_split_window_at(uint64_t a_hi0, uint32_t b
 }
 
 // The same for window wg of a staged tile (its panels 2wg, 2wg+1).
-template <int R>
+template <int R, class SG = StageHalo2>
 __device__ __forceinline__ void issue_split_window(uint64_t a_hi0, uint32_t band, uint32_t d,
                                                    int wg) {
-    issue_split_window_at<R>(a_hi0, band, d, 2 * wg);
+    issue_split_window_at<R, SG>(a_hi0, band, d, 2 * wg);
 }
 
 // MMAs of sub-tile h of a staged tile into accumulator columns from d.
@@ -278,7 +305,7 @@ __device__ __forceinline__ void issue_split_window(uint64_t a_hi0, uint32_t band
 //  split: per window and coefficient row, one N=96 MMA of hi with the stacked
 //    band (initialising its region on the first row) and one N=32 MMA of lo
 //    with cf into the region's middle part.
-template <int R, bool SPLIT>
+template <int R, bool SPLIT, class SG = StageHalo2>
 __device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint32_t band, uint32_t d, int h) {
     using M = Mode<SPLIT>;
     constexpr int NDY = 2 * R + 1;
@@ -293,7 +320,7 @@ __device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint32_t band, uin
 #pragma unroll
                 for (int w = parity; w < M::SUB_WIN; w += 2) {
                     const int wg = h * M::SUB_BLOCKS + w;  // window in the tile
-                    const uint64_t a_off = (uint64_t)((2 * wg * kChunkBytes + (2 - R + dy) * 16) >> 4);
+                    const uint64_t a_off = (uint64_t)((2 * wg * SG::CHUNK + (SG::TOP - R + dy) * 16) >> 4);
                     umma_f16(d + 16 * w, a_hi0 + a_off, b, kIdesc, acc);
                 }
             }
@@ -301,7 +328,7 @@ __device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint32_t band, uin
     } else {
 #pragma unroll
         for (int w = 0; w < M::SUB_WIN; w++)
-            issue_split_window<R>(a_hi0, band, d + split_region(w), h * M::SUB_BLOCKS + w);
+            issue_split_window<R, SG>(a_hi0, band, d + split_region(w), h * M::SUB_BLOCKS + w);
     }
 }
 

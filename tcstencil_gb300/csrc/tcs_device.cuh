@@ -103,6 +103,17 @@ __device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, u
         : "memory");
 }
 
+// 3-D tiled load into shared memory, completion counted on `bar` in bytes.
+// The innermost coordinate c0 is always 0 here (16-byte aligned).
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int c0, int c1, int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // 1-D bulk copy of `bytes` (a multiple of 16) from global to shared memory,
 // both addresses 16-byte aligned; completion counted on `bar` in bytes.
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes,

@@ -87,6 +87,14 @@ struct GridGeom {
     PlaneGeom p32;  // FP32 planes
 };
 
+// Tensor map of an FP16 (or split hi/lo) panel plane for the tensor-core
+// sweeps, in whole 128-byte lines: elements are 8-byte words, dimensions
+// (16 words = 8 rows of a panel, nyp / 8 row groups, npan panels), box
+// (16, 17, 18) = the 136 rows from Y0 - 4 of the 18 panels a 128 x 128 tile
+// reads, landing in shared memory as 18 row-contiguous 2176-byte runs (one
+// load instruction per plane and tile instead of 18 bulk copies).
+cudaError_t encode_panel_map(const uint16_t *plane, const PlaneGeom &pg, CUtensorMap *map);
+
 // Sets the thread's last-error message and returns `status`.
 int fail(int status, const char *fmt, ...);
 // Maps a CUDA runtime error to TCS_ERR_CUDA with a message (TCS_OK if none).
