@@ -281,10 +281,9 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 uint8_t *st = stage_base + (size_t)s * C::STAGE_BYTES;
                 mbar_arrive_expect_tx(&full[s], C::PLANES * SG::PLANE + band_bytes);
                 const int in = (g.state + it.t) & 1;
-                load_tile<SG>(in ? g.plane[1][0] : g.plane[0][0], in ? g.plane[1][1] : g.plane[0][1],
-                          C::PLANES, g.pg,
-                          (it.tile / g.tiles_x) * kTile, (it.tile % g.tiles_x) * kTile, st,
-                          &full[s]);
+                const CUtensorMap *maps = g.maps + 2 * in;
+                load_tile_map(maps, maps + 1, C::PLANES, (it.tile / g.tiles_x) * kTile,
+                              (it.tile % g.tiles_x) * kTile, st, &full[s]);
                 bulk_load(st + C::PLANES * SG::PLANE, p.bands + g.band_base, band_bytes, &full[s]);
                 last_issued = i;
                 // the next item: decoded, its descriptor loads in flight
@@ -293,6 +292,9 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     it = decode_item(step_off, tile_prefix, p.n_steps, p.n_grids, k);
                     g = p.grids[it.g];
                     k_next = (int)atomicAdd(p.work_counter, 1u);
+                    const CUtensorMap *maps = g.maps + 2 * ((g.state + it.t) & 1);
+                    tma_prefetch_map(maps);
+                    if (SPLIT) tma_prefetch_map(maps + 1);
                 }
             }
             for (int k = 0; k < NS && last_issued - k >= 0; k++) {
@@ -605,6 +607,7 @@ struct tcs_batch_s {
     // all grids, FP16 ones first then split ones, each part sorted by steps
     // (descending); one launch per part
     BatchGrid *d_grids = nullptr;
+    CUtensorMap *d_maps = nullptr;  // [grid][state][hi, lo]
     int n_grids = 0;
     struct Part {
         int first = 0, n_grids = 0;
@@ -626,7 +629,7 @@ struct tcs_batch_s {
     ~tcs_batch_s() {
         if (graph) cudaGraphExecDestroy(graph);
         if (capture_stream) cudaStreamDestroy(capture_stream);
-        for (void *p : {(void *)pool, (void *)d_grids, (void *)part[0].d_layout,
+        for (void *p : {(void *)pool, (void *)d_grids, (void *)d_maps, (void *)part[0].d_layout,
                         (void *)part[0].d_counters, (void *)part[1].d_layout,
                         (void *)part[1].d_counters, (void *)d_bands, (void *)d_coefs,
                         (void *)d_staging, (void *)d_max})
@@ -722,6 +725,15 @@ int batch_build(tcs_batch b) {
         if (!st) st = cuda_status(cudaMemcpy(P.d_layout, layout.data(), layout.size() * sizeof(int), cudaMemcpyHostToDevice), "layout copy");
         if (st) return st;
     }
+    // tensor maps of every grid's planes, then the descriptors that point at them
+    std::vector<CUtensorMap> maps(4 * grids.size());
+    st = cuda_status(cudaMalloc(&b->d_maps, maps.size() * sizeof(CUtensorMap)), "cudaMalloc(maps)");
+    for (size_t i = 0; i < grids.size() && !st; i++) {
+        st = cuda_status(encode_grid_maps(grids[i], &maps[4 * i]), "tensor map encode");
+        grids[i].maps = b->d_maps + 4 * i;
+    }
+    if (!st) st = cuda_status(cudaMemcpy(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "maps copy");
+    if (st) return st;
     st = cuda_status(cudaMalloc(&b->d_grids, grids.size() * sizeof(BatchGrid)), "cudaMalloc(grids)");
     if (!st) st = cuda_status(cudaMalloc(&b->d_bands, std::max(band, 1) * sizeof(uint16_t)), "cudaMalloc(bands)");
     if (!st) st = cuda_status(cudaMalloc(&b->d_coefs, coefs.size() * sizeof(float)), "cudaMalloc(coefs)");

@@ -23,7 +23,21 @@ struct BatchGrid {
     // external gate: step 0 starts once *gate >= gate_value (null: no gate)
     const unsigned *gate;
     unsigned gate_value;
+    // tensor maps of the planes in device memory, [state][hi, lo] (lo = hi for
+    // FP16 grids), from encode_grid_maps
+    const CUtensorMap *maps;
 };
+
+// Encodes the four tensor maps of a grid's planes ([state][hi, lo]).
+inline cudaError_t encode_grid_maps(const BatchGrid &g, CUtensorMap out[4]) {
+    for (int s = 0; s < 2; s++)
+        for (int pl = 0; pl < 2; pl++) {
+            const uint16_t *plane = (pl && g.plane[s][1]) ? g.plane[s][1] : g.plane[s][0];
+            const cudaError_t e = encode_panel_map(plane, g.pg, &out[2 * s + pl]);
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
 
 struct BatchItem {
     int g, t, tile;  // grid, step within the run, tile

@@ -141,6 +141,9 @@ struct tcs_server_s {
     // (each behind its round's end); compute: rounds
     cudaStream_t compute = nullptr, upload = nullptr, download = nullptr;
     uint16_t *d_bands = nullptr;
+    CUtensorMap *d_maps = nullptr;  // per slot: tensor maps of the request's planes
+    CUtensorMap *h_maps = nullptr;  // pinned staging of d_maps (a slot's entry is
+                                    // rewritten only after its request retired)
     unsigned *d_maxbits = nullptr;
     int *d_exp = nullptr;
     int *d_err = nullptr;       // sticky: the first failed wait of any round
@@ -387,6 +390,17 @@ void tcs_server_s::admit() {
             st = cuda_status(launch_pack_f16(stg, q->g.ny, q->g.nx, 0, 0.0f, plane(q, 0, 0), upload), "pack launch");
         }
         if (!st) st = cuda_status(launch_build_bands(q->coeffs, q->r, q->box, q->split, d_bands + (size_t)q->slot * kBatchMaxBandElems, upload), "band build");
+        if (!st) {
+            BatchGrid G{};
+            for (int s = 0; s < 2; s++) {
+                G.plane[s][0] = plane(q, s, 0);
+                G.plane[s][1] = q->split ? plane(q, s, 1) : nullptr;
+            }
+            G.pg = q->g.p16;
+            CUtensorMap *hm = h_maps + 4 * (size_t)q->slot;
+            st = cuda_status(encode_grid_maps(G, hm), "tensor map encode");
+            if (!st) st = cuda_status(cudaMemcpyAsync(d_maps + 4 * (size_t)q->slot, hm, 4 * sizeof(CUtensorMap), cudaMemcpyHostToDevice, upload), "tensor map upload");
+        }
         if (!st) st = cuda_status(cudaEventRecord(q->ready, upload), "cudaEventRecord");
         if (st) {
             fail_request(q, st);
@@ -503,6 +517,7 @@ bool tcs_server_s::launch_round() {
         G.state = q->done_steps & 1;
         G.gate = nullptr;
         G.gate_value = 0;
+        G.maps = d_maps + 4 * (size_t)q->slot;
         ctr += run_steps[i];
     }
 
@@ -621,6 +636,8 @@ int tcs_server_create(const tcs_server_config *config, tcs_server *out) {
     s->alloc.reset(s->cfg.hbm_budget_bytes);
     const int slots = s->cfg.max_active;
     if (!st) st = cuda_status(cudaMalloc(&s->d_bands, (size_t)slots * kBatchMaxBandElems * sizeof(uint16_t)), "cudaMalloc(bands)");
+    if (!st) st = cuda_status(cudaMalloc(&s->d_maps, (size_t)slots * 4 * sizeof(CUtensorMap)), "cudaMalloc(maps)");
+    if (!st) st = cuda_status(cudaMallocHost(&s->h_maps, (size_t)slots * 4 * sizeof(CUtensorMap)), "cudaMallocHost(maps)");
     if (!st) st = cuda_status(cudaMalloc(&s->d_maxbits, slots * sizeof(unsigned)), "cudaMalloc(max)");
     if (!st) st = cuda_status(cudaMalloc(&s->d_exp, slots * sizeof(int)), "cudaMalloc(exp)");
     if (!st) st = cuda_status(cudaMalloc(&s->d_err, sizeof(int)), "cudaMalloc(error)");
@@ -687,10 +704,11 @@ int tcs_server_destroy(tcs_server s) {
     for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
     for (void *p : s->retired.host) cudaFreeHost(p);
     for (void *p : s->retired.dev) cudaFree(p);
-    for (void *p : {(void *)s->pool, (void *)s->d_bands, (void *)s->d_maxbits, (void *)s->d_exp,
-                    (void *)s->d_err})
+    for (void *p : {(void *)s->pool, (void *)s->d_bands, (void *)s->d_maps, (void *)s->d_maxbits,
+                    (void *)s->d_exp, (void *)s->d_err})
         if (p) cudaFree(p);
     if (s->h_slot_err) cudaFreeHost(s->h_slot_err);
+    if (s->h_maps) cudaFreeHost(s->h_maps);
     if (s->compute) cudaStreamDestroy(s->compute);
     if (s->upload) cudaStreamDestroy(s->upload);
     if (s->download) cudaStreamDestroy(s->download);
