@@ -117,6 +117,19 @@ __device__ __forceinline__ BatchItem decode_item(const int *step_off, const int 
     return BatchItem{a, lo, local - tile_prefix[a]};
 }
 
+// The item after `it` (index k + 1), from two table reads: the next tile of
+// the grid, else the first tile of the next grid still running at this step,
+// else the first tile of the next step.
+__device__ __forceinline__ BatchItem next_item(const BatchItem &it, const int *step_off,
+                                               const int *tile_prefix) {
+    const int local = tile_prefix[it.g] + it.tile + 1;  // within step it.t
+    if (local < step_off[it.t + 1] - step_off[it.t]) {
+        if (local < tile_prefix[it.g + 1]) return BatchItem{it.g, it.t, it.tile + 1};
+        return BatchItem{it.g + 1, it.t, 0};
+    }
+    return BatchItem{0, it.t + 1, 0};
+}
+
 __global__ void build_bands_kernel(BatchGrid *grids, const float *coefs, uint16_t *bands) {
     const BatchGrid &g = grids[blockIdx.x];
     build_bands(bands + g.band_base, coefs + 25 * blockIdx.x, g.r, g.box, g.split, threadIdx.x,
@@ -205,12 +218,12 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
     if (warp == 0) {
         // ------------------------------------------------------ producer ---
         // Takes work indices in increasing order from the global counter,
-        // decodes each once and publishes it in ring slot i % kRing; an index
-        // past the end is published as the stop sentinel.  Software
-        // pipelined: once an item's copies are issued, the next item (whose
-        // index was requested an item earlier) is decoded and its grid
-        // descriptor loaded, and the index after it is requested, so those
-        // latencies overlap the stage and ring waits of the next iteration.
+        // p.grab at a time, decodes each once and publishes it in ring slot
+        // i % kRing; an index past the end is published as the stop sentinel.
+        // Software pipelined: once an item's copies are issued, the next item
+        // is decoded and its grid descriptor loaded (and, at the end of a
+        // group, the group after the next one requested), so those latencies
+        // overlap the stage and ring waits of the next iteration.
         if (lane == 0) {
             const int *step_off = tables_in_smem ? tables : p.step_off;
             const int *tile_prefix = tables_in_smem ? tables + p.n_steps + 1 : p.tile_prefix;
@@ -218,14 +231,16 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             // (grid, step) whose dependency this thread has already seen met;
             // later items of the same pair need no further poll or fence
             int met_g = -1, met_t = -1;
-            int k = (int)atomicAdd(p.work_counter, 1u);  // the item of this iteration
-            int k_next = k;                               // the index after it
+            const int grab = p.grab;
+            int k = (int)atomicAdd(p.work_counter, (unsigned)grab);  // the item of this iteration
+            int k_end = k + grab;                                   // end of its group
+            int k_next = k;                                          // start of the next group
             BatchItem it{};
             BatchGrid g{};
             if (k < p.n_items) {
                 it = decode_item(step_off, tile_prefix, p.n_steps, p.n_grids, k);
                 g = p.grids[it.g];
-                k_next = (int)atomicAdd(p.work_counter, 1u);
+                k_next = (int)atomicAdd(p.work_counter, (unsigned)grab);
             }
             for (int i = 0;; i++) {
                 const int s = i % NS, j = i % kRing;
@@ -287,11 +302,19 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 bulk_load(st + C::PLANES * SG::PLANE, p.bands + g.band_base, band_bytes, &full[s]);
                 last_issued = i;
                 // the next item: decoded, its descriptor loads in flight
-                k = k_next;
+                const int g_prev = it.g;
+                if (++k == k_end) {
+                    k = k_next;
+                    k_end = k + grab;
+                    if (k < p.n_items) {
+                        it = decode_item(step_off, tile_prefix, p.n_steps, p.n_grids, k);
+                        k_next = (int)atomicAdd(p.work_counter, (unsigned)grab);
+                    }
+                } else if (k < p.n_items) {
+                    it = next_item(it, step_off, tile_prefix);
+                }
                 if (k < p.n_items) {
-                    it = decode_item(step_off, tile_prefix, p.n_steps, p.n_grids, k);
-                    g = p.grids[it.g];
-                    k_next = (int)atomicAdd(p.work_counter, 1u);
+                    if (it.g != g_prev) g = p.grids[it.g];
                     const CUtensorMap *maps = g.maps + 2 * ((g.state + it.t) & 1);
                     tma_prefetch_map(maps);
                     if (SPLIT) tma_prefetch_map(maps + 1);
@@ -768,6 +791,7 @@ int batch_enqueue(tcs_batch b, cudaStream_t s) {
         p.error = reinterpret_cast<int *>(P.d_counters + P.n_counters + 1);
         p.bands = b->d_bands;
         p.wait_ns = b->wait_ns;
+        p.grab = batch_grab(k == 1);
         st = cuda_status(launch_batch(p, k == 1, g_sms, s), "batch kernel launch");
         if (st) return st;
     }

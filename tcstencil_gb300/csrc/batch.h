@@ -58,7 +58,18 @@ struct BatchParams {
     int *error;              // first failed wait of this launch (0 = none)
     const uint16_t *bands;
     unsigned long long wait_ns;  // limit of the dependency and gate waits
+    int grab;                    // work indices taken per atomic (batch_grab)
 };
+
+// Work indices a CTA takes per atomic: consecutive items mostly share a grid
+// (one dependency poll, incremental decode), but a small grid's tiles then
+// run on fewer SMs one after another, lengthening its step-to-step chain.
+// Measured on GB300 with 512 mixed grids: 4 for FP16 items, BATCH_GRAB_SPLIT
+// for the longer split items.
+#ifndef BATCH_GRAB_SPLIT
+#define BATCH_GRAB_SPLIT 1
+#endif
+constexpr int batch_grab(bool split) { return split ? BATCH_GRAB_SPLIT : 4; }
 
 // Default limit of a batched run's dependency and gate waits: one second.
 constexpr unsigned long long kBatchWaitNs = 1000000000ull;

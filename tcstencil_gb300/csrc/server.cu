@@ -546,6 +546,7 @@ bool tcs_server_s::launch_round() {
         p.error = d_err;
         p.bands = d_bands;
         p.wait_ns = kBatchWaitNs;
+        p.grab = batch_grab(k == 1);
         st = cuda_status(launch_batch(p, k == 1, sms, compute), "batch launch");
     }
     if (!st) st = cuda_status(cudaEventRecord(b.end, compute), "cudaEventRecord");

@@ -400,57 +400,70 @@ __device__ __forceinline__ bool walk_windows(int g, int ng, int nwin, Ready &&re
 // Converts and stores one 16-column output block of tile row y (cells xb ..
 // xb+15).  fast: the whole tile is inside the update rectangle; otherwise
 // cells outside it copy the input.
+//  split: fast blocks take the paired split (split_pair), others split each
+//    updated cell alone (split_fixed: the same bits) and copy the rest.
+//  plain: every cell is converted in pairs (pack_h2, the same bits as h_bits
+//    per cell); where a thread's 16 cells are not all inside, the input
+//    words are blended back in under a per-cell mask.
+// (Measured on GB300: the blend is faster for plain blocks, the separate
+// per-cell path faster for split ones, whose epilogue is sensitive to code
+// size.)
 template <bool SPLIT>
 __device__ __forceinline__ void store_block(const TileOut &o, const float (&f)[16], int y, int xb,
                                             bool fast, bool row_in) {
     const size_t off0 = plane_index(o.pg, y, xb);     // cells xb .. xb+7
     const size_t off1 = off0 + (size_t)o.pg.nyp * 8;  // cells xb+8 .. xb+15
     uint32_t hw[8], lw[8];
-    if (fast) {
+    if constexpr (SPLIT) {
+        if (fast) {
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-            if (SPLIT) {
-                split_pair(f[2 * c], f[2 * c + 1], hw[c], lw[c]);
-            } else {
-                hw[c] = pack_h2(f[2 * c], f[2 * c + 1]);
-                lw[c] = 0;
-            }
-        }
-    } else {
-        const uint4 i0 = *reinterpret_cast<const uint4 *>(o.in_hi + off0);
-        const uint4 i1 = *reinterpret_cast<const uint4 *>(o.in_hi + off1);
-        const uint32_t iw[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
-        uint32_t il[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (SPLIT) {
+            for (int c = 0; c < 8; c++) split_pair(f[2 * c], f[2 * c + 1], hw[c], lw[c]);
+        } else {
+            const uint4 i0 = *reinterpret_cast<const uint4 *>(o.in_hi + off0);
+            const uint4 i1 = *reinterpret_cast<const uint4 *>(o.in_hi + off1);
             const uint4 l0 = *reinterpret_cast<const uint4 *>(o.in_lo + off0);
             const uint4 l1 = *reinterpret_cast<const uint4 *>(o.in_lo + off1);
-            il[0] = l0.x; il[1] = l0.y; il[2] = l0.z; il[3] = l0.w;
-            il[4] = l1.x; il[5] = l1.y; il[6] = l1.z; il[7] = l1.w;
-        }
+            const uint32_t iw[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
+            const uint32_t il[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-            uint16_t hh[2], ll[2];
+            for (int c = 0; c < 8; c++) {
+                uint16_t hh[2], ll[2];
 #pragma unroll
-            for (int u = 0; u < 2; u++) {
-                const int x = xb + 2 * c + u;
-                const bool upd = row_in && x >= o.x0 && x < o.x1;
-                if (upd) {
-                    if (SPLIT) split_fixed(f[2 * c + u], hh[u], ll[u]);
-                    else { hh[u] = h_bits(f[2 * c + u]); ll[u] = 0; }
-                } else {
-                    hh[u] = (uint16_t)(iw[c] >> (16 * u));
-                    ll[u] = (uint16_t)(il[c] >> (16 * u));
+                for (int u = 0; u < 2; u++) {
+                    const int x = xb + 2 * c + u;
+                    if (row_in && x >= o.x0 && x < o.x1) {
+                        split_fixed(f[2 * c + u], hh[u], ll[u]);
+                    } else {
+                        hh[u] = (uint16_t)(iw[c] >> (16 * u));
+                        ll[u] = (uint16_t)(il[c] >> (16 * u));
+                    }
                 }
+                hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
+                lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
             }
-            hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
-            lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
         }
-    }
-    *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-    *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
-    if (SPLIT) {
+        *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
         *reinterpret_cast<uint4 *>(o.out_lo + off0) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
         *reinterpret_cast<uint4 *>(o.out_lo + off1) = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+    } else {
+        (void)lw;
+#pragma unroll
+        for (int c = 0; c < 8; c++) hw[c] = pack_h2(f[2 * c], f[2 * c + 1]);
+        if (!fast && !(row_in && xb >= o.x0 && xb + 16 <= o.x1)) {
+            const uint4 i0 = *reinterpret_cast<const uint4 *>(o.in_hi + off0);
+            const uint4 i1 = *reinterpret_cast<const uint4 *>(o.in_hi + off1);
+            const uint32_t iw[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                const int x = xb + 2 * c;
+                const uint32_t m = (row_in && x >= o.x0 && x < o.x1 ? 0x0000ffffu : 0u) |
+                                   (row_in && x + 1 >= o.x0 && x + 1 < o.x1 ? 0xffff0000u : 0u);
+                hw[c] = (hw[c] & m) | (iw[c] & ~m);
+            }
+        }
+        *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
     }
 }
 
