@@ -222,6 +222,22 @@ int tcs_sweep_host(const float *h_in, float *h_out, const tcs_problem *problem, 
 /* Frees the calling thread's cached plans. */
 void tcs_release_cache(void);
 
+/* ------------------------------------------------------------------ pipes
+ * Many grids of one shape streamed through the device: each submission
+ * copies a host FP32 grid in, runs `steps` steps and copies the result out,
+ * double-buffered over two plans and two streams, so one grid's transfers
+ * and packing overlap the other's sweeps.  Host buffers should be pinned
+ * (cudaHostAlloc / torch pin_memory) for the copies to overlap.  Submission
+ * k's h_in and h_out belong to the pipe until submission k + 2 has been
+ * submitted or tcs_pipe_wait has returned; every result is the same bits as
+ * tcs_sweep_host's for that grid. */
+typedef struct tcs_pipe_s *tcs_pipe;
+int tcs_pipe_create(const tcs_problem *problem, tcs_pipe *out);
+int tcs_pipe_destroy(tcs_pipe pipe);
+int tcs_pipe_submit(tcs_pipe pipe, const float *h_in, float *h_out, int steps);
+/* Waits for every submission; reports a device wait timeout as tcs_device_error. */
+int tcs_pipe_wait(tcs_pipe pipe);
+
 /* ---------------------------------------------------------------- batches
  * A batch advances many independent grids (any mix of sizes, stencils,
  * coefficients, FP16 or split precision, and step counts) with ONE persistent

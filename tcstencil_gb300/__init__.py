@@ -124,6 +124,10 @@ SIGNATURES = {
     "tcs_batch_info": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I),
                             ctypes.POINTER(_I)]),
     "tcs_batch_set_gate": (_I, [_P, _I, _P, ctypes.c_uint]),
+    "tcs_pipe_create": (_I, [ctypes.POINTER(Problem), ctypes.POINTER(_P)]),
+    "tcs_pipe_destroy": (_I, [_P]),
+    "tcs_pipe_submit": (_I, [_P, _P, _P, _I]),
+    "tcs_pipe_wait": (_I, [_P]),
     "tcs_batch_set_wait_limit": (_I, [_P, ctypes.c_double]),
     "tcs_drift_create": (_I, [ctypes.POINTER(Problem), ctypes.POINTER(_P)]),
     "tcs_drift_destroy": (_I, [_P]),
@@ -408,6 +412,46 @@ class Batch:
         pu, it, g = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
         _check(lib().tcs_batch_info(self._h, ctypes.byref(pu), ctypes.byref(it), ctypes.byref(g)))
         return pu.value, it.value, g.value
+
+
+class Pipe:
+    """Many grids of one shape through the device, double-buffered
+    (tcs_pipe_*): submit(h_in, h_out, steps) returns at once; submission k's
+    buffers are the pipe's until submission k + 2 or wait().  Pinned host
+    buffers let the copies overlap the sweeps."""
+
+    def __init__(self, ny: int, nx: int, stencil: str, coeffs, engine: str = "tensor",
+                 precision: str = "f16", rect=None):
+        self._c = _coeffs(coeffs, stencil)
+        y0, y1, x0, x1 = _rect(rect)
+        pr = Problem(ny, nx, STENCILS[stencil], ENGINES[engine], PRECISIONS[precision], y0, y1, x0,
+                     x1, self._c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        h = ctypes.c_void_p()
+        _check(lib().tcs_pipe_create(ctypes.byref(pr), ctypes.byref(h)))
+        self._h = h
+        self.shape = (ny, nx)
+        self._held = []
+
+    def submit(self, h_in: np.ndarray, h_out: np.ndarray, steps: int) -> None:
+        for a in (h_in, h_out):
+            if a.dtype != np.float32 or a.shape != self.shape or not a.flags.c_contiguous:
+                raise ValueError("pipe buffers are C-contiguous float32 grids of the pipe's shape")
+        _check(lib().tcs_pipe_submit(self._h, _ptr(h_in), _ptr(h_out), int(steps)))
+        self._held = (self._held + [(h_in, h_out)])[-2:]
+
+    def wait(self) -> None:
+        _check(lib().tcs_pipe_wait(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().tcs_pipe_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Drift:

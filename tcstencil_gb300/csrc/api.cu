@@ -630,6 +630,110 @@ void tcs_release_cache(void) {
     t_cache.plans.clear();
 }
 
+}  // extern "C"
+
+// ================================================================= pipes ==
+// Submission k runs on plan and stream k % 2; before a slot is reused its
+// previous submission is waited for on the host.  Split grids keep the scale
+// exponent in device memory (maximum, exponent and packing on the stream), so
+// no submission blocks the host; the exponent is the one tcs_plan_upload
+// computes on the host (the same rule), so results match tcs_sweep_host.
+struct tcs_pipe_s {
+    tcs_plan plan[2] = {nullptr, nullptr};
+    cudaStream_t stream[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    int *d_exp = nullptr;  // [2] split scale exponents
+    long long submitted = 0;
+    ~tcs_pipe_s() {
+        for (int k = 0; k < 2; k++) {
+            if (stream[k]) cudaStreamSynchronize(stream[k]);
+            if (done[k]) cudaEventDestroy(done[k]);
+            if (stream[k]) cudaStreamDestroy(stream[k]);
+            if (plan[k]) tcs_plan_destroy(plan[k]);
+        }
+        if (d_exp) cudaFree(d_exp);
+    }
+};
+
+namespace {
+
+int pipe_upload(tcs_plan p, int *d_exp, const float *h_in, cudaStream_t s) {
+    if (p->prob.precision != TCS_PREC_SPLIT) return tcs_plan_upload(p, h_in, 1, s);
+    int st = ensure_staging(p);
+    if (!st && !p->d_max) st = cuda_status(cudaMalloc(&p->d_max, sizeof(unsigned)), "cudaMalloc(max)");
+    if (st) return st;
+    const size_t n = (size_t)p->prob.ny * p->prob.nx;
+    st = cuda_status(cudaMemcpyAsync(p->staging, h_in, n * sizeof(float), cudaMemcpyHostToDevice, s), "upload copy");
+    if (!st) st = cuda_status(cudaMemsetAsync(p->d_max, 0, sizeof(unsigned), s), "memset(max)");
+    if (!st) st = cuda_status(launch_max_abs(p->staging, n, p->d_max, s), "max_abs launch");
+    if (!st) st = cuda_status(launch_pack_split_dev(p->staging, p->prob.ny, p->prob.nx, p->d_max, d_exp,
+                                                    static_cast<uint16_t *>(p->buf[0][0]),
+                                                    static_cast<uint16_t *>(p->buf[0][1]), s),
+                              "pack launch");
+    p->cur = 0;
+    return st;
+}
+
+int pipe_download(tcs_plan p, const int *d_exp, float *h_out, cudaStream_t s) {
+    if (p->prob.precision != TCS_PREC_SPLIT) return tcs_plan_download(p, h_out, 1, s);
+    const int c = p->cur;
+    int st = cuda_status(launch_unpack_split_dev(static_cast<uint16_t *>(p->buf[c][0]),
+                                                 static_cast<uint16_t *>(p->buf[c][1]),
+                                                 p->prob.ny, p->prob.nx, d_exp, p->staging, s),
+                         "unpack launch");
+    if (!st) st = cuda_status(cudaMemcpyAsync(h_out, p->staging, (size_t)p->prob.ny * p->prob.nx * sizeof(float),
+                                              cudaMemcpyDeviceToHost, s), "download copy");
+    return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tcs_pipe_create(const tcs_problem *pr, tcs_pipe *out) {
+    if (!pr || !out) return fail(TCS_ERR_INVALID, "tcs_pipe_create: null argument");
+    *out = nullptr;
+    std::unique_ptr<tcs_pipe_s> q(new tcs_pipe_s());
+    int st = TCS_OK;
+    for (int k = 0; k < 2 && !st; k++) {
+        st = tcs_plan_create(pr, &q->plan[k]);
+        if (!st) st = cuda_status(cudaStreamCreateWithFlags(&q->stream[k], cudaStreamNonBlocking), "cudaStreamCreate");
+        if (!st) st = cuda_status(cudaEventCreateWithFlags(&q->done[k], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    if (!st) st = cuda_status(cudaMalloc(&q->d_exp, 2 * sizeof(int)), "cudaMalloc(exp)");
+    if (st) return st;
+    *out = q.release();
+    return TCS_OK;
+}
+
+int tcs_pipe_destroy(tcs_pipe q) {
+    delete q;
+    return TCS_OK;
+}
+
+int tcs_pipe_submit(tcs_pipe q, const float *h_in, float *h_out, int steps) {
+    if (!q || !h_in || !h_out || steps < 0) return fail(TCS_ERR_INVALID, "tcs_pipe_submit: bad arguments");
+    const int k = (int)(q->submitted & 1);
+    cudaStream_t s = q->stream[k];
+    int st = TCS_OK;
+    if (q->submitted >= 2) st = cuda_status(cudaEventSynchronize(q->done[k]), "cudaEventSynchronize");
+    if (!st) st = pipe_upload(q->plan[k], q->d_exp + k, h_in, s);
+    if (!st) st = tcs_plan_run(q->plan[k], steps, 1, s);
+    if (!st) st = pipe_download(q->plan[k], q->d_exp + k, h_out, s);
+    if (!st) st = cuda_status(cudaEventRecord(q->done[k], s), "cudaEventRecord");
+    if (!st) q->submitted++;
+    return st;
+}
+
+int tcs_pipe_wait(tcs_pipe q) {
+    if (!q) return fail(TCS_ERR_INVALID, "tcs_pipe_wait: null pipe");
+    for (int k = 0; k < 2; k++) {
+        const int st = cuda_status(cudaStreamSynchronize(q->stream[k]), "cudaStreamSynchronize");
+        if (st) return st;
+    }
+    return tcs_device_error(nullptr);
+}
+
 // ============================================================ drop-in ==
 int tcs_host_code(float *h_A, float *h_B, float *h_C, int N, int n, int stencil, int engine,
                   int run_times, int skip_times, int step_times, int tile_size) {

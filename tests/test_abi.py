@@ -157,3 +157,14 @@ def test_server_config_is_validated_before_any_device_work(tcs):
     for cfg in [tcs.ServerConfig(0, 0, 0), tcs.ServerConfig(1 << 20, -1, 0),
                 tcs.ServerConfig(1 << 20, 0, -2)]:
         assert tcs.lib().tcs_server_create(ctypes.byref(cfg), ctypes.byref(h)) == tcs.TCS_ERR_INVALID
+
+
+def test_pipe_arguments_are_checked_before_device_work(tcs):
+    import ctypes
+
+    L = tcs.lib()
+    assert L.tcs_pipe_submit(None, None, None, 1) == tcs.TCS_ERR_INVALID
+    assert L.tcs_pipe_wait(None) == tcs.TCS_ERR_INVALID
+    assert L.tcs_pipe_destroy(None) == tcs.TCS_OK
+    h = ctypes.c_void_p()
+    assert L.tcs_pipe_create(None, ctypes.byref(h)) == tcs.TCS_ERR_INVALID
