@@ -217,6 +217,7 @@ def main():
     ap.add_argument("--sweep", action="store_true", help="engines for the benchmark shapes")
     ap.add_argument("--serve", action="store_true", help="server round quantum")
     ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--seconds", type=float, default=3.0, help="replay length per serve candidate")
     args = ap.parse_args()
     cache = Cache(args.cache)
     if args.sweep or not args.serve:
@@ -226,7 +227,7 @@ def main():
                     e = tune_sweep(stencil, precision, n, n, cache=cache)
                     print(json.dumps({"key": sweep_key(stencil, precision, n, n), **e}))
     if args.serve:
-        print(json.dumps(tune_serve(args.rate, cache=cache)))
+        print(json.dumps(tune_serve(args.rate, seconds=args.seconds, cache=cache)))
 
 
 if __name__ == "__main__":
