@@ -480,6 +480,10 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             o.y0 = g.y0; o.y1 = g.y1; o.x0 = g.x0; o.x1 = g.x1;
             const int Y0 = (it.tile / g.tiles_x) * kTile;
             const int X0 = (it.tile % g.tiles_x) * kTile;
+            // this warp's 32 rows all lie in the plane's padding below the grid:
+            // nothing of them to load or store (padding only has to stay finite,
+            // and it does: it keeps what it holds)
+            const bool rows_out = Y0 + 32 * q >= g.ny;
             if constexpr (SPLIT) {
                 const int y = Y0 + m;
                 const bool fast = tile_inside(o, Y0, X0);
@@ -499,6 +503,14 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 };
                 ok = walk_windows(grp, C::GROUPS, kBatchWindows, ready, release, [&](int jb) {
                     const int Ga = G0 + jb, Gb = Ga + 1;
+                    if (rows_out || X0 + 16 * jb >= g.nx) {  // all padding: release unread
+                        __syncwarp();
+                        if (lane == 0) {
+                            mbar_arrive(&acc_empty[Ga % kBatchRingSlots]);
+                            mbar_arrive(&acc_empty[Gb % kBatchRingSlots]);
+                        }
+                        return;
+                    }
                     tc_fence_after();
                     float f[16];
                     split_block_load(lane_base + (Ga % kBatchRingSlots) * kBatchRegion,
@@ -526,14 +538,20 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     stop = true;
                     break;
                 }
-                tc_fence_after();
-                float f[Mode<false>::SUB_BLOCKS / 2][16];
-                epilogue_load<false>(lane_base + col, grp, f);
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) slots.release(acc_empty, mask);
-                epilogue_store<false>(o, f, 0, grp, m, Y0, X0);
-                slots.used(mask);
+                if (rows_out || X0 + 64 * grp >= g.nx) {  // this half is all padding
+                    __syncwarp();
+                    if (lane == 0) slots.release(acc_empty, mask);
+                    slots.used(mask);
+                } else {
+                    tc_fence_after();
+                    float f[Mode<false>::SUB_BLOCKS / 2][16];
+                    epilogue_load<false>(lane_base + col, grp, f);
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) slots.release(acc_empty, mask);
+                    epilogue_store<false>(o, f, 0, grp, m, Y0, X0);
+                    slots.used(mask);
+                }
             }
             // this warp's stores are issued: the signal warp publishes them
             __syncwarp();
@@ -707,6 +725,8 @@ int batch_build(tcs_batch b) {
             G.plane[s][1] = split ? b->pool + e.offset[s][1] : nullptr;
         }
         G.pg = e.g.p16;
+        G.ny = e.g.ny;
+        G.nx = e.g.nx;
         G.y0 = e.g.y0; G.y1 = e.g.y1; G.x0 = e.g.x0; G.x1 = e.g.x1;
         G.tiles_x = (e.g.nx + kTile - 1) / kTile;
         G.n_tiles = G.tiles_x * ((e.g.ny + kTile - 1) / kTile);

@@ -12,6 +12,7 @@ namespace tcs {
 struct BatchGrid {
     uint16_t *plane[2][2];  // [ping-pong state][hi, lo]
     PlaneGeom pg;
+    int ny, nx;             // cells (beyond them: plane padding)
     int y0, y1, x0, x1;
     int tiles_x;
     int n_tiles;

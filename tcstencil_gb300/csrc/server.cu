@@ -505,6 +505,8 @@ bool tcs_server_s::launch_round() {
             G.plane[s][1] = q->split ? plane(q, s, 1) : nullptr;
         }
         G.pg = q->g.p16;
+        G.ny = q->g.ny;
+        G.nx = q->g.nx;
         G.y0 = q->g.y0; G.y1 = q->g.y1; G.x0 = q->g.x0; G.x1 = q->g.x1;
         G.tiles_x = (q->g.nx + kTile - 1) / kTile;
         G.n_tiles = tiles[i];
