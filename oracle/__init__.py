@@ -251,7 +251,9 @@ def gold_bench(init: np.ndarray, B, stencil: str, steps: int, threads: int) -> f
 # ------------------------------------------------------- reference build --
 class Ref:
     """The reference's own gold()/layout16 helpers, compiled by `make -C oracle
-    ref` from the reference sources.  Exists only where those sources were."""
+    ref` from the reference sources, and its GPU kernels as sm_103a cubins
+    (`make -C oracle refgpu`, launched by oracle/ref_gpu.py).  Exists only where
+    those sources were."""
 
     def __init__(self, ref_dir: str = REF_DIR):
         self.dir = ref_dir
@@ -264,7 +266,7 @@ class Ref:
         src = env.get("TCS_REF_DIR", "/root/reference")
         if not os.path.isdir(os.path.join(src, "common")):
             return False
-        subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref"], check=True, env=env)
+        subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref", "refgpu"], check=True, env=env)
         return True
 
     def available(self) -> bool:
