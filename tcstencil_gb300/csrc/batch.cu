@@ -20,9 +20,10 @@
 // t+1 overwrites the plane step t-1 read, and starts only after all of step t,
 // hence all of step t-1, finished.
 //
-// Per item the producer bulk-copies the tile's input panels AND the grid's
+// Per item the producer loads the tile's input panels (one tensor-map load per
+// plane, from the grid's maps in device memory) AND bulk-copies the grid's
 // coefficient bands (prebuilt in global memory by build_bands_kernel) into the
-// stage, so the MMA issuer needs nothing else; stencil radius and precision
+// stage, so the MMA issuers need nothing else; stencil radius and precision
 // select one of four fully unrolled MMA sequences (tc_core.cuh), the same code
 // the single-grid kernel runs, so every grid gets the same bits alone and in
 // a batch.  The run ends with a tiny kernel that flips each grid's ping-pong

@@ -14,18 +14,20 @@
 // cover the accumulator, the first of them with accumulate = 0) and odd
 // windows then add in.  Star stencils use the same windows with a one-tap
 // (diagonal) band on the off-centre rows.  FP16 operands, FP32 accumulators
-// in tensor memory (TMEM).  The split form works in two 64-column sub-tiles
-// so that its two accumulators per sub-tile still double-buffer in TMEM.
+// in tensor memory (TMEM).  The split form gives each window its own TMEM
+// region in a ring (tc_split_ring_kernel below), so that it streams windows
+// instead of whole accumulators.
 //
 // Staging.  Planes are column panels (8 cells x all rows, 16 bytes per row,
-// rows contiguous; see tcs_internal.h), so the 132 input rows a tile needs
-// from one panel (two halo rows above and below) are one contiguous 2112-byte
-// run: the producer fetches the 18 panels of a tile (16 + one each side) with
-// 18 1-D bulk copies.  The shared-memory image, chunk s = all 132 rows of
-// panel s at a 16-byte row stride, is directly a no-swizzle K-major UMMA
-// operand (8-row x 16-byte core matrices, SBO = 128 B between row groups,
-// LBO = 2112 B between K chunks), and a row shift dy is +16*dy bytes on the
-// descriptor start address.
+// rows contiguous; see tcs_internal.h).  A tile needs rows Y0-2 .. Y0+129 of
+// 18 panels (16 + one each side); it stages rows Y0-4 .. Y0+131 (136 rows),
+// which with the plane's 4 top padding rows start on a 128-byte line, so one
+// 3-D tensor-map load per plane moves 17 whole lines of each of the 18 panels
+// (tc_core.cuh StageLines, encode_panel_map).  The shared-memory image, chunk
+// s = all 136 rows of panel s at a 16-byte row stride, is directly a
+// no-swizzle K-major UMMA operand (8-row x 16-byte core matrices, SBO = 128 B
+// between row groups, LBO = 2176 B between K chunks), and a row shift dy is
+// +16*dy bytes on the descriptor start address.
 //
 // Split precision (hi + lo planes).  Data are stored as x' = x 2^-E with
 // hi = rint(x' 2^11) 2^-11 (fixed point) and lo = fp16((x' - hi) 2^11); a

@@ -218,24 +218,9 @@ __device__ __forceinline__ void build_bands(uint16_t *band, const float *coef, i
     }
 }
 
-// Producer: bulk copies of rows Y0-2 .. Y0+129 of panels X0/8 - 1 .. X0/8 + 16
-// of each input plane into a stage (plane pl at stage + pl*kPlaneStage).
-template <class SG = StageHalo2>
-__device__ __forceinline__ void load_tile(const uint16_t *hi, const uint16_t *lo, int planes,
-                                          const PlaneGeom &pg, int Y0, int X0, uint8_t *stage,
-                                          uint64_t *bar) {
-    const size_t src0 = plane_index(pg, Y0 - SG::TOP, X0 - 8);
-    for (int pl = 0; pl < planes; pl++) {
-        const uint16_t *src = (pl ? lo : hi) + src0;
-        uint8_t *st = stage + (size_t)pl * SG::PLANE;
-#pragma unroll 1
-        for (int c = 0; c < kSlots; c++)
-            bulk_load(st + c * SG::CHUNK, src + (size_t)c * pg.nyp * 8, SG::CHUNK, bar);
-    }
-}
-
-// The same tile in the line-aligned staging with one tensor-map load per
-// plane (maps from encode_panel_map): box origin (word 0, row group Y0 / 8 =
+// Producer: one tensor-map load per plane of a tile in the line-aligned
+// staging (maps from encode_panel_map): the 136 rows Y0 - 4 .. Y0 + 131 of
+// the 18 panels X0/8 - 1 .. X0/8 + 16, box origin (word 0, row group Y0 / 8 =
 // row Y0 - 4 + the plane's 4 top padding rows, panel of X0 - 8).
 __device__ __forceinline__ void load_tile_map(const CUtensorMap *hi, const CUtensorMap *lo,
                                               int planes, int Y0, int X0, uint8_t *stage,

@@ -91,18 +91,6 @@ __device__ __forceinline__ void tma_prefetch_map(const CUtensorMap *map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
-// 5-D tiled load into shared memory, completion counted on `bar` in bytes.
-// The innermost coordinate c0 is always 0 here (16-byte aligned).
-__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, uint64_t *bar,
-                                            int c0, int c1, int c2, int c3, int c4) {
-    asm volatile(
-        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4),
-        "r"(smem_u32(bar))
-        : "memory");
-}
-
 // 3-D tiled load into shared memory, completion counted on `bar` in bytes.
 // The innermost coordinate c0 is always 0 here (16-byte aligned).
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar,

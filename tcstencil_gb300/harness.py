@@ -70,7 +70,7 @@ def time_config(engine: str, stencil: str, precision: str, n: int, launches: int
     gpts = n * n / (ms * 1e-3) / 1e9
     achieved = gpts * BYTES_PER_UPDATE[precision]
     return {"variant": engine, "stencil": stencil, "precision": precision, "mesh_size": n,
-            "tile": "128x128" if precision != "split" else "128x96",
+            "tile": "128x128",
             "time_ms": round(ms, 5), "gpts": round(gpts, 2),
             "hbm_frac": round(achieved / peak_gbs(), 4)}
 
