@@ -101,6 +101,19 @@ def run_profile(args):
     print(f"profile run: {args.stencil}/{args.engine}/{args.precision} {n}^2 x {args.timesteps}")
 
 
+def max_over_ranks(values, device="cuda"):
+    """Each value's maximum over all ranks (the slowest replica's time); the
+    values themselves when the job runs on one process."""
+    import torch
+
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
@@ -431,11 +444,7 @@ def run_ours(args):
     barrier()
     t = timed_sweeps(torch, tcs, plan, args.steps, 0, args.timesteps, stream)
     clocks = ClockSampler.summarize(sampler.stop()) if sampler else None
-    tmax = t
-    if ws > 1:
-        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        tmax = float(tt.item())
+    (tmax,) = max_over_ranks([t])
     assert tcs.device_error() == 0
     value = ws * updates_per_step * args.steps / tmax / 1e9
     launch_s = t / (args.steps * args.timesteps)
@@ -458,10 +467,7 @@ def run_ours(args):
                        precision=args.precision, h_out=h_out)
     torch.cuda.synchronize()
     te = time.perf_counter() - t0
-    if ws > 1:
-        tt = torch.tensor([te], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        te = float(tt.item())
+    (te,) = max_over_ranks([te])
     e2e = {"value": ws * updates_per_step * e2e_steps / te / 1e9, "unit": "Gpts/s",
            "h2d_bytes_per_step": n * n * 4, "d2h_bytes_per_step": n * n * 4,
            "api": "tcs_sweep_host (pinned host FP32 grid in/out, cached plan)"}
@@ -479,10 +485,7 @@ def run_ours(args):
     pipe.wait()
     tp = time.perf_counter() - t0
     pipe.close()
-    if ws > 1:
-        tt = torch.tensor([tp], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        tp = float(tt.item())
+    (tp,) = max_over_ranks([tp])
     e2e_pipelined = {"value": ws * updates_per_step * e2e_steps / tp / 1e9, "unit": "Gpts/s",
                      "h2d_bytes_per_step": n * n * 4, "d2h_bytes_per_step": n * n * 4,
                      "api": "tcs_pipe_submit (two plans on two streams, pinned host FP32 grid in/out)"}
@@ -561,10 +564,7 @@ def run_batch(args):
     clocks = ClockSampler.summarize(sampler.stop()) if sampler else None
     t = r["ms_per_run"] * args.steps / 1e3
     te = r["point_updates_per_run"] / r["e2e_gpts"] / 1e9
-    if ws > 1:
-        tt = torch.tensor([t, te], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t, te = (float(v) for v in tt.tolist())
+    t, te = max_over_ranks([t, te])
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
