@@ -40,13 +40,14 @@
 // c3*hi, where cf*lo also carries the lo*(c - ch) term.  Both are combined in
 // FP32 with round-to-nearest in the epilogue.
 //
-// Pipeline (persistent, one CTA per SM, 10 warps):
-//   warp 0      producer: bulk copies of each tile's panels into NS stages
-//   warp 1      TMEM allocator and single-thread MMA issuer
-//   warps 2..9  epilogue (two warpgroups, one per column half):
-//               TMEM -> registers -> FP16 (or hi/lo) -> global
-// Two accumulator buffers let the epilogue of one (sub-)tile overlap the MMAs
-// of the next.  Every wait is bounded; on timeout the kernel records an error
+// Pipeline (persistent, one CTA per SM, 11 warps):
+//   warp 0       producer: one tensor-map load per plane of each tile into NS
+//                stages (StageLines: 136 rows, whole 128-byte lines)
+//   warps 1, 2   MMA issuers on alternate tiles (warp 1 also owns TMEM)
+//   warps 3..10  epilogue (two warpgroups, one per column half):
+//                TMEM -> registers -> FP16 -> global
+// Two accumulator slots let the epilogue of one tile overlap the MMAs of the
+// next; tile i uses slot i % 2, issued by warp 1 + i % 2.  Every wait is bounded; on timeout the kernel records an error
 // word, stops, drains its own copies and MMAs, frees TMEM and returns.
 #include "tc_core.cuh"
 
@@ -59,13 +60,25 @@ using SG = StageLines;  // line-aligned staging of the sweep kernels
 
 __device__ int g_tc_error = 0;
 
-// Plain form: three 38 KB stages.  Measured on GB300 (box2d1r / box2d2r /
-// star2d2r, 8196², Gpts/s): 3 stages 1310 / 1106 / 1114, 4 stages 1255 /
-// 1113 / 1110, 5 stages 1209 / 1104 / 1100 -- a smaller shared-memory
-// footprint leaves more of the SM's L1 to the output stream.
+// Plain form: four 39 KB stages, a multiple of the two MMA issuers (below).
+// Measured on GB300 with one issuer (box2d1r / box2d2r / star2d2r, 8196²,
+// Gpts/s): 3 stages 1310 / 1106 / 1114, 4 stages 1255 / 1113 / 1110, 5
+// stages 1209 / 1104 / 1100.
 #ifndef TCS_PLAIN_STAGES
-#define TCS_PLAIN_STAGES 3
+#define TCS_PLAIN_STAGES 4
 #endif
+
+// Plain form: two MMA issuer warps take alternate tiles (tile i uses
+// accumulator slot i % 2, so each issuer owns one slot); one issues while the
+// other waits for its stage or slot and commits.  With an even number of
+// stages, stage i % NS only ever holds tiles of one issuer, so every stage's
+// fills are waited for by one thread, in order.  (An mbarrier parity wait
+// also succeeds for the phase just before the barrier's current one: a thread
+// that skipped a stage's fill could take the next fill as already landed, and
+// one that fell two fills behind would wait for a phase that needs its own
+// next tile.)
+constexpr int kSweepIssuers = 2;
+constexpr int kSweepThreads = 32 * (1 + kSweepIssuers + kEpiWarps);
 
 template <int S, bool SPLIT>
 struct Cfg {
@@ -89,7 +102,7 @@ struct TcParams {
 };
 
 template <int S, bool SPLIT>
-__global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const __grid_constant__ TcParams p) {
+__global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid_constant__ TcParams p) {
     using C = Cfg<S, SPLIT>;
     using M = Mode<SPLIT>;
     constexpr int NS = C::STAGES;
@@ -125,7 +138,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const __grid_cons
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], kEpiWarps);
         }
-        mbar_init(drain, 1);
+        mbar_init(drain, kSweepIssuers);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -135,7 +148,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const __grid_cons
         tmem_relinquish();
     }
     build_bands(reinterpret_cast<uint16_t *>(band_base), p.coef, C::R, C::BOX, SPLIT, threadIdx.x,
-                kThreads);
+                kSweepThreads);
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -176,56 +189,58 @@ __global__ void __launch_bounds__(kThreads, 1) tc_sweep_kernel(const __grid_cons
                 }
             }
         }
-    } else if (warp == 1) {
-        // ---------------------------------------------------- MMA issuer ---
+    } else if (warp <= kSweepIssuers) {
+        // --------------------------------------------------- MMA issuers ---
+        static_assert(!SPLIT && NSUB == 1, "one plain sub-tile per tile");
+        static_assert(NS % kSweepIssuers == 0, "each stage holds one issuer's tiles");
         if (lane == 0) {
+            const int id = warp - 1;  // issues the tiles i with i % 2 == id
             int i = 0;
-            bool issued_any = false;
             bool stop = false;
-            AccSlots slots;
+            AccSlots slots;  // walks every tile, so both issuers see the same slot uses
             const uint32_t band = smem_u32(band_base);
             for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
-                const int s = i % NS;
+                const int s = i % NS;  // s % 2 == i % 2: this issuer's stages only
+                uint32_t col;
+                const uint32_t mask = slots.take(false, col);
+                if ((i & 1) != id) {
+                    slots.used(mask);
+                    continue;
+                }
                 if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
                     record_error(&g_tc_error, kErrWaitFull);
                     *abort_flag = 1;
                     break;
                 }
+                if (!slots.acquire(acc_empty, mask, abort_flag)) {
+                    record_error(&g_tc_error, kErrWaitAccum);
+                    *abort_flag = 1;
+                    stop = true;
+                    break;
+                }
                 const uint64_t a_hi0 = smem_desc(
                     smem_u32(stage_base + (size_t)s * NP * SG::PLANE), SG::CHUNK, 128);
-#pragma unroll
-                for (int h = 0; h < NSUB; h++) {
-                    uint32_t col;
-                    const uint32_t mask = slots.take(SPLIT, col);
-                    if (!slots.acquire(acc_empty, mask, abort_flag)) {
-                        record_error(&g_tc_error, kErrWaitAccum);
-                        *abort_flag = 1;
-                        stop = true;
-                        break;
-                    }
-                    tc_fence_after();
-                    issue_subtile<C::R, SPLIT, SG>(a_hi0, band, tmem_base + col, h);
-                    slots.commit(acc_full, mask);
-                    slots.used(mask);
-                    issued_any = true;
-                }
+                tc_fence_after();
+                issue_subtile<C::R, false, SG>(a_hi0, band, tmem_base + col, 0);
+                slots.commit(acc_full, mask);
+                slots.used(mask);
                 umma_commit(&empty[s]);
             }
-            if (issued_any) {
-                umma_commit(drain);
-                const uint64_t t0 = global_timer_ns();
-                while (!mbar_try_wait(drain, 0)) {
-                    if (global_timer_ns() - t0 > kWaitLimitNs) {
-                        record_error(&g_tc_error, kErrWaitDrain);
-                        break;
-                    }
+            // both issuers commit (one with nothing in flight completes at
+            // once), so the drain phase always completes
+            umma_commit(drain);
+            const uint64_t t0 = global_timer_ns();
+            while (!mbar_try_wait(drain, 0)) {
+                if (global_timer_ns() - t0 > kWaitLimitNs) {
+                    record_error(&g_tc_error, kErrWaitDrain);
+                    break;
                 }
             }
         }
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;            // TMEM lane quarter of this warp
-        const int half = (warp - 2) >> 2;  // which half of a sub-tile's column blocks
+        const int half = (warp - 1 - kSweepIssuers) >> 2;  // which half of a sub-tile's column blocks
         const int m = q * 32 + lane;       // output row within the tile
         TileOut o;
         o.in_hi = p.in_hi;
@@ -548,7 +563,7 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     for (int k = 0; k < C::NDY * C::NDY; k++) p.coef[k] = B[k];
     const int grid = p.n_tiles < g_num_sms ? p.n_tiles : g_num_sms;
     if constexpr (SPLIT) tc_split_ring_kernel<S><<<grid, kRingThreads, C::SMEM, s>>>(p);
-    else tc_sweep_kernel<S, SPLIT><<<grid, kThreads, C::SMEM, s>>>(p);
+    else tc_sweep_kernel<S, SPLIT><<<grid, kSweepThreads, C::SMEM, s>>>(p);
     return cudaGetLastError();
 }
 
