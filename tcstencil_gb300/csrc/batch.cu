@@ -56,15 +56,20 @@ constexpr int kRing = 8;  // published work items in flight
 constexpr int kTableInts = 2048;
 template <bool SPLIT>
 struct BatchCfg {
-    static constexpr int STAGES = SPLIT ? 2 : 3;
+    // FP16: four stages, a multiple of the two issuers, so stage i % 4 holds
+    // only one issuer's items (see the MMA issuers)
+    static constexpr int STAGES = SPLIT ? 2 : 4;
     static constexpr int PLANES = SPLIT ? 2 : 1;
     static constexpr int BAND_BYTES = (SPLIT ? 4 : 1) * 5 * kBandBytes;  // radius 2
     static constexpr int STAGE_BYTES = PLANES * SG::PLANE + BAND_BYTES;
     static constexpr int GROUPS = SPLIT ? 3 : 2;
     static constexpr int EPI_WARPS = 4 * GROUPS;
-    // MMA issuer warps 1 .. ISSUERS: split items alternate windows between two
-    // (one issues while the other waits on a region or commits)
-    static constexpr int ISSUERS = SPLIT ? 2 : 1;
+    // MMA issuer warps 1 and 2 (one issues while the other waits on a region
+    // or slot, or commits): split items alternate windows between them, FP16
+    // items alternate whole items
+    static constexpr int ISSUERS = 2;
+    // commits that free a stage: both issuers' (split), the item's issuer's (FP16)
+    static constexpr int STAGE_RELEASES = SPLIT ? 2 : 1;
     static constexpr int EPI_WARP0 = 1 + ISSUERS;
     static constexpr int SIGNAL_WARP = EPI_WARP0 + EPI_WARPS;
     static constexpr int THREADS = 32 * (SIGNAL_WARP + 1);
@@ -186,7 +191,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], C::ISSUERS);
+            mbar_init(&empty[s], C::STAGE_RELEASES);
         }
         for (int b = 0; b < NACC; b++) {
             mbar_init(&acc_full[b], 1);
@@ -334,9 +339,19 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
         }
     } else if (warp <= C::ISSUERS) {
         // --------------------------------------------------- MMA issuers ---
+        // Both issuers read every published item, in order (the slot sequence
+        // and the stop sentinel).  Split: both wait for every stage fill and
+        // issue alternate windows.  FP16: item i's issuer is i % 2 and it alone
+        // waits for the item's stage: with four stages a stage only holds one
+        // issuer's items, so each stage's fills are waited for by one thread in
+        // order (an mbarrier parity wait also succeeds for the phase before the
+        // current one, so a thread must never skip a fill it later waits past).
+        // A ring slot is republished only after the signal warp finished its
+        // item, which needs a lagging issuer's own earlier item, so neither
+        // issuer can be lapped on the ring.
         if (lane == 0) {
-            const int id = warp - 1;  // split: takes the windows G with G % 2 == id
-            AccSlots slots;  // plain
+            const int id = warp - 1;  // split: windows G % 2 == id; FP16: items i % 2 == id
+            AccSlots slots;  // FP16: walks every item, so both see the same slot uses
             int G = 0;       // split: global window counter of the ring
             bool stop = false;
             for (int i = 0; !stop; i++) {
@@ -348,6 +363,14 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 }
                 const BatchItem it = ring[i % kRing];
                 if (it.g < 0) break;
+                uint32_t col = 0, mask = 0;
+                if constexpr (!SPLIT) {
+                    mask = slots.take(false, col);
+                    if ((i & 1) != id) {
+                        slots.used(mask);
+                        continue;
+                    }
+                }
                 if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag, wait_lim)) {
                     batch_fail(p, kErrWaitFull);
                     *abort_flag = 1;
@@ -375,8 +398,6 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                         umma_commit(&acc_full[r]);
                     }
                 } else {
-                    uint32_t col;
-                    const uint32_t mask = slots.take(false, col);
                     if (!slots.acquire(acc_empty, mask, abort_flag, wait_lim)) {
                         batch_fail(p, kErrWaitAccum);
                         *abort_flag = 1;
