@@ -305,18 +305,26 @@ __global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid
 // window only after seeing it complete, so releases always count toward the
 // window they belong to.
 //
-// Two MMA issuers (warps 1 and 2) take the even and the odd windows.  Each
-// window costs its issuer a region wait and a commit; the tensor pipe takes
-// only a few MMAs ahead of the issuing thread, so with one issuer those
-// latencies would leave it idle for about 40 % of a window.  With two, one
-// issues while the other waits.  A region is reused five windows later, by
-// the other issuer, only after all twelve epilogue warps have released it;
-// a tile's stage is free when both issuers' commits for it have completed.
+// Three MMA issuers (warps 1..3) take windows G % 3.  Each window costs its
+// issuer a region wait and a commit; the tensor pipe takes only a few MMAs
+// ahead of the issuing thread, so with one issuer those latencies would leave
+// it idle for about 40 % of a window.  With several, one issues while the
+// others wait (measured per step at 8196²: box2d1r 124 -> 110 -> 109.5 us,
+// box2d2r 157 -> 117 -> 114 us for one, two, three issuers).  A region is
+// reused five windows later, by another issuer, after all twelve epilogue
+// warps have released it; an issuer's previous region wait (three windows
+// back) already covered the release before that, because every warp releases
+// windows in order, so no parity wait can alias.  Every issuer waits for
+// every stage fill in order, and a stage is free when all issuers' commits
+// for the tile have completed.
 constexpr int kRingSlots = 5;
 constexpr int kRegionCols = 96;
 constexpr int kRingGroups = 3;                     // epilogue block groups
 constexpr int kRingEpiWarps = 4 * kRingGroups;     // a lane quarter each
-constexpr int kRingIssuers = 2;                    // MMA issuer warps 1 and 2
+#ifndef TCS_SPLIT_ISSUERS
+#define TCS_SPLIT_ISSUERS 3
+#endif
+constexpr int kRingIssuers = TCS_SPLIT_ISSUERS;   // MMA issuer warps 1 .. kRingIssuers
 constexpr int kRingThreads = 32 * (1 + kRingIssuers + kRingEpiWarps);
 constexpr int kTileWindows = kTile / 16 + 1;
 static_assert(kRingSlots * kRegionCols <= kTmemCols, "window ring fits TMEM");
@@ -409,7 +417,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
     } else if (warp <= kRingIssuers) {
         // --------------------------------------------------- MMA issuers ---
         if (lane == 0) {
-            const int id = warp - 1;  // takes the windows G with G % 2 == id
+            const int id = warp - 1;  // takes the windows G with G % kRingIssuers == id
             int i = 0, G = 0;         // tiles, global windows
             bool stop = false;
             const uint32_t band = smem_u32(band_base);
@@ -424,7 +432,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
                     smem_u32(stage_base + (size_t)s * NP * SG::PLANE), SG::CHUNK, 128);
 #pragma unroll 1
                 for (int wg = 0; wg < kTileWindows; wg++, G++) {
-                    if ((G & 1) != id) continue;
+                    if (G % kRingIssuers != id) continue;
                     const int r = G % kRingSlots;
                     if (!mbar_wait(&win_empty[r], ((G / kRingSlots) & 1) ^ 1, abort_flag)) {
                         record_error(&g_tc_error, kErrWaitAccum);
