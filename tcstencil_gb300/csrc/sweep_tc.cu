@@ -60,25 +60,31 @@ using SG = StageLines;  // line-aligned staging of the sweep kernels
 
 __device__ int g_tc_error = 0;
 
-// Plain form: four 39 KB stages, a multiple of the two MMA issuers (below).
-// Measured on GB300 with one issuer (box2d1r / box2d2r / star2d2r, 8196²,
-// Gpts/s): 3 stages 1310 / 1106 / 1114, 4 stages 1255 / 1113 / 1110, 5
-// stages 1209 / 1104 / 1100.
-#ifndef TCS_PLAIN_STAGES
-#define TCS_PLAIN_STAGES 4
-#endif
+// Plain form: MMA issuers and accumulator slots (below); the stage count is
+// a multiple of the issuers.  Measured on GB300 with one issuer (box2d1r /
+// box2d2r / star2d2r, 8196², Gpts/s): 3 stages 1310 / 1106 / 1114, 4 stages
+// 1255 / 1113 / 1110, 5 stages 1209 / 1104 / 1100.  With two issuers and four
+// stages: 1330 / 1327 / 1325; with three and three: 1374 / 1238 / 1241.  So
+// radius-1 stencils take three issuers, radius-2 stencils two.
 
-// Plain form: two MMA issuer warps take alternate tiles (tile i uses
-// accumulator slot i % 2, so each issuer owns one slot); one issues while the
-// other waits for its stage or slot and commits.  With an even number of
-// stages, stage i % NS only ever holds tiles of one issuer, so every stage's
-// fills are waited for by one thread, in order.  (An mbarrier parity wait
-// also succeeds for the phase just before the barrier's current one: a thread
-// that skipped a stage's fill could take the next fill as already landed, and
-// one that fell two fills behind would wait for a phase that needs its own
-// next tile.)
-constexpr int kSweepIssuers = 2;
-constexpr int kSweepThreads = 32 * (1 + kSweepIssuers + kEpiWarps);
+// Plain form: ISSUERS MMA issuer warps take tiles in turn.  Tile i uses
+// accumulator slot i % ISSUERS (one 160-column slot per issuer) and stage
+// i % NS with NS a multiple of the issuers, so every slot and every stage
+// belongs to one issuer and its fills and releases are waited for by one
+// thread, in order.  (An mbarrier parity wait also succeeds for the phase
+// just before the barrier's current one: a thread that skipped a stage's fill
+// could take the next fill as already landed, and one that fell two fills
+// behind would wait for a phase that needs its own next tile.)  One issuer
+// issues while the others wait for their stage or slot and commit.
+template <int S>
+struct Sweep {
+    static constexpr int ISSUERS = stencil_r(S) == 1 ? 3 : 2;
+    static constexpr int SLOTS = ISSUERS;
+    static constexpr int STAGES = ISSUERS == 2 ? 4 : 3;
+    static constexpr int THREADS = 32 * (1 + ISSUERS + kEpiWarps);
+    static_assert(SLOTS * Mode<false>::ACC <= kTmemCols, "accumulator slots fit TMEM");
+    static_assert(STAGES % ISSUERS == 0, "each stage holds one issuer's tiles");
+};
 
 template <int S, bool SPLIT>
 struct Cfg {
@@ -86,7 +92,7 @@ struct Cfg {
     static constexpr int R = stencil_r(S);
     static constexpr bool BOX = stencil_box(S);
     static constexpr int NDY = 2 * R + 1;
-    static constexpr int STAGES = SPLIT ? 2 : TCS_PLAIN_STAGES;
+    static constexpr int STAGES = SPLIT ? 2 : Sweep<S>::STAGES;
     static constexpr size_t SMEM = 1024 + (size_t)STAGES * M::PLANES * SG::PLANE +
                                    (size_t)M::BAND_PLANES * NDY * kBandBytes + 256;
     static_assert(SMEM <= 232448, "shared memory budget");
@@ -102,7 +108,7 @@ struct TcParams {
 };
 
 template <int S, bool SPLIT>
-__global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid_constant__ TcParams p) {
+__global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __grid_constant__ TcParams p) {
     using C = Cfg<S, SPLIT>;
     using M = Mode<SPLIT>;
     constexpr int NS = C::STAGES;
@@ -116,12 +122,14 @@ __global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid
     uint8_t *band_base = smem + (size_t)NS * NP * SG::PLANE;     // [BAND_PLANES][NDY]
     uint64_t *bars =
         reinterpret_cast<uint64_t *>(band_base + M::BAND_PLANES * C::NDY * kBandBytes);
-    uint64_t *full = bars;                    // [NS]
-    uint64_t *empty = bars + NS;              // [NS]
-    uint64_t *acc_full = bars + 2 * NS;       // [2]
-    uint64_t *acc_empty = bars + 2 * NS + 2;  // [2]
-    uint64_t *drain = bars + 2 * NS + 4;      // [1]
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * NS + 5);
+    constexpr int NSL = Sweep<S>::SLOTS;
+    uint64_t *full = bars;                      // [NS]
+    uint64_t *empty = bars + NS;                // [NS]
+    uint64_t *acc_full = bars + 2 * NS;         // [NSL]
+    uint64_t *acc_empty = acc_full + NSL;       // [NSL]
+    uint64_t *drain = acc_empty + NSL;          // [1]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+    static_assert((2 * NS + 2 * NSL + 1) * 8 + 8 <= 256, "barrier area");
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5;
@@ -134,11 +142,11 @@ __global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; b++) {
+        for (int b = 0; b < NSL; b++) {
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], kEpiWarps);
         }
-        mbar_init(drain, kSweepIssuers);
+        mbar_init(drain, Sweep<S>::ISSUERS);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -148,7 +156,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid
         tmem_relinquish();
     }
     build_bands(reinterpret_cast<uint16_t *>(band_base), p.coef, C::R, C::BOX, SPLIT, threadIdx.x,
-                kSweepThreads);
+                Sweep<S>::THREADS);
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -189,30 +197,25 @@ __global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid
                 }
             }
         }
-    } else if (warp <= kSweepIssuers) {
+    } else if (warp <= Sweep<S>::ISSUERS) {
         // --------------------------------------------------- MMA issuers ---
         static_assert(!SPLIT && NSUB == 1, "one plain sub-tile per tile");
-        static_assert(NS % kSweepIssuers == 0, "each stage holds one issuer's tiles");
         if (lane == 0) {
-            const int id = warp - 1;  // issues the tiles i with i % 2 == id
-            int i = 0;
+            const int id = warp - 1;  // issues the tiles i with i % Sweep<S>::ISSUERS == id
             bool stop = false;
-            AccSlots slots;  // walks every tile, so both issuers see the same slot uses
             const uint32_t band = smem_u32(band_base);
-            for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
-                const int s = i % NS;  // s % 2 == i % 2: this issuer's stages only
-                uint32_t col;
-                const uint32_t mask = slots.take(false, col);
-                if ((i & 1) != id) {
-                    slots.used(mask);
-                    continue;
-                }
+            const uint32_t col = (uint32_t)(id * Mode<false>::ACC);  // this issuer's slot
+            int i = id;
+            for (int t = blockIdx.x + id * (int)gridDim.x; t < n_tiles && !stop;
+                 t += Sweep<S>::ISSUERS * (int)gridDim.x, i += Sweep<S>::ISSUERS) {
+                const int s = i % NS;  // one of this issuer's stages
                 if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
                     record_error(&g_tc_error, kErrWaitFull);
                     *abort_flag = 1;
                     break;
                 }
-                if (!slots.acquire(acc_empty, mask, abort_flag)) {
+                // the slot's previous tile (i - NSL) has been read out
+                if (!mbar_wait(&acc_empty[id], ((i / NSL) & 1) ^ 1, abort_flag)) {
                     record_error(&g_tc_error, kErrWaitAccum);
                     *abort_flag = 1;
                     stop = true;
@@ -222,8 +225,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid
                     smem_u32(stage_base + (size_t)s * NP * SG::PLANE), SG::CHUNK, 128);
                 tc_fence_after();
                 issue_subtile<C::R, false, SG>(a_hi0, band, tmem_base + col, 0);
-                slots.commit(acc_full, mask);
-                slots.used(mask);
+                umma_commit(&acc_full[id]);
                 umma_commit(&empty[s]);
             }
             // both issuers commit (one with nothing in flight completes at
@@ -240,7 +242,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;            // TMEM lane quarter of this warp
-        const int half = (warp - 1 - kSweepIssuers) >> 2;  // which half of a sub-tile's column blocks
+        const int half = (warp - 1 - Sweep<S>::ISSUERS) >> 2;  // which half of a sub-tile's column blocks
         const int m = q * 32 + lane;       // output row within the tile
         TileOut o;
         o.in_hi = p.in_hi;
@@ -250,35 +252,30 @@ __global__ void __launch_bounds__(kSweepThreads, 1) tc_sweep_kernel(const __grid
         o.pg = pg;
         o.y0 = p.g.y0; o.y1 = p.g.y1; o.x0 = p.g.x0; o.x1 = p.g.x1;
         bool stop = false;
-        AccSlots slots;
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
-        for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x) {
+        int i = 0;
+        for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
             const int Y0 = (t / tiles_x) * kTile;
             const int X0 = (t % tiles_x) * kTile;
-#pragma unroll 1
-            for (int h = 0; h < NSUB; h++) {
-                uint32_t col;
-                const uint32_t mask = slots.take(SPLIT, col);
-                bool ok = slots.ready(acc_full, mask, abort_flag);
-                ok = __all_sync(0xffffffffu, ok);
-                if (!ok) {
-                    if (lane == 0) {
-                        record_error(&g_tc_error, kErrWaitResult);
-                        *abort_flag = 1;
-                    }
-                    stop = true;
-                    break;
+            const int sl = i % NSL;  // tile i's accumulator slot
+            bool ok = mbar_wait(&acc_full[sl], (i / NSL) & 1, abort_flag);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) {
+                if (lane == 0) {
+                    record_error(&g_tc_error, kErrWaitResult);
+                    *abort_flag = 1;
                 }
-                tc_fence_after();
-                float f[M::SUB_BLOCKS / 2][16];
-                epilogue_load<SPLIT>(lane_base + col, half, f);
-                // accumulators read: the issuer may refill them while we store
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) slots.release(acc_empty, mask);
-                slots.used(mask);
-                epilogue_store<SPLIT>(o, f, h, half, m, Y0, X0);
+                stop = true;
+                break;
             }
+            tc_fence_after();
+            float f[M::SUB_BLOCKS / 2][16];
+            epilogue_load<SPLIT>(lane_base + (uint32_t)(sl * Mode<false>::ACC), half, f);
+            // accumulators read: the issuer may refill them while we store
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[sl]);
+            epilogue_store<SPLIT>(o, f, 0, half, m, Y0, X0);
         }
     }
 
@@ -571,7 +568,7 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     for (int k = 0; k < C::NDY * C::NDY; k++) p.coef[k] = B[k];
     const int grid = p.n_tiles < g_num_sms ? p.n_tiles : g_num_sms;
     if constexpr (SPLIT) tc_split_ring_kernel<S><<<grid, kRingThreads, C::SMEM, s>>>(p);
-    else tc_sweep_kernel<S, SPLIT><<<grid, kSweepThreads, C::SMEM, s>>>(p);
+    else tc_sweep_kernel<S, SPLIT><<<grid, Sweep<S>::THREADS, C::SMEM, s>>>(p);
     return cudaGetLastError();
 }
 
