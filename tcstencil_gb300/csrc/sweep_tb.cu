@@ -50,7 +50,13 @@ constexpr int kInPlane = kInPanels * kChunkBytes;    // one staged input plane
 constexpr int kMidPlane = kMidPanels * kChunkBytes;  // one intermediate plane
 constexpr int kTbGroups = 3;                          // epilogue block groups
 constexpr int kTbEpiWarps = 4 * kTbGroups;            // a lane quarter each
-constexpr int kTbThreads = 32 * (2 + kTbEpiWarps);
+// MMA issuer warps 1 and 2 take alternate windows (G % 2), as in the
+// single-step split kernel: both wait for every stage fill and every
+// intermediate, in order, and commit the stage after step 1 (the stage is
+// free when both have); an issuer's previous region wait, two windows back,
+// already covered the release before the one it now needs.
+constexpr int kTbIssuers = 2;
+constexpr int kTbThreads = 32 * (1 + kTbIssuers + kTbEpiWarps);
 
 template <int S>
 struct TbCfg {
@@ -109,14 +115,14 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
     if (threadIdx.x == 0) {
         for (int s = 0; s < kTbStages; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
+            mbar_init(&empty[s], kTbIssuers);
         }
         mbar_init(inter_ready, kTbEpiWarps);
         for (int r = 0; r < kTbRing; r++) {
             mbar_init(&win_full[r], 1);
             mbar_init(&win_empty[r], kTbEpiWarps);
         }
-        mbar_init(drain, 1);
+        mbar_init(drain, kTbIssuers);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -188,9 +194,10 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
                 }
             }
         }
-    } else if (warp == 1) {
+    } else if (warp <= kTbIssuers) {
         // ---------------------------------------------------- MMA issuer ---
         if (lane == 0) {
+            const int id = warp - 1;  // takes the windows G with G % 2 == id
             const uint32_t band = smem_u32(band_base);
             int G = 0;
             bool issued_any = false, stop = false;
@@ -199,6 +206,7 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
             auto run_step = [&](uint64_t a_hi0, int lo_bytes, int nwin) {
 #pragma unroll 1
                 for (int w = 0; w < nwin; w++, G++) {
+                    if (G % kTbIssuers != id) continue;
                     const int r = G % kTbRing;
                     if (!mbar_wait(&win_empty[r], ((G / kTbRing) & 1) ^ 1, abort_flag)) {
                         record_error(&g_tb_error, kErrWaitAccum);
@@ -234,21 +242,22 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
                 tc_fence_after();
                 run_step(mid_desc, kMidPlane, kS2Windows);
             }
-            if (issued_any) {
-                umma_commit(drain);
-                const uint64_t t0 = global_timer_ns();
-                while (!mbar_try_wait(drain, 0)) {
-                    if (global_timer_ns() - t0 > kWaitLimitNs) {
-                        record_error(&g_tb_error, kErrWaitDrain);
-                        break;
-                    }
+            // both issuers commit (one with nothing in flight completes at
+            // once), so the drain phase always completes
+            (void)issued_any;
+            umma_commit(drain);
+            const uint64_t t0 = global_timer_ns();
+            while (!mbar_try_wait(drain, 0)) {
+                if (global_timer_ns() - t0 > kWaitLimitNs) {
+                    record_error(&g_tb_error, kErrWaitDrain);
+                    break;
                 }
             }
         }
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;
-        const int grp = (warp - 2) >> 2;  // block group
+        const int grp = (warp - 1 - kTbIssuers) >> 2;  // block group
         const int m = q * 32 + lane;  // M row of the step (intermediate row Y0 - r + m)
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
         TileOut o;
