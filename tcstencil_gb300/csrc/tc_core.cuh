@@ -31,10 +31,9 @@ using StageHalo2 = Staging<kChunkBytes, 2>;
 using StageLines = Staging<(kTile + 8) * 16, 4>;
 constexpr int kBandElems = 32 * 16;             // one 16(K) x 32(N) FP16 band
 constexpr int kBandBytes = kBandElems * 2;
-constexpr int kEpiWarps = 8;                    // two warpgroups, one per column half
-constexpr int kThreads = 32 * (2 + kEpiWarps);  // producer, MMA issuer, epilogue
+constexpr int kEpiWarps = 8;                    // plain: two warpgroups, one per column half
 constexpr int kTmemCols = 512;                  // two accumulator slots of 256 columns
-constexpr int kSlotCols = 256;
+constexpr int kSlotCols = 256;                  // AccSlots: two slots of the batched FP16 items
 constexpr uint32_t kIdesc = idesc_f16_f32(128, 32);
 constexpr uint32_t kIdescStack = idesc_f16_f32(128, 96);
 
