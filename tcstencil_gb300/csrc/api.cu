@@ -642,12 +642,14 @@ struct tcs_pipe_s {
     tcs_plan plan[2] = {nullptr, nullptr};
     cudaStream_t stream[2] = {nullptr, nullptr};
     cudaEvent_t done[2] = {nullptr, nullptr};
+    cudaEvent_t swept[2] = {nullptr, nullptr};  // a slot's sweeps have finished
     int *d_exp = nullptr;  // [2] split scale exponents
     long long submitted = 0;
     ~tcs_pipe_s() {
         for (int k = 0; k < 2; k++) {
             if (stream[k]) cudaStreamSynchronize(stream[k]);
             if (done[k]) cudaEventDestroy(done[k]);
+            if (swept[k]) cudaEventDestroy(swept[k]);
             if (stream[k]) cudaStreamDestroy(stream[k]);
             if (plan[k]) tcs_plan_destroy(plan[k]);
         }
@@ -699,6 +701,7 @@ int tcs_pipe_create(const tcs_problem *pr, tcs_pipe *out) {
         st = tcs_plan_create(pr, &q->plan[k]);
         if (!st) st = cuda_status(cudaStreamCreateWithFlags(&q->stream[k], cudaStreamNonBlocking), "cudaStreamCreate");
         if (!st) st = cuda_status(cudaEventCreateWithFlags(&q->done[k], cudaEventDisableTiming), "cudaEventCreate");
+        if (!st) st = cuda_status(cudaEventCreateWithFlags(&q->swept[k], cudaEventDisableTiming), "cudaEventCreate");
     }
     if (!st) st = cuda_status(cudaMalloc(&q->d_exp, 2 * sizeof(int)), "cudaMalloc(exp)");
     if (st) return st;
@@ -718,7 +721,14 @@ int tcs_pipe_submit(tcs_pipe q, const float *h_in, float *h_out, int steps) {
     int st = TCS_OK;
     if (q->submitted >= 2) st = cuda_status(cudaEventSynchronize(q->done[k]), "cudaEventSynchronize");
     if (!st) st = pipe_upload(q->plan[k], q->d_exp + k, h_in, s);
+    // Sweeps take turns: a slot's sweeps start after the previous
+    // submission's, so that only copies (and the small pack and unpack
+    // kernels) overlap them.  Two sets of persistent sweeps sharing the SMs
+    // would each wait on CTAs of the other.
+    if (!st && q->submitted >= 1)
+        st = cuda_status(cudaStreamWaitEvent(s, q->swept[k ^ 1], 0), "cudaStreamWaitEvent");
     if (!st) st = tcs_plan_run(q->plan[k], steps, 1, s);
+    if (!st) st = cuda_status(cudaEventRecord(q->swept[k], s), "cudaEventRecord");
     if (!st) st = pipe_download(q->plan[k], q->d_exp + k, h_out, s);
     if (!st) st = cuda_status(cudaEventRecord(q->done[k], s), "cudaEventRecord");
     if (!st) q->submitted++;

@@ -138,6 +138,9 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
+    // the previous step's CTAs may still run: planes only after pdl_wait
+    pdl_launch_dependents();
+    pdl_wait();
 
     auto tile_origin = [&](int i, int &Y0, int &X0) {
         const int t = (int)blockIdx.x + i * (int)gridDim.x;
@@ -419,8 +422,7 @@ cudaError_t launch_tb(const GridGeom &g, const float *B, const uint16_t *in_hi,
     p.out_lo = out_lo;
     for (int k = 0; k < 25; k++) p.coef[k] = k < C::NDY * C::NDY ? B[k] : 0.0f;
     const int grid = p.n_tiles < g_tb_sms ? p.n_tiles : g_tb_sms;
-    tc_split_tb_kernel<S><<<grid, kTbThreads, C::SMEM, s>>>(p);
-    return cudaGetLastError();
+    return launch_step(tc_split_tb_kernel<S>, grid, kTbThreads, C::SMEM, s, p);
 }
 
 }  // namespace

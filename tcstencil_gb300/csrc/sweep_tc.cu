@@ -40,15 +40,17 @@
 // c3*hi, where cf*lo also carries the lo*(c - ch) term.  Both are combined in
 // FP32 with round-to-nearest in the epilogue.
 //
-// Pipeline (persistent, one CTA per SM, 11 warps):
+// Pipeline (persistent, one CTA per SM; plain form):
 //   warp 0       producer: one tensor-map load per plane of each tile into NS
 //                stages (StageLines: 136 rows, whole 128-byte lines)
-//   warps 1, 2   MMA issuers on alternate tiles (warp 1 also owns TMEM)
-//   warps 3..10  epilogue (two warpgroups, one per column half):
+//   warps 1..I   MMA issuers taking tiles in turn, I = 3 for radius-1 and 2
+//                for radius-2 stencils (warp 1 also owns TMEM)
+//   next 8       epilogue (two warpgroups, one per column half):
 //                TMEM -> registers -> FP16 -> global
-// Two accumulator slots let the epilogue of one tile overlap the MMAs of the
-// next; tile i uses slot i % 2, issued by warp 1 + i % 2.  Every wait is bounded; on timeout the kernel records an error
-// word, stops, drains its own copies and MMAs, frees TMEM and returns.
+// One accumulator slot per issuer lets the epilogue of one tile overlap the
+// MMAs of the next; tile i uses slot i % I, issued by warp 1 + i % I.  Every
+// wait is bounded; on timeout the kernel records an error word, stops,
+// drains its own copies and MMAs, frees TMEM and returns.
 #include "tc_core.cuh"
 
 namespace tcs {
@@ -162,6 +164,9 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
+    // the previous step's CTAs may still run: planes only after pdl_wait
+    pdl_launch_dependents();
+    pdl_wait();
 
     const int tiles_x = p.tiles_x;
     const int n_tiles = p.n_tiles;
@@ -378,6 +383,9 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
+    // the previous step's CTAs may still run: planes only after pdl_wait
+    pdl_launch_dependents();
+    pdl_wait();
 
     const int tiles_x = p.tiles_x;
     const int n_tiles = p.n_tiles;
@@ -567,9 +575,8 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     for (int k = 0; k < 25; k++) p.coef[k] = 0.0f;
     for (int k = 0; k < C::NDY * C::NDY; k++) p.coef[k] = B[k];
     const int grid = p.n_tiles < g_num_sms ? p.n_tiles : g_num_sms;
-    if constexpr (SPLIT) tc_split_ring_kernel<S><<<grid, kRingThreads, C::SMEM, s>>>(p);
-    else tc_sweep_kernel<S, SPLIT><<<grid, Sweep<S>::THREADS, C::SMEM, s>>>(p);
-    return cudaGetLastError();
+    if constexpr (SPLIT) return launch_step(tc_split_ring_kernel<S>, grid, kRingThreads, C::SMEM, s, p);
+    else return launch_step(tc_sweep_kernel<S, SPLIT>, grid, Sweep<S>::THREADS, C::SMEM, s, p);
 }
 
 template <bool SPLIT>

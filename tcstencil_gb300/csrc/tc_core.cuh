@@ -4,6 +4,8 @@
 // described at the top of sweep_tc.cu.
 #pragma once
 
+#include <stdlib.h>
+
 #include "tcs_device.cuh"
 #include "tcs_internal.h"
 
@@ -470,6 +472,34 @@ __device__ __forceinline__ void epilogue_store(const TileOut &o,
 #pragma unroll
     for (int gg = 0; gg < G; gg++)
         store_block<SPLIT>(o, f[gg], y, X0 + 16 * (h * M::SUB_BLOCKS + j0 + gg), fast, row_in);
+}
+
+// Launches a single-grid step kernel with programmatic stream serialization:
+// the next step's CTAs do their set-up (barriers, TMEM, bands) while this
+// step's last tiles finish, and wait in pdl_wait() before touching a plane.
+// Setting TCS_PDL=0 in the environment launches in plain stream order.
+inline bool pdl_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("TCS_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+template <typename Params>
+cudaError_t launch_step(void (*kernel)(Params), int grid, int threads, size_t smem,
+                        cudaStream_t s, const Params &p) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, p);
 }
 
 }  // namespace tc

@@ -38,6 +38,18 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
 // and clears every unit's word in tcs_device_error().
 __device__ __forceinline__ void record_error(int *word, int code) { atomicCAS(word, 0, code); }
 
+// ------------------------------------------ programmatic dependent launch ---
+// A step kernel launched with programmatic stream serialization may start
+// while the previous step is still running.  launch_dependents lets the next
+// launch in the stream begin once every CTA of this grid has passed it; wait
+// returns when the previous grid has completed and its stores are visible.
+// With no programmatic predecessor, wait returns at once.
+__device__ __forceinline__ void pdl_launch_dependents() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ------------------------------------------------------------- mbarrier ---
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
