@@ -80,7 +80,6 @@ struct BatchCfg {
 };
 constexpr int kBatchRingSlots = 5;  // split window regions in TMEM
 constexpr int kBatchRegion = 96;
-constexpr int kBatchWindows = kTile / 16 + 1;
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     unsigned v;
@@ -381,8 +380,9 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 const uint64_t a_hi0 = smem_desc(smem_u32(st), SG::CHUNK, 128);
                 const uint32_t band = smem_u32(st + C::PLANES * SG::PLANE);
                 if constexpr (SPLIT) {
+                    const int nwin = tile_windows(g.nx, (it.tile % g.tiles_x) * kTile);
 #pragma unroll 1
-                    for (int w = 0; w < kBatchWindows; w++, G++) {
+                    for (int w = 0; w < nwin; w++, G++) {
                         if ((G & 1) != id) continue;
                         const int r = G % kBatchRingSlots;
                         if (!mbar_wait(&acc_empty[r], ((G / kBatchRingSlots) & 1) ^ 1, abort_flag, wait_lim)) {
@@ -405,6 +405,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     } else {
                         tc_fence_after();
                         const uint32_t d = tmem_base + col;
+                        // all windows: FP16 items are bound by the producer, and a
+                        // second MMA sequence for edge tiles measured slower
                         if (g.r == 1) issue_subtile<1, false, SG>(a_hi0, band, d, 0);
                         else issue_subtile<2, false, SG>(a_hi0, band, d, 0);
                         slots.commit(acc_full, mask);
@@ -523,9 +525,10 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&acc_empty[(G0 + w) % kBatchRingSlots]);
                 };
-                ok = walk_windows(grp, C::GROUPS, kBatchWindows, ready, release, [&](int jb) {
+                const int nwin = tile_windows(g.nx, X0);
+                ok = walk_windows(grp, C::GROUPS, nwin, ready, release, [&](int jb) {
                     const int Ga = G0 + jb, Gb = Ga + 1;
-                    if (rows_out || X0 + 16 * jb >= g.nx) {  // all padding: release unread
+                    if (rows_out) {  // all padding: release unread
                         __syncwarp();
                         if (lane == 0) {
                             mbar_arrive(&acc_empty[Ga % kBatchRingSlots]);
@@ -545,7 +548,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     }
                     store_block<true>(o, f, y, X0 + 16 * jb, fast, row_in);
                 });
-                G0 += kBatchWindows;
+                G0 += nwin;
                 if (!ok) {
                     stop = true;
                     break;

@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
                 const uint64_t a_hi0 = smem_desc(
                     smem_u32(stage_base + (size_t)s * NP * SG::PLANE), SG::CHUNK, 128);
                 tc_fence_after();
-                issue_subtile<C::R, false, SG>(a_hi0, band, tmem_base + col, 0);
+                issue_plain_tile<C::R, SG>(a_hi0, band, tmem_base + col,
+                                           tile_windows(p.g.nx, (t % tiles_x) * kTile));
                 umma_commit(&acc_full[id]);
                 umma_commit(&empty[s]);
             }
@@ -272,6 +273,11 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
                 }
                 stop = true;
                 break;
+            }
+            if (X0 + 64 * half >= p.g.nx) {  // this half is all padding: release unread
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[sl]);
+                continue;
             }
             tc_fence_after();
             float f[M::SUB_BLOCKS / 2][16];
@@ -328,6 +334,9 @@ constexpr int kRingEpiWarps = 4 * kRingGroups;     // a lane quarter each
 #endif
 constexpr int kRingIssuers = TCS_SPLIT_ISSUERS;   // MMA issuer warps 1 .. kRingIssuers
 constexpr int kRingThreads = 32 * (1 + kRingIssuers + kRingEpiWarps);
+// Every tile computes all its windows: a runtime window count for the last
+// tile of a row slowed this epilogue-bound kernel by more than the skipped
+// MMAs saved (16386²: 380 -> 387 us per step).
 constexpr int kTileWindows = kTile / 16 + 1;
 static_assert(kRingSlots * kRegionCols <= kTmemCols, "window ring fits TMEM");
 

@@ -281,17 +281,29 @@ __device__ __forceinline__ void issue_split_window(uint64_t a_hi0, uint32_t band
     issue_split_window_at<R, SG>(a_hi0, band, d, 2 * wg);
 }
 
+// Windows a tile needs: output block j (columns X0 + 16j .. +15) takes
+// windows j and j + 1, and blocks from the grid's last column on are padding
+// (split: never stored; plain: stored only as the input copied back, the
+// cells being outside the update rectangle; padding keeps finite contents).
+// So a tile of a grid nx cells wide needs windows 0 .. nb, nb = its blocks
+// holding grid cells (kTile / 16 for every tile but the last of a row).
+__device__ __forceinline__ int tile_windows(int nx, int X0) {
+    const int nb = (nx - X0 + 15) >> 4;
+    return (nb < kTile / 16 ? nb : kTile / 16) + 1;
+}
+
 // MMAs of sub-tile h of a staged tile into accumulator columns from d.
 // a_hi0 is the descriptor of the stage's hi plane (lo follows at
 // +kPlaneStage); band is the shared-memory address of the stencil's bands.
 // Descriptors for base + offset are the base descriptor plus offset >> 4 (the
 // start-address field holds address >> 4 in its low bits).
 //  plain: even windows (disjoint outputs, the first of them initialising)
-//    before odd windows, which add into the overlaps.
+//    before odd windows, which add into the overlaps; NWIN windows (all, or
+//    the first half's, issue_plain_tile).
 //  split: per window and coefficient row, one N=96 MMA of hi with the stacked
 //    band (initialising its region on the first row) and one N=32 MMA of lo
 //    with cf into the region's middle part.
-template <int R, bool SPLIT, class SG = StageHalo2>
+template <int R, bool SPLIT, class SG = StageHalo2, int NWIN = Mode<SPLIT>::SUB_WIN>
 __device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint32_t band, uint32_t d, int h) {
     using M = Mode<SPLIT>;
     constexpr int NDY = 2 * R + 1;
@@ -304,7 +316,7 @@ __device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint32_t band, uin
                 const uint64_t b = b0 + (uint64_t)((dy * kBandBytes) >> 4);
                 const uint32_t acc = (parity == 1 || dy > 0) ? 1u : 0u;
 #pragma unroll
-                for (int w = parity; w < M::SUB_WIN; w += 2) {
+                for (int w = parity; w < NWIN; w += 2) {
                     const int wg = h * M::SUB_BLOCKS + w;  // window in the tile
                     const uint64_t a_off = (uint64_t)((2 * wg * SG::CHUNK + (SG::TOP - R + dy) * 16) >> 4);
                     umma_f16(d + 16 * w, a_hi0 + a_off, b, kIdesc, acc);
@@ -316,6 +328,18 @@ __device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint32_t band, uin
         for (int w = 0; w < M::SUB_WIN; w++)
             issue_split_window<R, SG>(a_hi0, band, d + split_region(w), h * M::SUB_BLOCKS + w);
     }
+}
+
+// A plain tile's MMAs: all windows, or, when the grid ends within the tile's
+// first 64 columns (nwin from tile_windows), only the windows of its first
+// column half, whose blocks are the only ones the epilogue reads.  Two
+// compile-time sequences: a window bound tested per MMA slowed the issuer.
+template <int R, class SG>
+__device__ __forceinline__ void issue_plain_tile(uint64_t a_hi0, uint32_t band, uint32_t d,
+                                                 int nwin) {
+    constexpr int HALF_WIN = Mode<false>::SUB_BLOCKS / 2 + 1;
+    if (nwin <= HALF_WIN) issue_subtile<R, false, SG, HALF_WIN>(a_hi0, band, d, 0);
+    else issue_subtile<R, false, SG>(a_hi0, band, d, 0);
 }
 
 // Epilogue, first half: this warp's accumulators of a sub-tile into
