@@ -144,14 +144,14 @@ def load_peaks():
 
 
 def load_traffic(stencil, engine, precision):
-    """DRAM bytes per launch from the committed ncu summary, if any."""
+    """DRAM bytes per step from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         d = json.load(f)
     e = d.get(f"{stencil}/{engine}/{precision}")
-    return e.get("dram_bytes_per_launch") if e else None
+    return e.get("dram_bytes_per_step") if e else None
 
 
 class ClockSampler:
@@ -447,11 +447,16 @@ def run_ours(args):
     (tmax,) = max_over_ranks([t])
     assert tcs.device_error() == 0
     value = ws * updates_per_step * args.steps / tmax / 1e9
-    launch_s = t / (args.steps * args.timesteps)
+    # the dominant kernel's launches: one per bench step when all timesteps
+    # run in one multi-step launch, else one per timestep (or step pair)
+    launches_per_run = plan.launches(args.timesteps)
+    steps_per_launch = args.timesteps / launches_per_run
+    launch_s = t / (args.steps * launches_per_run)
     bpu = BYTES_PER_UPDATE[args.precision]
-    achieved = bpu * args.interior * args.interior / launch_s / 1e9
+    achieved = bpu * args.interior * args.interior * steps_per_launch / launch_s / 1e9
     peak, peak_kind = load_peaks()
-    traffic = load_traffic(args.stencil, args.engine, args.precision)
+    traffic_step = load_traffic(args.stencil, args.engine, args.precision)
+    traffic = round(traffic_step * steps_per_launch) if traffic_step else None
 
     # e2e through the one-call C-ABI with pinned host buffers
     h_in = torch.from_numpy(A).pin_memory().numpy()
@@ -530,11 +535,13 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "peak_kind": peak_kind,
-                     "basis": f"{bpu} B per point-update x {args.interior}^2 updates per launch / "
-                              f"mean launch time {launch_s * 1e6:.2f} us (CUDA events)"},
+                     "basis": f"{bpu} B per point-update x {args.interior}^2 updates x "
+                              f"{steps_per_launch:g} steps per launch / mean launch time "
+                              f"{launch_s * 1e6:.2f} us (CUDA events); traffic = ncu DRAM bytes "
+                              f"per step x steps per launch"},
         "e2e": e2e,
         "e2e_pipelined": e2e_pipelined,
-        "gpu_launches": args.steps * args.timesteps,
+        "gpu_launches": args.steps * launches_per_run,
         "clocks": clocks,
         "tflops_useful": round(value * FLOPS_PER_UPDATE[args.stencil] / 1e3, 2),
         "comparators_gpts": extras,

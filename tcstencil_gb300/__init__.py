@@ -111,6 +111,8 @@ SIGNATURES = {
     "tcs_plan_state": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_SZ)]),
     "tcs_plan_set_coeffs": (_I, [_P, _P]),
     "tcs_plan_set_temporal_depth": (_I, [_P, _I]),
+    "tcs_plan_set_multistep": (_I, [_P, _I]),
+    "tcs_plan_launches": (_I, [_P, _I, _P]),
     "tcs_sweep_host": (_I, [_P, _P, ctypes.POINTER(Problem), _I]),
     "tcs_noalloc_scratch_bytes": (_SZ, []),
     "tcs_sweep_steps_noalloc": (_I, [ctypes.POINTER(StepArgs), _P, _P, _I, _P]),
@@ -310,6 +312,17 @@ class Plan:
 
     def set_temporal_depth(self, depth: int) -> None:
         _check(lib().tcs_plan_set_temporal_depth(self._h, int(depth)))
+
+    def launches(self, steps: int) -> int:
+        """Kernel launches run(steps) makes."""
+        n = ctypes.c_int(0)
+        _check(lib().tcs_plan_launches(self._h, int(steps), ctypes.byref(n)))
+        return n.value
+
+    def set_multistep(self, mode: int) -> None:
+        """Plain FP16 tensor plans: run(steps) as one launch (1), one launch
+        per step (0), or by grid size (-1, the default); same bits."""
+        _check(lib().tcs_plan_set_multistep(self._h, int(mode)))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -325,6 +325,21 @@ int tcs_sweep_step(const tcs_step_args *a, const void *d_in, const void *d_in_lo
 }  // extern "C"
 
 // ================================================================= plans ==
+namespace {
+
+// SM count of the device (read once).
+int device_sms() {
+    static const int n = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
+    return n;
+}
+
+}  // namespace
+
 struct tcs_plan_s {
     tcs_problem prob;
     float coeffs[25];
@@ -337,6 +352,7 @@ struct tcs_plan_s {
     float *staging = nullptr;   // ny*nx FP32, for host/row-major transfers
     cudaStream_t capture_stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, start state)
+    unsigned *rows_done = nullptr;  // plain tensor form: per tile row, for multi-step launches
 
     int planes() const { return prob.precision == TCS_PREC_SPLIT ? 2 : 1; }
 
@@ -352,6 +368,7 @@ struct tcs_plan_s {
                 if (p) cudaFree(p);
         if (staging) cudaFree(staging);
         if (d_max) cudaFree(d_max);
+        if (rows_done) cudaFree(rows_done);
         if (capture_stream) cudaStreamDestroy(capture_stream);
     }
 
@@ -372,13 +389,47 @@ struct tcs_plan_s {
                              static_cast<uint16_t *>(buf[1 - from][1]), s),
             "blocked sweep launch");
     }
-    // The state `steps` steps from `from` ends in: one flip per launch.
+    // Plain FP16 on the tensor engine runs all steps of a call in one
+    // launch, whose tiles of step j wait only for the neighbouring tile rows
+    // of step j-1 (tcs_plan_set_multistep; TCS_MULTI=0 in the environment:
+    // one launch per step).  Measured on GB300 (box2d2r, us per step, one
+    // launch per step -> one launch): 8196² 49.8 -> 42.2, 4096² 13.2 -> 10.4,
+    // 2048² 6.8 -> 6.9, 1026² 5.5 -> 6.3: small grids are latency-bound, and
+    // a step boundary between launches is quicker than the counters.
+    int multistep = -1;
+    bool multi() const {
+        static const bool on = [] {
+            const char *e = getenv("TCS_MULTI");
+            return !(e && e[0] == '0');
+        }();
+        if (!on || !rows_done || prob.engine != TCS_ENGINE_TENSOR || prob.precision != TCS_PREC_F16)
+            return false;
+        if (multistep >= 0) return multistep == 1;
+        const long long tiles = (long long)((g.ny + kTile - 1) / kTile) * ((g.nx + kTile - 1) / kTile);
+        return tiles > 2LL * device_sms();
+    }
+    int steps_in_one(int steps, int from, cudaStream_t s) {
+        const int tiles_y = (g.ny + kTile - 1) / kTile;
+        int st = cuda_status(
+            cudaMemsetAsync(rows_done, 0, (size_t)tiles_y * kRowCounterStride * sizeof(unsigned), s),
+            "row counter reset");
+        if (st) return st;
+        return cuda_status(
+            launch_tc_f16_steps(g, prob.stencil, coeffs, static_cast<const uint16_t *>(buf[from][0]),
+                                static_cast<uint16_t *>(buf[1 - from][0]), steps, rows_done, s),
+            "multi-step sweep launch");
+    }
+    // The state `steps` steps from `from` ends in: one flip per step.
     int final_state(int steps, int from) const {
         const int launches = pairs() ? steps / 2 + steps % 2 : steps;
         return from ^ (launches & 1);
     }
     // Enqueues `steps` steps from state `from`; returns the final state in *to.
     int enqueue(int steps, int from, cudaStream_t s, int *to) {
+        if (steps >= 2 && multi()) {
+            *to = from ^ (steps & 1);
+            return steps_in_one(steps, from, s);
+        }
         int st = TCS_OK;
         for (int t = 0; t < steps && !st;) {
             if (pairs() && steps - t >= 2) {
@@ -434,6 +485,12 @@ int tcs_plan_create(const tcs_problem *pr, tcs_plan *out) {
     if (pr->engine == TCS_ENGINE_TENSOR) {
         st = cuda_status(tc_prepare(pr->stencil, pr->precision == TCS_PREC_SPLIT), "tensor kernel set-up");
         if (st) return st;
+        if (pr->precision == TCS_PREC_F16) {
+            const int tiles_y = (pr->ny + kTile - 1) / kTile;
+            st = cuda_status(cudaMalloc(&p->rows_done, (size_t)tiles_y * kRowCounterStride * sizeof(unsigned)),
+                             "cudaMalloc(rows)");
+            if (st) return st;
+        }
     }
     *out = p.release();
     return TCS_OK;
@@ -525,6 +582,22 @@ int tcs_plan_set_temporal_depth(tcs_plan p, int depth) {
         p->temporal_depth = depth;
         p->drop_graphs();  // graphs hold the launch sequence
     }
+    return TCS_OK;
+}
+
+int tcs_plan_set_multistep(tcs_plan p, int mode) {
+    if (!p || mode < -1 || mode > 1) return fail(TCS_ERR_INVALID, "tcs_plan_set_multistep: mode is -1, 0 or 1");
+    if (mode != p->multistep) {
+        p->multistep = mode;
+        p->drop_graphs();  // graphs hold the launch sequence
+    }
+    return TCS_OK;
+}
+
+int tcs_plan_launches(tcs_plan p, int steps, int *launches) {
+    if (!p || steps < 0 || !launches) return fail(TCS_ERR_INVALID, "tcs_plan_launches: bad arguments");
+    if (steps >= 2 && p->multi()) *launches = 1;
+    else *launches = p->pairs() ? steps / 2 + steps % 2 : steps;
     return TCS_OK;
 }
 

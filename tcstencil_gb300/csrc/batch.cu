@@ -81,18 +81,6 @@ struct BatchCfg {
 constexpr int kBatchRingSlots = 5;  // split window regions in TMEM
 constexpr int kBatchRegion = 96;
 
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Completion count with release semantics: the warp's stores (ordered before
-// this lane's by the preceding __syncwarp) are visible at GPU scope before
-// the count, for the consumer's acquire load of it.
-__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
-    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 
 // A bounded wait gave up: record the code in the launch's error word (which

@@ -83,9 +83,12 @@ struct Sweep {
     static constexpr int ISSUERS = stencil_r(S) == 1 ? 3 : 2;
     static constexpr int SLOTS = ISSUERS;
     static constexpr int STAGES = ISSUERS == 2 ? 4 : 3;
-    static constexpr int THREADS = 32 * (1 + ISSUERS + kEpiWarps);
+    static constexpr int SIGNAL_WARP = 1 + ISSUERS + kEpiWarps;  // several steps: row counts
+    static constexpr int THREADS = 32 * (SIGNAL_WARP + 1);
+    static constexpr int SIG_SLOTS = 4;  // items the epilogue may finish ahead of the signal warp
     static_assert(SLOTS * Mode<false>::ACC <= kTmemCols, "accumulator slots fit TMEM");
     static_assert(STAGES % ISSUERS == 0, "each stage holds one issuer's tiles");
+    static_assert(SIG_SLOTS > SLOTS, "epilogue warps are at most SLOTS items apart");
 };
 
 template <int S, bool SPLIT>
@@ -102,8 +105,13 @@ struct Cfg {
 
 struct TcParams {
     CUtensorMap map_hi, map_lo;     // input planes (encode_panel_map)
+    CUtensorMap map_out;            // plain, several steps: the output plane (odd steps' input)
     GridGeom g;
     int tiles_x, n_tiles;
+    int steps;                      // plain: steps of this launch (1 for the split kernels)
+    unsigned *rows_done;            // plain, several steps: per tile row (every
+                                    // kRowCounterStride), epilogue-warp completions
+                                    // over the launch (zeroed before it)
     const uint16_t *in_hi, *in_lo;  // input planes
     uint16_t *out_hi, *out_lo;
     float coef[25];                 // n x n, row-major
@@ -130,8 +138,11 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
     uint64_t *acc_full = bars + 2 * NS;         // [NSL]
     uint64_t *acc_empty = acc_full + NSL;       // [NSL]
     uint64_t *drain = acc_empty + NSL;          // [1]
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
-    static_assert((2 * NS + 2 * NSL + 1) * 8 + 8 <= 256, "barrier area");
+    constexpr int NSG = Sweep<S>::SIG_SLOTS;
+    uint64_t *sig_done = drain + 1;             // [NSG] an item's stores are issued
+    uint64_t *sig_free = sig_done + NSG;        // [NSG] the signal warp has taken it
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sig_free + NSG);
+    static_assert((2 * NS + 2 * NSL + 1 + 2 * NSG) * 8 + 8 <= 256, "barrier area");
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5;
@@ -149,6 +160,10 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
             mbar_init(&acc_empty[b], kEpiWarps);
         }
         mbar_init(drain, Sweep<S>::ISSUERS);
+        for (int b = 0; b < NSG; b++) {
+            mbar_init(&sig_done[b], kEpiWarps);
+            mbar_init(&sig_free[b], 1);
+        }
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -170,23 +185,86 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
 
     const int tiles_x = p.tiles_x;
     const int n_tiles = p.n_tiles;
+    const int tiles_y = n_tiles / tiles_x;
+    const int n_items = p.steps * n_tiles;  // (step, tile), step-major; CTA b takes b, b + grid, ...
 
     if (warp == 0) {
         // ------------------------------------------------------ producer ---
         if (lane == 0) {
             int i = 0;
             int last_issued = -1;
-            for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, i++) {
+            // rows up to ver_hi of step ver_s (from this CTA's first tile row
+            // of that step on) are known complete
+            int ver_s = -1, ver_hi = -1;
+            const unsigned per_row = (unsigned)(kEpiWarps * tiles_x);
+            constexpr int kBurst = 8;  // rows read per poll
+            for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++) {
+                const int step = k / n_tiles;
+                const int t = k - step * n_tiles;
+                const int ty = t / tiles_x;
                 const int s = i % NS;
                 const uint32_t ph = (i / NS) & 1;
+                if (step > 0) {
+                    // Rows ty-1 .. ty+1 of the previous step: the tile's input
+                    // (it wrote them) and the plane this tile overwrites (it read
+                    // them).  A tile row's counts arrive in step order, since a
+                    // tile starts only after its own row finished the step before.
+                    const int lo = ty > 0 ? ty - 1 : 0;
+                    const int hi = ty + 1 < tiles_y ? ty + 1 : tiles_y - 1;
+                    if (ver_s != step - 1 || lo > ver_hi + 1) {
+                        ver_s = step - 1;
+                        ver_hi = lo - 1;
+                    }
+                    if (hi > ver_hi) {
+                        // One burst of relaxed reads over the next kBurst rows:
+                        // the known range grows over every complete one, so the
+                        // next tiles (a few rows further) usually need no poll.
+                        const unsigned target = (unsigned)step * per_row;
+                        const int first = ver_hi + 1;
+                        unsigned v[kBurst];
+#pragma unroll
+                        for (int b = 0; b < kBurst; b++)
+                            v[b] = first + b < tiles_y
+                                       ? ld_relaxed(p.rows_done + (first + b) * kRowCounterStride)
+                                       : 0u;
+                        int x = first;  // rows first .. x-1 are complete
+#pragma unroll
+                        for (int b = 0; b < kBurst; b++)
+                            if (x == first + b && first + b < tiles_y && v[b] >= target) x++;
+                        bool ok = true;
+                        for (int r = x; r <= hi && ok; r++) {  // rows this tile still needs
+                            const unsigned *ctr = p.rows_done + r * kRowCounterStride;
+                            const uint64_t t0 = global_timer_ns();
+                            while (ld_relaxed(ctr) < target) {
+                                if (*(volatile int *)&g_tc_error != 0 ||
+                                    global_timer_ns() - t0 > kWaitLimitNs) {
+                                    ok = false;
+                                    break;
+                                }
+                                __nanosleep(32);
+                            }
+                        }
+                        if (!ok) {
+                            record_error(&g_tc_error, kErrWaitDep);
+                            *abort_flag = 1;
+                            break;
+                        }
+                        ver_hi = x - 1 > hi ? x - 1 : hi;
+                        // acquire for the counts read above; then the tensor copies
+                        // below, which read what other SMs stored
+                        fence_acq_rel_gpu();
+                        fence_proxy_async_global();
+                    }
+                }
+                // (the poll above overlaps the wait for a free stage)
                 if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
                     record_error(&g_tc_error, kErrWaitEmpty);
                     *abort_flag = 1;
                     break;
                 }
                 mbar_arrive_expect_tx(&full[s], NP * SG::PLANE);
-                load_tile_map(&p.map_hi, &p.map_lo, NP, (t / tiles_x) * kTile,
-                              (t % tiles_x) * kTile, stage_base + (size_t)s * NP * SG::PLANE,
+                load_tile_map((step & 1) ? &p.map_out : &p.map_hi, &p.map_lo, NP, ty * kTile,
+                              (t - ty * tiles_x) * kTile, stage_base + (size_t)s * NP * SG::PLANE,
                               &full[s]);
                 last_issued = i;
             }
@@ -211,8 +289,9 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
             const uint32_t band = smem_u32(band_base);
             const uint32_t col = (uint32_t)(id * Mode<false>::ACC);  // this issuer's slot
             int i = id;
-            for (int t = blockIdx.x + id * (int)gridDim.x; t < n_tiles && !stop;
-                 t += Sweep<S>::ISSUERS * (int)gridDim.x, i += Sweep<S>::ISSUERS) {
+            for (int k = blockIdx.x + id * (int)gridDim.x; k < n_items && !stop;
+                 k += Sweep<S>::ISSUERS * (int)gridDim.x, i += Sweep<S>::ISSUERS) {
+                const int t = k % n_tiles;
                 const int s = i % NS;  // one of this issuer's stages
                 if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
                     record_error(&g_tc_error, kErrWaitFull);
@@ -245,6 +324,43 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
                 }
             }
         }
+    } else if (warp == Sweep<S>::SIGNAL_WARP) {
+        // -------------------------------------------------------- signal ---
+        // Several steps: once all epilogue warps have issued an item's stores
+        // (sig_done, release at CTA scope), the item's count for its tile row
+        // is published at GPU scope behind a fence that covers those stores.
+        // Items already finished are batched behind one fence (it waits for
+        // the stores to complete); before waiting for an unfinished item the
+        // batch is flushed, so no count is ever held while this thread waits.
+        if (p.rows_done && lane == 0) {
+            constexpr int kBatch = 4;
+            int pend[kBatch];
+            int n_pend = 0;
+            auto flush = [&]() {
+                if (!n_pend) return;
+                fence_acq_rel_gpu();
+                for (int j = 0; j < n_pend; j++)
+                    red_relaxed_add(p.rows_done + pend[j] * kRowCounterStride, kEpiWarps);
+                n_pend = 0;
+            };
+            int i = 0;
+            for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++) {
+                const int d = i % NSG;
+                const uint32_t ph = (i / NSG) & 1;
+                if (!mbar_try_wait(&sig_done[d], ph)) {
+                    flush();
+                    if (!mbar_wait(&sig_done[d], ph, abort_flag)) {
+                        record_error(&g_tc_error, kErrWaitResult);
+                        *abort_flag = 1;
+                        break;
+                    }
+                }
+                mbar_arrive(&sig_free[d]);
+                pend[n_pend++] = (k % n_tiles) / tiles_x;
+                if (n_pend == kBatch) flush();
+            }
+            flush();
+        }
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;            // TMEM lane quarter of this warp
@@ -260,9 +376,15 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
         bool stop = false;
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
         int i = 0;
-        for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
-            const int Y0 = (t / tiles_x) * kTile;
-            const int X0 = (t % tiles_x) * kTile;
+        for (int k = blockIdx.x; k < n_items && !stop; k += gridDim.x, i++) {
+            const int step = k / n_tiles;
+            const int t = k - step * n_tiles;
+            const int ty = t / tiles_x;
+            const int Y0 = ty * kTile;
+            const int X0 = (t - ty * tiles_x) * kTile;
+            // odd steps run from the output plane back into the input plane
+            o.in_hi = (step & 1) ? p.out_hi : p.in_hi;
+            o.out_hi = (step & 1) ? const_cast<uint16_t *>(p.in_hi) : p.out_hi;
             const int sl = i % NSL;  // tile i's accumulator slot
             bool ok = mbar_wait(&acc_full[sl], (i / NSL) & 1, abort_flag);
             ok = __all_sync(0xffffffffu, ok);
@@ -277,16 +399,33 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
             if (X0 + 64 * half >= p.g.nx) {  // this half is all padding: release unread
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&acc_empty[sl]);
-                continue;
+            } else {
+                tc_fence_after();
+                float f[M::SUB_BLOCKS / 2][16];
+                epilogue_load<SPLIT>(lane_base + (uint32_t)(sl * Mode<false>::ACC), half, f);
+                // accumulators read: the issuer may refill them while we store
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[sl]);
+                epilogue_store<SPLIT>(o, f, 0, half, m, Y0, X0);
             }
-            tc_fence_after();
-            float f[M::SUB_BLOCKS / 2][16];
-            epilogue_load<SPLIT>(lane_base + (uint32_t)(sl * Mode<false>::ACC), half, f);
-            // accumulators read: the issuer may refill them while we store
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&acc_empty[sl]);
-            epilogue_store<SPLIT>(o, f, 0, half, m, Y0, X0);
+            if (p.rows_done) {
+                // this warp's stores of the tile are issued: hand the count to
+                // the signal warp, whose release then covers them (a release
+                // here would hold the warp until its stores completed)
+                const int d = i % NSG;
+                bool okd = mbar_wait(&sig_free[d], ((i / NSG) & 1) ^ 1, abort_flag);
+                okd = __all_sync(0xffffffffu, okd);
+                if (!okd) {
+                    if (lane == 0) {
+                        record_error(&g_tc_error, kErrWaitResult);
+                        *abort_flag = 1;
+                    }
+                    break;
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&sig_done[d]);
+            }
         }
     }
 
@@ -563,9 +702,14 @@ cudaError_t prepare_tc() {
     return cudaSuccess;
 }
 
+// One launch of `steps` steps (plain form; the split kernels take one).  With
+// several, step j reads in_hi for even j and out_hi for odd j and writes the
+// other; rows_done holds one zeroed counter per tile row (kRowCounterStride apart), and the launch is
+// cooperative, so that all CTAs of the static tile order are resident at once.
 template <int S, bool SPLIT>
 cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
-                      const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s) {
+                      const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s,
+                      int steps = 1, unsigned *rows_done = nullptr) {
     using C = Cfg<S, SPLIT>;
     cudaError_t pe = prepare_tc<S, SPLIT>();
     if (pe != cudaSuccess) return pe;
@@ -581,21 +725,35 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     if (me != cudaSuccess) return me;
     p.out_hi = out_hi;
     p.out_lo = out_lo;
+    p.steps = 1;
+    p.rows_done = nullptr;
+    p.map_out = p.map_hi;
+    if (steps > 1) {
+        if (SPLIT || !rows_done) return cudaErrorInvalidValue;
+        me = encode_panel_map(out_hi, g.p16, &p.map_out);
+        if (me != cudaSuccess) return me;
+        p.steps = steps;
+        p.rows_done = rows_done;
+    }
     for (int k = 0; k < 25; k++) p.coef[k] = 0.0f;
     for (int k = 0; k < C::NDY * C::NDY; k++) p.coef[k] = B[k];
-    const int grid = p.n_tiles < g_num_sms ? p.n_tiles : g_num_sms;
+    const long long items = (long long)p.n_tiles * p.steps;
+    const int grid = items < g_num_sms ? (int)items : g_num_sms;
     if constexpr (SPLIT) return launch_step(tc_split_ring_kernel<S>, grid, kRingThreads, C::SMEM, s, p);
-    else return launch_step(tc_sweep_kernel<S, SPLIT>, grid, Sweep<S>::THREADS, C::SMEM, s, p);
+    else
+        return launch_step(tc_sweep_kernel<S, SPLIT>, grid, Sweep<S>::THREADS, C::SMEM, s, p,
+                           p.steps > 1);
 }
 
 template <bool SPLIT>
 cudaError_t dispatch_tc(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
-                        const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s) {
+                        const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s,
+                        int steps = 1, unsigned *rows_done = nullptr) {
     switch (stencil) {
-    case TCS_STAR2D1R: return launch_tc<TCS_STAR2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s);
-    case TCS_STAR2D2R: return launch_tc<TCS_STAR2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s);
-    case TCS_BOX2D1R: return launch_tc<TCS_BOX2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s);
-    case TCS_BOX2D2R: return launch_tc<TCS_BOX2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s);
+    case TCS_STAR2D1R: return launch_tc<TCS_STAR2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
+    case TCS_STAR2D2R: return launch_tc<TCS_STAR2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
+    case TCS_BOX2D1R: return launch_tc<TCS_BOX2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
+    case TCS_BOX2D2R: return launch_tc<TCS_BOX2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -622,6 +780,11 @@ cudaError_t tc_take_error(int *code) {
 cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
                           uint16_t *out, cudaStream_t s) {
     return dispatch_tc<false>(g, stencil, B, in, nullptr, out, nullptr, s);
+}
+
+cudaError_t launch_tc_f16_steps(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
+                                uint16_t *out, int steps, unsigned *rows_done, cudaStream_t s) {
+    return dispatch_tc<false>(g, stencil, B, in, nullptr, out, nullptr, s, steps, rows_done);
 }
 
 cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,

@@ -510,19 +510,26 @@ inline bool pdl_enabled() {
     return on;
 }
 
+// cooperative: a launch of several steps, whose CTAs wait on one another's
+// tile rows, must have all its CTAs resident at once (and is not overlapped).
 template <typename Params>
 cudaError_t launch_step(void (*kernel)(Params), int grid, int threads, size_t smem,
-                        cudaStream_t s, const Params &p) {
+                        cudaStream_t s, const Params &p, bool cooperative = false) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3((unsigned)threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    if (cooperative) {
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+    } else {
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+    }
     cfg.attrs = attr;
-    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cfg.numAttrs = (cooperative || pdl_enabled()) ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kernel, p);
 }
 

@@ -16,7 +16,7 @@ enum DeviceError : int {
     kErrWaitAccum = 3,    // MMA issuer waited too long for a free accumulator
     kErrWaitResult = 4,   // epilogue waited too long for an accumulator
     kErrWaitDrain = 5,    // final drain of in-flight copies / MMAs timed out
-    kErrWaitDep = 6,      // batched run: a step waited too long for its previous step
+    kErrWaitDep = 6,      // a step waited too long for its previous step (batch, multi-step)
 };
 
 // Upper bound on any single in-kernel wait: the hardware finishes each awaited
@@ -37,6 +37,36 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
 // wait that gives up writes its code there (first error wins); the host reads
 // and clears every unit's word in tcs_device_error().
 __device__ __forceinline__ void record_error(int *word, int code) { atomicCAS(word, 0, code); }
+
+// -------------------------------------------- cross-CTA completion counts ---
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Completion count with release semantics: the stores ordered before it (this
+// thread's, and its warp's or CTA's through the barrier that precedes it) are
+// visible at GPU scope before the count, for the consumer's acquire load.
+__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Relaxed read of a count; a following fence_acq_rel_gpu makes it an acquire.
+__device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Relaxed count, published by a preceding fence_acq_rel_gpu (release pattern).
+__device__ __forceinline__ void red_relaxed_add(unsigned *p, unsigned v) {
+    asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void fence_acq_rel_gpu() {
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
 
 // ------------------------------------------ programmatic dependent launch ---
 // A step kernel launched with programmatic stream serialization may start

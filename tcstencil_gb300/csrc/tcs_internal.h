@@ -130,6 +130,13 @@ cudaError_t tc_prepare(int stencil, bool split);
 
 cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
                           uint16_t *out, cudaStream_t s);
+// Several plain steps in one launch (in -> out -> in ...); rows_done: one
+// counter per tile row (ceil(ny / 128)) every kRowCounterStride unsigneds,
+// zeroed before the launch.  Each counter has its own 128-byte line: every SM
+// polls and counts them, and on shared lines those accesses serialise.
+constexpr int kRowCounterStride = 32;
+cudaError_t launch_tc_f16_steps(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
+                                uint16_t *out, int steps, unsigned *rows_done, cudaStream_t s);
 cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
                             const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
                             cudaStream_t s);

@@ -70,6 +70,7 @@ def test_invalid_arguments_are_rejected_before_any_device_work(tcs):
     with pytest.raises(tcs.TcsError):  # n does not match the stencil
         tcs.host_code(np.zeros((32, 32), np.float32), np.zeros((3, 3), np.float32),
                       np.zeros((32, 32), np.float32), 32, 3, "box2d2r")
+    assert tcs.lib().tcs_plan_set_multistep(None, 1) == tcs.TCS_ERR_INVALID
 
 
 @pytest.mark.parametrize("stencil", STENCILS)
