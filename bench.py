@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--serve-round-steps", type=int, default=None,
                     help="steps per request per server round (default: autotuned or 16)")
     ap.add_argument("--batch-grids", type=int, default=512)
+    ap.add_argument("--multistep", type=int, default=-1, choices=(-1, 0, 1),
+                    help="plain FP16 tensor plans: all timesteps in one launch (1), one launch "
+                         "per timestep (0), or by grid size (-1, default)")
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: upload the grid, run --timesteps single-step "
                          "launches (no graph), exit; for ncu captures")
@@ -93,6 +96,7 @@ def run_profile(args):
     A, B = make_inputs(n, args.stencil, 1000)
     plan = tcs.Plan(n, n, args.stencil, B, engine=args.engine, precision=args.precision,
                     temporal_depth=args.temporal_depth)
+    plan.set_multistep(args.multistep)
     plan.upload(A)
     plan.run(args.timesteps, use_graph=False)
     torch.cuda.synchronize()
@@ -427,6 +431,7 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     plan = tcs.Plan(n, n, args.stencil, B, engine=args.engine, precision=args.precision,
                     temporal_depth=args.temporal_depth)
+    plan.set_multistep(args.multistep)
     plan.upload(A)
     torch.cuda.synchronize()
     updates_per_step = args.interior * args.interior * args.timesteps
