@@ -214,12 +214,13 @@ int tcs_plan_set_coeffs(tcs_plan plan, const float *coeffs);
  * steps per launch, intermediate kept on chip; split precision on the tensor
  * engine).  Results are bit-identical either way; the autotuner picks. */
 int tcs_plan_set_temporal_depth(tcs_plan plan, int depth);
-/* Plain FP16 on the tensor engine: run(steps >= 2) as ONE launch whose tiles
- * of step j wait only for the neighbouring tile rows of step j-1 (per-row
- * completion counts), instead of one launch per step.  mode -1 (default):
- * when a step has more than two tiles per SM; 0: never; 1: always.  Results
- * are bit-identical either way.  TCS_MULTI=0 in the environment turns it off
- * for the process. */
+/* Tensor engine (FP16 or split, temporal depth 1): run(steps >= 2) as ONE
+ * launch whose tiles of step j wait only for the neighbouring tile rows of
+ * step j-1 (per-row completion counts), instead of one launch per step.
+ * mode -1 (default): FP16 when a step has more than two tiles per SM, split
+ * when it has more than one and at most twelve (where each measured
+ * faster); 0: never; 1: always.  Results are bit-identical either way.
+ * TCS_MULTI=0 in the environment turns it off for the process. */
 int tcs_plan_set_multistep(tcs_plan plan, int mode);
 /* Kernel launches tcs_plan_run(plan, steps, ...) makes (the device work of
  * one call: 1 for a multi-step launch, else one per step or step pair). */

@@ -320,8 +320,9 @@ class Plan:
         return n.value
 
     def set_multistep(self, mode: int) -> None:
-        """Plain FP16 tensor plans: run(steps) as one launch (1), one launch
-        per step (0), or by grid size (-1, the default); same bits."""
+        """Tensor plans (FP16 or split, temporal depth 1): run(steps) as one
+        launch (1), one launch per step (0), or by grid size (-1, the
+        default); same bits."""
         _check(lib().tcs_plan_set_multistep(self._h, int(mode)))
 
     def close(self) -> None:

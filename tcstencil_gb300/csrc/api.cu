@@ -389,10 +389,10 @@ struct tcs_plan_s {
                              static_cast<uint16_t *>(buf[1 - from][1]), s),
             "blocked sweep launch");
     }
-    // Plain FP16 on the tensor engine runs all steps of a call in one
-    // launch, whose tiles of step j wait only for the neighbouring tile rows
-    // of step j-1 (tcs_plan_set_multistep; TCS_MULTI=0 in the environment:
-    // one launch per step).  Measured on GB300 (box2d2r, us per step, one
+    // Tensor-engine plans (FP16 or split, temporal depth 1) run all steps of
+    // a call in one launch, whose tiles of step j wait only for the
+    // neighbouring tile rows of step j-1 (tcs_plan_set_multistep; TCS_MULTI=0
+    // in the environment: one launch per step).  Measured on GB300 (FP16 box2d2r, us per step, one
     // launch per step -> one launch): 8196² 49.8 -> 42.2, 4096² 13.2 -> 10.4,
     // 2048² 6.8 -> 6.9, 1026² 5.5 -> 6.3: small grids are latency-bound, and
     // a step boundary between launches is quicker than the counters.
@@ -402,11 +402,16 @@ struct tcs_plan_s {
             const char *e = getenv("TCS_MULTI");
             return !(e && e[0] == '0');
         }();
-        if (!on || !rows_done || prob.engine != TCS_ENGINE_TENSOR || prob.precision != TCS_PREC_F16)
-            return false;
+        if (!on || !rows_done || prob.engine != TCS_ENGINE_TENSOR || pairs()) return false;
         if (multistep >= 0) return multistep == 1;
         const long long tiles = (long long)((g.ny + kTile - 1) / kTile) * ((g.nx + kTile - 1) / kTile);
-        return tiles > 2LL * device_sms();
+        const long long sms = device_sms();
+        // Split, box2d1r, us per step, one launch per step -> one launch:
+        // 2048² 11.1 -> 8.8, 4096² 30.4 -> 27.1, 8196² 103.3 -> 107.0, 16386²
+        // 379.6 -> 417.5: the multi-step split kernel spends ~10 % more per
+        // tile, which only the mid sizes' step overheads repay.
+        if (prob.precision == TCS_PREC_SPLIT) return tiles > sms && tiles <= 12 * sms;
+        return tiles > 2 * sms;
     }
     int steps_in_one(int steps, int from, cudaStream_t s) {
         const int tiles_y = (g.ny + kTile - 1) / kTile;
@@ -414,10 +419,15 @@ struct tcs_plan_s {
             cudaMemsetAsync(rows_done, 0, (size_t)tiles_y * kRowCounterStride * sizeof(unsigned), s),
             "row counter reset");
         if (st) return st;
-        return cuda_status(
-            launch_tc_f16_steps(g, prob.stencil, coeffs, static_cast<const uint16_t *>(buf[from][0]),
-                                static_cast<uint16_t *>(buf[1 - from][0]), steps, rows_done, s),
-            "multi-step sweep launch");
+        const cudaError_t e =
+            prob.precision == TCS_PREC_SPLIT
+                ? launch_tc_split_steps(g, prob.stencil, coeffs, static_cast<const uint16_t *>(buf[from][0]),
+                                        static_cast<const uint16_t *>(buf[from][1]),
+                                        static_cast<uint16_t *>(buf[1 - from][0]),
+                                        static_cast<uint16_t *>(buf[1 - from][1]), steps, rows_done, s)
+                : launch_tc_f16_steps(g, prob.stencil, coeffs, static_cast<const uint16_t *>(buf[from][0]),
+                                      static_cast<uint16_t *>(buf[1 - from][0]), steps, rows_done, s);
+        return cuda_status(e, "multi-step sweep launch");
     }
     // The state `steps` steps from `from` ends in: one flip per step.
     int final_state(int steps, int from) const {
@@ -485,7 +495,7 @@ int tcs_plan_create(const tcs_problem *pr, tcs_plan *out) {
     if (pr->engine == TCS_ENGINE_TENSOR) {
         st = cuda_status(tc_prepare(pr->stencil, pr->precision == TCS_PREC_SPLIT), "tensor kernel set-up");
         if (st) return st;
-        if (pr->precision == TCS_PREC_F16) {
+        {
             const int tiles_y = (pr->ny + kTile - 1) / kTile;
             st = cuda_status(cudaMalloc(&p->rows_done, (size_t)tiles_y * kRowCounterStride * sizeof(unsigned)),
                              "cudaMalloc(rows)");

@@ -62,12 +62,116 @@ using SG = StageLines;  // line-aligned staging of the sweep kernels
 
 __device__ int g_tc_error = 0;
 
-// Plain form: MMA issuers and accumulator slots (below); the stage count is
-// a multiple of the issuers.  Measured on GB300 with one issuer (box2d1r /
-// box2d2r / star2d2r, 8196², Gpts/s): 3 stages 1310 / 1106 / 1114, 4 stages
-// 1255 / 1113 / 1110, 5 stages 1209 / 1104 / 1100.  With two issuers and four
-// stages: 1330 / 1327 / 1325; with three and three: 1374 / 1238 / 1241.  So
-// radius-1 stencils take three issuers, radius-2 stencils two.
+// ---------------------------------------------- several steps per launch ---
+// Items are (step, tile), step-major; CTA b takes items b, b + grid, ...  A
+// tile of step j needs tile rows ty-1 .. ty+1 of step j-1 finished: they hold
+// its input, and they were the last readers of the plane it overwrites.  One
+// counter per tile row (kRowCounterStride apart, a 128-byte line each) counts
+// epilogue-warp completions over the launch.  A row's counts arrive in step
+// order, as a tile starts only after its own row finished the step before, so
+// "row r finished step j-1" is count >= j * (epilogue warps) * tiles_x.
+
+// The producer's side: which rows of which step it already knows finished.
+struct RowDeps {
+    int ver_s = -1, ver_hi = -1;  // rows from this CTA's first row of step ver_s up to ver_hi
+
+    // Waits (bounded) for rows ty-1 .. ty+1 of step `step - 1`.  One burst of
+    // relaxed reads over the next kBurst rows extends the known range over
+    // every finished one, so the next tiles (a few rows on) seldom poll; then
+    // one acquire fence, and the proxy fence that orders the tensor copies
+    // after it (they read what other SMs stored).  Returns false on give-up.
+    __device__ bool wait(const unsigned *rows_done, int step, int ty, int tiles_y,
+                         unsigned per_row) {
+        constexpr int kBurst = 8;
+        const int lo = ty > 0 ? ty - 1 : 0;
+        const int hi = ty + 1 < tiles_y ? ty + 1 : tiles_y - 1;
+        if (ver_s != step - 1 || lo > ver_hi + 1) {
+            ver_s = step - 1;
+            ver_hi = lo - 1;
+        }
+        if (hi <= ver_hi) return true;
+        const unsigned target = (unsigned)step * per_row;
+        const int first = ver_hi + 1;
+        unsigned v[kBurst];
+#pragma unroll
+        for (int b = 0; b < kBurst; b++)
+            v[b] = first + b < tiles_y ? ld_relaxed(rows_done + (first + b) * kRowCounterStride) : 0u;
+        int x = first;  // rows first .. x-1 are finished
+#pragma unroll
+        for (int b = 0; b < kBurst; b++)
+            if (x == first + b && first + b < tiles_y && v[b] >= target) x++;
+        for (int r = x; r <= hi; r++) {  // rows this tile still needs
+            const unsigned *ctr = rows_done + r * kRowCounterStride;
+            const uint64_t t0 = global_timer_ns();
+            while (ld_relaxed(ctr) < target) {
+                if (*(volatile int *)&g_tc_error != 0 || global_timer_ns() - t0 > kWaitLimitNs)
+                    return false;
+                __nanosleep(32);
+            }
+        }
+        ver_hi = x - 1 > hi ? x - 1 : hi;
+        fence_acq_rel_gpu();
+        fence_proxy_async_global();
+        return true;
+    }
+};
+
+// An epilogue warp's side: after its stores of its `done`-th item (counting
+// from 1) are issued, it publishes the count in its own shared word (a
+// release store, after the warp barrier that orders its lanes' stores).  It
+// never waits here: the words only grow.
+__device__ __forceinline__ void count_item(uint32_t *warp_done, int w, uint32_t done) {
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) st_release_cta(&warp_done[w], done);
+}
+
+// The signal warp's side (one thread): item i is finished when every
+// epilogue warp's word has reached i + 1 (acquire at CTA scope); its count
+// for its tile row is then published at GPU scope behind a fence that covers
+// those stores.  Items already finished are batched behind one fence (it
+// waits for their stores to complete); before waiting for an unfinished item
+// the batch is flushed, so no count is ever held while this thread waits.
+template <int NW>
+__device__ void signal_rows(unsigned *rows_done, int n_items, int n_tiles, int tiles_x,
+                            const uint32_t *warp_done, const volatile int *abort_flag) {
+    constexpr int kBatch = 4;
+    int pend[kBatch];
+    int n_pend = 0;
+    auto flush = [&]() {
+        if (!n_pend) return;
+        fence_acq_rel_gpu();
+        for (int j = 0; j < n_pend; j++) red_relaxed_add(rows_done + pend[j] * kRowCounterStride, NW);
+        n_pend = 0;
+    };
+    auto finished = [&](uint32_t target) {
+#pragma unroll
+        for (int w = 0; w < NW; w++)
+            if (ld_acquire_cta(&warp_done[w]) < target) return false;
+        return true;
+    };
+    uint32_t i = 0;
+    int t = (int)blockIdx.x - (int)gridDim.x;  // the item's tile (k mod n_tiles)
+    for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++) {
+        for (t += gridDim.x; t >= n_tiles;) t -= n_tiles;
+        if (!finished(i + 1)) {
+            flush();
+            const uint64_t t0 = global_timer_ns();
+            while (!finished(i + 1)) {
+                if (*abort_flag || global_timer_ns() - t0 > kWaitLimitNs) {
+                    record_error(&g_tc_error, kErrWaitResult);
+                    *(volatile int *)abort_flag = 1;
+                    return;
+                }
+                // items take microseconds; a tight poll would take issue slots
+                // from the epilogue warps sharing this warp's scheduler
+                __nanosleep(256);
+            }
+        }
+        pend[n_pend++] = t / tiles_x;
+        if (n_pend == kBatch) flush();
+    }
+    flush();
+}
 
 // Plain form: ISSUERS MMA issuer warps take tiles in turn.  Tile i uses
 // accumulator slot i % ISSUERS (one 160-column slot per issuer) and stage
@@ -85,10 +189,8 @@ struct Sweep {
     static constexpr int STAGES = ISSUERS == 2 ? 4 : 3;
     static constexpr int SIGNAL_WARP = 1 + ISSUERS + kEpiWarps;  // several steps: row counts
     static constexpr int THREADS = 32 * (SIGNAL_WARP + 1);
-    static constexpr int SIG_SLOTS = 4;  // items the epilogue may finish ahead of the signal warp
     static_assert(SLOTS * Mode<false>::ACC <= kTmemCols, "accumulator slots fit TMEM");
     static_assert(STAGES % ISSUERS == 0, "each stage holds one issuer's tiles");
-    static_assert(SIG_SLOTS > SLOTS, "epilogue warps are at most SLOTS items apart");
 };
 
 template <int S, bool SPLIT>
@@ -105,7 +207,7 @@ struct Cfg {
 
 struct TcParams {
     CUtensorMap map_hi, map_lo;     // input planes (encode_panel_map)
-    CUtensorMap map_out;            // plain, several steps: the output plane (odd steps' input)
+    CUtensorMap map_out, map_out_lo;  // several steps: the output planes (odd steps' input)
     GridGeom g;
     int tiles_x, n_tiles;
     int steps;                      // plain: steps of this launch (1 for the split kernels)
@@ -138,11 +240,9 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
     uint64_t *acc_full = bars + 2 * NS;         // [NSL]
     uint64_t *acc_empty = acc_full + NSL;       // [NSL]
     uint64_t *drain = acc_empty + NSL;          // [1]
-    constexpr int NSG = Sweep<S>::SIG_SLOTS;
-    uint64_t *sig_done = drain + 1;             // [NSG] an item's stores are issued
-    uint64_t *sig_free = sig_done + NSG;        // [NSG] the signal warp has taken it
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sig_free + NSG);
-    static_assert((2 * NS + 2 * NSL + 1 + 2 * NSG) * 8 + 8 <= 256, "barrier area");
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+    uint32_t *warp_done = tmem_slot + 2;        // [kEpiWarps] several steps: items stored
+    static_assert((2 * NS + 2 * NSL + 1) * 8 + (2 + kEpiWarps) * 4 <= 256, "barrier area");
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5;
@@ -160,10 +260,7 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
             mbar_init(&acc_empty[b], kEpiWarps);
         }
         mbar_init(drain, Sweep<S>::ISSUERS);
-        for (int b = 0; b < NSG; b++) {
-            mbar_init(&sig_done[b], kEpiWarps);
-            mbar_init(&sig_free[b], 1);
-        }
+        for (int w = 0; w < kEpiWarps; w++) warp_done[w] = 0;
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -193,68 +290,18 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
         if (lane == 0) {
             int i = 0;
             int last_issued = -1;
-            // rows up to ver_hi of step ver_s (from this CTA's first tile row
-            // of that step on) are known complete
-            int ver_s = -1, ver_hi = -1;
+            RowDeps deps;
             const unsigned per_row = (unsigned)(kEpiWarps * tiles_x);
-            constexpr int kBurst = 8;  // rows read per poll
             for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++) {
                 const int step = k / n_tiles;
                 const int t = k - step * n_tiles;
                 const int ty = t / tiles_x;
                 const int s = i % NS;
                 const uint32_t ph = (i / NS) & 1;
-                if (step > 0) {
-                    // Rows ty-1 .. ty+1 of the previous step: the tile's input
-                    // (it wrote them) and the plane this tile overwrites (it read
-                    // them).  A tile row's counts arrive in step order, since a
-                    // tile starts only after its own row finished the step before.
-                    const int lo = ty > 0 ? ty - 1 : 0;
-                    const int hi = ty + 1 < tiles_y ? ty + 1 : tiles_y - 1;
-                    if (ver_s != step - 1 || lo > ver_hi + 1) {
-                        ver_s = step - 1;
-                        ver_hi = lo - 1;
-                    }
-                    if (hi > ver_hi) {
-                        // One burst of relaxed reads over the next kBurst rows:
-                        // the known range grows over every complete one, so the
-                        // next tiles (a few rows further) usually need no poll.
-                        const unsigned target = (unsigned)step * per_row;
-                        const int first = ver_hi + 1;
-                        unsigned v[kBurst];
-#pragma unroll
-                        for (int b = 0; b < kBurst; b++)
-                            v[b] = first + b < tiles_y
-                                       ? ld_relaxed(p.rows_done + (first + b) * kRowCounterStride)
-                                       : 0u;
-                        int x = first;  // rows first .. x-1 are complete
-#pragma unroll
-                        for (int b = 0; b < kBurst; b++)
-                            if (x == first + b && first + b < tiles_y && v[b] >= target) x++;
-                        bool ok = true;
-                        for (int r = x; r <= hi && ok; r++) {  // rows this tile still needs
-                            const unsigned *ctr = p.rows_done + r * kRowCounterStride;
-                            const uint64_t t0 = global_timer_ns();
-                            while (ld_relaxed(ctr) < target) {
-                                if (*(volatile int *)&g_tc_error != 0 ||
-                                    global_timer_ns() - t0 > kWaitLimitNs) {
-                                    ok = false;
-                                    break;
-                                }
-                                __nanosleep(32);
-                            }
-                        }
-                        if (!ok) {
-                            record_error(&g_tc_error, kErrWaitDep);
-                            *abort_flag = 1;
-                            break;
-                        }
-                        ver_hi = x - 1 > hi ? x - 1 : hi;
-                        // acquire for the counts read above; then the tensor copies
-                        // below, which read what other SMs stored
-                        fence_acq_rel_gpu();
-                        fence_proxy_async_global();
-                    }
+                if (step > 0 && !deps.wait(p.rows_done, step, ty, tiles_y, per_row)) {
+                    record_error(&g_tc_error, kErrWaitDep);
+                    *abort_flag = 1;
+                    break;
                 }
                 // (the poll above overlaps the wait for a free stage)
                 if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
@@ -326,41 +373,8 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
         }
     } else if (warp == Sweep<S>::SIGNAL_WARP) {
         // -------------------------------------------------------- signal ---
-        // Several steps: once all epilogue warps have issued an item's stores
-        // (sig_done, release at CTA scope), the item's count for its tile row
-        // is published at GPU scope behind a fence that covers those stores.
-        // Items already finished are batched behind one fence (it waits for
-        // the stores to complete); before waiting for an unfinished item the
-        // batch is flushed, so no count is ever held while this thread waits.
-        if (p.rows_done && lane == 0) {
-            constexpr int kBatch = 4;
-            int pend[kBatch];
-            int n_pend = 0;
-            auto flush = [&]() {
-                if (!n_pend) return;
-                fence_acq_rel_gpu();
-                for (int j = 0; j < n_pend; j++)
-                    red_relaxed_add(p.rows_done + pend[j] * kRowCounterStride, kEpiWarps);
-                n_pend = 0;
-            };
-            int i = 0;
-            for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++) {
-                const int d = i % NSG;
-                const uint32_t ph = (i / NSG) & 1;
-                if (!mbar_try_wait(&sig_done[d], ph)) {
-                    flush();
-                    if (!mbar_wait(&sig_done[d], ph, abort_flag)) {
-                        record_error(&g_tc_error, kErrWaitResult);
-                        *abort_flag = 1;
-                        break;
-                    }
-                }
-                mbar_arrive(&sig_free[d]);
-                pend[n_pend++] = (k % n_tiles) / tiles_x;
-                if (n_pend == kBatch) flush();
-            }
-            flush();
-        }
+        if (p.rows_done && lane == 0)
+            signal_rows<kEpiWarps>(p.rows_done, n_items, n_tiles, tiles_x, warp_done, abort_flag);
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;            // TMEM lane quarter of this warp
@@ -409,23 +423,7 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
                 if (lane == 0) mbar_arrive(&acc_empty[sl]);
                 epilogue_store<SPLIT>(o, f, 0, half, m, Y0, X0);
             }
-            if (p.rows_done) {
-                // this warp's stores of the tile are issued: hand the count to
-                // the signal warp, whose release then covers them (a release
-                // here would hold the warp until its stores completed)
-                const int d = i % NSG;
-                bool okd = mbar_wait(&sig_free[d], ((i / NSG) & 1) ^ 1, abort_flag);
-                okd = __all_sync(0xffffffffu, okd);
-                if (!okd) {
-                    if (lane == 0) {
-                        record_error(&g_tc_error, kErrWaitResult);
-                        *abort_flag = 1;
-                    }
-                    break;
-                }
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&sig_done[d]);
-            }
+            if (p.rows_done) count_item(warp_done, warp - 1 - Sweep<S>::ISSUERS, (uint32_t)(i + 1));
         }
     }
 
@@ -472,15 +470,21 @@ constexpr int kRingEpiWarps = 4 * kRingGroups;     // a lane quarter each
 #define TCS_SPLIT_ISSUERS 3
 #endif
 constexpr int kRingIssuers = TCS_SPLIT_ISSUERS;   // MMA issuer warps 1 .. kRingIssuers
-constexpr int kRingThreads = 32 * (1 + kRingIssuers + kRingEpiWarps);
+constexpr int kRingSignalWarp = 1 + kRingIssuers + kRingEpiWarps;  // several steps: row counts
+// MULTI: the kernel runs several steps (p.steps) with the row counts and a
+// signal warp; without it, one step in the single-step kernel's exact form
+// (a kernel carrying the multi-step code ran single steps 8-11 % slower:
+// 8196² box2d1r 106.7 -> 114.9 us).
+template <bool MULTI>
+constexpr int ring_threads() { return 32 * (kRingSignalWarp + (MULTI ? 1 : 0)); }
 // Every tile computes all its windows: a runtime window count for the last
 // tile of a row slowed this epilogue-bound kernel by more than the skipped
 // MMAs saved (16386²: 380 -> 387 us per step).
 constexpr int kTileWindows = kTile / 16 + 1;
 static_assert(kRingSlots * kRegionCols <= kTmemCols, "window ring fits TMEM");
 
-template <int S>
-__global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __grid_constant__ TcParams p) {
+template <int S, bool MULTI>
+__global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel(const __grid_constant__ TcParams p) {
     using C = Cfg<S, true>;
     using M = Mode<true>;
     constexpr int NS = C::STAGES;
@@ -500,7 +504,8 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
     uint64_t *drain = bars + 2 * NS + 2 * kRingSlots;         // [1]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-    static_assert((2 * NS + 2 * kRingSlots + 1) * 8 + 8 <= 256, "barrier area");
+    uint32_t *warp_done = tmem_slot + 2;  // [kRingEpiWarps] several steps: items stored
+    static_assert((2 * NS + 2 * kRingSlots + 1) * 8 + (2 + kRingEpiWarps) * 4 <= 256, "barrier area");
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -516,6 +521,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
             mbar_init(&win_empty[r], kRingEpiWarps);
         }
         mbar_init(drain, kRingIssuers);
+        for (int w = 0; w < kRingEpiWarps; w++) warp_done[w] = 0;
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -525,7 +531,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
         tmem_relinquish();
     }
     build_bands(reinterpret_cast<uint16_t *>(band_base), p.coef, C::R, C::BOX, true, threadIdx.x,
-                kRingThreads);
+                ring_threads<MULTI>());
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -537,22 +543,38 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
 
     const int tiles_x = p.tiles_x;
     const int n_tiles = p.n_tiles;
+    const int tiles_y = n_tiles / tiles_x;
+    // (step, tile), step-major; CTA b takes b, b + grid, ...
+    const int n_items = MULTI ? p.steps * n_tiles : n_tiles;
 
     if (warp == 0) {
         // ------------------------------------------------------ producer ---
         if (lane == 0) {
             int i = 0;
             int last_issued = -1;
-            for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, i++) {
+            RowDeps deps;
+            const unsigned per_row = (unsigned)(kRingEpiWarps * tiles_x);
+            int step = 0, t = (int)blockIdx.x - (int)gridDim.x;  // the item's step and tile
+            for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++) {
+                for (t += gridDim.x; t >= n_tiles; t -= n_tiles) step++;
+                const int ty = t / tiles_x;
                 const int s = i % NS;
+                if (MULTI && step > 0 && !deps.wait(p.rows_done, step, ty, tiles_y, per_row)) {
+                    record_error(&g_tc_error, kErrWaitDep);
+                    *abort_flag = 1;
+                    break;
+                }
+                // (the poll above overlaps the wait for a free stage)
                 if (!mbar_wait(&empty[s], ((i / NS) & 1) ^ 1, abort_flag)) {
                     record_error(&g_tc_error, kErrWaitEmpty);
                     *abort_flag = 1;
                     break;
                 }
                 mbar_arrive_expect_tx(&full[s], NP * SG::PLANE);
-                load_tile_map(&p.map_hi, &p.map_lo, NP, (t / tiles_x) * kTile,
-                              (t % tiles_x) * kTile, stage_base + (size_t)s * NP * SG::PLANE,
+                // odd steps run from the output planes back into the input planes
+                load_tile_map((step & 1) ? &p.map_out : &p.map_hi,
+                              (step & 1) ? &p.map_out_lo : &p.map_lo, NP, ty * kTile,
+                              (t - ty * tiles_x) * kTile, stage_base + (size_t)s * NP * SG::PLANE,
                               &full[s]);
                 last_issued = i;
             }
@@ -574,7 +596,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
             int i = 0, G = 0;         // tiles, global windows
             bool stop = false;
             const uint32_t band = smem_u32(band_base);
-            for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, i++) {
+            for (int k = blockIdx.x; k < n_items && !stop; k += gridDim.x, i++) {
                 const int s = i % NS;
                 if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
                     record_error(&g_tc_error, kErrWaitFull);
@@ -610,6 +632,10 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
                 }
             }
         }
+    } else if (MULTI && warp == kRingSignalWarp) {
+        // -------------------------------------------------------- signal ---
+        if (lane == 0)
+            signal_rows<kRingEpiWarps>(p.rows_done, n_items, n_tiles, tiles_x, warp_done, abort_flag);
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;                          // TMEM lane quarter
@@ -640,9 +666,19 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
             __syncwarp();
             if (lane == 0) mbar_arrive(&win_empty[(G0 + w) % kRingSlots]);
         };
-        for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, G0 += kTileWindows) {
+        int i = 0;
+        int step = 0, t = (int)blockIdx.x - (int)gridDim.x;  // the item's step and tile
+        for (int k = blockIdx.x; k < n_items; k += gridDim.x, G0 += kTileWindows, i++) {
+            for (t += gridDim.x; t >= n_tiles; t -= n_tiles) step++;
             const int Y0 = (t / tiles_x) * kTile;
             const int X0 = (t % tiles_x) * kTile;
+            if (MULTI) {
+                // odd steps run from the output planes back into the input planes
+                o.in_hi = (step & 1) ? p.out_hi : p.in_hi;
+                o.in_lo = (step & 1) ? p.out_lo : p.in_lo;
+                o.out_hi = (step & 1) ? const_cast<uint16_t *>(p.in_hi) : p.out_hi;
+                o.out_lo = (step & 1) ? const_cast<uint16_t *>(p.in_lo) : p.out_lo;
+            }
             const int y = Y0 + m;
             const bool fast = tile_inside(o, Y0, X0);
             const bool row_in = y >= o.y0 && y < o.y1;
@@ -661,6 +697,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) tc_split_ring_kernel(const __
                 store_block<true>(o, f, y, X0 + 16 * j, fast, row_in);
             });
             if (!ok) break;
+            if (MULTI) count_item(warp_done, warp - 1 - kRingIssuers, (uint32_t)(i + 1));
         }
     }
 
@@ -683,9 +720,15 @@ cudaError_t prepare_tc() {
     if (!configured) {
         cudaError_t e;
         if constexpr (SPLIT)
-            e = cudaFuncSetAttribute(tc_split_ring_kernel<S>,
+        {
+            e = cudaFuncSetAttribute(tc_split_ring_kernel<S, false>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(Cfg<S, SPLIT>::SMEM));
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(tc_split_ring_kernel<S, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(Cfg<S, SPLIT>::SMEM));
+        }
         else
             e = cudaFuncSetAttribute(tc_sweep_kernel<S, SPLIT>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -702,9 +745,8 @@ cudaError_t prepare_tc() {
     return cudaSuccess;
 }
 
-// One launch of `steps` steps (plain form; the split kernels take one).  With
-// several, step j reads in_hi for even j and out_hi for odd j and writes the
-// other; rows_done holds one zeroed counter per tile row (kRowCounterStride apart), and the launch is
+// One launch of `steps` steps.  With several, step j reads the in planes for
+// even j and the out planes for odd j and writes the others; rows_done holds one zeroed counter per tile row (kRowCounterStride apart), and the launch is
 // cooperative, so that all CTAs of the static tile order are resident at once.
 template <int S, bool SPLIT>
 cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
@@ -728,9 +770,11 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     p.steps = 1;
     p.rows_done = nullptr;
     p.map_out = p.map_hi;
+    p.map_out_lo = p.map_lo;
     if (steps > 1) {
-        if (SPLIT || !rows_done) return cudaErrorInvalidValue;
+        if (!rows_done) return cudaErrorInvalidValue;
         me = encode_panel_map(out_hi, g.p16, &p.map_out);
+        if (me == cudaSuccess && SPLIT) me = encode_panel_map(out_lo, g.p16, &p.map_out_lo);
         if (me != cudaSuccess) return me;
         p.steps = steps;
         p.rows_done = rows_done;
@@ -739,7 +783,10 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     for (int k = 0; k < C::NDY * C::NDY; k++) p.coef[k] = B[k];
     const long long items = (long long)p.n_tiles * p.steps;
     const int grid = items < g_num_sms ? (int)items : g_num_sms;
-    if constexpr (SPLIT) return launch_step(tc_split_ring_kernel<S>, grid, kRingThreads, C::SMEM, s, p);
+    if constexpr (SPLIT)
+        return p.steps > 1
+                   ? launch_step(tc_split_ring_kernel<S, true>, grid, ring_threads<true>(), C::SMEM, s, p, true)
+                   : launch_step(tc_split_ring_kernel<S, false>, grid, ring_threads<false>(), C::SMEM, s, p);
     else
         return launch_step(tc_sweep_kernel<S, SPLIT>, grid, Sweep<S>::THREADS, C::SMEM, s, p,
                            p.steps > 1);
@@ -785,6 +832,12 @@ cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const 
 cudaError_t launch_tc_f16_steps(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
                                 uint16_t *out, int steps, unsigned *rows_done, cudaStream_t s) {
     return dispatch_tc<false>(g, stencil, B, in, nullptr, out, nullptr, s, steps, rows_done);
+}
+
+cudaError_t launch_tc_split_steps(const GridGeom &g, int stencil, const float *B,
+                                  const uint16_t *in_hi, const uint16_t *in_lo, uint16_t *out_hi,
+                                  uint16_t *out_lo, int steps, unsigned *rows_done, cudaStream_t s) {
+    return dispatch_tc<true>(g, stencil, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
 }
 
 cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,

@@ -52,6 +52,19 @@ __device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Per-warp progress words in shared memory: the writer's earlier stores
+// (its warp's, ordered by a preceding __syncwarp) happen before a reader's
+// acquire that sees the value.
+__device__ __forceinline__ void st_release_cta(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_cta(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
+
 // Relaxed read of a count; a following fence_acq_rel_gpu makes it an acquire.
 __device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
     unsigned v;

@@ -137,6 +137,9 @@ cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const 
 constexpr int kRowCounterStride = 32;
 cudaError_t launch_tc_f16_steps(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
                                 uint16_t *out, int steps, unsigned *rows_done, cudaStream_t s);
+cudaError_t launch_tc_split_steps(const GridGeom &g, int stencil, const float *B,
+                                  const uint16_t *in_hi, const uint16_t *in_lo, uint16_t *out_hi,
+                                  uint16_t *out_lo, int steps, unsigned *rows_done, cudaStream_t s);
 cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
                             const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
                             cudaStream_t s);

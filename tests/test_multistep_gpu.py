@@ -1,6 +1,6 @@
-"""Several plain tensor steps in one launch against one launch per step.
+"""Several tensor steps in one launch against one launch per step.
 
-A plan's run(steps) with steps >= 2 on the tensor engine in FP16 can be one
+A plan's run(steps) with steps >= 2 on the tensor engine (FP16 or split) can be one
 cooperative launch whose tiles of step j wait for the neighbouring tile rows
 of step j-1 (per-row completion counters; set_multistep(1) forces it, the
 default takes it from a grid size on); run(1) is one launch of one step.
@@ -25,8 +25,10 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _plan_out(tcs, A, B, stencil, steps, one_by_one, rect=None, use_graph=True, mode=1):
-    p = tcs.Plan(A.shape[0], A.shape[1], stencil, B, engine="tensor", precision="f16", rect=rect)
+def _plan_out(tcs, A, B, stencil, steps, one_by_one, rect=None, use_graph=True, mode=1,
+              precision="f16"):
+    p = tcs.Plan(A.shape[0], A.shape[1], stencil, B, engine="tensor", precision=precision, rect=rect,
+                 temporal_depth=1)
     p.set_multistep(mode)
     p.upload(A)
     if one_by_one:
@@ -41,46 +43,51 @@ def _plan_out(tcs, A, B, stencil, steps, one_by_one, rect=None, use_graph=True, 
     return out
 
 
+@pytest.mark.parametrize("precision", ["f16", "split"])
 @pytest.mark.parametrize("stencil", STENCILS)
 @pytest.mark.parametrize("shape", [(20, 37), (100, 700), (257, 129), (600, 140), (140, 1100)])
 @pytest.mark.parametrize("steps", [2, 3, 8])
-def test_one_launch_equals_one_step_per_launch(tcs, torch_cuda, stencil, shape, steps):
+def test_one_launch_equals_one_step_per_launch(tcs, torch_cuda, precision, stencil, shape, steps):
     rng = np.random.default_rng(zlib.crc32(repr((stencil, shape, steps)).encode()))
     A = grid(rng, *shape)
     B = normalized_coeffs(rng, stencil)
-    a = _plan_out(tcs, A, B, stencil, steps, one_by_one=False)
-    b = _plan_out(tcs, A, B, stencil, steps, one_by_one=True)
+    a = _plan_out(tcs, A, B, stencil, steps, one_by_one=False, precision=precision)
+    b = _plan_out(tcs, A, B, stencil, steps, one_by_one=True, precision=precision)
     np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("stencil", ["box2d2r", "star2d1r"])
-def test_many_tiles_per_cta_and_eager_launch(tcs, torch_cuda, stencil):
+@pytest.mark.parametrize("stencil,precision", [("box2d2r", "f16"), ("star2d1r", "f16"),
+                                               ("box2d1r", "split"), ("star2d2r", "split")])
+def test_many_tiles_per_cta_and_eager_launch(tcs, torch_cuda, stencil, precision):
     # 33 x 33 tiles = 1089 > 152 CTAs per step, over 12 steps
     rng = np.random.default_rng(77)
     A = grid(rng, 4100, 4100)
     B = normalized_coeffs(rng, stencil)
-    a = _plan_out(tcs, A, B, stencil, 12, one_by_one=False)
-    b = _plan_out(tcs, A, B, stencil, 12, one_by_one=True)
-    c = _plan_out(tcs, A, B, stencil, 12, one_by_one=False, use_graph=False)
-    d = _plan_out(tcs, A, B, stencil, 12, one_by_one=False, mode=-1)  # by size: one launch
-    e = _plan_out(tcs, A, B, stencil, 12, one_by_one=False, mode=0)
+    kw = dict(precision=precision)
+    a = _plan_out(tcs, A, B, stencil, 12, one_by_one=False, **kw)
+    b = _plan_out(tcs, A, B, stencil, 12, one_by_one=True, **kw)
+    c = _plan_out(tcs, A, B, stencil, 12, one_by_one=False, use_graph=False, **kw)
+    d = _plan_out(tcs, A, B, stencil, 12, one_by_one=False, mode=-1, **kw)  # by size: one launch
+    e = _plan_out(tcs, A, B, stencil, 12, one_by_one=False, mode=0, **kw)
     for x in (b, c, d, e):
         np.testing.assert_array_equal(a, x)
 
 
+@pytest.mark.parametrize("precision", ["f16", "split"])
 @pytest.mark.parametrize("stencil", STENCILS)
-def test_rectangle_outside_cells_kept(tcs, torch_cuda, stencil):
+def test_rectangle_outside_cells_kept(tcs, torch_cuda, stencil, precision):
     rng = np.random.default_rng(91)
     A = grid(rng, 300, 270)  # nonzero everywhere, also outside the rectangle
     B = normalized_coeffs(rng, stencil)
     rect = (9, 290, 3, 250)
-    a = _plan_out(tcs, A, B, stencil, 6, one_by_one=False, rect=rect)
-    b = _plan_out(tcs, A, B, stencil, 6, one_by_one=True, rect=rect)
+    a = _plan_out(tcs, A, B, stencil, 6, one_by_one=False, rect=rect, precision=precision)
+    b = _plan_out(tcs, A, B, stencil, 6, one_by_one=True, rect=rect, precision=precision)
     np.testing.assert_array_equal(a, b)
-    inside = np.zeros(A.shape, bool)
-    inside[rect[0]:rect[1], rect[2]:rect[3]] = True
-    A16 = oracle.f16_to_f32(oracle.f32_to_f16(A))
-    np.testing.assert_array_equal(a[~inside], A16[~inside])
+    if precision == "f16":
+        inside = np.zeros(A.shape, bool)
+        inside[rect[0]:rect[1], rect[2]:rect[3]] = True
+        A16 = oracle.f16_to_f32(oracle.f32_to_f16(A))
+        np.testing.assert_array_equal(a[~inside], A16[~inside])
 
 
 _CHILD = r"""
@@ -91,9 +98,9 @@ from helpers import grid, normalized_coeffs
 rng = np.random.default_rng(5)
 A = grid(rng, 700, 500)
 out = []
-for st in ("box2d2r", "star2d1r"):
+for st, prec in (("box2d2r", "f16"), ("star2d1r", "f16"), ("box2d1r", "split")):
     B = normalized_coeffs(rng, st)
-    p = tcs.Plan(700, 500, st, B, engine="tensor", precision="f16")
+    p = tcs.Plan(700, 500, st, B, engine="tensor", precision=prec, temporal_depth=1)
     p.set_multistep(1)
     p.upload(A); p.run(9)
     o = np.empty_like(A); p.download(o); p.close()
