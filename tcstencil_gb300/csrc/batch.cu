@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 if (it.g == met_g && it.t == met_t) {
                     // met before, and the proxy fence after that poll still orders the copies below
                 } else if (it.t > 0) {
-                    ctr = p.counters + g.ctr_base + it.t - 1;
+                    ctr = p.counters + (size_t)(g.ctr_base + it.t - 1) * kRowCounterStride;
                     target = (unsigned)(g.n_tiles * C::EPI_WARPS);
                 } else if (g.gate) {
                     ctr = g.gate;
@@ -439,7 +439,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 }
                 const BatchItem it = ring[j];
                 unsigned *ctr = nullptr;
-                if (it.g >= 0) ctr = p.counters + p.grids[it.g].ctr_base + it.t;
+                if (it.g >= 0)
+                    ctr = p.counters + (size_t)(p.grids[it.g].ctr_base + it.t) * kRowCounterStride;
                 if (n_pend && ctr != pend) {
                     red_release_add(pend, n_pend);
                     n_pend = 0;
@@ -666,7 +667,8 @@ struct tcs_batch_s {
     struct Part {
         int first = 0, n_grids = 0;
         int *d_layout = nullptr;        // step_off then tile_prefix
-        unsigned *d_counters = nullptr; // per (grid, step), then work counter, error word
+        unsigned *d_counters = nullptr; // per (grid, step), then work counter, error word;
+                                        // each on its own 128-byte line (kRowCounterStride)
         int n_items = 0, n_steps = 0, n_counters = 0;
     } part[2];                          // [FP16, split]
     uint16_t *d_bands = nullptr;
@@ -777,7 +779,7 @@ int batch_build(tcs_batch b) {
         if (n_items < 0) return fail(TCS_ERR_INVALID, "tcs_batch: more than 2^31 work items per run");
         P.n_items = (int)n_items;
         st = cuda_status(cudaMalloc(&P.d_layout, layout.size() * sizeof(int)), "cudaMalloc(layout)");
-        if (!st) st = cuda_status(cudaMalloc(&P.d_counters, (P.n_counters + 2) * sizeof(unsigned)), "cudaMalloc(counters)");
+        if (!st) st = cuda_status(cudaMalloc(&P.d_counters, (size_t)(P.n_counters + 2) * kRowCounterStride * sizeof(unsigned)), "cudaMalloc(counters)");
         if (!st) st = cuda_status(cudaMemcpy(P.d_layout, layout.data(), layout.size() * sizeof(int), cudaMemcpyHostToDevice), "layout copy");
         if (st) return st;
     }
@@ -809,7 +811,7 @@ int batch_enqueue(tcs_batch b, cudaStream_t s) {
     for (int k = 0; k < 2; k++) {
         auto &P = b->part[k];
         if (!P.n_grids) continue;
-        int st = cuda_status(cudaMemsetAsync(P.d_counters, 0, (P.n_counters + 2) * sizeof(unsigned), s),
+        int st = cuda_status(cudaMemsetAsync(P.d_counters, 0, (size_t)(P.n_counters + 2) * kRowCounterStride * sizeof(unsigned), s),
                              "counter reset");
         if (st) return st;
         BatchParams p;
@@ -820,8 +822,8 @@ int batch_enqueue(tcs_batch b, cudaStream_t s) {
         p.n_grids = P.n_grids;
         p.n_items = P.n_items;
         p.counters = P.d_counters;
-        p.work_counter = P.d_counters + P.n_counters;
-        p.error = reinterpret_cast<int *>(P.d_counters + P.n_counters + 1);
+        p.work_counter = P.d_counters + (size_t)P.n_counters * kRowCounterStride;
+        p.error = reinterpret_cast<int *>(P.d_counters + (size_t)(P.n_counters + 1) * kRowCounterStride);
         p.bands = b->d_bands;
         p.wait_ns = b->wait_ns;
         p.grab = batch_grab(k == 1);

@@ -54,7 +54,7 @@ struct BatchParams {
     const int *step_off;     // [n_steps + 1]: first work index of each step
     const int *tile_prefix;  // [n_grids + 1]: first tile of each grid within a step
     int n_steps, n_grids, n_items;
-    unsigned *counters;      // one per (grid, step), zero at launch
+    unsigned *counters;      // one per (grid, step), kRowCounterStride apart, zero at launch
     unsigned *work_counter;  // next work index, zero at launch
     int *error;              // first failed wait of this launch (0 = none)
     const uint16_t *bands;

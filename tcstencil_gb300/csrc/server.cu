@@ -483,7 +483,7 @@ bool tcs_server_s::launch_round() {
     if (!st) st = grow_pinned(&b.h_layout, &b.cap_hl, n_layout, retired);
     if (!st) st = grow_device(&b.d_grids, &b.cap_dg, part.size(), retired);
     if (!st) st = grow_device(&b.d_layout, &b.cap_dl, n_layout, retired);
-    if (!st) st = grow_device(&b.d_counters, &b.cap_dc, n_ctr + 2, retired);
+    if (!st) st = grow_device(&b.d_counters, &b.cap_dc, (n_ctr + 2) * kRowCounterStride, retired);
     long long n_items[2] = {0, 0};
     for (int k = 0; k < 2 && !st; k++) {
         if (!count[k]) continue;
@@ -531,7 +531,7 @@ bool tcs_server_s::launch_round() {
         }
     if (!st) st = cuda_status(cudaMemcpyAsync(b.d_grids, b.h_grids, part.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice, compute), "round descriptors");
     if (!st) st = cuda_status(cudaMemcpyAsync(b.d_layout, b.h_layout, n_layout * sizeof(int), cudaMemcpyHostToDevice, compute), "round layout");
-    if (!st) st = cuda_status(cudaMemsetAsync(b.d_counters, 0, (n_ctr + 2) * sizeof(unsigned), compute), "round counters");
+    if (!st) st = cuda_status(cudaMemsetAsync(b.d_counters, 0, (n_ctr + 2) * kRowCounterStride * sizeof(unsigned), compute), "round counters");
     if (!st) st = cuda_status(cudaEventRecord(b.start, compute), "cudaEventRecord");
     for (int k = 0; k < 2 && !st; k++) {
         if (!count[k]) continue;
@@ -544,7 +544,7 @@ bool tcs_server_s::launch_round() {
         p.n_grids = count[k];
         p.n_items = (int)n_items[k];
         p.counters = b.d_counters;  // ctr_base is absolute across both parts
-        p.work_counter = b.d_counters + n_ctr + k;
+        p.work_counter = b.d_counters + (n_ctr + k) * kRowCounterStride;
         p.error = d_err;
         p.bands = d_bands;
         p.wait_ns = kBatchWaitNs;
