@@ -82,7 +82,7 @@ struct RowDeps {
     // after it (they read what other SMs stored).  Returns false on give-up.
     __device__ bool wait(const unsigned *rows_done, int step, int ty, int tiles_y,
                          unsigned per_row) {
-        constexpr int kBurst = 8;
+        constexpr int kBurst = 32;
         const int lo = ty > 0 ? ty - 1 : 0;
         const int hi = ty + 1 < tiles_y ? ty + 1 : tiles_y - 1;
         if (ver_s != step - 1 || lo > ver_hi + 1) {
