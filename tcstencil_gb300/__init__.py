@@ -291,14 +291,16 @@ class Plan:
     def __init__(self, ny: int, nx: int, stencil: str, coeffs, engine: str = "tensor",
                  precision: str = "f16", rect=None, temporal_depth: int | None = None):
         """engine "auto" takes the autotuner's choice for this problem class
-        (engine and temporal depth); temporal_depth 2 runs steps in blocked
-        pairs (split precision, tensor engine)."""
+        (engine, temporal depth and launch form); temporal_depth 2 runs steps
+        in blocked pairs (split precision, tensor engine)."""
+        tuned_launch = -1
         if engine == "auto":
-            from .autotune import best_config
+            from .autotune import best_config, best_launch
 
             engine, tuned_depth = best_config(stencil, precision, ny, nx)
             if temporal_depth is None:
                 temporal_depth = tuned_depth
+            tuned_launch = best_launch(stencil, precision, ny, nx)
         self._c = _coeffs(coeffs, stencil)
         y0, y1, x0, x1 = _rect(rect)
         self.ny, self.nx, self.stencil, self.engine, self.precision = ny, nx, stencil, engine, precision
@@ -309,6 +311,8 @@ class Plan:
         self._h = h
         if temporal_depth and temporal_depth != 1:
             self.set_temporal_depth(temporal_depth)
+        if tuned_launch >= 0 and engine == "tensor":
+            self.set_multistep(tuned_launch)
 
     def set_temporal_depth(self, depth: int) -> None:
         _check(lib().tcs_plan_set_temporal_depth(self._h, int(depth)))

@@ -6,8 +6,10 @@ variants and reading ncu durations (script/param.py:5, script/nvcc_compile.py,
 script/process_data.py:29-43).  Here the candidates are run-time choices of
 one library, timed with CUDA events:
 
-  sweep  (stencil, precision, size class) -> engine ("tensor" | "cudacore")
-                                             and temporal depth (1 | 2)
+  sweep  (stencil, precision, size class) -> engine ("tensor" | "cudacore"),
+                                             temporal depth (1 | 2) and launch
+                                             form (one launch per step, or one
+                                             launch for all steps of a call)
   serve  (offered load)                   -> round_steps of the request server
 
 Size classes are powers of two of each side, so one entry covers grids of
@@ -32,10 +34,15 @@ import numpy as np
 from .workloads import RADIUS, normalized_coeffs
 
 ENGINES_FOR = {"f16": ("tensor", "cudacore"), "split": ("tensor",), "f32": ("cudacore",)}
-# (engine, temporal depth) candidates per precision
-CANDIDATES = {"f16": (("tensor", 1), ("cudacore", 1)),
-              "split": (("tensor", 1), ("tensor", 2)),
-              "f32": (("cudacore", 1),)}
+# (engine, temporal depth, one launch for all steps) candidates per precision
+CANDIDATES = {"f16": (("tensor", 1, 0), ("tensor", 1, 1), ("cudacore", 1, 0)),
+              "split": (("tensor", 1, 0), ("tensor", 1, 1), ("tensor", 2, 0)),
+              "f32": (("cudacore", 1, 0),)}
+
+
+def candidate_key(engine: str, depth: int, multistep: int) -> str:
+    """"tensor/1" (one launch per step), "tensor/1/m" (one launch), ..."""
+    return f"{engine}/{depth}" + ("/m" if multistep else "")
 DEFAULT_ROUND_STEPS = 16
 
 
@@ -108,7 +115,7 @@ def pick_fastest(timings: dict) -> str:
 
 
 def time_sweep(engine: str, depth: int, stencil: str, precision: str, ny: int, nx: int,
-               steps: int, reps: int = 3) -> float:
+               steps: int, multistep: int = 0, reps: int = 3) -> float:
     """Seconds per step of a plan on the device (CUDA-graph runs, CUDA events)."""
     import torch
 
@@ -119,6 +126,8 @@ def time_sweep(engine: str, depth: int, stencil: str, precision: str, ny: int, n
     p = tcs.Plan(ny, nx, stencil, normalized_coeffs(rng, stencil), engine=engine,
                  precision=precision, temporal_depth=depth)
     try:
+        if engine == "tensor" and depth == 1:
+            p.set_multistep(multistep)
         p.upload(g)
         p.run(steps, use_graph=True)
         torch.cuda.synchronize()
@@ -138,14 +147,16 @@ def time_sweep(engine: str, depth: int, stencil: str, precision: str, ny: int, n
 
 def tune_sweep(stencil: str, precision: str, ny: int, nx: int, steps: int = 20,
                cache: Cache | None = None, timer=time_sweep) -> dict:
-    """Times every (engine, temporal depth) that supports the precision; stores
-    and returns {"engine", "temporal_depth", "s_per_step": {"engine/depth": s}}."""
+    """Times every (engine, temporal depth, launch form) that supports the
+    precision; stores and returns {"engine", "temporal_depth", "multistep",
+    "s_per_step": {candidate_key: s}}."""
     cache = cache or Cache()
-    timings = {f"{e}/{d}": timer(e, d, stencil, precision, ny, nx, steps)
-               for e, d in CANDIDATES[precision]}
+    timings = {candidate_key(e, d, m): timer(e, d, stencil, precision, ny, nx, steps, m)
+               for e, d, m in CANDIDATES[precision]}
     best = pick_fastest(timings)
-    engine, depth = best.split("/")
-    entry = {"engine": engine, "temporal_depth": int(depth), "s_per_step": timings,
+    parts = best.split("/")
+    entry = {"engine": parts[0], "temporal_depth": int(parts[1]),
+             "multistep": int(len(parts) > 2), "s_per_step": timings,
              "measured_on": [ny, nx], "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
     cache.section("sweep")[sweep_key(stencil, precision, ny, nx)] = entry
     cache.save()
@@ -161,7 +172,16 @@ def best_config(stencil: str, precision: str, ny: int, nx: int,
     e = cache.lookup("sweep", sweep_key(stencil, precision, ny, nx))
     if e:
         return e["engine"], int(e.get("temporal_depth", 1))
-    return CANDIDATES[precision][0]
+    return CANDIDATES[precision][0][:2]
+
+
+def best_launch(stencil: str, precision: str, ny: int, nx: int, cache: Cache | None = None) -> int:
+    """The tuned launch form for this problem class: 1 (one launch for all
+    steps of a call), 0 (one launch per step), or -1 (not tuned: the
+    library's size rule)."""
+    cache = cache or Cache()
+    e = cache.lookup("sweep", sweep_key(stencil, precision, ny, nx))
+    return int(e["multistep"]) if e and "multistep" in e else -1
 
 
 def best_engine(stencil: str, precision: str, ny: int, nx: int, cache: Cache | None = None) -> str:
@@ -223,7 +243,7 @@ def main():
     if args.sweep or not args.serve:
         for stencil in RADIUS:
             for precision in ("f16", "split"):
-                for n in (256, 1024, 4096, 8196):
+                for n in (256, 1024, 2048, 4096, 8196):
                     e = tune_sweep(stencil, precision, n, n, cache=cache)
                     print(json.dumps({"key": sweep_key(stencil, precision, n, n), **e}))
     if args.serve:

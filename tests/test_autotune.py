@@ -37,15 +37,26 @@ def test_shipped_results_back_up_an_empty_cache(tmp_path):
     assert autotune.best_round_steps(2000.0, cache=c) == 8
 
 
-def test_split_tries_both_temporal_depths(tmp_path):
+def test_split_tries_both_temporal_depths_and_launch_forms(tmp_path):
     seen = []
     cache = autotune.Cache(str(tmp_path / "t.json"), shipped=None)
     e = autotune.tune_sweep("box2d1r", "split", 64, 64, cache=cache,
-                            timer=lambda eng, depth, *a: seen.append((eng, depth)) or 1.0 / depth)
-    assert seen == [("tensor", 1), ("tensor", 2)]
-    assert e["engine"] == "tensor" and e["temporal_depth"] == 2
+                            timer=lambda eng, depth, *a: seen.append((eng, depth, a[-1])) or 1.0 / depth)
+    assert seen == [("tensor", 1, 0), ("tensor", 1, 1), ("tensor", 2, 0)]
+    assert set(e["s_per_step"]) == {"tensor/1", "tensor/1/m", "tensor/2"}
+    assert e["engine"] == "tensor" and e["temporal_depth"] == 2 and e["multistep"] == 0
     assert autotune.best_config("box2d1r", "split", 60, 33, cache=cache) == ("tensor", 2)
     assert autotune.best_config("box2d2r", "split", 60, 33, cache=cache) == ("tensor", 1)
+
+
+def test_launch_form_is_tuned_and_looked_up(tmp_path):
+    cache = autotune.Cache(str(tmp_path / "t.json"), shipped=None)
+    times = {("tensor", 1, 0): 3.0, ("tensor", 1, 1): 2.0, ("cudacore", 1, 0): 9.0}
+    e = autotune.tune_sweep("box2d2r", "f16", 5000, 5000, cache=cache,
+                            timer=lambda eng, depth, *a: times[(eng, depth, a[-1])])
+    assert e["engine"] == "tensor" and e["temporal_depth"] == 1 and e["multistep"] == 1
+    assert autotune.best_launch("box2d2r", "f16", 4500, 6000, cache=cache) == 1
+    assert autotune.best_launch("box2d2r", "f16", 300, 300, cache=cache) == -1  # not tuned
 
 
 def test_serve_choice_prefers_low_p99_among_those_keeping_up(tmp_path):
@@ -68,7 +79,7 @@ def test_real_tuning_pass_and_auto_engine(tcs, torch_cuda, tmp_path, monkeypatch
     assert e["engine"] in ("tensor", "cudacore")
     assert all(t > 0 for t in e["s_per_step"].values())
     s = autotune.tune_sweep("star2d2r", "split", 512, 512, steps=6)
-    assert set(s["s_per_step"]) == {"tensor/1", "tensor/2"}
+    assert set(s["s_per_step"]) == {"tensor/1", "tensor/1/m", "tensor/2"}
     p = tcs.Plan(512, 512, "star2d2r", np.full((5, 5), 0.04, np.float32), engine="auto")
     g = np.random.default_rng(0).uniform(-1, 1, (512, 512)).astype(np.float32)
     p.upload(g)
