@@ -47,10 +47,17 @@
 //                for radius-2 stencils (warp 1 also owns TMEM)
 //   next 8       epilogue (two warpgroups, one per column half):
 //                TMEM -> registers -> FP16 -> global
+//   last         signal: with several steps per launch, publishes finished
+//                tile rows (see "several steps per launch" below)
 // One accumulator slot per issuer lets the epilogue of one tile overlap the
 // MMAs of the next; tile i uses slot i % I, issued by warp 1 + i % I.  Every
 // wait is bounded; on timeout the kernel records an error word, stops,
 // drains its own copies and MMAs, frees TMEM and returns.
+//
+// Launches: one step per launch, overlapped with the next step's set-up by
+// programmatic dependent launch; or, for a plan's multi-step call on a large
+// grid, all steps in one cooperative launch whose tiles of step j wait only
+// for the neighbouring tile rows of step j-1.
 #include "tc_core.cuh"
 
 namespace tcs {

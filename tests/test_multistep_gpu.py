@@ -125,3 +125,25 @@ def test_launch_switches_change_no_bits(tmp_path, torch_cuda, env):
     base = run({"TCS_PDL": "1", "TCS_MULTI": "1"}, "base.npy")
     got = run(env, "got.npy")
     np.testing.assert_array_equal(base, got)
+
+
+def test_launch_count_query(tcs, torch_cuda):
+    """tcs_plan_launches reports what run(steps) launches: the size rule, the
+    forced forms, and temporal-depth pairs."""
+    B = normalized_coeffs(np.random.default_rng(1), "box2d2r")
+    big = tcs.Plan(4100, 4100, "box2d2r", B, engine="tensor", precision="f16")
+    assert big.launches(100) == 1 and big.launches(1) == 1
+    big.set_multistep(0)
+    assert big.launches(100) == 100
+    big.close()
+    small = tcs.Plan(300, 300, "box2d2r", B, engine="tensor", precision="f16")
+    assert small.launches(10) == 10  # few tiles per SM: one launch per step
+    small.set_multistep(1)
+    assert small.launches(10) == 1
+    small.close()
+    pairs = tcs.Plan(300, 300, "box2d2r", B, engine="tensor", precision="split", temporal_depth=2)
+    assert pairs.launches(7) == 4
+    pairs.close()
+    cc = tcs.Plan(300, 300, "box2d2r", B, engine="cudacore", precision="f16")
+    assert cc.launches(5) == 5
+    cc.close()
