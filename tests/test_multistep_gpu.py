@@ -96,17 +96,19 @@ sys.path.insert(0, sys.argv[1])
 import tcstencil_gb300 as tcs
 from helpers import grid, normalized_coeffs
 rng = np.random.default_rng(5)
-A = grid(rng, 700, 500)
 out = []
-for st, prec in (("box2d2r", "f16"), ("star2d1r", "f16"), ("box2d1r", "split")):
+for (ny, nx), st, prec in (((700, 500), "box2d2r", "f16"), ((700, 500), "star2d1r", "f16"),
+                           ((700, 500), "box2d1r", "split"), ((2100, 1500), "box2d1r", "f16"),
+                           ((2100, 1500), "star2d2r", "f16")):
+    A = grid(rng, ny, nx)
     B = normalized_coeffs(rng, st)
-    p = tcs.Plan(700, 500, st, B, engine="tensor", precision=prec, temporal_depth=1)
+    p = tcs.Plan(ny, nx, st, B, engine="tensor", precision=prec, temporal_depth=1)
     p.set_multistep(1)
     p.upload(A); p.run(9)
     o = np.empty_like(A); p.download(o); p.close()
-    out.append(o)
+    out.append(o.ravel())
 assert tcs.device_error() == 0
-np.save(sys.argv[2], np.stack(out))
+np.save(sys.argv[2], np.concatenate(out))
 """
 
 
