@@ -343,9 +343,14 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
             const uint32_t band = smem_u32(band_base);
             const uint32_t col = (uint32_t)(id * Mode<false>::ACC);  // this issuer's slot
             int i = id;
-            for (int k = blockIdx.x + id * (int)gridDim.x; k < n_items && !stop;
-                 k += Sweep<S>::ISSUERS * (int)gridDim.x, i += Sweep<S>::ISSUERS) {
-                const int t = k % n_tiles;
+            // the tile's column, kept incrementally (t mod tiles_x; the step
+            // wrap, a multiple of tiles_x, leaves it unchanged)
+            const int k0 = blockIdx.x + id * (int)gridDim.x;
+            const int dtx = (Sweep<S>::ISSUERS * (int)gridDim.x) % tiles_x;
+            int tx = k0 % tiles_x;
+            for (int k = k0; k < n_items && !stop;
+                 k += Sweep<S>::ISSUERS * (int)gridDim.x, i += Sweep<S>::ISSUERS,
+                 tx = tx + dtx >= tiles_x ? tx + dtx - tiles_x : tx + dtx) {
                 const int s = i % NS;  // one of this issuer's stages
                 if (!mbar_wait(&full[s], (i / NS) & 1, abort_flag)) {
                     record_error(&g_tc_error, kErrWaitFull);
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
                     smem_u32(stage_base + (size_t)s * NP * SG::PLANE), SG::CHUNK, 128);
                 tc_fence_after();
                 issue_plain_tile<C::R, SG>(a_hi0, band, tmem_base + col,
-                                           tile_windows(p.g.nx, (t % tiles_x) * kTile));
+                                           tile_windows(p.g.nx, tx * kTile));
                 umma_commit(&acc_full[id]);
                 umma_commit(&empty[s]);
             }
