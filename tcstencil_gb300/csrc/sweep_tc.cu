@@ -78,6 +78,35 @@ __device__ int g_tc_error = 0;
 // order, as a tile starts only after its own row finished the step before, so
 // "row r finished step j-1" is count >= j * (epilogue warps) * tiles_x.
 
+// Walks a CTA's items k0, k0 + stride, ... as (step, tile row, tile column)
+// without a division per item: item k is step * n_tiles + ty * tiles_x + tx.
+struct TileWalk {
+    int step, ty, tx, dy, dx, tiles_x, tiles_y;
+    __device__ void init(int k0, int stride, int tiles_x_, int tiles_y_) {
+        tiles_x = tiles_x_;
+        tiles_y = tiles_y_;
+        const int n_tiles = tiles_x * tiles_y;
+        step = k0 / n_tiles;
+        const int t = k0 - step * n_tiles;
+        ty = t / tiles_x;
+        tx = t - ty * tiles_x;
+        dy = stride / tiles_x;
+        dx = stride - dy * tiles_x;
+    }
+    __device__ void advance() {
+        tx += dx;
+        ty += dy;
+        if (tx >= tiles_x) {
+            tx -= tiles_x;
+            ty++;
+        }
+        while (ty >= tiles_y) {
+            ty -= tiles_y;
+            step++;
+        }
+    }
+};
+
 // The producer's side: which rows of which step it already knows finished.
 struct RowDeps {
     int ver_s = -1, ver_hi = -1;  // rows from this CTA's first row of step ver_s up to ver_hi
@@ -299,10 +328,11 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
             int last_issued = -1;
             RowDeps deps;
             const unsigned per_row = (unsigned)(kEpiWarps * tiles_x);
-            for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++) {
-                const int step = k / n_tiles;
-                const int t = k - step * n_tiles;
-                const int ty = t / tiles_x;
+            TileWalk w;
+            w.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+            for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++, w.advance()) {
+                const int step = w.step;
+                const int ty = w.ty;
                 const int s = i % NS;
                 const uint32_t ph = (i / NS) & 1;
                 if (step > 0 && !deps.wait(p.rows_done, step, ty, tiles_y, per_row)) {
@@ -318,8 +348,7 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
                 }
                 mbar_arrive_expect_tx(&full[s], NP * SG::PLANE);
                 load_tile_map((step & 1) ? &p.map_out : &p.map_hi, &p.map_lo, NP, ty * kTile,
-                              (t - ty * tiles_x) * kTile, stage_base + (size_t)s * NP * SG::PLANE,
-                              &full[s]);
+                              w.tx * kTile, stage_base + (size_t)s * NP * SG::PLANE, &full[s]);
                 last_issued = i;
             }
             // Drain: every stage armed last must have landed before exit.
@@ -402,12 +431,12 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
         bool stop = false;
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
         int i = 0;
-        for (int k = blockIdx.x; k < n_items && !stop; k += gridDim.x, i++) {
-            const int step = k / n_tiles;
-            const int t = k - step * n_tiles;
-            const int ty = t / tiles_x;
-            const int Y0 = ty * kTile;
-            const int X0 = (t - ty * tiles_x) * kTile;
+        TileWalk w;
+        w.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+        for (int k = blockIdx.x; k < n_items && !stop; k += gridDim.x, i++, w.advance()) {
+            const int step = w.step;
+            const int Y0 = w.ty * kTile;
+            const int X0 = w.tx * kTile;
             // odd steps run from the output plane back into the input plane
             o.in_hi = (step & 1) ? p.out_hi : p.in_hi;
             o.out_hi = (step & 1) ? const_cast<uint16_t *>(p.in_hi) : p.out_hi;
