@@ -595,10 +595,11 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
             int last_issued = -1;
             RowDeps deps;
             const unsigned per_row = (unsigned)(kRingEpiWarps * tiles_x);
-            int step = 0, t = (int)blockIdx.x - (int)gridDim.x;  // the item's step and tile
-            for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++) {
-                for (t += gridDim.x; t >= n_tiles; t -= n_tiles) step++;
-                const int ty = t / tiles_x;
+            TileWalk w;
+            w.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+            for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++, w.advance()) {
+                const int step = w.step;
+                const int ty = w.ty;
                 const int s = i % NS;
                 if (MULTI && step > 0 && !deps.wait(p.rows_done, step, ty, tiles_y, per_row)) {
                     record_error(&g_tc_error, kErrWaitDep);
@@ -615,8 +616,7 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
                 // odd steps run from the output planes back into the input planes
                 load_tile_map((step & 1) ? &p.map_out : &p.map_hi,
                               (step & 1) ? &p.map_out_lo : &p.map_lo, NP, ty * kTile,
-                              (t - ty * tiles_x) * kTile, stage_base + (size_t)s * NP * SG::PLANE,
-                              &full[s]);
+                              w.tx * kTile, stage_base + (size_t)s * NP * SG::PLANE, &full[s]);
                 last_issued = i;
             }
             for (int k = 0; k < NS && last_issued - k >= 0; k++) {
@@ -708,11 +708,12 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
             if (lane == 0) mbar_arrive(&win_empty[(G0 + w) % kRingSlots]);
         };
         int i = 0;
-        int step = 0, t = (int)blockIdx.x - (int)gridDim.x;  // the item's step and tile
-        for (int k = blockIdx.x; k < n_items; k += gridDim.x, G0 += kTileWindows, i++) {
-            for (t += gridDim.x; t >= n_tiles; t -= n_tiles) step++;
-            const int Y0 = (t / tiles_x) * kTile;
-            const int X0 = (t % tiles_x) * kTile;
+        TileWalk w;
+        w.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+        for (int k = blockIdx.x; k < n_items; k += gridDim.x, G0 += kTileWindows, i++, w.advance()) {
+            const int step = w.step;
+            const int Y0 = w.ty * kTile;
+            const int X0 = w.tx * kTile;
             if (MULTI) {
                 // odd steps run from the output planes back into the input planes
                 o.in_hi = (step & 1) ? p.out_hi : p.in_hi;
