@@ -165,7 +165,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(ring + kRing);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     volatile int *grid_error = p.error;
-    static_assert((2 * NS + 2 * NACC + 1 + 3 * kRing) * 8 + kRing * 12 + 8 <= 512, "barrier area");
+    static_assert((2 * NS + 2 * NACC + 1 + 3 * kRing) * 8 + kRing * sizeof(BatchItem) + 8 <= 512,
+                  "barrier area");
     int *tables = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(bars) + 512);
     const int n_table = p.n_steps + 1 + p.n_grids + 1;
     const bool tables_in_smem = n_table <= kTableInts;
@@ -248,6 +249,9 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     mbar_arrive(&item_ready[j]);
                     break;
                 }
+                // the tile's row and column, once, for every role
+                it.ty = it.tile / g.tiles_x;
+                it.tx = it.tile - it.ty * g.tiles_x;
                 ring[j] = it;
                 mbar_arrive(&item_ready[j]);
                 // step t > 0: every tile of the grid's previous step is stored;
@@ -290,8 +294,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 mbar_arrive_expect_tx(&full[s], C::PLANES * SG::PLANE + band_bytes);
                 const int in = (g.state + it.t) & 1;
                 const CUtensorMap *maps = g.maps + 2 * in;
-                load_tile_map(maps, maps + 1, C::PLANES, (it.tile / g.tiles_x) * kTile,
-                              (it.tile % g.tiles_x) * kTile, st, &full[s]);
+                load_tile_map(maps, maps + 1, C::PLANES, it.ty * kTile, it.tx * kTile, st, &full[s]);
                 bulk_load(st + C::PLANES * SG::PLANE, p.bands + g.band_base, band_bytes, &full[s]);
                 last_issued = i;
                 // the next item: decoded, its descriptor loads in flight
@@ -368,7 +371,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 const uint64_t a_hi0 = smem_desc(smem_u32(st), SG::CHUNK, 128);
                 const uint32_t band = smem_u32(st + C::PLANES * SG::PLANE);
                 if constexpr (SPLIT) {
-                    const int nwin = tile_windows(g.nx, (it.tile % g.tiles_x) * kTile);
+                    const int nwin = tile_windows(g.nx, it.tx * kTile);
 #pragma unroll 1
                     for (int w = 0; w < nwin; w++, G++) {
                         if ((G & 1) != id) continue;
@@ -491,8 +494,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             o.out_lo = in ? g.plane[0][1] : g.plane[1][1];
             o.pg = g.pg;
             o.y0 = g.y0; o.y1 = g.y1; o.x0 = g.x0; o.x1 = g.x1;
-            const int Y0 = (it.tile / g.tiles_x) * kTile;
-            const int X0 = (it.tile % g.tiles_x) * kTile;
+            const int Y0 = it.ty * kTile;
+            const int X0 = it.tx * kTile;
             // this warp's 32 rows all lie in the plane's padding below the grid:
             // nothing of them to load or store (padding only has to stay finite,
             // and it does: it keeps what it holds)

@@ -42,6 +42,7 @@ inline cudaError_t encode_grid_maps(const BatchGrid &g, CUtensorMap out[4]) {
 
 struct BatchItem {
     int g, t, tile;  // grid, step within the run, tile
+    int ty, tx;      // the tile's row and column (set by the producer when it publishes)
 };
 
 // One run's work: items are ordered step major and, within a step, by grid
