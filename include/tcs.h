@@ -218,7 +218,7 @@ int tcs_plan_set_temporal_depth(tcs_plan plan, int depth);
  * launch whose tiles of step j wait only for the neighbouring tile rows of
  * step j-1 (per-row completion counts), instead of one launch per step.
  * mode -1 (default): FP16 when a step has more than two tiles per SM, split
- * when it has more than one and at most twelve (where each measured
+ * when it has more than one and at most eight (where each measured
  * faster); 0: never; 1: always.  Results are bit-identical either way.
  * TCS_MULTI=0 in the environment turns it off for the process. */
 int tcs_plan_set_multistep(tcs_plan plan, int mode);

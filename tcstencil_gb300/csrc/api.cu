@@ -409,8 +409,10 @@ struct tcs_plan_s {
         // Split, box2d1r, us per step, one launch per step -> one launch:
         // 2048² 11.1 -> 8.8, 4096² 30.4 -> 27.1, 8196² 103.3 -> 107.0, 16386²
         // 379.6 -> 417.5: the multi-step split kernel spends ~10 % more per
-        // tile, which only the mid sizes' step overheads repay.
-        if (prob.precision == TCS_PREC_SPLIT) return tiles > sms && tiles <= 12 * sms;
+        // tile, which only the mid sizes' step overheads repay (the sweep
+        // harness: 4800², 9.5 tiles per SM, 44.5 us per step in one launch,
+        // slower than 3200² and 7200² per point).
+        if (prob.precision == TCS_PREC_SPLIT) return tiles > sms && tiles <= 8 * sms;
         return tiles > 2 * sms;
     }
     int steps_in_one(int steps, int from, cudaStream_t s) {
