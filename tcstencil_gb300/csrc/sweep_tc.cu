@@ -59,6 +59,7 @@
 // grid, all steps in one cooperative launch whose tiles of step j wait only
 // for the neighbouring tile rows of step j-1.
 #include "tc_core.cuh"
+#include "tile_walk.h"
 
 namespace tcs {
 
@@ -77,35 +78,6 @@ __device__ int g_tc_error = 0;
 // epilogue-warp completions over the launch.  A row's counts arrive in step
 // order, as a tile starts only after its own row finished the step before, so
 // "row r finished step j-1" is count >= j * (epilogue warps) * tiles_x.
-
-// Walks a CTA's items k0, k0 + stride, ... as (step, tile row, tile column)
-// without a division per item: item k is step * n_tiles + ty * tiles_x + tx.
-struct TileWalk {
-    int step, ty, tx, dy, dx, tiles_x, tiles_y;
-    __device__ void init(int k0, int stride, int tiles_x_, int tiles_y_) {
-        tiles_x = tiles_x_;
-        tiles_y = tiles_y_;
-        const int n_tiles = tiles_x * tiles_y;
-        step = k0 / n_tiles;
-        const int t = k0 - step * n_tiles;
-        ty = t / tiles_x;
-        tx = t - ty * tiles_x;
-        dy = stride / tiles_x;
-        dx = stride - dy * tiles_x;
-    }
-    __device__ void advance() {
-        tx += dx;
-        ty += dy;
-        if (tx >= tiles_x) {
-            tx -= tiles_x;
-            ty++;
-        }
-        while (ty >= tiles_y) {
-            ty -= tiles_y;
-            step++;
-        }
-    }
-};
 
 // The producer's side: which rows of which step it already knows finished.
 struct RowDeps {
@@ -186,9 +158,9 @@ __device__ void signal_rows(unsigned *rows_done, int n_items, int n_tiles, int t
         return true;
     };
     uint32_t i = 0;
-    int t = (int)blockIdx.x - (int)gridDim.x;  // the item's tile (k mod n_tiles)
-    for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++) {
-        for (t += gridDim.x; t >= n_tiles;) t -= n_tiles;
+    TileWalk w;
+    w.init(blockIdx.x, gridDim.x, tiles_x, n_tiles / tiles_x);
+    for (int k = blockIdx.x; k < n_items; k += gridDim.x, i++, w.advance()) {
         if (!finished(i + 1)) {
             flush();
             const uint64_t t0 = global_timer_ns();
@@ -203,7 +175,7 @@ __device__ void signal_rows(unsigned *rows_done, int n_items, int n_tiles, int t
                 __nanosleep(256);
             }
         }
-        pend[n_pend++] = t / tiles_x;
+        pend[n_pend++] = w.ty;
         if (n_pend == kBatch) flush();
     }
     flush();
