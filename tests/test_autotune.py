@@ -94,3 +94,21 @@ def test_real_tuning_pass_and_auto_engine(tcs, torch_cuda, tmp_path, monkeypatch
     ref.download(out2)
     torch_cuda.cuda.synchronize()
     np.testing.assert_array_equal(out, out2)
+
+
+def test_shipped_tuning_is_consistent():
+    """Every shipped sweep entry names a candidate the tuner tries for its
+    precision, and its choice is the fastest recorded time."""
+    shipped = json.load(open(autotune.SHIPPED))
+    assert shipped, "tuned.json is empty"
+    for dev, sections in shipped.items():
+        for key, e in sections.get("sweep", {}).items():
+            stencil, precision, size = key.split("/")
+            assert stencil in ("star2d1r", "star2d2r", "box2d1r", "box2d2r")
+            valid = {autotune.candidate_key(*c) for c in autotune.CANDIDATES[precision]}
+            assert set(e["s_per_step"]) <= valid, (dev, key)
+            chosen = autotune.candidate_key(e["engine"], e["temporal_depth"], e.get("multistep", 0))
+            assert chosen in e["s_per_step"], (dev, key)
+            assert e["s_per_step"][chosen] == min(e["s_per_step"].values()), (dev, key)
+        for key, e in sections.get("serve", {}).items():
+            assert int(e["round_steps"]) >= 0 and str(e["round_steps"]) in e["candidates"]
