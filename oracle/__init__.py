@@ -22,6 +22,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
+
+def ref_src_dir() -> str:
+    """Where the reference's sources are: $TCS_REF_DIR, else a TCStencil
+    checkout named `reference` beside this repository."""
+    return os.environ.get("TCS_REF_DIR") or os.path.abspath(
+        os.path.join(HERE, "..", "..", "reference"))
+
 STENCILS = {"star2d1r": 0, "star2d2r": 1, "box2d1r": 2, "box2d2r": 3}
 RADIUS = {"star2d1r": 1, "star2d2r": 2, "box2d1r": 1, "box2d2r": 2}
 SPLIT_SCALE = 2048.0
@@ -68,6 +75,10 @@ def lib() -> ctypes.CDLL:
         L.oracle_check_error_2d.argtypes = [I, P, P, I, I, I, I, ctypes.c_double, P]
         L.oracle_gold_bench.argtypes = [P, P, I, I, I, I, I]
         L.oracle_gold_bench.restype = ctypes.c_double
+        L.oracle_gold_loop_step.argtypes = [P, P, P, I, I, I]
+        L.oracle_gold_loop_step.restype = I
+        L.oracle_gold_bench_bands.argtypes = [P, P, I, I, I, I, I, I, P]
+        L.oracle_gold_bench_bands.restype = ctypes.c_double
         L.oracle_stencil_taps.argtypes = [I, P, P]
         L.oracle_stencil_taps.restype = I
         _lib = L
@@ -248,6 +259,32 @@ def gold_bench(init: np.ndarray, B, stencil: str, steps: int, threads: int) -> f
                                    STENCILS[stencil], steps, threads)
 
 
+def gold_loop_step(A: np.ndarray, B, stencil: str, C: np.ndarray | None = None):
+    """One gold step in gold's own loop shape (per-tap store into the output
+    cell for box stencils); the same bits as gold_step."""
+    A = np.ascontiguousarray(A, np.float32)
+    C = np.zeros_like(A) if C is None else np.ascontiguousarray(C, np.float32).copy()
+    Bc = _coef(B, stencil)
+    assert lib().oracle_gold_loop_step(_p(A), _p(Bc), _p(C), A.shape[0], A.shape[1],
+                                       STENCILS[stencil]) == 0
+    return C
+
+
+def gold_bench_bands(init: np.ndarray, B, stencil: str, steps: int, threads: int,
+                     loop_shape: bool = True, want_out: bool = False):
+    """Wall seconds for `steps` ping-pong gold steps of ONE grid, `threads`
+    threads on row bands; loop_shape selects gold's own loop shape.  With
+    want_out, returns (seconds, final grid)."""
+    init = np.ascontiguousarray(init, np.float32)
+    Bc = _coef(B, stencil)
+    out = np.empty_like(init) if want_out else None
+    t = lib().oracle_gold_bench_bands(_p(init), _p(Bc), init.shape[0], init.shape[1],
+                                      STENCILS[stencil], steps, threads, int(loop_shape),
+                                      _p(out) if want_out else None)
+    assert t >= 0, t
+    return (t, out) if want_out else t
+
+
 # ------------------------------------------------------- reference build --
 class Ref:
     """The reference's own gold()/layout16 helpers, compiled by `make -C oracle
@@ -261,9 +298,8 @@ class Ref:
     @staticmethod
     def build(ref_src: str | None = None) -> bool:
         env = dict(os.environ)
-        if ref_src:
-            env["TCS_REF_DIR"] = ref_src
-        src = env.get("TCS_REF_DIR", "/root/reference")
+        src = ref_src or ref_src_dir()
+        env["TCS_REF_DIR"] = src
         if not os.path.isdir(os.path.join(src, "common")):
             return False
         subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref", "refgpu"], check=True, env=env)

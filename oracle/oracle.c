@@ -498,6 +498,55 @@ void oracle_check_error_2d(int N, const float *output, const float *reference, i
     out[2] = sqrt(r2 / cnt);
 }
 
+/* ------------------------------------------------ gold's own loop shape --- */
+/* One gold step written the way common/gold_*.cpp writes it, for timing the
+ * reference's CPU code as it runs (oracle_gold_step_f32 above is the same
+ * arithmetic with a register accumulator and a tap table):
+ *   box stencils (gold_box2d1r.cpp:8-14, gold_box2d2r.cpp:8-14): the output
+ *     cell is zeroed and then accumulated in place, one tap at a time, with
+ *     the tap's row and column taken as k / n and k % n.  C may alias A as far
+ *     as the compiler knows, so every tap reloads and stores the cell;
+ *   star stencils (gold_star2d1r.cpp:8-13, gold_star2d2r.cpp:8-15): one
+ *     expression of products summed left to right.
+ * Rows [row0, row1) of the interior [r, ny-r) x [r, nx-r) are written. */
+static void gold_loop_rows(const float *A, const float *B, float *C, int ny, int nx, int stencil,
+                           int row0, int row1) {
+    (void)ny;
+    if (stencil == ST_BOX2D1R || stencil == ST_BOX2D2R) {
+        int n = stencil == ST_BOX2D1R ? 3 : 5, r = n / 2;
+        for (int i = row0; i < row1; i++)
+            for (int j = r; j < nx - r; j++) {
+                float *c = C + (long)i * nx + j;
+                *c = 0;
+                for (int k = 0; k < n * n; k++)
+                    *c += A[(long)(i - r + k / n) * nx + (j - r + k % n)] * B[(k / n) * n + k % n];
+            }
+    } else if (stencil == ST_STAR2D1R) {
+        for (int i = row0; i < row1; i++)
+            for (int j = 1; j < nx - 1; j++) {
+                const float *a = A + (long)i * nx + j;
+                C[(long)i * nx + j] = a[-nx] * B[1] + a[0] * B[4] + a[nx] * B[7] + a[-1] * B[3] +
+                                      a[1] * B[5];
+            }
+    } else {
+        for (int i = row0; i < row1; i++)
+            for (int j = 2; j < nx - 2; j++) {
+                const float *a = A + (long)i * nx + j;
+                C[(long)i * nx + j] = a[-2 * nx] * B[2] + a[-nx] * B[7] + a[0] * B[12] +
+                                      a[nx] * B[17] + a[2 * nx] * B[22] + a[-2] * B[10] +
+                                      a[-1] * B[11] + a[1] * B[13] + a[2] * B[14];
+            }
+    }
+}
+
+/* One step in gold's loop shape over gold's whole interior. */
+int oracle_gold_loop_step(const float *A, const float *B, float *C, int ny, int nx, int stencil) {
+    int r = oracle_stencil_radius(stencil);
+    if (r < 0) return -1;
+    gold_loop_rows(A, B, C, ny, nx, stencil, r, ny - r);
+    return 0;
+}
+
 /* ---------------------------------------------- CPU throughput harness --- */
 /* Runs `threads` POSIX threads, each sweeping its own copy of an ny x nx FP32
  * grid with gold for `steps` steps (the all-cores plan: independent copies,
@@ -542,5 +591,71 @@ double oracle_gold_bench(const float *init, const float *B, int ny, int nx, int 
     clock_gettime(CLOCK_MONOTONIC, &t1);
     for (int t = 0; t < threads; t++) { free(args[t].a); free(args[t].b); }
     free(args); free(tid);
+    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+/* One grid, `threads` POSIX threads on row bands of gold's interior, `steps`
+ * ping-pong steps with a barrier between steps (both buffers start as the
+ * input, so the border stays fixed).  loop_shape 1 runs gold's own loop shape
+ * (gold_loop_rows), 0 the register-accumulator form (oracle_gold_step_f32).
+ * Returns elapsed wall seconds of the steps (buffers are set up before the
+ * clock starts), or < 0 on error.  If `out` is not NULL the final state is
+ * copied there. */
+typedef struct {
+    float *a, *b;
+    const float *B;
+    int ny, nx, stencil, steps, row0, row1, loop_shape;
+    pthread_barrier_t *bar;
+} band_arg;
+
+static void *band_worker(void *p) {
+    band_arg *g = (band_arg *)p;
+    float *cur = g->a, *nxt = g->b;
+    int r = oracle_stencil_radius(g->stencil);
+    for (int t = 0; t < g->steps; t++) {
+        if (g->row1 > g->row0) {
+            if (g->loop_shape)
+                gold_loop_rows(cur, g->B, nxt, g->ny, g->nx, g->stencil, g->row0, g->row1);
+            else
+                oracle_gold_step_f32(cur, g->B, nxt, g->ny, g->nx, g->stencil, g->row0, g->row1,
+                                     r, g->nx - r);
+        }
+        pthread_barrier_wait(g->bar);
+        float *s = cur; cur = nxt; nxt = s;
+    }
+    return NULL;
+}
+
+double oracle_gold_bench_bands(const float *init, const float *B, int ny, int nx, int stencil,
+                               int steps, int threads, int loop_shape, float *out) {
+    int r = oracle_stencil_radius(stencil);
+    if (r < 0 || threads < 1 || steps < 0 || ny <= 2 * r) return -1.0;
+    long cells = (long)ny * nx;
+    float *a = (float *)malloc(cells * sizeof(float));
+    float *b = (float *)malloc(cells * sizeof(float));
+    band_arg *args = (band_arg *)calloc(threads, sizeof(band_arg));
+    pthread_t *tid = (pthread_t *)calloc(threads, sizeof(pthread_t));
+    if (!a || !b || !args || !tid) { free(a); free(b); free(args); free(tid); return -2.0; }
+    memcpy(a, init, cells * sizeof(float));
+    memcpy(b, init, cells * sizeof(float));
+    pthread_barrier_t bar;
+    pthread_barrier_init(&bar, NULL, (unsigned)threads);
+    int rows = ny - 2 * r;
+    for (int t = 0; t < threads; t++) {
+        args[t].a = a; args[t].b = b; args[t].B = B;
+        args[t].ny = ny; args[t].nx = nx; args[t].stencil = stencil; args[t].steps = steps;
+        args[t].row0 = r + (int)((long)rows * t / threads);
+        args[t].row1 = r + (int)((long)rows * (t + 1) / threads);
+        args[t].loop_shape = loop_shape;
+        args[t].bar = &bar;
+    }
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int t = 0; t < threads; t++) pthread_create(&tid[t], NULL, band_worker, &args[t]);
+    for (int t = 0; t < threads; t++) pthread_join(tid[t], NULL);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    pthread_barrier_destroy(&bar);
+    if (out) memcpy(out, steps % 2 ? b : a, cells * sizeof(float));
+    free(a); free(b); free(args); free(tid);
     return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }

@@ -57,7 +57,7 @@ def ref_sweep(R: oracle.Ref, A: np.ndarray, B: np.ndarray, stencil: str, steps: 
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-src", default=os.environ.get("TCS_REF_DIR", "/root/reference"))
+    ap.add_argument("--ref-src", default=oracle.ref_src_dir())
     args = ap.parse_args()
     if not oracle.Ref.build(args.ref_src):
         sys.exit(f"reference sources not found at {args.ref_src}")

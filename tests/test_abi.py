@@ -96,7 +96,7 @@ def test_band_builders_bit_exact(tcs, golden, stencil):
 def test_reference_driver_links_against_the_shim(tcs, tmp_path):
     """common/main_1r.cu and main_2r.cu of the reference, unchanged, link with the
     per-variant host_code libraries (where the reference sources exist)."""
-    ref = os.environ.get("TCS_REF_DIR", "/root/reference")
+    ref = oracle.ref_src_dir()
     if not os.path.isdir(os.path.join(ref, "common")):
         pytest.skip("reference sources not present")
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"

@@ -28,6 +28,23 @@ def test_gold_sweep_matches_reference_fixtures(golden, stencil):
         np.testing.assert_array_equal(out.view(np.uint32), g[f"sweep5_{N}"].view(np.uint32))
 
 
+@pytest.mark.parametrize("stencil", STENCILS)
+def test_gold_loop_shape_port_matches_reference_fixtures(golden, stencil):
+    """The port in gold's own loop shape (timed as the CPU baseline) gives the
+    reference's bits, alone and as the threaded row-band ping-pong."""
+    g = golden(f"gold_{stencil}.npz")
+    for N in (16, 37, 64):
+        for tag in ("refB", "normB"):
+            A, B = g[f"A_{N}_{tag}"], g[f"B_{N}_{tag}"]
+            out = oracle.gold_loop_step(A, B, stencil, g[f"Cin_{N}_{tag}"])
+            np.testing.assert_array_equal(out.view(np.uint32), g[f"Cout_{N}_{tag}"].view(np.uint32))
+        for threads in (1, 3, 8):
+            for shape in (True, False):
+                _, out = oracle.gold_bench_bands(g[f"A_{N}_normB"], g[f"B_{N}_normB"], stencil, 5,
+                                                 threads, loop_shape=shape, want_out=True)
+                np.testing.assert_array_equal(out.view(np.uint32), g[f"sweep5_{N}"].view(np.uint32))
+
+
 def test_layout_helpers_match_reference_fixtures(golden):
     g = golden("layout16.npz")
     one = int(np.float16(1.0).view(np.uint16))
