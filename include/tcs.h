@@ -164,21 +164,24 @@ int tcs_sweep_step(const tcs_step_args *args, const void *d_in, const void *d_in
 
 /* ------------------------------------------------ sweeps without allocation
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
- * where they sweep: code running while a CUDA graph is being captured, real-
- * time loops that forbid allocator calls and the synchronisation they bring,
- * and hosts whose device memory is all handed out by a pool or budget they do
- * not own.  d_out receives `steps` FP16 Jacobi steps of d_in (planes as in
- * tcs_sweep_step; d_in is only read; precision must be TCS_PREC_F16).  The
- * ping-pong partner plane is a library-owned static device array of
+ * where they sweep: real-time loops that forbid allocator calls and the device
+ * synchronisation they may bring, and hosts whose device memory is all handed
+ * out by a pool or budget they do not own.  d_out receives `steps` FP16 Jacobi
+ * steps of d_in (planes as in tcs_sweep_step; d_in is only read, and its
+ * padding must be finite; precision must be TCS_PREC_F16).  The ping-pong
+ * partner plane is a library-owned static device array of
  * tcs_noalloc_scratch_bytes() = 32 MiB, held by every GPU that loads the
  * library until exit: grids whose plane (tcs_plane_elems) has up to
- * 16,777,216 cells (e.g. 4000 x 4000); larger ones are rejected with
- * TCS_ERR_INVALID.  No device memory is
- * allocated.  The first call on a device looks up the array's device address
- * (and configures the tensor kernel): make that first call before any stream
- * capture.  All calls on a device share the array, so calls that overlap on
- * the GPU (other streams or threads) race on it; each call overwrites what it
- * uses, so nothing needs clearing between calls. */
+ * 16,777,216 cells (square grids up to 3968 x 3968); larger ones are rejected
+ * with TCS_ERR_INVALID.  No device memory is allocated.  The first call on a
+ * device looks up the array's device address (and configures the tensor
+ * kernel): make that first call before any stream capture.  The address is
+ * kept for the process, so after cudaDeviceReset the entry point must not be
+ * used on that device again.  All calls on a device share the array and keep
+ * the last call's contents; each call first copies d_in (padding included)
+ * over the part of the array it uses and over d_out, so nothing left by an
+ * earlier call is read.  Calls that overlap on the GPU (other streams or
+ * threads) race on the array. */
 size_t tcs_noalloc_scratch_bytes(void);
 int tcs_sweep_steps_noalloc(const tcs_step_args *args, const void *d_in, void *d_out, int steps,
                             void *stream);

@@ -73,8 +73,6 @@ def lib() -> ctypes.CDLL:
         L.oracle_init_coe_star.argtypes = [P, I, P, P]
         L.oracle_init_coe_box.argtypes = [P, I, P]
         L.oracle_check_error_2d.argtypes = [I, P, P, I, I, I, I, ctypes.c_double, P]
-        L.oracle_gold_bench.argtypes = [P, P, I, I, I, I, I]
-        L.oracle_gold_bench.restype = ctypes.c_double
         L.oracle_gold_loop_step.argtypes = [P, P, P, I, I, I]
         L.oracle_gold_loop_step.restype = I
         L.oracle_gold_bench_bands.argtypes = [P, P, I, I, I, I, I, I, P]
@@ -249,14 +247,6 @@ def check_error_2d(N, output, reference, y_lb, y_ub, x_lb, x_ub, min_number=1e-6
     r = np.ascontiguousarray(reference, np.float32)
     lib().oracle_check_error_2d(N, _p(o), _p(r), y_lb, y_ub, x_lb, x_ub, min_number, _p(out))
     return {"rms_abs": out[0], "max_abs": out[1], "rms_rel": out[2]}
-
-
-def gold_bench(init: np.ndarray, B, stencil: str, steps: int, threads: int) -> float:
-    """Wall seconds for `threads` threads each sweeping its own copy with gold."""
-    init = np.ascontiguousarray(init, np.float32)
-    Bc = _coef(B, stencil)
-    return lib().oracle_gold_bench(_p(init), _p(Bc), init.shape[0], init.shape[1],
-                                   STENCILS[stencil], steps, threads)
 
 
 def gold_loop_step(A: np.ndarray, B, stencil: str, C: np.ndarray | None = None):

@@ -31,8 +31,14 @@
  *                       sum in double (split tensor kernel).
  *   oracle_step_f64     the same stencil in double (error reference).
  *
+ * Threaded CPU timing of gold (the CPU baseline of bench.py):
+ *   oracle_gold_loop_step,  gold's own loop shape (per-tap store into the
+ *   oracle_gold_bench_bands output cell for box stencils), one grid, threads
+ *                           on row bands.
+ *
  * The FP16 conversion below is the IEEE-754 binary16 round-to-nearest-even
- * rule, written from the format definition.
+ * rule, written from the format definition.  Steps of large grids run on row
+ * bands over POSIX threads; each cell's arithmetic is the same either way.
  */
 #include <math.h>
 #include <pthread.h>
@@ -40,6 +46,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#include <unistd.h>
 
 enum { ST_STAR2D1R = 0, ST_STAR2D2R = 1, ST_BOX2D1R = 2, ST_BOX2D2R = 3 };
 
@@ -223,6 +230,23 @@ void oracle_init_coe_box(const uint16_t *B, int n, uint16_t *coe) {
 }
 
 /* ------------------------------------------------------------- sweeps --- */
+/* Every step below computes each output cell with the same scalar code; a
+ * step of a large grid splits its rows into bands over POSIX threads
+ * (ORACLE_THREADS, default: the online processors), which changes no result
+ * bit.  FP16 inputs are widened through a table of all 65536 values, built
+ * once from f16_to_f64. */
+
+static double g_f16tab[65536];
+static pthread_once_t g_f16tab_once = PTHREAD_ONCE_INIT;
+
+static void f16tab_init(void) {
+    for (int h = 0; h < 65536; h++) g_f16tab[h] = f16_to_f64((uint16_t)h);
+}
+
+static const double *f16tab(void) {
+    pthread_once(&g_f16tab_once, f16tab_init);
+    return g_f16tab;
+}
 
 static void rect_default(int ny, int nx, int r, int *y0, int *y1, int *x0, int *x1) {
     if (*y0 == 0 && *y1 == 0 && *x0 == 0 && *x1 == 0) {
@@ -230,47 +254,224 @@ static void rect_default(int ny, int nx, int r, int *y0, int *y1, int *x0, int *
     }
 }
 
+enum { K_GOLD32, K_F64, K_F16CC, K_F32, K_F16TC, K_SPLIT };
+
+typedef struct {
+    int kind, ny, nx, stencil, y0, y1, x0, x1, nt, r, n, box;
+    int tdy[MAX_TAPS], tdx[MAX_TAPS];
+    long off[MAX_TAPS];
+    const void *A, *Al;
+    void *C, *Cl;
+    const float *Bf;
+    const double *Bd;
+    float cf[MAX_TAPS];
+    double cd[MAX_TAPS], chi[MAX_TAPS], cfl[MAX_TAPS], clo[MAX_TAPS], c3[MAX_TAPS];
+} step_ctx;
+
+/* Fills the tap table and the coefficient forms of each kind.  Returns -1 for
+ * an unknown stencil. */
+static int ctx_init(step_ctx *c, int kind, int ny, int nx, int stencil, int y0, int y1, int x0,
+                    int x1) {
+    memset(c, 0, sizeof(*c));
+    c->kind = kind; c->ny = ny; c->nx = nx; c->stencil = stencil;
+    c->nt = taps_for(stencil, &c->r, &c->n, c->tdy, c->tdx);
+    if (c->nt < 0) return -1;
+    rect_default(ny, nx, c->r, &y0, &y1, &x0, &x1);
+    c->y0 = y0; c->y1 = y1; c->x0 = x0; c->x1 = x1;
+    c->box = is_box(stencil);
+    for (int k = 0; k < c->nt; k++) c->off[k] = (long)c->tdy[k] * nx + c->tdx[k];
+    return 0;
+}
+
+static int coef_index(const step_ctx *c, int k) {
+    return (c->tdy[k] + c->r) * c->n + c->tdx[k] + c->r;
+}
+
+static void ctx_coeffs(step_ctx *c) {
+    for (int k = 0; k < c->nt; k++) {
+        int q = coef_index(c, k);
+        if (c->kind == K_F64) { c->cd[k] = c->Bd[q]; continue; }
+        double v = c->Bf[q];
+        c->cf[k] = c->Bf[q];
+        if (c->kind == K_F16TC) c->cd[k] = f16_to_f64(f64_to_f16(v));
+        if (c->kind == K_SPLIT) {
+            c->chi[k] = nearbyint(v * 2048.0) / 2048.0;
+            c->cfl[k] = f16_to_f64(f64_to_f16(v));
+            double rem = (v - c->chi[k]) * 2048.0;
+            c->clo[k] = f16_to_f64(f64_to_f16(rem));
+            c->c3[k] = f16_to_f64(f64_to_f16(rem - c->clo[k]));
+        }
+    }
+}
+
+static int inside(const step_ctx *c, int i, int j) {
+    return i >= c->y0 && i < c->y1 && j >= c->x0 && j < c->x1;
+}
+
+/* Rows [i0, i1) of one step. */
+static void step_rows(const step_ctx *c, int i0, int i1) {
+    const double *H = f16tab();
+    const int nx = c->nx, nt = c->nt;
+    for (int i = i0; i < i1; i++) {
+        int row_in = i >= c->y0 && i < c->y1;
+        switch (c->kind) {
+        case K_GOLD32: { /* gold: only the rectangle is written */
+            if (!row_in) break;
+            const float *A = (const float *)c->A;
+            float *C = (float *)c->C;
+            for (int j = c->x0; j < c->x1; j++) {
+                const float *p = A + (long)i * nx + j;
+                float s;
+                int k0;
+                if (c->box) { s = 0.0f; k0 = 0; }             /* C[i][j] = 0; C += ... */
+                else { s = p[c->off[0]] * c->cf[0]; k0 = 1; } /* a*b + c*d + ...      */
+                for (int k = k0; k < nt; k++) s = s + p[c->off[k]] * c->cf[k];
+                C[(long)i * nx + j] = s;
+            }
+            break;
+        }
+        case K_F32: { /* gold plus the fixed-border copy */
+            const float *A = (const float *)c->A;
+            float *C = (float *)c->C;
+            for (int j = 0; j < nx; j++) {
+                long o = (long)i * nx + j;
+                if (!inside(c, i, j)) { C[o] = A[o]; continue; }
+                const float *p = A + o;
+                float s;
+                int k0;
+                if (c->box) { s = 0.0f; k0 = 0; }
+                else { s = p[c->off[0]] * c->cf[0]; k0 = 1; }
+                for (int k = k0; k < nt; k++) s = s + p[c->off[k]] * c->cf[k];
+                C[o] = s;
+            }
+            break;
+        }
+        case K_F64: { /* only the rectangle is written */
+            if (!row_in) break;
+            const double *A = (const double *)c->A;
+            double *C = (double *)c->C;
+            for (int j = c->x0; j < c->x1; j++) {
+                long o = (long)i * nx + j;
+                double s = 0.0;
+                for (int k = 0; k < nt; k++) s += A[o + c->off[k]] * c->cd[k];
+                C[o] = s;
+            }
+            break;
+        }
+        case K_F16CC: {
+            const uint16_t *A = (const uint16_t *)c->A;
+            uint16_t *C = (uint16_t *)c->C;
+            for (int j = 0; j < nx; j++) {
+                long o = (long)i * nx + j;
+                if (!inside(c, i, j)) { C[o] = A[o]; continue; }
+                float acc = 0.0f;
+                for (int k = 0; k < nt; k++) acc = fmaf((float)H[A[o + c->off[k]]], c->cf[k], acc);
+                C[o] = f64_to_f16((double)acc);
+            }
+            break;
+        }
+        case K_F16TC: {
+            const uint16_t *A = (const uint16_t *)c->A;
+            uint16_t *C = (uint16_t *)c->C;
+            for (int j = 0; j < nx; j++) {
+                long o = (long)i * nx + j;
+                if (!inside(c, i, j)) { C[o] = A[o]; continue; }
+                double s = 0.0;
+                for (int k = 0; k < nt; k++) s += H[A[o + c->off[k]]] * c->cd[k];
+                C[o] = f64_to_f16(s);
+            }
+            break;
+        }
+        case K_SPLIT: {
+            const uint16_t *Ah = (const uint16_t *)c->A, *Al = (const uint16_t *)c->Al;
+            uint16_t *Ch = (uint16_t *)c->C, *Cl = (uint16_t *)c->Cl;
+            for (int j = 0; j < nx; j++) {
+                long o = (long)i * nx + j;
+                if (!inside(c, i, j)) { Ch[o] = Ah[o]; Cl[o] = Al[o]; continue; }
+                double main = 0.0, corr = 0.0;
+                for (int k = 0; k < nt; k++) {
+                    long q = o + c->off[k];
+                    double xh = H[Ah[q]], xl = H[Al[q]];
+                    main += c->chi[k] * xh;
+                    corr += c->cfl[k] * xl + c->clo[k] * xh + c->c3[k] * xh;
+                }
+                double v = main + corr / 2048.0;
+                uint16_t h = f64_to_f16(nearbyint(v * 2048.0) / 2048.0);
+                Ch[o] = h;
+                Cl[o] = f64_to_f16((v - H[h]) * 2048.0);
+            }
+            break;
+        }
+        }
+    }
+}
+
+static int oracle_threads(void) {
+    const char *e = getenv("ORACLE_THREADS");
+    long t = e ? atol(e) : sysconf(_SC_NPROCESSORS_ONLN);
+    return t < 1 ? 1 : t > 64 ? 64 : (int)t;
+}
+
+typedef struct { const step_ctx *c; int i0, i1; } band_job;
+
+static void *band_job_run(void *p) {
+    band_job *b = (band_job *)p;
+    step_rows(b->c, b->i0, b->i1);
+    return NULL;
+}
+
+/* One step over all ny rows, on row bands when the grid is large. */
+static void run_step(const step_ctx *c) {
+    int T = oracle_threads();
+    if ((long)c->ny * c->nx < (1L << 18) || T == 1 || c->ny < 2 * T) {
+        step_rows(c, 0, c->ny);
+        return;
+    }
+    pthread_t tid[64];
+    band_job jobs[64];
+    for (int t = 0; t < T; t++) {
+        jobs[t].c = c;
+        jobs[t].i0 = (int)((long)c->ny * t / T);
+        jobs[t].i1 = (int)((long)c->ny * (t + 1) / T);
+        if (pthread_create(&tid[t], NULL, band_job_run, &jobs[t])) {
+            step_rows(c, jobs[t].i0, jobs[t].i1);
+            tid[t] = 0;
+        }
+    }
+    for (int t = 0; t < T; t++)
+        if (tid[t]) pthread_join(tid[t], NULL);
+}
+
 /* One gold step in FP32 over the update rectangle [y0,y1) x [x0,x1) (all zero
  * = gold's interior [r, n-r)).  C outside the rectangle is not written. */
 int oracle_gold_step_f32(const float *A, const float *B, float *C, int ny, int nx, int stencil,
                          int y0, int y1, int x0, int x1) {
-    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
-    int nt = taps_for(stencil, &r, &n, tdy, tdx);
-    if (nt < 0) return -1;
-    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
-    float cf[MAX_TAPS];
-    long off[MAX_TAPS];
-    for (int k = 0; k < nt; k++) {
-        cf[k] = B[(tdy[k] + r) * n + tdx[k] + r];
-        off[k] = (long)tdy[k] * nx + tdx[k];
-    }
-    int box = is_box(stencil);
-    for (int i = y0; i < y1; i++)
-        for (int j = x0; j < x1; j++) {
-            const float *p = A + (long)i * nx + j;
-            float s;
-            int k0;
-            if (box) { s = 0.0f; k0 = 0; }         /* C[i][j] = 0; C += ... */
-            else { s = p[off[0]] * cf[0]; k0 = 1; } /* a*b + c*d + ...      */
-            for (int k = k0; k < nt; k++) s = s + p[off[k]] * cf[k];
-            C[(long)i * nx + j] = s;
-        }
+    step_ctx c;
+    if (ctx_init(&c, K_GOLD32, ny, nx, stencil, y0, y1, x0, x1)) return -1;
+    c.A = A; c.C = C; c.Bf = B;
+    ctx_coeffs(&c);
+    run_step(&c);
     return 0;
+}
+
+/* The register-accumulator gold step on rows [row0, row1) only, in the
+ * calling thread (for the threaded CPU harness below). */
+static void gold_f32_rows(const float *A, const float *B, float *C, int ny, int nx, int stencil,
+                          int row0, int row1) {
+    step_ctx c;
+    if (ctx_init(&c, K_GOLD32, ny, nx, stencil, 0, 0, 0, 0)) return;
+    c.A = A; c.C = C; c.Bf = B;
+    ctx_coeffs(&c);
+    step_rows(&c, row0, row1);
 }
 
 int oracle_step_f64(const double *A, const double *B, double *C, int ny, int nx, int stencil,
                     int y0, int y1, int x0, int x1) {
-    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
-    int nt = taps_for(stencil, &r, &n, tdy, tdx);
-    if (nt < 0) return -1;
-    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
-    for (int i = y0; i < y1; i++)
-        for (int j = x0; j < x1; j++) {
-            double s = 0.0;
-            for (int k = 0; k < nt; k++)
-                s += A[(long)(i + tdy[k]) * nx + j + tdx[k]] * B[(tdy[k] + r) * n + tdx[k] + r];
-            C[(long)i * nx + j] = s;
-        }
+    step_ctx c;
+    if (ctx_init(&c, K_F64, ny, nx, stencil, y0, y1, x0, x1)) return -1;
+    c.A = A; c.C = C; c.Bd = B;
+    ctx_coeffs(&c);
+    run_step(&c);
     return 0;
 }
 
@@ -279,21 +480,11 @@ int oracle_step_f64(const double *A, const double *B, double *C, int ny, int nx,
  * rectangle copy the input. */
 int oracle_step_f16cc(const uint16_t *A, const float *B, uint16_t *C, int ny, int nx, int stencil,
                       int y0, int y1, int x0, int x1) {
-    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
-    int nt = taps_for(stencil, &r, &n, tdy, tdx);
-    if (nt < 0) return -1;
-    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
-    for (int i = 0; i < ny; i++)
-        for (int j = 0; j < nx; j++) {
-            long o = (long)i * nx + j;
-            if (i < y0 || i >= y1 || j < x0 || j >= x1) { C[o] = A[o]; continue; }
-            float acc = 0.0f;
-            for (int k = 0; k < nt; k++) {
-                float x = (float)f16_to_f64(A[o + (long)tdy[k] * nx + tdx[k]]);
-                acc = fmaf(x, B[(tdy[k] + r) * n + tdx[k] + r], acc);
-            }
-            C[o] = f64_to_f16((double)acc);
-        }
+    step_ctx c;
+    if (ctx_init(&c, K_F16CC, ny, nx, stencil, y0, y1, x0, x1)) return -1;
+    c.A = A; c.C = C; c.Bf = B;
+    ctx_coeffs(&c);
+    run_step(&c);
     return 0;
 }
 
@@ -301,33 +492,23 @@ int oracle_step_f16cc(const uint16_t *A, const float *B, uint16_t *C, int ny, in
  * copy the input (this is gold plus the fixed-border copy of a ping-pong). */
 int oracle_step_f32(const float *A, const float *B, float *C, int ny, int nx, int stencil,
                     int y0, int y1, int x0, int x1) {
-    int r = oracle_stencil_radius(stencil);
-    if (r < 0) return -1;
-    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
-    for (int i = 0; i < ny; i++)
-        for (int j = 0; j < nx; j++)
-            if (i < y0 || i >= y1 || j < x0 || j >= x1) C[(long)i * nx + j] = A[(long)i * nx + j];
-    return oracle_gold_step_f32(A, B, C, ny, nx, stencil, y0, y1, x0, x1);
+    step_ctx c;
+    if (ctx_init(&c, K_F32, ny, nx, stencil, y0, y1, x0, x1)) return -1;
+    c.A = A; c.C = C; c.Bf = B;
+    ctx_coeffs(&c);
+    run_step(&c);
+    return 0;
 }
 
 /* Tensor-core FP16 contract: FP16 in, coefficients rounded to FP16, exact
  * products, the sum taken in double, RNE to FP16. */
 int oracle_step_f16tc(const uint16_t *A, const float *B, uint16_t *C, int ny, int nx, int stencil,
                       int y0, int y1, int x0, int x1) {
-    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
-    int nt = taps_for(stencil, &r, &n, tdy, tdx);
-    if (nt < 0) return -1;
-    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
-    double ch[MAX_TAPS];
-    for (int k = 0; k < nt; k++) ch[k] = f16_to_f64(f64_to_f16(B[(tdy[k] + r) * n + tdx[k] + r]));
-    for (int i = 0; i < ny; i++)
-        for (int j = 0; j < nx; j++) {
-            long o = (long)i * nx + j;
-            if (i < y0 || i >= y1 || j < x0 || j >= x1) { C[o] = A[o]; continue; }
-            double s = 0.0;
-            for (int k = 0; k < nt; k++) s += f16_to_f64(A[o + (long)tdy[k] * nx + tdx[k]]) * ch[k];
-            C[o] = f64_to_f16(s);
-        }
+    step_ctx c;
+    if (ctx_init(&c, K_F16TC, ny, nx, stencil, y0, y1, x0, x1)) return -1;
+    c.A = A; c.C = C; c.Bf = B;
+    ctx_coeffs(&c);
+    run_step(&c);
     return 0;
 }
 
@@ -359,35 +540,11 @@ void oracle_join_f64(const uint16_t *hi, const uint16_t *lo, double *x, long n, 
  * ch*xh is a multiple of 2^-22, so the first sum is exact on the GPU too. */
 int oracle_step_split(const uint16_t *Ah, const uint16_t *Al, const float *B, uint16_t *Ch,
                       uint16_t *Cl, int ny, int nx, int stencil, int y0, int y1, int x0, int x1) {
-    int r, n, tdy[MAX_TAPS], tdx[MAX_TAPS];
-    int nt = taps_for(stencil, &r, &n, tdy, tdx);
-    if (nt < 0) return -1;
-    rect_default(ny, nx, r, &y0, &y1, &x0, &x1);
-    double chi[MAX_TAPS], cfl[MAX_TAPS], clo[MAX_TAPS], c3[MAX_TAPS];
-    for (int k = 0; k < nt; k++) {
-        double c = B[(tdy[k] + r) * n + tdx[k] + r];
-        chi[k] = nearbyint(c * SPLIT_SCALE) / SPLIT_SCALE;
-        cfl[k] = f16_to_f64(f64_to_f16(c));
-        double rem = (c - chi[k]) * SPLIT_SCALE;
-        clo[k] = f16_to_f64(f64_to_f16(rem));
-        c3[k] = f16_to_f64(f64_to_f16(rem - clo[k]));
-    }
-    for (int i = 0; i < ny; i++)
-        for (int j = 0; j < nx; j++) {
-            long o = (long)i * nx + j;
-            if (i < y0 || i >= y1 || j < x0 || j >= x1) { Ch[o] = Ah[o]; Cl[o] = Al[o]; continue; }
-            double main = 0.0, corr = 0.0;
-            for (int k = 0; k < nt; k++) {
-                long q = o + (long)tdy[k] * nx + tdx[k];
-                double xh = f16_to_f64(Ah[q]), xl = f16_to_f64(Al[q]);
-                main += chi[k] * xh;
-                corr += cfl[k] * xl + clo[k] * xh + c3[k] * xh;
-            }
-            double v = main + corr / SPLIT_SCALE;
-            uint16_t h = f64_to_f16(nearbyint(v * SPLIT_SCALE) / SPLIT_SCALE);
-            Ch[o] = h;
-            Cl[o] = f64_to_f16((v - f16_to_f64(h)) * SPLIT_SCALE);
-        }
+    step_ctx c;
+    if (ctx_init(&c, K_SPLIT, ny, nx, stencil, y0, y1, x0, x1)) return -1;
+    c.A = Ah; c.Al = Al; c.C = Ch; c.Cl = Cl; c.Bf = B;
+    ctx_coeffs(&c);
+    run_step(&c);
     return 0;
 }
 
@@ -548,52 +705,6 @@ int oracle_gold_loop_step(const float *A, const float *B, float *C, int ny, int 
 }
 
 /* ---------------------------------------------- CPU throughput harness --- */
-/* Runs `threads` POSIX threads, each sweeping its own copy of an ny x nx FP32
- * grid with gold for `steps` steps (the all-cores plan: independent copies,
- * gold itself unchanged).  Returns elapsed wall seconds, or < 0 on error. */
-
-typedef struct {
-    float *a, *b;
-    const float *B;
-    int ny, nx, stencil, steps;
-} bench_arg;
-
-static void *bench_worker(void *p) {
-    bench_arg *g = (bench_arg *)p;
-    float *cur = g->a, *nxt = g->b;
-    for (int t = 0; t < g->steps; t++) {
-        oracle_gold_step_f32(cur, g->B, nxt, g->ny, g->nx, g->stencil, 0, 0, 0, 0);
-        float *s = cur; cur = nxt; nxt = s;
-    }
-    return NULL;
-}
-
-double oracle_gold_bench(const float *init, const float *B, int ny, int nx, int stencil, int steps,
-                         int threads) {
-    if (threads < 1) threads = 1;
-    long cells = (long)ny * nx;
-    bench_arg *args = (bench_arg *)calloc(threads, sizeof(bench_arg));
-    pthread_t *tid = (pthread_t *)calloc(threads, sizeof(pthread_t));
-    if (!args || !tid) { free(args); free(tid); return -2.0; }
-    for (int t = 0; t < threads; t++) {
-        args[t].a = (float *)malloc(cells * sizeof(float));
-        args[t].b = (float *)malloc(cells * sizeof(float));
-        if (!args[t].a || !args[t].b) return -2.0;
-        memcpy(args[t].a, init, cells * sizeof(float));
-        memcpy(args[t].b, init, cells * sizeof(float));
-        args[t].B = B; args[t].ny = ny; args[t].nx = nx;
-        args[t].stencil = stencil; args[t].steps = steps;
-    }
-    struct timespec t0, t1;
-    clock_gettime(CLOCK_MONOTONIC, &t0);
-    for (int t = 0; t < threads; t++) pthread_create(&tid[t], NULL, bench_worker, &args[t]);
-    for (int t = 0; t < threads; t++) pthread_join(tid[t], NULL);
-    clock_gettime(CLOCK_MONOTONIC, &t1);
-    for (int t = 0; t < threads; t++) { free(args[t].a); free(args[t].b); }
-    free(args); free(tid);
-    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
-}
-
 /* One grid, `threads` POSIX threads on row bands of gold's interior, `steps`
  * ping-pong steps with a barrier between steps (both buffers start as the
  * input, so the border stays fixed).  loop_shape 1 runs gold's own loop shape
@@ -611,14 +722,12 @@ typedef struct {
 static void *band_worker(void *p) {
     band_arg *g = (band_arg *)p;
     float *cur = g->a, *nxt = g->b;
-    int r = oracle_stencil_radius(g->stencil);
     for (int t = 0; t < g->steps; t++) {
         if (g->row1 > g->row0) {
             if (g->loop_shape)
                 gold_loop_rows(cur, g->B, nxt, g->ny, g->nx, g->stencil, g->row0, g->row1);
             else
-                oracle_gold_step_f32(cur, g->B, nxt, g->ny, g->nx, g->stencil, g->row0, g->row1,
-                                     r, g->nx - r);
+                gold_f32_rows(cur, g->B, nxt, g->ny, g->nx, g->stencil, g->row0, g->row1);
         }
         pthread_barrier_wait(g->bar);
         float *s = cur; cur = nxt; nxt = s;

@@ -274,9 +274,10 @@ def sweep_steps_noalloc(d_in, d_out, ny: int, nx: int, stencil: str, coeffs, ste
                         engine: str = "tensor", rect=None, stream=None) -> None:
     """`steps` FP16 sweep steps from d_in to d_out with no device allocation
     (tcs_sweep_steps_noalloc): for callers that may not call cudaMalloc where
-    they sweep, e.g. inside CUDA graph capture.  The ping-pong plane is a
-    32 MiB static device array shared by all calls on a GPU, so overlapping
-    calls race; make the first call on a device before any capture."""
+    they sweep (allocator-free loops, device memory owned by a pool or budget
+    they do not control).  The ping-pong plane is a 32 MiB static device array
+    shared by all calls on a GPU, so overlapping calls race; make the first
+    call on a device before any stream capture."""
     c = _coeffs(coeffs, stencil)
     y0, y1, x0, x1 = _rect(rect)
     a = StepArgs(ny, nx, STENCILS[stencil], ENGINES[engine], PRECISIONS["f16"], y0, y1, x0, x1,

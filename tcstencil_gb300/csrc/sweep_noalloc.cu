@@ -1,15 +1,20 @@
 // Multi-step sweeps for callers that must not allocate device memory.
 //
 // A sweep of T > 1 steps from a read-only input to an output needs a third
-// brick plane for the ping-pong.  tcs_plan_* and tcs_sweep_host get it from
+// plane for the ping-pong.  tcs_plan_* and tcs_sweep_host get it from
 // cudaMalloc.  Some callers cannot call cudaMalloc at the point where they
-// sweep: code running while a CUDA graph is being captured (allocation is not
-// a stream operation and breaks the capture), real-time loops that forbid
-// allocator calls and the synchronisation they may cause, and hosts whose
-// device memory is entirely handed out by a pool or budget they do not own.
-// For them, tcs_sweep_steps_noalloc keeps that third plane in a file-scope
-// device array of kNoAllocScratchBytes, which every GPU that loads this
-// library holds until the process exits.
+// sweep: real-time loops that forbid allocator calls and the device
+// synchronisation they may bring, and hosts whose device memory is entirely
+// handed out by a pool or budget they do not own.  For them,
+// tcs_sweep_steps_noalloc keeps that third plane in a file-scope device array
+// of kNoAllocScratchBytes, which every GPU that loads this library holds until
+// the process exits.
+//
+// The sweeps write only grid cells, never a plane's padding rows and panels,
+// yet the tensor kernel multiplies padding into its sums (a zero band entry
+// times a non-finite padding value is NaN).  So each call first copies d_in,
+// padding included, over the part of the scratch it uses and over d_out:
+// whatever an earlier call of another shape left in the scratch is never read.
 #include <mutex>
 
 #include "tcs_internal.h"
@@ -18,15 +23,17 @@ namespace tcs {
 
 namespace {
 
-// 32 MiB: one FP16 plane of up to 16,777,216 cells, padding included (e.g. a
-// 4000 x 4000 grid; tcs_plane_elems gives a grid's plane size).
+// 32 MiB: one FP16 plane of up to 16,777,216 cells, padding included
+// (tcs_plane_elems gives a grid's plane size): square grids up to 3968 x 3968.
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Device address of g_noalloc_scratch per device ordinal, looked up once per
 // device with that device current.  (In host code the array's name is only a
-// host-side stand-in, never a device address.)
+// host-side stand-in, never a device address.)  The cached address belongs to
+// the device's current context: after cudaDeviceReset it is stale, so a
+// process that resets a device must not call this entry point on it again.
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 void *g_scratch_ptr[kMaxDevices] = {};
@@ -88,6 +95,14 @@ int tcs_sweep_steps_noalloc(const tcs_step_args *a, const void *d_in, void *d_ou
         st = cuda_status(tc_prepare(a->stencil, false), "tensor kernel set-up");
         if (st) return st;
     }
+    // Padding of the planes the steps read: d_in's, copied into the scratch
+    // (read from step 2 on) and into d_out (read from step 3 on).
+    st = cuda_status(cudaMemcpyAsync(scratch, d_in, plane_bytes, cudaMemcpyDeviceToDevice, s),
+                     "no-alloc scratch copy");
+    if (st) return st;
+    st = cuda_status(cudaMemcpyAsync(d_out, d_in, plane_bytes, cudaMemcpyDeviceToDevice, s),
+                     "no-alloc output copy");
+    if (st) return st;
     const TapCoeffs c = tap_coeffs(a->stencil, a->coeffs);
     // Steps alternate between d_out and the scratch plane so that the last
     // one lands in d_out; d_in is only read.

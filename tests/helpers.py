@@ -60,3 +60,34 @@ def plane16(torch, g16: np.ndarray):
 def grid16(plane, ny: int, nx: int) -> np.ndarray:
     """Row-major FP16 bits of a device panel plane."""
     return plane.cpu().numpy().view(np.uint16)[plane_index(ny, nx)]
+
+
+def f16tc_step_bound(prev16: np.ndarray, B, stencil: str, rect=None):
+    """One tensor-contract oracle step from the FP16 state prev16, and the
+    per-cell bound a GPU tensor step from the same state must meet:
+
+        ulp16(|oracle|) + 2^-16 * sum_k |c_k x_k|
+
+    i.e. one FP16 rounding step (the GPU rounds an FP32 sum, the oracle the
+    exact sum, so a sum next to a rounding boundary may round the other way)
+    plus a wide margin for the FP32 accumulation error of the tensor core's
+    sums (a few 2^-24 of the sum of |terms|).  A tile computed from the wrong
+    data, or not at all, misses it by the size of the values."""
+    ref = oracle.f16_to_f32(oracle.sweep_f16tc(prev16, B, stencil, 1, rect=rect)).astype(np.float64)
+    absx = np.abs(oracle.f16_to_f32(prev16)).astype(np.float64)
+    c16 = np.abs(oracle.f16_to_f32(oracle.f32_to_f16(B))).astype(np.float64)
+    s = oracle.sweep_f64(absx, c16, stencil, 1, rect=rect)
+    return ref, f16_ulp(ref) + 2.0 ** -16 * s
+
+
+def assert_f16tc_step(gpu: np.ndarray, prev16: np.ndarray, B, stencil: str, what: str, rect=None):
+    """Checks a GPU tensor FP16 step cell by cell against f16tc_step_bound;
+    returns the fraction of cells that differ from the oracle at all."""
+    ref, bound = f16tc_step_bound(prev16, B, stencil, rect)
+    d = np.abs(np.asarray(gpu, np.float64) - ref)
+    bad = d > bound
+    if bad.any():
+        idx = np.argwhere(bad)[:5].tolist()
+        raise AssertionError(f"{what}: {int(bad.sum())} cells beyond one FP16 step of the oracle, "
+                             f"e.g. {idx}; max |d| {d.max():.3g}")
+    return float((d > 0).mean())
