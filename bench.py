@@ -298,10 +298,11 @@ def build_batch(tcs, specs):
     return b
 
 
-def batch_leg(torch, tcs, K, W, stream, count=512):
+def batch_leg(torch, tcs, K, W, stream, count=512, check=16):
     """Batched mixed stencils (512 grids, sides log-uniform in [64, 2048], 1-64
     steps, FP16 and split 50/50): one persistent launch per run, replayed as a
-    CUDA graph.  Returns device-timed and end-to-end figures."""
+    CUDA graph.  Returns device-timed and end-to-end figures, and the error
+    against FP64 of `check` grids (half FP16, half split) after one run."""
     from tcstencil_gb300.workloads import mixed_batch
 
     specs = mixed_batch(count)
@@ -336,12 +337,31 @@ def batch_leg(torch, tcs, K, W, stream, count=512):
             b.download(k, o.numpy(), stream=stream)
         torch.cuda.synchronize()
     te = (time.perf_counter() - t0) / Ke
+    # accuracy: every grid from its input, one run, a sample against FP64
+    for k, g in enumerate(grids):
+        b.upload(k, g.numpy(), stream=stream)
+    b.run(use_graph=True, stream=stream)
+    errs = {"f16": [], "split": []}
+    picks = [k for k in range(len(specs)) if specs[k].precision == "f16"][:check // 2] + \
+            [k for k in range(len(specs)) if specs[k].precision == "split"][:check // 2]
+    for k in picks:
+        sp = specs[k]
+        b.download(k, outs[k].numpy(), stream=stream)
+        torch.cuda.synchronize()
+        rel, mx = fp64_error(torch, tcs, grids[k].numpy(), sp.coeffs, sp.stencil, sp.steps,
+                             outs[k].numpy())
+        errs[sp.precision].append((rel, mx))
     b.close()
+    accuracy_sample = {p: {"grids": len(v), "rel_l2_vs_fp64_max": float(f"{max(e[0] for e in v):.4g}"),
+                           "rel_l2_vs_fp64_median": float(f"{statistics.median(e[0] for e in v):.4g}"),
+                           "max_abs_vs_fp64_max": float(f"{max(e[1] for e in v):.4g}")}
+                       for p, v in errs.items() if v}
     host_bytes = sum(g.numel() * 4 for g in grids)
     return {"gpts": pu / t / 1e9, "ms_per_run": 1e3 * t, "point_updates_per_run": pu,
             "items_per_run": items, "grids": ngrids, "algorithmic_bytes_per_run": byts,
             "achieved_gbs": byts / t / 1e9, "e2e_gpts": pu / te / 1e9,
-            "e2e_h2d_bytes": host_bytes, "e2e_d2h_bytes": host_bytes}
+            "e2e_h2d_bytes": host_bytes, "e2e_d2h_bytes": host_bytes,
+            "accuracy_sample": accuracy_sample}
 
 
 def serve_round_steps(args):
@@ -352,19 +372,43 @@ def serve_round_steps(args):
     return best_round_steps(args.serve_rate)
 
 
-def serve_leg(tcs, seconds=10.0, rate=2000.0, budget_gb=120.0, round_steps=16):
+def serve_leg(tcs, seconds=10.0, rate=2000.0, budget_gb=120.0, round_steps=16, check=16):
     """Served stencil solves: Poisson arrivals at `rate`/s for `seconds`, sides
     log-uniform in [128, 4096] per axis, random stencil and coefficients, 1-200
-    steps, FP16 or split; admission against a `budget_gb` HBM budget."""
+    steps, FP16 or split; admission against a `budget_gb` HBM budget.  Then
+    `check` of the requests are served again and checked against FP64."""
     from tcstencil_gb300.serving import InputPool, OutputRing, replay
     from tcstencil_gb300.workloads import poisson_requests
 
+    import torch
+
     reqs = poisson_requests(rate=rate, duration=seconds)
     srv = tcs.Server(int(budget_gb * 2**30), round_steps=round_steps)
+    pool = InputPool(1 << 26)
     try:
-        res = replay(srv, reqs, InputPool(1 << 26), OutputRing(1 << 30))
+        res = replay(srv, reqs, pool, OutputRing(1 << 30))
+        # accuracy of served results: a sample of the requests, served again
+        # together, each against its FP64 shadow
+        sample = reqs[::max(1, len(reqs) // check)][:check]
+        held = []
+        for rq in sample:
+            sp = rq.spec
+            g = np.ascontiguousarray(pool.grid(sp.ny, sp.nx, sp.seed))
+            out = np.empty((sp.ny, sp.nx), np.float32)
+            held.append((srv.submit(g, out, sp.stencil, sp.coeffs, sp.steps, sp.precision),
+                         sp, g, out))
+        errs = {"f16": [], "split": []}
+        for t, sp, g, out in held:
+            srv.wait(t, 60.0)
+            errs[sp.precision].append(fp64_error(torch, tcs, g, sp.coeffs, sp.stencil,
+                                                 sp.steps, out))
     finally:
         srv.close()
+    res["accuracy_sample"] = {
+        p: {"requests": len(v), "rel_l2_vs_fp64_max": float(f"{max(e[0] for e in v):.4g}"),
+            "rel_l2_vs_fp64_median": float(f"{statistics.median(e[0] for e in v):.4g}"),
+            "max_abs_vs_fp64_max": float(f"{max(e[1] for e in v):.4g}")}
+        for p, v in errs.items() if v}
     res["algorithmic_bytes"] = sum(r.spec.bytes for r in reqs)
     res["achieved_gbs"] = res["algorithmic_bytes"] / res["span_s"] / 1e9
     res["offered_gpts"] = res["point_updates"] / seconds / 1e9
@@ -373,14 +417,9 @@ def serve_leg(tcs, seconds=10.0, rate=2000.0, budget_gb=120.0, round_steps=16):
     return res
 
 
-def split_config_leg(torch, tcs, stream, interior=16384, steps=200, check_every=50,
-                     stencil="box2d1r"):
-    """Split-precision configuration: box2d1r on a 16384^2 interior + 1-cell
-    zero halo, input U[-1,1) + sin(2 pi x) sin(2 pi y), 200 steps.  Times the
-    200 steps (CUDA events, graph replay), then replays them one by one beside
-    the FP64 shadow (tcs_drift) and reports the error after every step, with
-    the drift checks every 50 steps called out."""
-    from tcstencil_gb300.autotune import best_config
+def split_input(interior, stencil):
+    """The split configuration's input: U[-1,1) + sin(2 pi x) sin(2 pi y) on
+    the interior, a zero halo of the stencil's radius, normalised coefficients."""
     from tcstencil_gb300.workloads import normalized_coeffs
 
     r = 1 if stencil in ("star2d1r", "box2d1r") else 2
@@ -392,7 +431,21 @@ def split_config_leg(torch, tcs, stream, interior=16384, steps=200, check_every=
     A[r:-r, r:-r] = (rng.uniform(-1, 1, (interior, interior)) +
                      np.sin(2 * np.pi * xx) * np.sin(2 * np.pi * yy))
     del xx, yy
-    B = normalized_coeffs(rng, stencil)
+    return A, normalized_coeffs(rng, stencil)
+
+
+def split_config_leg(torch, tcs, stream, interior=16384, steps=200, check_every=50,
+                     stencil="box2d1r"):
+    """Split-precision configuration: box2d1r on a 16384^2 interior + 1-cell
+    zero halo, input U[-1,1) + sin(2 pi x) sin(2 pi y), 200 steps.  Times the
+    200 steps (CUDA events, graph replay), then replays them one by one beside
+    the FP64 shadow (tcs_drift) and reports the error after every step, with
+    the drift checks every 50 steps called out."""
+    from tcstencil_gb300.autotune import best_config
+
+    r = 1 if stencil in ("star2d1r", "box2d1r") else 2
+    n = interior + 2 * r
+    A, B = split_input(interior, stencil)
     _, depth = best_config(stencil, "split", n, n)
     plan = tcs.Plan(n, n, stencil, B, engine="tensor", precision="split", temporal_depth=depth)
     plan.upload(A)
@@ -419,7 +472,8 @@ def split_config_leg(torch, tcs, stream, interior=16384, steps=200, check_every=
         plan.run(1, use_graph=False, stream=stream)
         drift.run(1)
         plan.download(out, stream=stream)
-        errs.append(drift.compare(out, stream=stream)[0])
+        rel, mx = drift.compare(out, stream=stream)
+        errs.append(rel)
     drift.close()
     plan.close()
     peak, _ = load_peaks()
@@ -427,7 +481,7 @@ def split_config_leg(torch, tcs, stream, interior=16384, steps=200, check_every=
                         f"{steps} steps, U[-1,1) + sin(2 pi x) sin(2 pi y)",
             "gpts": pts / t / 1e9, "ms_per_step": 1e3 * t / steps,
             "roofline_frac": 8 * pts / t / 1e9 / peak, "temporal_depth": depth,
-            "rel_l2_vs_fp64_max": max(errs),
+            "rel_l2_vs_fp64_max": max(errs), "max_abs_vs_fp64_final": mx,
             "drift_checks": {str(s): errs[s - 1] for s in range(check_every, steps + 1, check_every)},
             "rel_l2_vs_fp64_every_10_steps": [round(e, 10) for e in errs[9::10]]}
 
@@ -444,6 +498,157 @@ def timed_sweeps(torch, tcs, plan, K, W, timesteps, stream):
     stop.record(stream)
     torch.cuda.synchronize()
     return start.elapsed_time(stop) / 1e3
+
+
+def fp64_error(torch, tcs, A, B, stencil, steps, result, rect=None):
+    """(relative L2, max abs) of an FP32 result (device tensor or host array)
+    against the device FP64 shadow of the same problem (tcs_drift: the
+    oracle's FP64 restatement of gold, bit for bit) after `steps` steps."""
+    ny, nx = A.shape
+    d = tcs.Drift(ny, nx, stencil, B, rect=rect)
+    d.upload(np.ascontiguousarray(A, np.float32))
+    d.run(steps)
+    if isinstance(result, np.ndarray):
+        result = torch.from_numpy(np.ascontiguousarray(result, np.float32)).cuda()
+    rel, mx = d.compare(result)
+    d.close()
+    return rel, mx
+
+
+def plan_result(torch, tcs, A, B, stencil, steps, engine, precision, stream):
+    """The device FP32 result of `steps` steps of A through a plan."""
+    n0, n1 = A.shape
+    p = tcs.Plan(n0, n1, stencil, B, engine=engine, precision=precision)
+    p.upload(A)
+    p.run(steps, use_graph=True, stream=stream)
+    out = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
+    p.download(out, stream=stream)
+    torch.cuda.synchronize()
+    p.close()
+    return out
+
+
+def accuracy(torch, tcs, A, B, stencil, steps, out, stream, gold=True):
+    """Error of a result against FP64 and, with gold=True, against FP32 gold
+    (the CUDA-core F32 engine, which reproduces common/gold_*.cpp bit for bit)."""
+    rel, mx = fp64_error(torch, tcs, A, B, stencil, steps, out)
+    acc = {"rel_l2_vs_fp64": rel, "max_abs_vs_fp64": mx}
+    if gold:
+        g = plan_result(torch, tcs, A, B, stencil, steps, "cudacore", "f32", stream)
+        d = (out.double() - g.double())
+        acc["max_abs_vs_gold_f32"] = float(d.abs().max())
+        acc["rel_l2_vs_gold_f32"] = float(d.norm() / g.double().norm())
+        del g, d
+    return {k: float(f"{v:.4g}") for k, v in acc.items()}
+
+
+def flush_l2(torch, scratch):
+    scratch.add_(1)
+
+
+def events_timed(torch, stream, fn, reps, scratch):
+    """Seconds of `reps` calls of fn, each timed alone with CUDA events on
+    `stream`, L2 flushed (a write larger than L2) between them."""
+    total = 0.0
+    for _ in range(reps):
+        flush_l2(torch, scratch)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        total += a.elapsed_time(b) / 1e3
+    return total
+
+
+def config1_leg(torch, tcs, stream, reps=200):
+    """The first configuration: star2d1r on a 1024^2 interior + 1-cell zero
+    halo (1026^2), U[0,1) inputs, 5 coefficients U[0,1) normalised to sum 1,
+    10 ping-pong steps, FP16 storage / FP32 accumulate, both engines; each of
+    `reps` runs timed alone with L2 flushed before it; errors against FP64
+    and FP32 gold; gold on the host cores beside it."""
+    import oracle
+    from tcstencil_gb300.workloads import normalized_coeffs
+
+    n, steps, st = 1026, 10, "star2d1r"
+    rng = np.random.default_rng(1000)
+    A = np.zeros((n, n), np.float32)
+    A[1:-1, 1:-1] = rng.random((n - 2, n - 2), dtype=np.float32)
+    B = normalized_coeffs(rng, st)
+    scratch = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    peak, _ = load_peaks()
+    pts = (n - 2) ** 2 * steps
+    res = {"workload": "star2d1r, 1024^2 interior + 1-cell zero halo, U[0,1), 10 steps, FP16 "
+                       "storage / FP32 accumulate; each run timed alone, L2 flushed before it"}
+    for eng in ("tensor", "cudacore"):
+        p = tcs.Plan(n, n, st, B, engine=eng, precision="f16")
+        p.upload(A)
+        for _ in range(5):
+            p.run(steps, use_graph=True, stream=stream)
+        t = events_timed(torch, stream, lambda: p.run(steps, use_graph=True, stream=stream),
+                         reps, scratch)
+        launches = p.launches(steps)
+        p.close()
+        out = plan_result(torch, tcs, A, B, st, steps, eng, "f16", stream)
+        g = pts * reps / t / 1e9
+        res[eng] = {"gpts": round(g, 2), "us_per_run": round(1e6 * t / reps, 2),
+                    "launches_per_run": launches,
+                    "roofline_frac": round(4 * g / peak, 4),
+                    **accuracy(torch, tcs, A, B, st, steps, out, stream)}
+    threads = os.cpu_count() or 1
+    tc = oracle.gold_bench_bands(A, B, st, steps, threads, loop_shape=True)
+    res["cpu_gold"] = {"gpts": round(pts / tc / 1e9, 3), "cores": threads, "kind": "port",
+                       "sample": "the whole configuration: gold's loop shape, 10 steps, "
+                                 "threads on row bands"}
+    del scratch
+    return res
+
+
+def equal_accuracy_leg(torch, tcs, stream, split_res, interior=16384, steps=200):
+    """The split configuration's grid run by the FP32 CUDA-core engine (gold's
+    arithmetic, FP32 storage, 8 B per point-update like split) and by the plain
+    FP16 tensor engine, each timed (CUDA events around one graph replay of the
+    200 steps) and checked against FP64, beside the split tensor figures."""
+    from tcstencil_gb300.workloads import normalized_coeffs
+
+    st = "box2d1r"
+    A, B = split_input(interior, st)
+    n = A.shape[0]
+    peak, _ = load_peaks()
+    pts = interior * interior * steps
+    res = {"workload": split_res["workload"],
+           "split_tensor": {"gpts": split_res["gpts"], "roofline_frac": split_res["roofline_frac"],
+                            "rel_l2_vs_fp64": split_res["rel_l2_vs_fp64_max"]}}
+    for key, eng, prec, bpu in (("f32_cudacore", "cudacore", "f32", 8),
+                                ("f16_tensor", "tensor", "f16", 4)):
+        p = tcs.Plan(n, n, st, B, engine=eng, precision=prec)
+        p.upload(A)
+        p.run(10, use_graph=True, stream=stream)
+        p.upload(A)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        p.run(steps, use_graph=True, stream=stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b) / 1e3
+        out = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        p.download(out, stream=stream)
+        torch.cuda.synchronize()
+        p.close()
+        rel, mx = fp64_error(torch, tcs, A, B, st, steps, out)
+        del out
+        g = pts / t / 1e9
+        res[key] = {"gpts": round(g, 2), "roofline_frac": round(bpu * g / peak, 4),
+                    "rel_l2_vs_fp64": float(f"{rel:.4g}"), "max_abs_vs_fp64": float(f"{mx:.4g}")}
+    ok = [k for k in ("split_tensor", "f32_cudacore", "f16_tensor")
+          if res[k]["rel_l2_vs_fp64"] <= 1e-6]
+    res["at_1e-6"] = {"forms": ok,
+                      "split_over_f32_cudacore": round(res["split_tensor"]["gpts"] /
+                                                       res["f32_cudacore"]["gpts"], 3)}
+    return res
 
 
 def run_ours(args):
@@ -530,8 +735,17 @@ def run_ours(args):
     e2e_pipelined = {"value": ws * updates_per_step * e2e_steps / tp / 1e9, "unit": "Gpts/s",
                      "h2d_bytes_per_step": n * n * 4, "d2h_bytes_per_step": n * n * 4,
                      "api": "tcs_pipe_submit (two plans on two streams, pinned host FP32 grid in/out)"}
+    # the headline result's error: the same timesteps from the same input,
+    # against FP64 and against FP32 gold
+    plan.upload(A)
+    plan.run(args.timesteps, use_graph=True, stream=stream)
+    out = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    plan.download(out, stream=stream)
+    torch.cuda.synchronize()
     plan.close()
     tcs.lib().tcs_release_cache()
+    head_acc = accuracy(torch, tcs, A, B, args.stencil, args.timesteps, out, stream)
+    del out
 
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -545,10 +759,17 @@ def run_ours(args):
                 p2.upload(A2)
                 t2 = timed_sweeps(torch, tcs, p2, max(5, args.steps // 4), 2, args.timesteps, stream)
                 p2.close()
-                extras[f"{st}/{eng}/f16"] = round(updates_per_step * max(5, args.steps // 4) / t2 / 1e9, 2)
+                g2 = updates_per_step * max(5, args.steps // 4) / t2 / 1e9
+                o2 = plan_result(torch, tcs, A2, B2, st, args.timesteps, eng, "f16", stream)
+                extras[f"{st}/{eng}/f16"] = {
+                    "gpts": round(g2, 2), "roofline_frac": round(4 * g2 / load_peaks()[0], 4),
+                    **accuracy(torch, tcs, A2, B2, st, args.timesteps, o2, stream)}
+                del o2
+        extras["config1_star2d1r_1026"] = config1_leg(torch, tcs, stream)
         r = split_config_leg(torch, tcs, stream)
         extras["split_16384_box2d1r"] = {k: (round(v, 10) if isinstance(v, float) else v)
                                          for k, v in r.items()}
+        extras["equal_accuracy_16384_box2d1r"] = equal_accuracy_leg(torch, tcs, stream, r)
         r = batch_leg(torch, tcs, 10, 3, stream)
         extras["batched_512_mixed"] = {k: round(v, 3) if isinstance(v, float) else v
                                        for k, v in r.items()}
@@ -575,6 +796,9 @@ def run_ours(args):
                               f"{steps_per_launch:g} steps per launch / mean launch time "
                               f"{launch_s * 1e6:.2f} us (CUDA events); traffic = ncu DRAM bytes "
                               f"per step x steps per launch"},
+        "accuracy": {**head_acc, "basis": "the headline's timesteps from its input, against the "
+                                          "device FP64 shadow (tcs_drift) and FP32 gold (the "
+                                          "CUDA-core F32 engine, bit-exact with gold)"},
         "e2e": e2e,
         "e2e_pipelined": e2e_pipelined,
         "gpu_launches": args.steps * launches_per_run,
