@@ -72,7 +72,9 @@ def lib() -> ctypes.CDLL:
         L.oracle_unbrick_2d.argtypes = [P, P, I, I, I]
         L.oracle_init_coe_star.argtypes = [P, I, P, P]
         L.oracle_init_coe_box.argtypes = [P, I, P]
-        L.oracle_check_error_2d.argtypes = [I, P, P, I, I, I, I, ctypes.c_double, P]
+        D = ctypes.c_double
+        L.oracle_check_error_2d.argtypes = [I, P, P, I, I, I, I, I, D, D, P, P, P, P, P, P, I]
+        L.oracle_check_error_2d.restype = D
         L.oracle_gold_loop_step.argtypes = [P, P, P, I, I, I]
         L.oracle_gold_loop_step.restype = I
         L.oracle_gold_bench_bands.argtypes = [P, P, I, I, I, I, I, I, P]
@@ -241,12 +243,22 @@ def sweep_f32_fixed(A, B, stencil, steps, rect=None):
     return sweep_f32(A, B, stencil, steps, rect)
 
 
-def check_error_2d(N, output, reference, y_lb, y_ub, x_lb, x_ub, min_number=1e-6):
-    out = np.zeros(3, np.float64)
+def check_error_2d(N, output, reference, y_lb, y_ub, x_lb, x_ub, relative=False,
+                   tolerance=0.01, min_number=1e-6):
+    """checkError2D / checkRelativeError2D (common/common.hpp:38-92): the RMS
+    result, the final maximum and its cell, and the cells the reference
+    reports with a "Values at index (j,k) differ" line, in order."""
     o = np.ascontiguousarray(output, np.float32)
     r = np.ascontiguousarray(reference, np.float32)
-    lib().oracle_check_error_2d(N, _p(o), _p(r), y_lb, y_ub, x_lb, x_ub, min_number, _p(out))
-    return {"rms_abs": out[0], "max_abs": out[1], "rms_rel": out[2]}
+    cap = (y_ub - y_lb) * (x_ub - x_lb)
+    mj, mk = np.zeros(max(cap, 1), np.int32), np.zeros(max(cap, 1), np.int32)
+    mx = ctypes.c_double()
+    j, k, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    rms = lib().oracle_check_error_2d(N, _p(o), _p(r), y_lb, y_ub, x_lb, x_ub, int(relative),
+                                      tolerance, min_number, ctypes.byref(mx), ctypes.byref(j),
+                                      ctypes.byref(k), ctypes.byref(n), _p(mj), _p(mk), cap)
+    return {"rms": rms, "max_error": mx.value, "max_at": (j.value, k.value),
+            "reported": list(zip(mj[:n.value].tolist(), mk[:n.value].tolist()))}
 
 
 def gold_loop_step(A: np.ndarray, B, stencil: str, C: np.ndarray | None = None):

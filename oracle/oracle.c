@@ -19,7 +19,8 @@
  *   oracle_init_coe_star   layout16/host_star2d1r.cu:33-61, host_star2d2r.cu:33-67
  *   oracle_init_coe_box    layout16/host_box2d1r.cu:29-46,  host_box2d2r.cu:29-50
  *   oracle_check_error_2d  common/common.hpp:38-92 (checkError2D /
- *                          checkRelativeError2D; RMS, without the printing)
+ *                          checkRelativeError2D: results and reported cells,
+ *                          without the printing)
  *
  * Arithmetic contracts of the GPU engine (used as tighter checks than gold):
  *   oracle_step_f16cc   FP16 storage, FP32 coefficients, fmaf chain in gold's
@@ -632,27 +633,50 @@ int oracle_sweep_split(uint16_t *hi, uint16_t *lo, const float *B, int ny, int n
 }
 
 /* ------------------------------------------------------ error metrics --- */
-/* checkError2D / checkRelativeError2D (common/common.hpp:38-92) without the
- * printing: out[0] = RMS absolute error, out[1] = max absolute error,
- * out[2] = RMS relative error with |ref| < min_number dividing by min_number,
- * over rows [y_lb, y_ub) and columns [x_lb, x_ub) of an N-wide grid. */
-void oracle_check_error_2d(int N, const float *output, const float *reference, int y_lb, int y_ub,
-                           int x_lb, int x_ub, double min_number, double *out) {
-    double e2 = 0.0, emax = 0.0, r2 = 0.0;
+/* checkError2D (relative = 0) and checkRelativeError2D (relative = 1) of
+ * common/common.hpp:38-92, as the reference's nvcc build computes them, over
+ * rows [y_lb, y_ub) and columns [x_lb, x_ub) of an N-wide grid:
+ *   - each cell's error is the FLOAT difference output - reference, widened
+ *     to double; checkError2D takes its magnitude, checkRelativeError2D
+ *     divides it (sign kept) by the reference, or by min_number (MIN_NUMBER,
+ *     1e-6) where |reference| (a float magnitude) is below it;
+ *   - the squares are summed in row-major order; the result is
+ *     sqrt(sum / cells);
+ *   - a running maximum starts at `tolerance` (TOLERANCE, 0.01); every cell
+ *     whose error exceeds it (signed, for the relative form) is reported by a
+ *     "Values at index (j,k) differ" line and becomes the new maximum.
+ * Instead of printing, the cells of those lines go to msg_j / msg_k (up to
+ * msg_cap of them) and their count to *messages; *max_error, *max_j, *max_k
+ * get the final maximum and its cell (the "[Test] Max ... Error" line, which
+ * the reference prints only when that cell is not (0, 0)). */
+double oracle_check_error_2d(int N, const float *output, const float *reference, int y_lb,
+                             int y_ub, int x_lb, int x_ub, int relative, double tolerance,
+                             double min_number, double *max_error, int *max_j, int *max_k,
+                             int *messages, int *msg_j, int *msg_k, int msg_cap) {
+    double error = 0.0, mx = tolerance;
+    int mj = 0, mk = 0, nmsg = 0;
     for (int j = y_lb; j < y_ub; j++)
         for (int k = x_lb; k < x_ub; k++) {
-            double ref = reference[(long)j * N + k];
-            double d = (double)output[(long)j * N + k] - ref;
-            double ad = d < 0 ? -d : d;
-            e2 += ad * ad;
-            if (ad > emax) emax = ad;
-            double rel = fabs(ref) < min_number ? d / min_number : d / ref;
-            r2 += rel * rel;
+            float o = output[(long)j * N + k], r = reference[(long)j * N + k];
+            double e = (double)(o - r);
+            if (relative)
+                e = fabsf(r) < min_number ? e / min_number : e / (double)r;
+            else
+                e = e < 0.0 ? -e : e;
+            error += e * e;
+            if (e > mx) {
+                if (nmsg < msg_cap) { msg_j[nmsg] = j; msg_k[nmsg] = k; }
+                nmsg++;
+                mx = e;
+                mk = k;
+                mj = j;
+            }
         }
-    double cnt = (double)(y_ub - y_lb) * (double)(x_ub - x_lb);
-    out[0] = sqrt(e2 / cnt);
-    out[1] = emax;
-    out[2] = sqrt(r2 / cnt);
+    *max_error = mx;
+    *max_j = mj;
+    *max_k = mk;
+    *messages = nmsg;
+    return sqrt(error / ((y_ub - y_lb) * (x_ub - x_lb)));
 }
 
 /* ------------------------------------------------ gold's own loop shape --- */

@@ -12,7 +12,11 @@ from __future__ import annotations
 
 import argparse
 import os
+import re
+import struct
+import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -53,6 +57,54 @@ def ref_sweep(R: oracle.Ref, A: np.ndarray, B: np.ndarray, stencil: str, steps: 
         nxt = R.gold(cur, B, stencil, nxt)
         cur, nxt = nxt, cur
     return cur
+
+
+def ref_check_error(N, out, ref, region):
+    """Runs the reference's checkError2D and checkRelativeError2D (through
+    oracle/_ref/ref_check_error) and parses what they print and return."""
+    with tempfile.NamedTemporaryFile(delete=False) as f:
+        f.write(struct.pack("5i", N, *region))
+        f.write(np.ascontiguousarray(out, np.float32).tobytes())
+        f.write(np.ascontiguousarray(ref, np.float32).tobytes())
+    try:
+        r = subprocess.run([os.path.join(oracle.REF_DIR, "ref_check_error"), f.name],
+                           capture_output=True, text=True, check=True)
+    finally:
+        os.unlink(f.name)
+    res, part = {}, "abs"
+    res["abs_reported"], res["rel_reported"] = [], []
+    for line in r.stdout.splitlines():
+        m = re.match(r"Values at index \((\d+),(\d+)\) differ", line)
+        if m:
+            res[f"{part}_reported"].append((int(m.group(1)), int(m.group(2))))
+        m = re.match(r"\[Test\] Max (Relative )?Error : (\S+) @ \(,(\d+),(\d+)\)", line)
+        if m:
+            res[f"{part}_max_line"] = (m.group(2), int(m.group(3)), int(m.group(4)))
+        if line.startswith("RMS "):
+            res["rms"] = float(line.split()[1])
+            part = "rel"
+        if line.startswith("REL "):
+            res["rel"] = float(line.split()[1])
+    return res
+
+
+def error_metric_cases(rng):
+    """Inputs for checkError2D / checkRelativeError2D: noise below and above
+    TOLERANCE, references with exact zeros and values below MIN_NUMBER, both
+    signs, maxima at (0, 0) and elsewhere."""
+    cases = []
+    for N, region, noise in ((8, (1, 7, 1, 7), 0.02), (33, (2, 31, 2, 31), 1e-3),
+                             (64, (0, 64, 0, 64), 0.05), (40, (1, 39, 3, 37), 1e-4),
+                             (16, (0, 16, 0, 16), 0.0)):
+        ref = rng.uniform(-1, 1, (N, N)).astype(np.float32)
+        ref[region[0], region[2]:region[2] + 3] = [0.0, 5e-7, -3e-7]
+        out = (ref + rng.normal(0, noise, (N, N))).astype(np.float32) if noise else ref.copy()
+        if noise != 1e-4:
+            out[region[0] + 1, region[2] + 1] += 0.3  # one large error
+        if N == 16:
+            out[0, 0] += 2.0  # the largest error at (0, 0): no "Max" line
+        cases.append((N, region, out, ref))
+    return cases
 
 
 def main() -> None:
@@ -122,6 +174,23 @@ def main() -> None:
             else:
                 coe[f"{st}_{tag}_coe"] = R.init_coe(B16, st)
     np.savez_compressed(os.path.join(HERE, "init_coe.npz"), **coe)
+
+    # error metrics (common/common.hpp:38-92), as the reference's build runs them
+    err = {}
+    for c, (N, region, out, ref) in enumerate(error_metric_cases(rng)):
+        res = ref_check_error(N, out, ref, region)
+        err[f"c{c}_N"] = np.int32(N)
+        err[f"c{c}_region"] = np.array(region, np.int32)
+        err[f"c{c}_out"] = out
+        err[f"c{c}_ref"] = ref
+        err[f"c{c}_rms"] = np.float64(res["rms"])
+        err[f"c{c}_rel"] = np.float64(res["rel"])
+        for part in ("abs", "rel"):
+            err[f"c{c}_{part}_reported"] = np.array(res[f"{part}_reported"], np.int32).reshape(-1, 2)
+            line = res.get(f"{part}_max_line")
+            err[f"c{c}_{part}_max_line"] = np.array([] if line is None else [line[0]])
+            err[f"c{c}_{part}_max_at"] = np.array([] if line is None else line[1:], np.int32)
+    np.savez_compressed(os.path.join(HERE, "check_error.npz"), **err)
     print("fixtures written to", HERE)
 
 

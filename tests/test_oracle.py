@@ -129,3 +129,29 @@ def test_reference_build_matches_restatement_on_random_cases():
             C = rng.random((N, N)).astype(np.float32)
             np.testing.assert_array_equal(R.gold(A, B, st, C).view(np.uint32),
                                           oracle.gold_step(A, B, st, C).view(np.uint32))
+
+
+def test_error_metrics_match_the_reference(golden):
+    """checkError2D / checkRelativeError2D (common/common.hpp:38-92), run from
+    the reference header by tests/golden/make_golden.py: the same RMS results
+    bit for bit, the same reported cells in the same order, the same final
+    maximum (as the reference prints it, %e) and its cell."""
+    g = golden("check_error.npz")
+    cases = sorted({k.split("_")[0] for k in g.files})
+    assert len(cases) == 5
+    for c in cases:
+        N, region = int(g[f"{c}_N"]), [int(v) for v in g[f"{c}_region"]]
+        for part, relative, key in (("abs", False, "rms"), ("rel", True, "rel")):
+            r = oracle.check_error_2d(N, g[f"{c}_out"], g[f"{c}_ref"], *region, relative=relative)
+            assert r["rms"] == float(g[f"{c}_{key}"]), (c, part)
+            assert r["reported"] == [tuple(x) for x in g[f"{c}_{part}_reported"].tolist()], (c, part)
+            line = g[f"{c}_{part}_max_line"]
+            if line.size:  # printed only when the maximum's cell is not (0, 0)
+                assert "%e" % r["max_error"] == str(line[0]), (c, part)
+                assert r["max_at"] == tuple(g[f"{c}_{part}_max_at"].tolist()), (c, part)
+            else:
+                assert r["max_at"] == (0, 0), (c, part)
+    # the fixtures cover messages, none, both signs and the MIN_NUMBER branch
+    assert any(g[f"{c}_rel_reported"].size for c in cases)
+    assert any(not g[f"{c}_abs_reported"].size for c in cases)
+    assert any(not g[f"{c}_abs_max_line"].size and g[f"{c}_abs_reported"].size for c in cases)
