@@ -582,7 +582,10 @@ def config1_leg(torch, tcs, stream, reps=200):
     res = {"workload": "star2d1r, 1024^2 interior + 1-cell zero halo, U[0,1), 10 steps, FP16 "
                        "storage / FP32 accumulate; each run timed alone, L2 flushed before it"}
     for eng in ("tensor", "cudacore"):
-        p = tcs.Plan(n, n, st, B, engine=eng, precision="f16")
+        # the tensor plan takes the autotuner's tile shape and launch form
+        p = tcs.Plan(n, n, st, B, engine="auto" if eng == "tensor" else eng, precision="f16")
+        assert p.engine == eng
+        tile_w = p.tile_width()
         p.upload(A)
         for _ in range(5):
             p.run(steps, use_graph=True, stream=stream)
@@ -593,7 +596,7 @@ def config1_leg(torch, tcs, stream, reps=200):
         out = plan_result(torch, tcs, A, B, st, steps, eng, "f16", stream)
         g = pts * reps / t / 1e9
         res[eng] = {"gpts": round(g, 2), "us_per_run": round(1e6 * t / reps, 2),
-                    "launches_per_run": launches,
+                    "launches_per_run": launches, "tile": f"128x{tile_w}",
                     "roofline_frac": round(4 * g / peak, 4),
                     **accuracy(torch, tcs, A, B, st, steps, out, stream)}
     threads = os.cpu_count() or 1

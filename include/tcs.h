@@ -225,6 +225,15 @@ int tcs_plan_set_temporal_depth(tcs_plan plan, int depth);
  * faster); 0: never; 1: always.  Results are bit-identical either way.
  * TCS_MULTI=0 in the environment turns it off for the process. */
 int tcs_plan_set_multistep(tcs_plan plan, int mode);
+/* Tile shape of the plain FP16 tensor sweeps: 128 rows by tile_w = 128
+ * (default), 96 or 64 columns.  Narrower tiles give a grid more tiles: on
+ * grids with few tiles per SM more SMs share a step, and each tile's MMAs and
+ * epilogue shrink with its width.  Results are bit-identical at every width;
+ * the autotuner picks the width per size class (it replaces the reference's
+ * TILE_SIZE sweep, script/param.py:5).  TCS_ERR_UNSUPPORTED for widths below
+ * 128 on other engines and precisions. */
+int tcs_plan_set_tile_width(tcs_plan plan, int tile_w);
+int tcs_plan_tile_width(tcs_plan plan, int *tile_w);
 /* Kernel launches tcs_plan_run(plan, steps, ...) makes (the device work of
  * one call: 1 for a multi-step launch, else one per step or step pair). */
 int tcs_plan_launches(tcs_plan plan, int steps, int *launches);

@@ -112,6 +112,8 @@ SIGNATURES = {
     "tcs_plan_set_coeffs": (_I, [_P, _P]),
     "tcs_plan_set_temporal_depth": (_I, [_P, _I]),
     "tcs_plan_set_multistep": (_I, [_P, _I]),
+    "tcs_plan_set_tile_width": (_I, [_P, _I]),
+    "tcs_plan_tile_width": (_I, [_P, ctypes.POINTER(_I)]),
     "tcs_plan_launches": (_I, [_P, _I, _P]),
     "tcs_sweep_host": (_I, [_P, _P, ctypes.POINTER(Problem), _I]),
     "tcs_noalloc_scratch_bytes": (_SZ, []),
@@ -290,18 +292,22 @@ class Plan:
     """Device-resident sweep of one grid (tcs_plan_*)."""
 
     def __init__(self, ny: int, nx: int, stencil: str, coeffs, engine: str = "tensor",
-                 precision: str = "f16", rect=None, temporal_depth: int | None = None):
+                 precision: str = "f16", rect=None, temporal_depth: int | None = None,
+                 tile_w: int | None = None):
         """engine "auto" takes the autotuner's choice for this problem class
-        (engine, temporal depth and launch form); temporal_depth 2 runs steps
-        in blocked pairs (split precision, tensor engine)."""
+        (engine, temporal depth, launch form and tile width); temporal_depth 2
+        runs steps in blocked pairs (split precision, tensor engine); tile_w
+        (128, 96 or 64) is the tile width of plain FP16 tensor sweeps."""
         tuned_launch = -1
         if engine == "auto":
-            from .autotune import best_config, best_launch
+            from .autotune import best_config, best_launch, best_tile_width
 
             engine, tuned_depth = best_config(stencil, precision, ny, nx)
             if temporal_depth is None:
                 temporal_depth = tuned_depth
             tuned_launch = best_launch(stencil, precision, ny, nx)
+            if tile_w is None and engine == "tensor" and precision == "f16":
+                tile_w = best_tile_width(stencil, ny, nx)
         self._c = _coeffs(coeffs, stencil)
         y0, y1, x0, x1 = _rect(rect)
         self.ny, self.nx, self.stencil, self.engine, self.precision = ny, nx, stencil, engine, precision
@@ -314,6 +320,8 @@ class Plan:
             self.set_temporal_depth(temporal_depth)
         if tuned_launch >= 0 and engine == "tensor":
             self.set_multistep(tuned_launch)
+        if tile_w and tile_w != 128:
+            self.set_tile_width(tile_w)
 
     def set_temporal_depth(self, depth: int) -> None:
         _check(lib().tcs_plan_set_temporal_depth(self._h, int(depth)))
@@ -329,6 +337,16 @@ class Plan:
         launch (1), one launch per step (0), or by grid size (-1, the
         default); same bits."""
         _check(lib().tcs_plan_set_multistep(self._h, int(mode)))
+
+    def set_tile_width(self, tile_w: int) -> None:
+        """Plain FP16 tensor plans: tiles of 128 rows by tile_w = 128, 96 or
+        64 columns; same bits."""
+        _check(lib().tcs_plan_set_tile_width(self._h, int(tile_w)))
+
+    def tile_width(self) -> int:
+        w = ctypes.c_int()
+        _check(lib().tcs_plan_tile_width(self._h, ctypes.byref(w)))
+        return w.value
 
     def close(self) -> None:
         if getattr(self, "_h", None):

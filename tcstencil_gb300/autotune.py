@@ -7,13 +7,15 @@ script/process_data.py:29-43).  Here the candidates are run-time choices of
 one library, timed with CUDA events:
 
   sweep  (stencil, precision, size class) -> engine ("tensor" | "cudacore"),
-                                             temporal depth (1 | 2) and launch
+                                             temporal depth (1 | 2), launch
                                              form (one launch per step, or one
                                              launch for all steps of a call)
+                                             and tile shape (128 rows by 128,
+                                             96 or 64 columns; plain FP16)
   serve  (offered load)                   -> round_steps of the request server
 
-Size classes are powers of two of each side, so one entry covers grids of
-similar shape.  The cache file is TCS_AUTOTUNE_CACHE, else
+Size classes are half octaves of each side (sqrt(2) steps), so one entry
+covers grids of similar shape.  The cache file is TCS_AUTOTUNE_CACHE, else
 ~/.cache/tcstencil_gb300/autotune.json; entries are keyed by GPU name, so one
 file can hold several machines' results.  Lookups fall back to the results
 shipped with the package (tuned.json, measured on GB300 by this module) when
@@ -34,16 +36,30 @@ import numpy as np
 from .workloads import RADIUS, normalized_coeffs
 
 ENGINES_FOR = {"f16": ("tensor", "cudacore"), "split": ("tensor",), "f32": ("cudacore",)}
-# (engine, temporal depth, one launch for all steps) candidates per precision
-CANDIDATES = {"f16": (("tensor", 1, 0), ("tensor", 1, 1), ("cudacore", 1, 0)),
-              "split": (("tensor", 1, 0), ("tensor", 1, 1), ("tensor", 2, 0)),
-              "f32": (("cudacore", 1, 0),)}
+# (engine, temporal depth, one launch for all steps, tile width) candidates
+# per precision
+CANDIDATES = {"f16": (("tensor", 1, 0, 128), ("tensor", 1, 1, 128), ("tensor", 1, 0, 96),
+                      ("tensor", 1, 1, 96), ("tensor", 1, 0, 64), ("tensor", 1, 1, 64),
+                      ("cudacore", 1, 0, 128)),
+              "split": (("tensor", 1, 0, 128), ("tensor", 1, 1, 128), ("tensor", 2, 0, 128)),
+              "f32": (("cudacore", 1, 0, 128),)}
 
 
-def candidate_key(engine: str, depth: int, multistep: int) -> str:
-    """"tensor/1" (one launch per step), "tensor/1/m" (one launch), ..."""
-    return f"{engine}/{depth}" + ("/m" if multistep else "")
+def candidate_key(engine: str, depth: int, multistep: int, tile_w: int = 128) -> str:
+    """"tensor/1" (one launch per step), "tensor/1/m" (one launch),
+    "tensor/1/m/w64" (and 64-column tiles), ..."""
+    return f"{engine}/{depth}" + ("/m" if multistep else "") + (f"/w{tile_w}" if tile_w != 128 else "")
+
+
+def parse_candidate(key: str) -> tuple:
+    """(engine, depth, multistep, tile_w) of a candidate_key."""
+    parts = key.split("/")
+    w = [int(p[1:]) for p in parts[2:] if p.startswith("w")]
+    return parts[0], int(parts[1]), int("m" in parts[2:]), w[0] if w else 128
 DEFAULT_ROUND_STEPS = 16
+# one square grid per half-octave class from 256 to 8196 (1026 and 8196 are
+# the first two benchmark configurations' grids)
+SWEEP_SIDES = (256, 362, 512, 724, 1024, 1026, 1600, 2896, 4096, 5792, 8192, 8196)
 
 
 def cache_path() -> str:
@@ -65,7 +81,11 @@ def device_key() -> str:
 
 
 def size_class(ny: int, nx: int) -> str:
-    return f"{int(math.ceil(math.log2(max(ny, 1))))}x{int(math.ceil(math.log2(max(nx, 1))))}"
+    """Half-octave class of each side: ceil(2 log2 n) / 2, e.g. "10.5x10.5"
+    for sides 1025 .. 1448 and "11x11" for 1449 .. 2048."""
+    def c(n):
+        return f"{math.ceil(2 * math.log2(max(n, 1)) - 1e-9) / 2:g}"
+    return f"{c(ny)}x{c(nx)}"
 
 
 SHIPPED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned.json")
@@ -115,7 +135,7 @@ def pick_fastest(timings: dict) -> str:
 
 
 def time_sweep(engine: str, depth: int, stencil: str, precision: str, ny: int, nx: int,
-               steps: int, multistep: int = 0, reps: int = 3) -> float:
+               steps: int, multistep: int = 0, tile_w: int = 128, reps: int = 3) -> float:
     """Seconds per step of a plan on the device (CUDA-graph runs, CUDA events)."""
     import torch
 
@@ -128,6 +148,8 @@ def time_sweep(engine: str, depth: int, stencil: str, precision: str, ny: int, n
     try:
         if engine == "tensor" and depth == 1:
             p.set_multistep(multistep)
+        if tile_w != 128:
+            p.set_tile_width(tile_w)
         p.upload(g)
         p.run(steps, use_graph=True)
         torch.cuda.synchronize()
@@ -147,16 +169,16 @@ def time_sweep(engine: str, depth: int, stencil: str, precision: str, ny: int, n
 
 def tune_sweep(stencil: str, precision: str, ny: int, nx: int, steps: int = 20,
                cache: Cache | None = None, timer=time_sweep) -> dict:
-    """Times every (engine, temporal depth, launch form) that supports the
-    precision; stores and returns {"engine", "temporal_depth", "multistep",
-    "s_per_step": {candidate_key: s}}."""
+    """Times every (engine, temporal depth, launch form, tile width) that
+    supports the precision; stores and returns {"engine", "temporal_depth",
+    "multistep", "tile_w", "s_per_step": {candidate_key: s}}."""
     cache = cache or Cache()
-    timings = {candidate_key(e, d, m): timer(e, d, stencil, precision, ny, nx, steps, m)
-               for e, d, m in CANDIDATES[precision]}
-    best = pick_fastest(timings)
-    parts = best.split("/")
-    entry = {"engine": parts[0], "temporal_depth": int(parts[1]),
-             "multistep": int(len(parts) > 2), "s_per_step": timings,
+    timings = {candidate_key(e, d, m, w): timer(e, d, stencil, precision, ny, nx, steps, m,
+                                                **({"tile_w": w} if w != 128 else {}))
+               for e, d, m, w in CANDIDATES[precision]}
+    engine, depth, multistep, tile_w = parse_candidate(pick_fastest(timings))
+    entry = {"engine": engine, "temporal_depth": depth, "multistep": multistep,
+             "tile_w": tile_w, "s_per_step": timings,
              "measured_on": [ny, nx], "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
     cache.section("sweep")[sweep_key(stencil, precision, ny, nx)] = entry
     cache.save()
@@ -182,6 +204,14 @@ def best_launch(stencil: str, precision: str, ny: int, nx: int, cache: Cache | N
     cache = cache or Cache()
     e = cache.lookup("sweep", sweep_key(stencil, precision, ny, nx))
     return int(e["multistep"]) if e and "multistep" in e else -1
+
+
+def best_tile_width(stencil: str, ny: int, nx: int, cache: Cache | None = None) -> int:
+    """The tuned tile width of plain FP16 tensor sweeps for this problem class
+    (128 when not tuned)."""
+    cache = cache or Cache()
+    e = cache.lookup("sweep", sweep_key(stencil, "f16", ny, nx))
+    return int(e.get("tile_w", 128)) if e else 128
 
 
 def best_engine(stencil: str, precision: str, ny: int, nx: int, cache: Cache | None = None) -> str:
@@ -243,7 +273,7 @@ def main():
     if args.sweep or not args.serve:
         for stencil in RADIUS:
             for precision in ("f16", "split"):
-                for n in (256, 1024, 2048, 4096, 8196):
+                for n in SWEEP_SIDES:
                     e = tune_sweep(stencil, precision, n, n, cache=cache)
                     print(json.dumps({"key": sweep_key(stencil, precision, n, n), **e}))
     if args.serve:

@@ -111,7 +111,8 @@ int check_mode(int engine, int precision) {
 
 // One step from the input planes to the output planes.
 int run_step(const GridGeom &g, int stencil, int engine, int precision, const float *B,
-             const void *in, const void *in_lo, void *out, void *out_lo, cudaStream_t s) {
+             const void *in, const void *in_lo, void *out, void *out_lo, cudaStream_t s,
+             int tile_w = kTile) {
     cudaError_t e;
     if (engine == TCS_ENGINE_CUDACORE) {
         const TapCoeffs c = tap_coeffs(stencil, B);
@@ -127,7 +128,7 @@ int run_step(const GridGeom &g, int stencil, int engine, int precision, const fl
                             static_cast<uint16_t *>(out_lo), s);
     } else {
         e = launch_tc_f16(g, stencil, B, static_cast<const uint16_t *>(in),
-                          static_cast<uint16_t *>(out), s);
+                          static_cast<uint16_t *>(out), s, tile_w);
     }
     return cuda_status(e, "sweep kernel launch");
 }
@@ -372,9 +373,16 @@ struct tcs_plan_s {
         if (capture_stream) cudaStreamDestroy(capture_stream);
     }
 
+    // Tile columns of the plain FP16 tensor sweeps (64, 96 or 128,
+    // tcs_plan_set_tile_width); the other forms use 128.
+    int tile_w = kTile;
+    long long tiles() const {
+        return (long long)((g.ny + kTile - 1) / kTile) * ((g.nx + tile_w - 1) / tile_w);
+    }
+
     int step(int from, cudaStream_t s) {
         return run_step(g, prob.stencil, prob.engine, prob.precision, coeffs, buf[from][0],
-                        buf[from][1], buf[1 - from][0], buf[1 - from][1], s);
+                        buf[from][1], buf[1 - from][0], buf[1 - from][1], s, tile_w);
     }
 
     // Temporal depth 2 (split precision on the tensor engine): steps run in
@@ -404,7 +412,7 @@ struct tcs_plan_s {
         }();
         if (!on || !rows_done || prob.engine != TCS_ENGINE_TENSOR || pairs()) return false;
         if (multistep >= 0) return multistep == 1;
-        const long long tiles = (long long)((g.ny + kTile - 1) / kTile) * ((g.nx + kTile - 1) / kTile);
+        const long long tiles = this->tiles();
         const long long sms = device_sms();
         // Split, box2d1r, us per step, one launch per step -> one launch:
         // 2048² 11.1 -> 8.8, 4096² 30.4 -> 27.1, 8196² 103.3 -> 107.0, 16386²
@@ -428,7 +436,8 @@ struct tcs_plan_s {
                                         static_cast<uint16_t *>(buf[1 - from][0]),
                                         static_cast<uint16_t *>(buf[1 - from][1]), steps, rows_done, s)
                 : launch_tc_f16_steps(g, prob.stencil, coeffs, static_cast<const uint16_t *>(buf[from][0]),
-                                      static_cast<uint16_t *>(buf[1 - from][0]), steps, rows_done, s);
+                                      static_cast<uint16_t *>(buf[1 - from][0]), steps, rows_done, s,
+                                      tile_w);
         return cuda_status(e, "multi-step sweep launch");
     }
     // The state `steps` steps from `from` ends in: one flip per step.
@@ -603,6 +612,25 @@ int tcs_plan_set_multistep(tcs_plan p, int mode) {
         p->multistep = mode;
         p->drop_graphs();  // graphs hold the launch sequence
     }
+    return TCS_OK;
+}
+
+int tcs_plan_set_tile_width(tcs_plan p, int tile_w) {
+    if (!p || !valid_tile_width(tile_w))
+        return fail(TCS_ERR_INVALID, "tcs_plan_set_tile_width: the width is 64, 96 or 128");
+    if (tile_w != kTile &&
+        !(p->prob.engine == TCS_ENGINE_TENSOR && p->prob.precision == TCS_PREC_F16))
+        return fail(TCS_ERR_UNSUPPORTED, "tile widths below 128 are built for FP16 tensor sweeps");
+    if (tile_w != p->tile_w) {
+        p->tile_w = tile_w;
+        p->drop_graphs();  // graphs hold the launch parameters
+    }
+    return TCS_OK;
+}
+
+int tcs_plan_tile_width(tcs_plan p, int *tile_w) {
+    if (!p || !tile_w) return fail(TCS_ERR_INVALID, "tcs_plan_tile_width: null argument");
+    *tile_w = p->tile_w;
     return TCS_OK;
 }
 

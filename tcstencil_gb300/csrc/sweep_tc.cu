@@ -218,6 +218,7 @@ struct TcParams {
     CUtensorMap map_out, map_out_lo;  // several steps: the output planes (odd steps' input)
     GridGeom g;
     int tiles_x, n_tiles;
+    int tile_w;                     // plain: tile columns, 64, 96 or 128 (split: 128)
     int steps;                      // plain: steps of this launch (1 for the split kernels)
     unsigned *rows_done;            // plain, several steps: per tile row (every
                                     // kRowCounterStride), epilogue-warp completions
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
                 }
                 mbar_arrive_expect_tx(&full[s], NP * SG::PLANE);
                 load_tile_map((step & 1) ? &p.map_out : &p.map_hi, &p.map_lo, NP, ty * kTile,
-                              w.tx * kTile, stage_base + (size_t)s * NP * SG::PLANE, &full[s]);
+                              w.tx * p.tile_w, stage_base + (size_t)s * NP * SG::PLANE, &full[s]);
                 last_issued = i;
             }
             // Drain: every stage armed last must have landed before exit.
@@ -369,7 +370,7 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
                     smem_u32(stage_base + (size_t)s * NP * SG::PLANE), SG::CHUNK, 128);
                 tc_fence_after();
                 issue_plain_tile<C::R, SG>(a_hi0, band, tmem_base + col,
-                                           tile_windows(p.g.nx, tx * kTile));
+                                           tile_windows(p.g.nx, tx * p.tile_w, p.tile_w));
                 umma_commit(&acc_full[id]);
                 umma_commit(&empty[s]);
             }
@@ -405,10 +406,13 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
         int i = 0;
         TileWalk w;
         w.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+        const int W = p.tile_w;
+        const int G = W / 32;  // output blocks per warpgroup
+        const int j0 = half * G;
         for (int k = blockIdx.x; k < n_items && !stop; k += gridDim.x, i++, w.advance()) {
             const int step = w.step;
             const int Y0 = w.ty * kTile;
-            const int X0 = w.tx * kTile;
+            const int X0 = w.tx * W;
             // odd steps run from the output plane back into the input plane
             o.in_hi = (step & 1) ? p.out_hi : p.in_hi;
             o.out_hi = (step & 1) ? const_cast<uint16_t *>(p.in_hi) : p.out_hi;
@@ -423,18 +427,25 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
                 stop = true;
                 break;
             }
-            if (X0 + 64 * half >= p.g.nx) {  // this half is all padding: release unread
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&acc_empty[sl]);
-            } else {
-                tc_fence_after();
-                float f[M::SUB_BLOCKS / 2][16];
-                epilogue_load<SPLIT>(lane_base + (uint32_t)(sl * Mode<false>::ACC), half, f);
+            const int nblk = tile_windows(p.g.nx, X0, W) - 1;  // blocks holding grid cells
+            auto release = [&]() {
                 // accumulators read: the issuer may refill them while we store
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&acc_empty[sl]);
-                epilogue_store<SPLIT>(o, f, 0, half, m, Y0, X0);
+            };
+            if (j0 >= nblk) {  // none of this warpgroup's blocks hold grid cells
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[sl]);
+            } else {
+                tc_fence_after();
+                const uint32_t lc = lane_base + (uint32_t)(sl * Mode<false>::ACC);
+                const int y = Y0 + m;
+                const bool fast = tile_inside_w(o, Y0, X0, W);
+                const bool row_in = y >= o.y0 && y < o.y1;
+                if (G == 4) plain_epilogue<4>(o, lc, j0, nblk, y, X0, fast, row_in, release);
+                else if (G == 3) plain_epilogue<3>(o, lc, j0, nblk, y, X0, fast, row_in, release);
+                else plain_epilogue<2>(o, lc, j0, nblk, y, X0, fast, row_in, release);
             }
             if (p.rows_done) count_item(warp_done, warp - 1 - Sweep<S>::ISSUERS, (uint32_t)(i + 1));
         }
@@ -765,14 +776,16 @@ cudaError_t prepare_tc() {
 template <int S, bool SPLIT>
 cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
                       const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s,
-                      int steps = 1, unsigned *rows_done = nullptr) {
+                      int steps = 1, unsigned *rows_done = nullptr, int tile_w = kTile) {
     using C = Cfg<S, SPLIT>;
+    if (!valid_tile_width(tile_w) || (SPLIT && tile_w != kTile)) return cudaErrorInvalidValue;
     cudaError_t pe = prepare_tc<S, SPLIT>();
     if (pe != cudaSuccess) return pe;
     TcParams p;
     p.g = g;
+    p.tile_w = tile_w;
     const int tiles_y = (g.ny + kTile - 1) / kTile;
-    p.tiles_x = (g.nx + kTile - 1) / kTile;
+    p.tiles_x = (g.nx + tile_w - 1) / tile_w;
     p.n_tiles = tiles_y * p.tiles_x;
     p.in_hi = in_hi;
     p.in_lo = in_lo;
@@ -809,12 +822,12 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
 template <bool SPLIT>
 cudaError_t dispatch_tc(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
                         const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s,
-                        int steps = 1, unsigned *rows_done = nullptr) {
+                        int steps = 1, unsigned *rows_done = nullptr, int tile_w = kTile) {
     switch (stencil) {
-    case TCS_STAR2D1R: return launch_tc<TCS_STAR2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
-    case TCS_STAR2D2R: return launch_tc<TCS_STAR2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
-    case TCS_BOX2D1R: return launch_tc<TCS_BOX2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
-    case TCS_BOX2D2R: return launch_tc<TCS_BOX2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
+    case TCS_STAR2D1R: return launch_tc<TCS_STAR2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w);
+    case TCS_STAR2D2R: return launch_tc<TCS_STAR2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w);
+    case TCS_BOX2D1R: return launch_tc<TCS_BOX2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w);
+    case TCS_BOX2D2R: return launch_tc<TCS_BOX2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -839,13 +852,14 @@ cudaError_t tc_take_error(int *code) {
 }
 
 cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
-                          uint16_t *out, cudaStream_t s) {
-    return dispatch_tc<false>(g, stencil, B, in, nullptr, out, nullptr, s);
+                          uint16_t *out, cudaStream_t s, int tile_w) {
+    return dispatch_tc<false>(g, stencil, B, in, nullptr, out, nullptr, s, 1, nullptr, tile_w);
 }
 
 cudaError_t launch_tc_f16_steps(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
-                                uint16_t *out, int steps, unsigned *rows_done, cudaStream_t s) {
-    return dispatch_tc<false>(g, stencil, B, in, nullptr, out, nullptr, s, steps, rows_done);
+                                uint16_t *out, int steps, unsigned *rows_done, cudaStream_t s,
+                                int tile_w) {
+    return dispatch_tc<false>(g, stencil, B, in, nullptr, out, nullptr, s, steps, rows_done, tile_w);
 }
 
 cudaError_t launch_tc_split_steps(const GridGeom &g, int stencil, const float *B,

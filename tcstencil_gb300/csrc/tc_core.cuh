@@ -285,11 +285,12 @@ __device__ __forceinline__ void issue_split_window(uint64_t a_hi0, uint32_t band
 // windows j and j + 1, and blocks from the grid's last column on are padding
 // (split: never stored; plain: stored only as the input copied back, the
 // cells being outside the update rectangle; padding keeps finite contents).
-// So a tile of a grid nx cells wide needs windows 0 .. nb, nb = its blocks
-// holding grid cells (kTile / 16 for every tile but the last of a row).
-__device__ __forceinline__ int tile_windows(int nx, int X0) {
+// So a tile W columns wide of a grid nx cells wide needs windows 0 .. nb,
+// nb = its blocks holding grid cells (W / 16 for every tile but the last of a
+// row).
+__device__ __forceinline__ int tile_windows(int nx, int X0, int W = kTile) {
     const int nb = (nx - X0 + 15) >> 4;
-    return (nb < kTile / 16 ? nb : kTile / 16) + 1;
+    return (nb < W / 16 ? nb : W / 16) + 1;
 }
 
 // MMAs of sub-tile h of a staged tile into accumulator columns from d.
@@ -330,15 +331,16 @@ __device__ __forceinline__ void issue_subtile(uint64_t a_hi0, uint32_t band, uin
     }
 }
 
-// A plain tile's MMAs: all windows, or, when the grid ends within the tile's
-// first 64 columns (nwin from tile_windows), only the windows of its first
-// column half, whose blocks are the only ones the epilogue reads.  Two
-// compile-time sequences: a window bound tested per MMA slowed the issuer.
+// A plain tile's MMAs: the windows of its first 64, 96 or 128 columns, the
+// smallest of these that covers the nwin windows (tile_windows) its blocks
+// need, so that 64- and 96-column tiles, and tiles at the end of a row, skip
+// the rest.  Three compile-time sequences: a window bound tested per MMA
+// slowed the issuer.
 template <int R, class SG>
 __device__ __forceinline__ void issue_plain_tile(uint64_t a_hi0, uint32_t band, uint32_t d,
                                                  int nwin) {
-    constexpr int HALF_WIN = Mode<false>::SUB_BLOCKS / 2 + 1;
-    if (nwin <= HALF_WIN) issue_subtile<R, false, SG, HALF_WIN>(a_hi0, band, d, 0);
+    if (nwin <= 5) issue_subtile<R, false, SG, 5>(a_hi0, band, d, 0);
+    else if (nwin <= 7) issue_subtile<R, false, SG, 7>(a_hi0, band, d, 0);
     else issue_subtile<R, false, SG>(a_hi0, band, d, 0);
 }
 
@@ -496,6 +498,40 @@ __device__ __forceinline__ void epilogue_store(const TileOut &o,
 #pragma unroll
     for (int gg = 0; gg < G; gg++)
         store_block<SPLIT>(o, f[gg], y, X0 + 16 * (h * M::SUB_BLOCKS + j0 + gg), fast, row_in);
+}
+
+// Plain tiles of W = 64, 96 or 128 columns (the plain sweep kernel's
+// tile_w): the W / 16 output blocks are shared evenly by the two epilogue
+// warpgroups, G = W / 32 each, and only blocks holding grid cells (nblk, from
+// tile_windows) are stored.  Widths are multiples of 32 so that every window
+// keeps its parity (even windows initialise the accumulator, odd ones add)
+// from 128-column tiles: each output sums the same products in the same
+// order, and results are bit-identical whatever the width.
+__device__ __forceinline__ bool tile_inside_w(const TileOut &o, int Y0, int X0, int W) {
+    return Y0 >= o.y0 && Y0 + kTile <= o.y1 && X0 >= o.x0 && X0 + W <= o.x1;
+}
+
+// This warp's blocks j0 .. j0+G-1 of a plain accumulator (lane_col: its lane
+// quarter at the slot's first column) into registers; then `release` (the
+// accumulator may be refilled); then the blocks below nblk are stored.
+template <int G, typename Release>
+__device__ __forceinline__ void plain_epilogue(const TileOut &o, uint32_t lane_col, int j0,
+                                               int nblk, int y, int X0, bool fast, bool row_in,
+                                               Release &&release) {
+    uint32_t v[G][16];
+#pragma unroll
+    for (int gg = 0; gg < G; gg++) tmem_ld_x16(lane_col + 16 * (j0 + gg + 1), v[gg]);
+    tmem_ld_wait();
+    release();
+#pragma unroll
+    for (int gg = 0; gg < G; gg++) {
+        if (j0 + gg < nblk) {
+            float f[16];
+#pragma unroll
+            for (int c = 0; c < 16; c++) f[c] = __uint_as_float(v[gg][c]);
+            store_block<false>(o, f, y, X0 + 16 * (j0 + gg), fast, row_in);
+        }
+    }
 }
 
 // Launches a single-grid step kernel with programmatic stream serialization:

@@ -51,6 +51,9 @@ struct TapCoeffs {
 // inside the allocation.  Cell (y, x) is at
 //   ((x / cpp + 1) * nyp + (y + kPadTop)) * cpp + x % cpp.
 constexpr int kTile = 128;
+// Plain FP16 tensor sweeps may use narrower tiles (128 rows by 64 or 96
+// columns, tcs_plan_set_tile_width): more tiles for grids with few of them.
+__host__ __device__ constexpr bool valid_tile_width(int w) { return w == 64 || w == 96 || w == kTile; }
 constexpr int kPadTop = 4;
 constexpr int kPadRows = 8;
 
@@ -129,14 +132,15 @@ cudaError_t tb_take_error(int *code);
 cudaError_t tc_prepare(int stencil, bool split);
 
 cudaError_t launch_tc_f16(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
-                          uint16_t *out, cudaStream_t s);
+                          uint16_t *out, cudaStream_t s, int tile_w = kTile);
 // Several plain steps in one launch (in -> out -> in ...); rows_done: one
 // counter per tile row (ceil(ny / 128)) every kRowCounterStride unsigneds,
 // zeroed before the launch.  Each counter has its own 128-byte line: every SM
 // polls and counts them, and on shared lines those accesses serialise.
 constexpr int kRowCounterStride = 32;
 cudaError_t launch_tc_f16_steps(const GridGeom &g, int stencil, const float *B, const uint16_t *in,
-                                uint16_t *out, int steps, unsigned *rows_done, cudaStream_t s);
+                                uint16_t *out, int steps, unsigned *rows_done, cudaStream_t s,
+                                int tile_w = kTile);
 cudaError_t launch_tc_split_steps(const GridGeom &g, int stencil, const float *B,
                                   const uint16_t *in_hi, const uint16_t *in_lo, uint16_t *out_hi,
                                   uint16_t *out_lo, int steps, unsigned *rows_done, cudaStream_t s);

@@ -7,9 +7,13 @@ script/nvcc_compile.py, script/run_file_with_ncu.sh, script/process_data.py).
 Here one process covers the whole sweep: each configuration is a plan on the
 device, timed with CUDA events over `--launches` single-step launches after a
 warm-up, and reported as the reference's metric (update points per second,
-script/draw.py:19) and as a fraction of the measured HBM roofline.
+script/draw.py:19) and as a fraction of the measured HBM roofline.  The
+reference's TILE_SIZE axis is the tile width here (`--tiles`, plain FP16
+tensor sweeps: 128 rows by 128, 96 or 64 columns); as process_data.py:29-43
+keeps the default-tile row and the best-tile row, each row says whether it is
+the fastest tile of its (variant, stencil, precision, mesh size).
 
-    python -m tcstencil_gb300.harness --sizes 1600,3200,7200 --csv out.csv
+    python -m tcstencil_gb300.harness --sizes 1600,3200,7200 --tiles 128,96,64 --csv out.csv
 """
 from __future__ import annotations
 
@@ -38,7 +42,7 @@ def peak_gbs() -> float:
 
 
 def time_config(engine: str, stencil: str, precision: str, n: int, launches: int,
-                warmup: int = 5) -> dict:
+                warmup: int = 5, tile_w: int = 128) -> dict:
     import torch
 
     rng = np.random.default_rng(n)
@@ -55,6 +59,8 @@ def time_config(engine: str, stencil: str, precision: str, n: int, launches: int
     A = np.zeros((n + 2 * r, n + 2 * r), np.float32)
     A[r:-r, r:-r] = rng.uniform(-1, 1, (n, n)).astype(np.float32)
     plan = Plan(n + 2 * r, n + 2 * r, stencil, B, engine=engine, precision=precision)
+    if tile_w != 128:
+        plan.set_tile_width(tile_w)
     kernel_launches = plan.launches(launches)  # 1: all steps in one launch
     plan.upload(A)
     stream = torch.cuda.current_stream()
@@ -73,7 +79,7 @@ def time_config(engine: str, stencil: str, precision: str, n: int, launches: int
     gpts = n * n / (ms * 1e-3) / 1e9
     achieved = gpts * BYTES_PER_UPDATE[precision]
     return {"variant": engine, "stencil": stencil, "precision": precision, "mesh_size": n,
-            "tile": "128x128", "steps": launches, "kernel_launches": kernel_launches,
+            "tile": f"128x{tile_w}", "steps": launches, "kernel_launches": kernel_launches,
             "time_ms": round(ms, 5), "gpts": round(gpts, 2),
             "hbm_frac": round(achieved / peak_gbs(), 4)}
 
@@ -86,6 +92,8 @@ def main(argv=None) -> int:
     ap.add_argument("--sizes", default="1600,3200,4800,7200",
                     help="comma list, or 'reference' for script/param.py's 160*i sizes")
     ap.add_argument("--launches", type=int, default=50)
+    ap.add_argument("--tiles", default="128",
+                    help="comma list of tile widths (128, 96, 64) for plain FP16 tensor sweeps")
     ap.add_argument("--csv", default="-")
     args = ap.parse_args(argv)
     sizes = REFERENCE_SIZES if args.sizes == "reference" else [int(s) for s in args.sizes.split(",")]
@@ -97,7 +105,14 @@ def main(argv=None) -> int:
             assert engine in ENGINES and precision in PRECISIONS
             for stencil in args.stencils.split(","):
                 for n in sizes:
-                    rows.append(time_config(engine, stencil, precision, n, args.launches))
+                    widths = ([int(w) for w in args.tiles.split(",")]
+                              if (engine, precision) == ("tensor", "f16") else [128])
+                    group = [time_config(engine, stencil, precision, n, args.launches, tile_w=w)
+                             for w in widths]
+                    best = min(group, key=lambda row: row["time_ms"])
+                    for row in group:
+                        row["best_tile"] = int(row is best)
+                    rows.extend(group)
     out = sys.stdout if args.csv == "-" else open(args.csv, "w", newline="")
     w = csv.DictWriter(out, fieldnames=list(rows[0].keys()))
     w.writeheader()

@@ -13,16 +13,16 @@ def test_sweep_choice_is_persisted_per_class(tmp_path):
     fake = {"tensor": 2e-5, "cudacore": 1e-5}
     cache = autotune.Cache(path, shipped=None)
     e = autotune.tune_sweep("star2d1r", "f16", 300, 300, cache=cache,
-                            timer=lambda eng, depth, *a: fake[eng])
+                            timer=lambda eng, depth, *a, **kw: fake[eng])
     assert e["engine"] == "cudacore" and e["temporal_depth"] == 1
     # a fresh reader sees it, for any grid of the same size class only
     c2 = autotune.Cache(path, shipped=None)
-    assert autotune.best_engine("star2d1r", "f16", 500, 270, cache=c2) == "cudacore"
-    assert autotune.best_engine("star2d1r", "f16", 600, 300, cache=c2) == "tensor"
+    assert autotune.best_engine("star2d1r", "f16", 350, 270, cache=c2) == "cudacore"
+    assert autotune.best_engine("star2d1r", "f16", 400, 300, cache=c2) == "tensor"
     assert autotune.best_engine("box2d2r", "f16", 300, 300, cache=c2) == "tensor"
     assert autotune.best_engine("box2d2r", "f32", 300, 300, cache=c2) == "cudacore"
     data = json.load(open(path))
-    assert list(data.values())[0]["sweep"]["star2d1r/f16/9x9"]["engine"] == "cudacore"
+    assert list(data.values())[0]["sweep"]["star2d1r/f16/8.5x8.5"]["engine"] == "cudacore"
 
 
 def test_shipped_results_back_up_an_empty_cache(tmp_path):
@@ -45,18 +45,41 @@ def test_split_tries_both_temporal_depths_and_launch_forms(tmp_path):
     assert seen == [("tensor", 1, 0), ("tensor", 1, 1), ("tensor", 2, 0)]
     assert set(e["s_per_step"]) == {"tensor/1", "tensor/1/m", "tensor/2"}
     assert e["engine"] == "tensor" and e["temporal_depth"] == 2 and e["multistep"] == 0
-    assert autotune.best_config("box2d1r", "split", 60, 33, cache=cache) == ("tensor", 2)
-    assert autotune.best_config("box2d2r", "split", 60, 33, cache=cache) == ("tensor", 1)
+    assert autotune.best_config("box2d1r", "split", 60, 50, cache=cache) == ("tensor", 2)
+    assert autotune.best_config("box2d2r", "split", 60, 50, cache=cache) == ("tensor", 1)
 
 
 def test_launch_form_is_tuned_and_looked_up(tmp_path):
     cache = autotune.Cache(str(tmp_path / "t.json"), shipped=None)
     times = {("tensor", 1, 0): 3.0, ("tensor", 1, 1): 2.0, ("cudacore", 1, 0): 9.0}
     e = autotune.tune_sweep("box2d2r", "f16", 5000, 5000, cache=cache,
-                            timer=lambda eng, depth, *a: times[(eng, depth, a[-1])])
+                            timer=lambda eng, depth, *a, tile_w=128: times[(eng, depth, a[-1])]
+                            + (tile_w != 128))
     assert e["engine"] == "tensor" and e["temporal_depth"] == 1 and e["multistep"] == 1
-    assert autotune.best_launch("box2d2r", "f16", 4500, 6000, cache=cache) == 1
+    assert e["tile_w"] == 128
+    assert autotune.best_launch("box2d2r", "f16", 4500, 5500, cache=cache) == 1
     assert autotune.best_launch("box2d2r", "f16", 300, 300, cache=cache) == -1  # not tuned
+
+
+def test_tile_width_is_tuned_and_looked_up(tmp_path):
+    """Plain FP16 tensor candidates come in 128-, 96- and 64-column tiles;
+    the fastest width is stored and Plan(engine="auto") takes it."""
+    cache = autotune.Cache(str(tmp_path / "t.json"), shipped=None)
+    seen = []
+
+    def timer(eng, depth, *a, tile_w=128):
+        seen.append((eng, a[-1], tile_w))
+        return {128: 3.0, 96: 2.0, 64: 2.5}[tile_w] + (0.5 if a[-1] else 0) + (eng == "cudacore")
+
+    e = autotune.tune_sweep("star2d1r", "f16", 1026, 1026, cache=cache, timer=timer)
+    assert sorted(seen) == sorted([("tensor", m, w) for w in (128, 96, 64) for m in (0, 1)] +
+                                  [("cudacore", 0, 128)])
+    assert (e["engine"], e["multistep"], e["tile_w"]) == ("tensor", 0, 96)
+    assert "tensor/1/w96" in e["s_per_step"] and "tensor/1/m/w64" in e["s_per_step"]
+    assert autotune.best_tile_width("star2d1r", 1100, 1300, cache=cache) == 96
+    assert autotune.best_tile_width("star2d1r", 3000, 3000, cache=cache) == 128  # not tuned
+    assert autotune.parse_candidate("tensor/1/m/w64") == ("tensor", 1, 1, 64)
+    assert autotune.parse_candidate("cudacore/1") == ("cudacore", 1, 0, 128)
 
 
 def test_serve_choice_prefers_low_p99_among_those_keeping_up(tmp_path):
@@ -107,7 +130,8 @@ def test_shipped_tuning_is_consistent():
             assert stencil in ("star2d1r", "star2d2r", "box2d1r", "box2d2r")
             valid = {autotune.candidate_key(*c) for c in autotune.CANDIDATES[precision]}
             assert set(e["s_per_step"]) <= valid, (dev, key)
-            chosen = autotune.candidate_key(e["engine"], e["temporal_depth"], e.get("multistep", 0))
+            chosen = autotune.candidate_key(e["engine"], e["temporal_depth"], e.get("multistep", 0),
+                                            e.get("tile_w", 128))
             assert chosen in e["s_per_step"], (dev, key)
             assert e["s_per_step"][chosen] == min(e["s_per_step"].values()), (dev, key)
         for key, e in sections.get("serve", {}).items():
