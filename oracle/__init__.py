@@ -61,7 +61,7 @@ def lib() -> ctypes.CDLL:
                      "oracle_sweep_f16tc"):
             getattr(L, name).argtypes = [P, P, I, I, I, I, I, I, I, I]
             getattr(L, name).restype = I
-        L.oracle_sweep_split.argtypes = [P, P, P, I, I, I, I, I, I, I, I]
+        L.oracle_sweep_split.argtypes = [P, P, P, I, I, I, I, I, I, I, I, P]
         L.oracle_sweep_split.restype = I
         L.oracle_f32_to_f16.argtypes = [P, P, ctypes.c_long]
         L.oracle_f16_to_f32.argtypes = [P, P, ctypes.c_long]
@@ -229,13 +229,17 @@ def sweep_f16tc(A16, B, stencil, steps, rect=None):
     return g
 
 
-def sweep_split(hi, lo, B, stencil, steps, rect=None):
+def sweep_split(hi, lo, B, stencil, steps, rect=None, scale_exp=0):
+    """One run of `steps` split steps from planes in units of 2^scale_exp, with
+    the engine's per-step scale; returns (hi, lo, the final exponent)."""
     h = np.ascontiguousarray(hi, np.uint16).copy()
     l = np.ascontiguousarray(lo, np.uint16).copy()
     Bc = _coef(B, stencil)
+    e = ctypes.c_int(int(scale_exp))
     assert lib().oracle_sweep_split(_p(h), _p(l), _p(Bc), h.shape[0], h.shape[1],
-                                    STENCILS[stencil], steps, *_rect(rect)) == 0
-    return h, l
+                                    STENCILS[stencil], steps, *_rect(rect),
+                                    ctypes.byref(e)) == 0
+    return h, l, e.value
 
 
 def sweep_f32_fixed(A, B, stencil, steps, rect=None):

@@ -29,7 +29,9 @@
  *                       in double, RNE to FP16   (tensor-core FP16 kernel).
  *   oracle_step_split   fixed-point hi + lo*2^-11 FP16 pair storage,
  *                       coefficients in three FP16 pieces, four products,
- *                       sum in double (split tensor kernel).
+ *                       sum in double (split tensor kernel); the run of
+ *                       several steps, oracle_sweep_split, follows the
+ *                       engine's per-step scale exponent.
  *   oracle_step_f64     the same stencil in double (error reference).
  *
  * Threaded CPU timing of gold (the CPU baseline of bench.py):
@@ -267,6 +269,8 @@ typedef struct {
     const double *Bd;
     float cf[MAX_TAPS];
     double cd[MAX_TAPS], chi[MAX_TAPS], cfl[MAX_TAPS], clo[MAX_TAPS], c3[MAX_TAPS];
+    int shift;        /* split: the step's values are multiplied by 2^shift */
+    double *rowmax;   /* split: per row, the largest |x'| stored (or NULL) */
 } step_ctx;
 
 /* Fills the tap table and the coefficient forms of each kind.  Returns -1 for
@@ -386,9 +390,25 @@ static void step_rows(const step_ctx *c, int i0, int i1) {
         case K_SPLIT: {
             const uint16_t *Ah = (const uint16_t *)c->A, *Al = (const uint16_t *)c->Al;
             uint16_t *Ch = (uint16_t *)c->C, *Cl = (uint16_t *)c->Cl;
+            const double sc = ldexp(1.0, c->shift);
+            double m = 0.0; /* units of 2^-11 */
             for (int j = 0; j < nx; j++) {
                 long o = (long)i * nx + j;
-                if (!inside(c, i, j)) { Ch[o] = Ah[o]; Cl[o] = Al[o]; continue; }
+                if (!inside(c, i, j)) {
+                    uint16_t h = Ah[o], l = Al[o];
+                    if (c->shift) { /* the pair scaled by 2^shift, split again exactly */
+                        double a = H[h] * 2048.0 * sc, ai = trunc(a);
+                        double bb = (a - ai) + H[l] * sc, rb = nearbyint(bb);
+                        h = f64_to_f16((ai + rb) / 2048.0);
+                        l = f64_to_f16(bb - rb);
+                        m = fmax(m, fabs(ai + bb));
+                    } else {
+                        m = fmax(m, fabs(H[h] * 2048.0 + H[l]));
+                    }
+                    Ch[o] = h;
+                    Cl[o] = l;
+                    continue;
+                }
                 double main = 0.0, corr = 0.0;
                 for (int k = 0; k < nt; k++) {
                     long q = o + c->off[k];
@@ -396,11 +416,13 @@ static void step_rows(const step_ctx *c, int i0, int i1) {
                     main += c->chi[k] * xh;
                     corr += c->cfl[k] * xl + c->clo[k] * xh + c->c3[k] * xh;
                 }
-                double v = main + corr / 2048.0;
+                double v = (main + corr / 2048.0) * sc;
                 uint16_t h = f64_to_f16(nearbyint(v * 2048.0) / 2048.0);
                 Ch[o] = h;
                 Cl[o] = f64_to_f16((v - H[h]) * 2048.0);
+                m = fmax(m, fabs(v * 2048.0));
             }
+            if (c->rowmax) c->rowmax[i] = m / 2048.0;
             break;
         }
         }
@@ -613,23 +635,59 @@ int oracle_sweep_f16tc(uint16_t *grid, const float *B, int ny, int nx, int stenc
     return sweep16(oracle_step_f16tc, grid, B, ny, nx, stencil, steps, y0, y1, x0, x1);
 }
 
+/* e(M): the frexp exponent of M as an FP32 value (M 2^-e in [0.5, 1)), 0 for
+ * zero, subnormal or non-finite M, clamped to [-64, 64] (the engine's rule). */
+static int split_exp_of(double M) {
+    float f = (float)M;
+    if (!(f > 0.0f) || !isfinite(f) || f < 1.17549435e-38f) return 0;
+    int e;
+    frexpf(f, &e);
+    return e < -64 ? -64 : e > 64 ? 64 : e;
+}
+
+/* A split sweep of one run with the engine's per-step scale: the planes start
+ * in units of 2^E (*exp_io, the packing exponent) and end in units of 2^E_T
+ * (written back to *exp_io).  Step t's exponent is E_t = E_{t-2} + e(M_{t-2})
+ * (E_{-1} = E_0 = the input's, e(M_{-1}) = e(M_0) = 0), M_t the largest |x'|
+ * the step stores; the step's values are multiplied by 2^(E_{t-1} - E_t). */
 int oracle_sweep_split(uint16_t *hi, uint16_t *lo, const float *B, int ny, int nx, int stencil,
-                       int steps, int y0, int y1, int x0, int x1) {
+                       int steps, int y0, int y1, int x0, int x1, int *exp_io) {
     long cells = (long)ny * nx;
     uint16_t *th = (uint16_t *)malloc(cells * sizeof(uint16_t));
     uint16_t *tl = (uint16_t *)malloc(cells * sizeof(uint16_t));
-    if (!th || !tl) { free(th); free(tl); return -2; }
+    double *rowmax = (double *)malloc((size_t)ny * sizeof(double));
+    int *E = (int *)malloc((size_t)(steps + 2) * sizeof(int));
+    int *eM = (int *)malloc((size_t)(steps + 2) * sizeof(int));
+    if (!th || !tl || !rowmax || !E || !eM) {
+        free(th); free(tl); free(rowmax); free(E); free(eM);
+        return -2;
+    }
+    E[0] = E[1] = *exp_io; /* index t + 1 */
+    eM[0] = eM[1] = 0;
     uint16_t *ch = hi, *cl = lo, *nh = th, *nl = tl;
-    for (int t = 0; t < steps; t++) {
-        if (oracle_step_split(ch, cl, B, nh, nl, ny, nx, stencil, y0, y1, x0, x1)) {
-            free(th); free(tl); return -1;
-        }
+    int rc = 0;
+    for (int t = 1; t <= steps; t++) {
+        int et = E[t - 1] + eM[t - 1];
+        int k = E[t] - et;
+        k = k < -64 ? -64 : k > 64 ? 64 : k;
+        step_ctx c;
+        if (ctx_init(&c, K_SPLIT, ny, nx, stencil, y0, y1, x0, x1)) { rc = -1; break; }
+        c.A = ch; c.Al = cl; c.C = nh; c.Cl = nl; c.Bf = B;
+        ctx_coeffs(&c);
+        c.shift = k;
+        c.rowmax = rowmax;
+        run_step(&c);
+        double M = 0.0;
+        for (int i = 0; i < ny; i++) M = fmax(M, rowmax[i]);
+        E[t + 1] = et;
+        eM[t + 1] = split_exp_of(M);
         uint16_t *s = ch; ch = nh; nh = s;
         s = cl; cl = nl; nl = s;
     }
+    if (!rc) *exp_io = E[steps + 1];
     if (ch != hi) { memcpy(hi, ch, cells * 2); memcpy(lo, cl, cells * 2); }
-    free(th); free(tl);
-    return 0;
+    free(th); free(tl); free(rowmax); free(E); free(eM);
+    return rc;
 }
 
 /* ------------------------------------------------------ error metrics --- */

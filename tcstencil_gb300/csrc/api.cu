@@ -112,7 +112,7 @@ int check_mode(int engine, int precision) {
 // One step from the input planes to the output planes.
 int run_step(const GridGeom &g, int stencil, int engine, int precision, const float *B,
              const void *in, const void *in_lo, void *out, void *out_lo, cudaStream_t s,
-             int tile_w = kTile) {
+             int tile_w = kTile, SplitScale *scale = nullptr, int t0 = 0) {
     cudaError_t e;
     if (engine == TCS_ENGINE_CUDACORE) {
         const TapCoeffs c = tap_coeffs(stencil, B);
@@ -125,7 +125,7 @@ int run_step(const GridGeom &g, int stencil, int engine, int precision, const fl
     } else if (precision == TCS_PREC_SPLIT) {
         e = launch_tc_split(g, stencil, B, static_cast<const uint16_t *>(in),
                             static_cast<const uint16_t *>(in_lo), static_cast<uint16_t *>(out),
-                            static_cast<uint16_t *>(out_lo), s);
+                            static_cast<uint16_t *>(out_lo), s, scale, t0);
     } else {
         e = launch_tc_f16(g, stencil, B, static_cast<const uint16_t *>(in),
                           static_cast<uint16_t *>(out), s, tile_w);
@@ -348,8 +348,8 @@ struct tcs_plan_s {
     size_t plane_bytes = 0;
     void *buf[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [state][hi, lo]
     int cur = 0;
-    int scale_exp = 0;          // split form: planes hold x 2^-scale_exp
-    unsigned *d_max = nullptr;  // split form: max |x| scratch (float bits)
+    SplitScale *d_scale = nullptr;  // split form: per-step scale; the planes hold x 2^-E
+    unsigned *d_max = nullptr;      // split form: max |x| scratch (float bits)
     float *staging = nullptr;   // ny*nx FP32, for host/row-major transfers
     cudaStream_t capture_stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, start state)
@@ -369,6 +369,7 @@ struct tcs_plan_s {
                 if (p) cudaFree(p);
         if (staging) cudaFree(staging);
         if (d_max) cudaFree(d_max);
+        if (d_scale) cudaFree(d_scale);
         if (rows_done) cudaFree(rows_done);
         if (capture_stream) cudaStreamDestroy(capture_stream);
     }
@@ -380,21 +381,22 @@ struct tcs_plan_s {
         return (long long)((g.ny + kTile - 1) / kTile) * ((g.nx + tile_w - 1) / tile_w);
     }
 
-    int step(int from, cudaStream_t s) {
+    // t0: steps of the current run done before this one (split scale slots)
+    int step(int from, cudaStream_t s, int t0 = 0) {
         return run_step(g, prob.stencil, prob.engine, prob.precision, coeffs, buf[from][0],
-                        buf[from][1], buf[1 - from][0], buf[1 - from][1], s, tile_w);
+                        buf[from][1], buf[1 - from][0], buf[1 - from][1], s, tile_w, d_scale, t0);
     }
 
     // Temporal depth 2 (split precision on the tensor engine): steps run in
     // blocked pairs, with the same bits as single steps.
     int temporal_depth = 1;
     bool pairs() const { return temporal_depth == 2; }
-    int step2(int from, cudaStream_t s) {
+    int step2(int from, cudaStream_t s, int t0) {
         return cuda_status(
             launch_tc_split2(g, prob.stencil, coeffs, static_cast<const uint16_t *>(buf[from][0]),
                              static_cast<const uint16_t *>(buf[from][1]),
                              static_cast<uint16_t *>(buf[1 - from][0]),
-                             static_cast<uint16_t *>(buf[1 - from][1]), s),
+                             static_cast<uint16_t *>(buf[1 - from][1]), s, d_scale, t0),
             "blocked sweep launch");
     }
     // Tensor-engine plans (FP16 or split, temporal depth 1) run all steps of
@@ -434,7 +436,8 @@ struct tcs_plan_s {
                 ? launch_tc_split_steps(g, prob.stencil, coeffs, static_cast<const uint16_t *>(buf[from][0]),
                                         static_cast<const uint16_t *>(buf[from][1]),
                                         static_cast<uint16_t *>(buf[1 - from][0]),
-                                        static_cast<uint16_t *>(buf[1 - from][1]), steps, rows_done, s)
+                                        static_cast<uint16_t *>(buf[1 - from][1]), steps, rows_done, s,
+                                        d_scale, 0)
                 : launch_tc_f16_steps(g, prob.stencil, coeffs, static_cast<const uint16_t *>(buf[from][0]),
                                       static_cast<uint16_t *>(buf[1 - from][0]), steps, rows_done, s,
                                       tile_w);
@@ -445,24 +448,29 @@ struct tcs_plan_s {
         const int launches = pairs() ? steps / 2 + steps % 2 : steps;
         return from ^ (launches & 1);
     }
-    // Enqueues `steps` steps from state `from`; returns the final state in *to.
+    // Enqueues `steps` steps from state `from` (one run); returns the final
+    // state in *to.  A split run ends by moving its last two steps' scale
+    // records into the places the next run starts from.
     int enqueue(int steps, int from, cudaStream_t s, int *to) {
+        int st = TCS_OK;
         if (steps >= 2 && multi()) {
             *to = from ^ (steps & 1);
-            return steps_in_one(steps, from, s);
-        }
-        int st = TCS_OK;
-        for (int t = 0; t < steps && !st;) {
-            if (pairs() && steps - t >= 2) {
-                st = step2(from, s);
-                t += 2;
-            } else {
-                st = step(from, s);
-                t += 1;
+            st = steps_in_one(steps, from, s);
+        } else {
+            for (int t = 0; t < steps && !st;) {
+                if (pairs() && steps - t >= 2) {
+                    st = step2(from, s, t);
+                    t += 2;
+                } else {
+                    st = step(from, s, t);
+                    t += 1;
+                }
+                from ^= 1;
             }
-            from ^= 1;
+            *to = from;
         }
-        *to = from;
+        if (!st && d_scale)
+            st = cuda_status(launch_split_scale_end_run(d_scale, steps, s), "scale end of run");
         return st;
     }
 };
@@ -503,6 +511,11 @@ int tcs_plan_create(const tcs_problem *pr, tcs_plan *out) {
             if (!st) st = cuda_status(cudaMemset(p->buf[s][pl], 0, p->plane_bytes), "cudaMemset(plane)");
             if (st) return st;
         }
+    if (pr->precision == TCS_PREC_SPLIT) {
+        st = cuda_status(cudaMalloc(&p->d_scale, sizeof(SplitScale)), "cudaMalloc(scale)");
+        if (!st) st = cuda_status(cudaMemset(p->d_scale, 0, sizeof(SplitScale)), "cudaMemset(scale)");
+        if (st) return st;
+    }
     if (pr->engine == TCS_ENGINE_TENSOR) {
         st = cuda_status(tc_prepare(pr->stencil, pr->precision == TCS_PREC_SPLIT), "tensor kernel set-up");
         if (st) return st;
@@ -551,20 +564,19 @@ int tcs_plan_upload(tcs_plan p, const float *grid, int on_host, void *stream) {
     if (p->prob.precision == TCS_PREC_F32)
         e = launch_pack_f32(src, p->prob.ny, p->prob.nx, 0, 0.0f, static_cast<float *>(p->buf[0][0]), s);
     else if (p->prob.precision == TCS_PREC_SPLIT) {
-        // scale so that max |x| 2^-E <= 1 (needs the maximum on the host)
+        // scale so that max |x| 2^-E < 1, all on the device: the maximum, the
+        // packing with its exponent, and the scale record's starting history
         int st = TCS_OK;
         if (!p->d_max) st = cuda_status(cudaMalloc(&p->d_max, sizeof(unsigned)), "cudaMalloc(max)");
         if (!st) st = cuda_status(cudaMemsetAsync(p->d_max, 0, sizeof(unsigned), s), "memset(max)");
         if (!st) st = cuda_status(launch_max_abs(src, (size_t)p->prob.ny * p->prob.nx, p->d_max, s), "max_abs launch");
-        unsigned bits = 0;
-        if (!st) st = cuda_status(cudaMemcpyAsync(&bits, p->d_max, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "max copy");
-        if (!st) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        if (!st)
+            st = cuda_status(launch_pack_split_dev(src, p->prob.ny, p->prob.nx, p->d_max, nullptr,
+                                                   static_cast<uint16_t *>(p->buf[0][0]),
+                                                   static_cast<uint16_t *>(p->buf[0][1]), s),
+                             "pack launch");
         if (st) return st;
-        float mx;
-        std::memcpy(&mx, &bits, sizeof(mx));
-        p->scale_exp = split_scale_exp(mx);
-        e = launch_pack_split(src, p->prob.ny, p->prob.nx, 0, 0.0f, p->scale_exp,
-                              static_cast<uint16_t *>(p->buf[0][0]), static_cast<uint16_t *>(p->buf[0][1]), s);
+        e = launch_split_scale_init(p->d_scale, p->d_max, s);
     }
     else
         e = launch_pack_f16(src, p->prob.ny, p->prob.nx, 0, 0.0f, static_cast<uint16_t *>(p->buf[0][0]), s);
@@ -585,8 +597,8 @@ int tcs_plan_download(tcs_plan p, float *grid, int on_host, void *stream) {
     if (p->prob.precision == TCS_PREC_F32)
         e = launch_unpack_f32(static_cast<float *>(p->buf[c][0]), p->prob.ny, p->prob.nx, 0, dst, s);
     else if (p->prob.precision == TCS_PREC_SPLIT)
-        e = launch_unpack_split(static_cast<uint16_t *>(p->buf[c][0]), static_cast<uint16_t *>(p->buf[c][1]),
-                                p->prob.ny, p->prob.nx, 0, p->scale_exp, dst, s);
+        e = launch_unpack_split_dev(static_cast<uint16_t *>(p->buf[c][0]), static_cast<uint16_t *>(p->buf[c][1]),
+                                    p->prob.ny, p->prob.nx, split_scale_exp_ptr(p->d_scale), dst, s);
     else
         e = launch_unpack_f16(static_cast<uint16_t *>(p->buf[c][0]), p->prob.ny, p->prob.nx, 0, dst, s);
     int st = cuda_status(e, "unpack launch");
@@ -651,8 +663,11 @@ int tcs_plan_state(tcs_plan p, void **hi, void **lo, size_t *plane_bytes) {
 
 int tcs_plan_scale_exp(tcs_plan p, int *scale_exp) {
     if (!p || !scale_exp) return fail(TCS_ERR_INVALID, "tcs_plan_scale_exp: null argument");
-    *scale_exp = p->scale_exp;
-    return TCS_OK;
+    *scale_exp = 0;
+    if (!p->d_scale) return TCS_OK;
+    return cuda_status(cudaMemcpy(scale_exp, split_scale_exp_ptr(p->d_scale), sizeof(int),
+                                  cudaMemcpyDeviceToHost),
+                       "scale exponent copy");
 }
 
 int tcs_plan_run(tcs_plan p, int steps, int use_graph, void *stream) {
@@ -747,16 +762,14 @@ void tcs_release_cache(void) {
 
 // ================================================================= pipes ==
 // Submission k runs on plan and stream k % 2; before a slot is reused its
-// previous submission is waited for on the host.  Split grids keep the scale
-// exponent in device memory (maximum, exponent and packing on the stream), so
-// no submission blocks the host; the exponent is the one tcs_plan_upload
-// computes on the host (the same rule), so results match tcs_sweep_host.
+// previous submission is waited for on the host.  Split plans keep their scale
+// in device memory (maximum, exponent and packing on the stream), so no
+// submission blocks the host, and results match tcs_sweep_host.
 struct tcs_pipe_s {
     tcs_plan plan[2] = {nullptr, nullptr};
     cudaStream_t stream[2] = {nullptr, nullptr};
     cudaEvent_t done[2] = {nullptr, nullptr};
     cudaEvent_t swept[2] = {nullptr, nullptr};  // a slot's sweeps have finished
-    int *d_exp = nullptr;  // [2] split scale exponents
     long long submitted = 0;
     ~tcs_pipe_s() {
         for (int k = 0; k < 2; k++) {
@@ -766,42 +779,8 @@ struct tcs_pipe_s {
             if (stream[k]) cudaStreamDestroy(stream[k]);
             if (plan[k]) tcs_plan_destroy(plan[k]);
         }
-        if (d_exp) cudaFree(d_exp);
     }
 };
-
-namespace {
-
-int pipe_upload(tcs_plan p, int *d_exp, const float *h_in, cudaStream_t s) {
-    if (p->prob.precision != TCS_PREC_SPLIT) return tcs_plan_upload(p, h_in, 1, s);
-    int st = ensure_staging(p);
-    if (!st && !p->d_max) st = cuda_status(cudaMalloc(&p->d_max, sizeof(unsigned)), "cudaMalloc(max)");
-    if (st) return st;
-    const size_t n = (size_t)p->prob.ny * p->prob.nx;
-    st = cuda_status(cudaMemcpyAsync(p->staging, h_in, n * sizeof(float), cudaMemcpyHostToDevice, s), "upload copy");
-    if (!st) st = cuda_status(cudaMemsetAsync(p->d_max, 0, sizeof(unsigned), s), "memset(max)");
-    if (!st) st = cuda_status(launch_max_abs(p->staging, n, p->d_max, s), "max_abs launch");
-    if (!st) st = cuda_status(launch_pack_split_dev(p->staging, p->prob.ny, p->prob.nx, p->d_max, d_exp,
-                                                    static_cast<uint16_t *>(p->buf[0][0]),
-                                                    static_cast<uint16_t *>(p->buf[0][1]), s),
-                              "pack launch");
-    p->cur = 0;
-    return st;
-}
-
-int pipe_download(tcs_plan p, const int *d_exp, float *h_out, cudaStream_t s) {
-    if (p->prob.precision != TCS_PREC_SPLIT) return tcs_plan_download(p, h_out, 1, s);
-    const int c = p->cur;
-    int st = cuda_status(launch_unpack_split_dev(static_cast<uint16_t *>(p->buf[c][0]),
-                                                 static_cast<uint16_t *>(p->buf[c][1]),
-                                                 p->prob.ny, p->prob.nx, d_exp, p->staging, s),
-                         "unpack launch");
-    if (!st) st = cuda_status(cudaMemcpyAsync(h_out, p->staging, (size_t)p->prob.ny * p->prob.nx * sizeof(float),
-                                              cudaMemcpyDeviceToHost, s), "download copy");
-    return st;
-}
-
-}  // namespace
 
 extern "C" {
 
@@ -816,7 +795,6 @@ int tcs_pipe_create(const tcs_problem *pr, tcs_pipe *out) {
         if (!st) st = cuda_status(cudaEventCreateWithFlags(&q->done[k], cudaEventDisableTiming), "cudaEventCreate");
         if (!st) st = cuda_status(cudaEventCreateWithFlags(&q->swept[k], cudaEventDisableTiming), "cudaEventCreate");
     }
-    if (!st) st = cuda_status(cudaMalloc(&q->d_exp, 2 * sizeof(int)), "cudaMalloc(exp)");
     if (st) return st;
     *out = q.release();
     return TCS_OK;
@@ -833,7 +811,7 @@ int tcs_pipe_submit(tcs_pipe q, const float *h_in, float *h_out, int steps) {
     cudaStream_t s = q->stream[k];
     int st = TCS_OK;
     if (q->submitted >= 2) st = cuda_status(cudaEventSynchronize(q->done[k]), "cudaEventSynchronize");
-    if (!st) st = pipe_upload(q->plan[k], q->d_exp + k, h_in, s);
+    if (!st) st = tcs_plan_upload(q->plan[k], h_in, 1, s);
     // Sweeps take turns: a slot's sweeps start after the previous
     // submission's, so that only copies (and the small pack and unpack
     // kernels) overlap them.  Two sets of persistent sweeps sharing the SMs
@@ -842,7 +820,7 @@ int tcs_pipe_submit(tcs_pipe q, const float *h_in, float *h_out, int steps) {
         st = cuda_status(cudaStreamWaitEvent(s, q->swept[k ^ 1], 0), "cudaStreamWaitEvent");
     if (!st) st = tcs_plan_run(q->plan[k], steps, 1, s);
     if (!st) st = cuda_status(cudaEventRecord(q->swept[k], s), "cudaEventRecord");
-    if (!st) st = pipe_download(q->plan[k], q->d_exp + k, h_out, s);
+    if (!st) st = tcs_plan_download(q->plan[k], h_out, 1, s);
     if (!st) st = cuda_status(cudaEventRecord(q->done[k], s), "cudaEventRecord");
     if (!st) q->submitted++;
     return st;

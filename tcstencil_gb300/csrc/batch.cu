@@ -73,7 +73,7 @@ struct BatchCfg {
     static constexpr int EPI_WARP0 = 1 + ISSUERS;
     static constexpr int SIGNAL_WARP = EPI_WARP0 + EPI_WARPS;
     static constexpr int THREADS = 32 * (SIGNAL_WARP + 1);
-    static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 512 + kTableInts * 4;
+    static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 576 + kTableInts * 4;
     static_assert(kRing > STAGES + 2, "a ring slot is reused only after its item's epilogue");
     static_assert(SMEM <= 232448, "shared memory budget");
     static_assert(STAGE_BYTES % 16 == 0, "bulk copy alignment");
@@ -164,10 +164,15 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
     BatchItem *ring = reinterpret_cast<BatchItem *>(ring_free + kRing);  // [kRing]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(ring + kRing);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    // split: per ring slot, the item's largest |x'| (FP32 bits) and exponent,
+    // which the signal warp adds to the grid's scale record
+    unsigned *item_max = reinterpret_cast<unsigned *>(tmem_slot + 2);  // [kRing]
+    int *item_exp = reinterpret_cast<int *>(item_max + kRing);          // [kRing]
     volatile int *grid_error = p.error;
-    static_assert((2 * NS + 2 * NACC + 1 + 3 * kRing) * 8 + kRing * sizeof(BatchItem) + 8 <= 512,
+    static_assert((2 * NS + 2 * NACC + 1 + 3 * kRing) * 8 + kRing * sizeof(BatchItem) + 8 +
+                          8 * kRing <= 576,
                   "barrier area");
-    int *tables = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(bars) + 512);
+    int *tables = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(bars) + 576);
     const int n_table = p.n_steps + 1 + p.n_grids + 1;
     const bool tables_in_smem = n_table <= kTableInts;
 
@@ -190,6 +195,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             mbar_init(&item_ready[j], 1);
             mbar_init(&item_done[j], C::EPI_WARPS);
             mbar_init(&ring_free[j], 1);
+            item_max[j] = 0u;
+            item_exp[j] = 0;
         }
         *abort_flag = 0;
         fence_mbar_init();
@@ -453,6 +460,18 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     give_up();
                     break;
                 }
+                if (SPLIT) {
+                    // the item's maximum and the step's exponent into the
+                    // grid's scale record, before its count is released
+                    SplitScale *sc = p.grids[it.g].scale;
+                    if (sc) {
+                        const int t = it.t + 1;  // the step within the run, from 1
+                        atomicMax(&sc->maxbits[t & (kScaleRing - 1)], item_max[j]);
+                        sc->exp[t & (kScaleRing - 1)] = item_exp[j];
+                        sc->maxbits[(t + 3) & (kScaleRing - 1)] = 0u;
+                    }
+                    item_max[j] = 0u;
+                }
                 mbar_arrive(&ring_free[j]);
                 pend = ctr;
                 n_pend += C::EPI_WARPS;
@@ -494,6 +513,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             o.out_lo = in ? g.plane[0][1] : g.plane[1][1];
             o.pg = g.pg;
             o.y0 = g.y0; o.y1 = g.y1; o.x0 = g.x0; o.x1 = g.x1;
+            o.ny = g.ny; o.nx = g.nx;
             const int Y0 = it.ty * kTile;
             const int X0 = it.tx * kTile;
             // this warp's 32 rows all lie in the plane's padding below the grid:
@@ -504,6 +524,33 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 const int y = Y0 + m;
                 const bool fast = tile_inside(o, Y0, X0);
                 const bool row_in = y >= o.y0 && y < o.y1;
+                // the step's scale: steps t-2 and t-3 of the grid have
+                // finished (the producer waited for all of step t-1 before
+                // this item's stage filled); one acquire of that count orders
+                // this warp's reads of the scale record after them
+                StepScale ss = step_scale(nullptr, 0);
+                if (g.scale) {
+                    if (it.t > 0) {
+                        const unsigned *ctr =
+                            p.counters + (size_t)(g.ctr_base + it.t - 1) * kRowCounterStride;
+                        const unsigned target = (unsigned)(g.n_tiles * C::EPI_WARPS);
+                        const uint64_t t0 = global_timer_ns();
+                        bool okc = true;
+                        while (ld_acquire(ctr) < target) {
+                            if (*abort_flag || global_timer_ns() - t0 > wait_lim) {
+                                okc = false;
+                                break;
+                            }
+                            __nanosleep(64);
+                        }
+                        if (!__all_sync(0xffffffffu, okc)) {
+                            fail_result();
+                            break;
+                        }
+                    }
+                    ss = step_scale(g.scale, it.t + 1);
+                }
+                float mx = 0.0f;
                 auto ready = [&](int w) {
                     const int Gw = G0 + w;
                     bool okw = mbar_wait(&acc_full[Gw % kBatchRingSlots],
@@ -538,12 +585,21 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                         mbar_arrive(&acc_empty[Ga % kBatchRingSlots]);
                         mbar_arrive(&acc_empty[Gb % kBatchRingSlots]);
                     }
-                    store_block<true>(o, f, y, X0 + 16 * jb, fast, row_in);
+                    store_block_split(o, f, y, X0 + 16 * jb, fast, row_in, ss, ss, mx);
                 });
                 G0 += nwin;
                 if (!ok) {
                     stop = true;
                     break;
+                }
+                if (g.scale) {
+#pragma unroll
+                    for (int sh = 16; sh > 0; sh >>= 1)
+                        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, sh));
+                    if (lane == 0) {
+                        atomicMax(&item_max[j], __float_as_uint(mx * (1.0f / 2048.0f)));
+                        item_exp[j] = ss.e;
+                    }
                 }
             } else {
                 uint32_t col;
@@ -612,16 +668,37 @@ cudaError_t batch_prepare(int *num_sms) {
     return cudaSuccess;
 }
 
+// After a split run: every split grid's scale record ends the run of its
+// steps (as launch_split_scale_end_run), one thread per grid.
+__global__ void batch_scale_end_run_kernel(const BatchGrid *grids, int n_grids) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_grids) return;
+    SplitScale *sc = grids[i].scale;
+    const int T = grids[i].steps;
+    if (!sc || T <= 0) return;
+    const unsigned m1 = sc->maxbits[(T - 1) & (kScaleRing - 1)];
+    const unsigned m0 = sc->maxbits[T & (kScaleRing - 1)];
+    const int e1 = sc->exp[(T - 1) & (kScaleRing - 1)];
+    const int e0 = sc->exp[T & (kScaleRing - 1)];
+    for (int k = 1; k < kScaleRing - 1; k++) sc->maxbits[k] = 0;
+    sc->maxbits[kScaleRing - 1] = m1;
+    sc->exp[kScaleRing - 1] = e1;
+    sc->maxbits[0] = m0;
+    sc->exp[0] = e0;
+}
+
 // One CTA per SM.  Work is taken dynamically in index order, so a CTA waits
 // only on items already taken by running CTAs: progress needs no guarantee
 // that all CTAs are resident at once.
 cudaError_t launch_batch(const BatchParams &p, bool split, int num_sms, cudaStream_t s) {
     if (p.n_items <= 0) return cudaSuccess;
     const int grid = p.n_items < num_sms ? p.n_items : num_sms;
-    if (split)
+    if (split) {
         tc_batch_kernel<true><<<grid, BatchCfg<true>::THREADS, BatchCfg<true>::SMEM, s>>>(p);
-    else
+        batch_scale_end_run_kernel<<<(p.n_grids + 127) / 128, 128, 0, s>>>(p.grids, p.n_grids);
+    } else {
         tc_batch_kernel<false><<<grid, BatchCfg<false>::THREADS, BatchCfg<false>::SMEM, s>>>(p);
+    }
     return cudaGetLastError();
 }
 
@@ -652,7 +729,6 @@ struct tcs_batch_s {
         float coeffs[25];
         GridGeom g;
         int steps;
-        int scale_exp;
         size_t plane_elems;
         size_t offset[2][2];  // element offsets of the planes in the pool
         const unsigned *gate = nullptr;
@@ -679,6 +755,7 @@ struct tcs_batch_s {
     float *d_staging = nullptr;
     size_t staging_elems = 0;
     unsigned *d_max = nullptr;
+    SplitScale *d_scales = nullptr;  // [entry] the split grids' per-step scales
     long long point_updates = 0;
     bool built = false;
     int runs = 0;  // completed runs (each flips states by steps & 1)
@@ -691,7 +768,7 @@ struct tcs_batch_s {
         for (void *p : {(void *)pool, (void *)d_grids, (void *)d_maps, (void *)part[0].d_layout,
                         (void *)part[0].d_counters, (void *)part[1].d_layout,
                         (void *)part[1].d_counters, (void *)d_bands, (void *)d_coefs,
-                        (void *)d_staging, (void *)d_max})
+                        (void *)d_staging, (void *)d_max, (void *)d_scales})
             if (p) cudaFree(p);
     }
 
@@ -717,6 +794,8 @@ int batch_build(tcs_batch b) {
             }
     int st = cuda_status(cudaMalloc(&b->pool, total * sizeof(uint16_t)), "cudaMalloc(batch planes)");
     if (!st) st = cuda_status(cudaMemset(b->pool, 0, total * sizeof(uint16_t)), "cudaMemset(batch planes)");
+    if (!st) st = cuda_status(cudaMalloc(&b->d_scales, b->entries.size() * sizeof(SplitScale)), "cudaMalloc(scales)");
+    if (!st) st = cuda_status(cudaMemset(b->d_scales, 0, b->entries.size() * sizeof(SplitScale)), "cudaMemset(scales)");
     if (st) return st;
     b->pool_elems = total;
     // descriptors (FP16 grids then split grids, each sorted by steps,
@@ -757,6 +836,7 @@ int batch_build(tcs_batch b) {
         G.state = 0;
         G.gate = e.gate;
         G.gate_value = e.gate_value;
+        G.scale = split ? b->d_scales + order[i] : nullptr;
         steps[i] = e.steps;
         tiles[i] = G.n_tiles;
         ctr[split] += std::max(e.steps, 1);
@@ -878,7 +958,6 @@ int tcs_batch_add(tcs_batch b, const tcs_problem *pr, int steps, int *index) {
     if (pr->precision == TCS_PREC_SPLIT && !(tap_abs_sum(pr->stencil, e.coeffs) <= kSplitMaxAbsSum))
         return fail(TCS_ERR_UNSUPPORTED, "split precision needs a non-expanding stencil (sum of |c| <= 1)");
     e.steps = steps;
-    e.scale_exp = 0;
     e.plane_elems = plane_elems(e.g.p16);
     if (index) *index = (int)b->entries.size();
     b->entries.push_back(e);
@@ -903,19 +982,14 @@ int tcs_batch_upload(tcs_batch b, int index, const float *grid, int on_host, voi
     const int cur = b->state_of(e);
     uint16_t *hi = b->pool + e.offset[cur][0];
     if (e.prob.precision == TCS_PREC_SPLIT) {
-        // scale so that max |x| 2^-E <= 1 (needs the maximum on the host)
+        // scale so that max |x| 2^-E < 1, on the device: the maximum, the
+        // packing with its exponent, and the scale record's starting history
         if (!b->d_max) st = cuda_status(cudaMalloc(&b->d_max, sizeof(unsigned)), "cudaMalloc(max)");
         if (!st) st = cuda_status(cudaMemsetAsync(b->d_max, 0, sizeof(unsigned), s), "memset(max)");
         if (!st) st = cuda_status(launch_max_abs(src, cells, b->d_max, s), "max_abs launch");
-        unsigned bits = 0;
-        if (!st) st = cuda_status(cudaMemcpyAsync(&bits, b->d_max, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "max copy");
-        if (!st) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-        if (st) return st;
-        float mx;
-        std::memcpy(&mx, &bits, sizeof(mx));
-        e.scale_exp = split_scale_exp(mx);
-        st = cuda_status(launch_pack_split(src, e.g.ny, e.g.nx, 0, 0.0f, e.scale_exp, hi,
-                                           b->pool + e.offset[cur][1], s), "pack launch");
+        if (!st) st = cuda_status(launch_pack_split_dev(src, e.g.ny, e.g.nx, b->d_max, nullptr, hi,
+                                                        b->pool + e.offset[cur][1], s), "pack launch");
+        if (!st) st = cuda_status(launch_split_scale_init(b->d_scales + index, b->d_max, s), "scale init");
     } else {
         st = cuda_status(launch_pack_f16(src, e.g.ny, e.g.nx, 0, 0.0f, hi, s), "pack launch");
     }
@@ -938,8 +1012,9 @@ int tcs_batch_download(tcs_batch b, int index, float *grid, int on_host, void *s
     }
     const int cur = b->state_of(e);
     if (e.prob.precision == TCS_PREC_SPLIT)
-        st = cuda_status(launch_unpack_split(b->pool + e.offset[cur][0], b->pool + e.offset[cur][1],
-                                             e.g.ny, e.g.nx, 0, e.scale_exp, dst, s), "unpack launch");
+        st = cuda_status(launch_unpack_split_dev(b->pool + e.offset[cur][0], b->pool + e.offset[cur][1],
+                                                 e.g.ny, e.g.nx, split_scale_exp_ptr(b->d_scales + index),
+                                                 dst, s), "unpack launch");
     else
         st = cuda_status(launch_unpack_f16(b->pool + e.offset[cur][0], e.g.ny, e.g.nx, 0, dst, s),
                          "unpack launch");

@@ -27,6 +27,8 @@ struct BatchGrid {
     // tensor maps of the planes in device memory, [state][hi, lo] (lo = hi for
     // FP16 grids), from encode_grid_maps
     const CUtensorMap *maps;
+    // split grids: the per-step scale (SplitScale; step t of a run is slot t+1)
+    SplitScale *scale;
 };
 
 // Encodes the four tensor maps of a grid's planes ([state][hi, lo]).
@@ -105,6 +107,8 @@ constexpr int kBatchMaxBandElems = 4 * 5 * 512;
 cudaError_t batch_prepare(int *num_sms);
 // One persistent launch over p's work (all grids of one precision: split or
 // FP16); grid = min(items, SMs).  A run launches one per precision present.
+// A split launch is followed by the end of the run of every split grid's
+// scale record (as launch_split_scale_end_run, with the grid's steps).
 cudaError_t launch_batch(const BatchParams &p, bool split, int num_sms, cudaStream_t s);
 // Bands of one stencil (coefficients n x n row-major, n = 2r+1) into dst.
 cudaError_t launch_build_bands(const float *coef, int r, bool box, bool split, uint16_t *dst,

@@ -329,6 +329,39 @@ cudaError_t launch_unpack_f16(const uint16_t *plane, int ny, int nx, int pad, fl
     return cudaGetLastError();
 }
 
+__global__ void split_scale_init_kernel(SplitScale *sc, const unsigned *max_bits) {
+    const int e = scale_exp_of(*max_bits);
+    const float m = ldexpf(__uint_as_float(*max_bits), -e);
+    for (int i = 0; i < kScaleRing; i++) {
+        sc->maxbits[i] = 0;
+        sc->exp[i] = e;
+    }
+    sc->maxbits[0] = sc->maxbits[kScaleRing - 1] = __float_as_uint(isfinite(m) ? m : 0.0f);
+}
+
+__global__ void split_scale_end_run_kernel(SplitScale *sc, int steps) {
+    const unsigned m1 = sc->maxbits[(steps - 1) & (kScaleRing - 1)];
+    const unsigned m0 = sc->maxbits[steps & (kScaleRing - 1)];
+    const int e1 = sc->exp[(steps - 1) & (kScaleRing - 1)];
+    const int e0 = sc->exp[steps & (kScaleRing - 1)];
+    for (int i = 1; i < kScaleRing - 1; i++) sc->maxbits[i] = 0;
+    sc->maxbits[kScaleRing - 1] = m1;
+    sc->exp[kScaleRing - 1] = e1;
+    sc->maxbits[0] = m0;
+    sc->exp[0] = e0;
+}
+
+cudaError_t launch_split_scale_init(SplitScale *sc, const unsigned *max_bits, cudaStream_t s) {
+    split_scale_init_kernel<<<1, 1, 0, s>>>(sc, max_bits);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_scale_end_run(SplitScale *sc, int steps, cudaStream_t s) {
+    if (steps <= 0) return cudaSuccess;
+    split_scale_end_run_kernel<<<1, 1, 0, s>>>(sc, steps);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pack_f32(const float *in, int ny, int nx, int pad, float pad_value,
                             float *plane, cudaStream_t s) {
     const PackShape ps = pack_shape(ny, nx, pad, 4);

@@ -145,7 +145,7 @@ struct tcs_server_s {
     CUtensorMap *h_maps = nullptr;  // pinned staging of d_maps (a slot's entry is
                                     // rewritten only after its request retired)
     unsigned *d_maxbits = nullptr;
-    int *d_exp = nullptr;
+    SplitScale *d_scale = nullptr;  // per slot: a split request's per-step scale
     int *d_err = nullptr;       // sticky: the first failed wait of any round
     int *h_slot_err = nullptr;  // pinned, per slot: d_err as seen at completion
     std::vector<int> free_slots;
@@ -265,7 +265,7 @@ int tcs_server_s::finish(Request *q, int cur, bool wait_round, cudaEvent_t round
     int st = TCS_OK;
     if (wait_round) st = cuda_status(cudaStreamWaitEvent(download, round_end, 0), "cudaStreamWaitEvent");
     if (!st) {
-        if (q->split) st = cuda_status(launch_unpack_split_dev(plane(q, cur, 0), plane(q, cur, 1), q->g.ny, q->g.nx, d_exp + q->slot, stg, download), "unpack launch");
+        if (q->split) st = cuda_status(launch_unpack_split_dev(plane(q, cur, 0), plane(q, cur, 1), q->g.ny, q->g.nx, split_scale_exp_ptr(d_scale + q->slot), stg, download), "unpack launch");
         else st = cuda_status(launch_unpack_f16(plane(q, cur, 0), q->g.ny, q->g.nx, 0, stg, download), "unpack launch");
     }
     if (!st) st = cuda_status(cudaMemcpyAsync(q->h_out, stg, cells * sizeof(float), cudaMemcpyDeviceToHost, download), "request download");
@@ -385,7 +385,8 @@ void tcs_server_s::admit() {
         if (!st && q->split) {
             st = cuda_status(cudaMemsetAsync(mx, 0, sizeof(unsigned), upload), "max clear");
             if (!st) st = cuda_status(launch_max_abs(stg, cells, mx, upload), "max_abs launch");
-            if (!st) st = cuda_status(launch_pack_split_dev(stg, q->g.ny, q->g.nx, mx, d_exp + q->slot, plane(q, 0, 0), plane(q, 0, 1), upload), "pack launch");
+            if (!st) st = cuda_status(launch_pack_split_dev(stg, q->g.ny, q->g.nx, mx, nullptr, plane(q, 0, 0), plane(q, 0, 1), upload), "pack launch");
+            if (!st) st = cuda_status(launch_split_scale_init(d_scale + q->slot, mx, upload), "scale init");
         } else if (!st) {
             st = cuda_status(launch_pack_f16(stg, q->g.ny, q->g.nx, 0, 0.0f, plane(q, 0, 0), upload), "pack launch");
         }
@@ -520,6 +521,7 @@ bool tcs_server_s::launch_round() {
         G.gate = nullptr;
         G.gate_value = 0;
         G.maps = d_maps + 4 * (size_t)q->slot;
+        G.scale = q->split ? d_scale + q->slot : nullptr;
         ctr += run_steps[i];
     }
 
@@ -642,7 +644,7 @@ int tcs_server_create(const tcs_server_config *config, tcs_server *out) {
     if (!st) st = cuda_status(cudaMalloc(&s->d_maps, (size_t)slots * 4 * sizeof(CUtensorMap)), "cudaMalloc(maps)");
     if (!st) st = cuda_status(cudaMallocHost(&s->h_maps, (size_t)slots * 4 * sizeof(CUtensorMap)), "cudaMallocHost(maps)");
     if (!st) st = cuda_status(cudaMalloc(&s->d_maxbits, slots * sizeof(unsigned)), "cudaMalloc(max)");
-    if (!st) st = cuda_status(cudaMalloc(&s->d_exp, slots * sizeof(int)), "cudaMalloc(exp)");
+    if (!st) st = cuda_status(cudaMalloc(&s->d_scale, slots * sizeof(SplitScale)), "cudaMalloc(scales)");
     if (!st) st = cuda_status(cudaMalloc(&s->d_err, sizeof(int)), "cudaMalloc(error)");
     if (!st) st = cuda_status(cudaMemset(s->d_err, 0, sizeof(int)), "cudaMemset(error)");
     if (!st) st = cuda_status(cudaMallocHost(&s->h_slot_err, slots * sizeof(int)), "cudaMallocHost(errors)");
@@ -708,7 +710,7 @@ int tcs_server_destroy(tcs_server s) {
     for (void *p : s->retired.host) cudaFreeHost(p);
     for (void *p : s->retired.dev) cudaFree(p);
     for (void *p : {(void *)s->pool, (void *)s->d_bands, (void *)s->d_maps, (void *)s->d_maxbits,
-                    (void *)s->d_exp, (void *)s->d_err})
+                    (void *)s->d_scale, (void *)s->d_err})
         if (p) cudaFree(p);
     if (s->h_slot_err) cudaFreeHost(s->h_slot_err);
     if (s->h_maps) cudaFreeHost(s->h_maps);

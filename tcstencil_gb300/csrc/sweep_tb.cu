@@ -75,6 +75,8 @@ struct TbParams {
     int tiles_x, n_tiles;
     const uint16_t *in_hi, *in_lo;
     uint16_t *out_hi, *out_lo;
+    SplitScale *scale;  // the grid's per-step scale (null: fixed scale)
+    int t0;             // steps of the run done before this pair
     float coef[25];
 };
 
@@ -270,6 +272,7 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
         o.out_lo = p.out_lo;
         o.pg = pg;
         o.y0 = p.g.y0; o.y1 = p.g.y1; o.x0 = p.g.x0; o.x1 = p.g.x1;
+        o.ny = p.g.ny; o.nx = p.g.nx;
         int G0 = 0;
         bool stop = false;
         // bounded wait for window w of the current step (from G0)
@@ -308,6 +311,15 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
             if (!ok) stop = true;
             G0 += nwin;
         };
+        // The pair's two scales, both from steps finished before the launch
+        // (step t reads steps t-2 and t-3); the second step's copies come
+        // from the input, two steps back, so they take both shifts.
+        const StepScale ss1 = step_scale(p.scale, p.t0 + 1);
+        const StepScale ss2 = step_scale(p.scale, p.t0 + 2);
+        StepScale cs2 = ss2;
+        cs2.k = ss1.k + ss2.k;
+        cs2.s = __int_as_float((127 + 11 + cs2.k) << 23);
+        float mx1 = 0.0f, mx2 = 0.0f;
         for (int i = 0; i < n_mine && !stop; i++) {
             int Y0, X0;
             tile_origin(i, Y0, X0);
@@ -323,7 +335,8 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
                     uint32_t hw[8], lw[8];
                     if (fast) {
 #pragma unroll
-                        for (int c = 0; c < 8; c++) split_pair(f[2 * c], f[2 * c + 1], hw[c], lw[c]);
+                        for (int c = 0; c < 8; c++)
+                            split_pair_s(f[2 * c], f[2 * c + 1], ss1.s, hw[c], lw[c], mx1);
                     } else {
                         const uint4 a0 = load_panel_row(o.in_hi, pg, y, xb);
                         const uint4 a1 = load_panel_row(o.in_hi, pg, y, xb + 8);
@@ -338,10 +351,15 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
                             for (int u2 = 0; u2 < 2; u2++) {
                                 const int x = xb + 2 * c + u2;
                                 if (row_in && x >= o.x0 && x < o.x1) {
-                                    split_fixed(f[2 * c + u2], hh[u2], ll[u2]);
+                                    split_fixed_s(f[2 * c + u2], ss1.s, hh[u2], ll[u2], mx1);
                                 } else {
                                     hh[u2] = (uint16_t)(iw[c] >> (16 * u2));
                                     ll[u2] = (uint16_t)(il[c] >> (16 * u2));
+                                    float mc = 0.0f;
+                                    if (ss1.k != 0) resplit_pair(hh[u2], ll[u2], ss1, mc);
+                                    else mc = fabsf(fmaf(h_val(hh[u2]), 2048.0f, h_val(ll[u2])));
+                                    if (y >= 0 && y < p.g.ny && x >= 0 && x < p.g.nx)
+                                        mx1 = fmaxf(mx1, mc);
                                 }
                             }
                             hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
@@ -377,9 +395,14 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
                 const bool row_in = y >= o.y0 && y < o.y1;
                 run_step(kS2Windows, [&](int j, const float (&f)[16]) {
                     const int xb = X0 + 16 * j;
-                    if (mine && xb < p.g.nx) store_block<true>(o, f, y, xb, fast, row_in);
+                    if (mine && xb < p.g.nx)
+                        store_block_split(o, f, y, xb, fast, row_in, ss2, cs2, mx2);
                 });
             }
+        }
+        if (!stop && p.scale) {
+            flush_step_max(p.scale, p.t0 + 1, ss1, mx1);
+            flush_step_max(p.scale, p.t0 + 2, ss2, mx2);
         }
     }
 
@@ -396,7 +419,8 @@ int g_tb_sms = 0;
 
 template <int S>
 cudaError_t launch_tb(const GridGeom &g, const float *B, const uint16_t *in_hi,
-                      const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s) {
+                      const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s,
+                      SplitScale *scale, int t0) {
     using C = TbCfg<S>;
     static bool configured = false;
     if (!configured) {
@@ -420,6 +444,8 @@ cudaError_t launch_tb(const GridGeom &g, const float *B, const uint16_t *in_hi,
     p.in_lo = in_lo;
     p.out_hi = out_hi;
     p.out_lo = out_lo;
+    p.scale = scale;
+    p.t0 = t0;
     for (int k = 0; k < 25; k++) p.coef[k] = k < C::NDY * C::NDY ? B[k] : 0.0f;
     const int grid = p.n_tiles < g_tb_sms ? p.n_tiles : g_tb_sms;
     return launch_step(tc_split_tb_kernel<S>, grid, kTbThreads, C::SMEM, s, p);
@@ -429,12 +455,12 @@ cudaError_t launch_tb(const GridGeom &g, const float *B, const uint16_t *in_hi,
 
 cudaError_t launch_tc_split2(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
                              const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
-                             cudaStream_t s) {
+                             cudaStream_t s, SplitScale *scale, int t0) {
     switch (stencil) {
-    case TCS_STAR2D1R: return launch_tb<TCS_STAR2D1R>(g, B, in_hi, in_lo, out_hi, out_lo, s);
-    case TCS_STAR2D2R: return launch_tb<TCS_STAR2D2R>(g, B, in_hi, in_lo, out_hi, out_lo, s);
-    case TCS_BOX2D1R: return launch_tb<TCS_BOX2D1R>(g, B, in_hi, in_lo, out_hi, out_lo, s);
-    case TCS_BOX2D2R: return launch_tb<TCS_BOX2D2R>(g, B, in_hi, in_lo, out_hi, out_lo, s);
+    case TCS_STAR2D1R: return launch_tb<TCS_STAR2D1R>(g, B, in_hi, in_lo, out_hi, out_lo, s, scale, t0);
+    case TCS_STAR2D2R: return launch_tb<TCS_STAR2D2R>(g, B, in_hi, in_lo, out_hi, out_lo, s, scale, t0);
+    case TCS_BOX2D1R: return launch_tb<TCS_BOX2D1R>(g, B, in_hi, in_lo, out_hi, out_lo, s, scale, t0);
+    case TCS_BOX2D2R: return launch_tb<TCS_BOX2D2R>(g, B, in_hi, in_lo, out_hi, out_lo, s, scale, t0);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -225,8 +225,33 @@ struct TcParams {
                                     // over the launch (zeroed before it)
     const uint16_t *in_hi, *in_lo;  // input planes
     uint16_t *out_hi, *out_lo;
+    SplitScale *scale;              // split: the grid's per-step scale (null: fixed scale)
+    int t0;                         // split: steps of the run done before this launch
     float coef[25];                 // n x n, row-major
 };
+
+// Several split steps per launch: before the first tile of launch step j >= 2
+// an epilogue warp waits (bounded, acquire) until every tile row has finished
+// launch step j - 2, whose maxima and exponents its scale reads (tiles only
+// wait for their neighbouring rows of step j - 1).  No cycle: every tile of
+// step j - 2 is an earlier item of its CTA and depends only on earlier
+// items.  Returns false on give-up.
+__device__ __forceinline__ bool wait_all_rows(const unsigned *rows_done, int tiles_y,
+                                              unsigned target, const volatile int *abort_flag) {
+    const uint64_t t0 = global_timer_ns();
+    for (;;) {
+        bool done = true;
+        for (int r = (int)(threadIdx.x & 31); r < tiles_y; r += 32)
+            done = done && ld_relaxed(rows_done + r * kRowCounterStride) >= target;
+        if (__all_sync(0xffffffffu, done)) break;
+        if (*abort_flag || *(volatile int *)&g_tc_error != 0 ||
+            global_timer_ns() - t0 > kWaitLimitNs)
+            return false;
+        __nanosleep(128);
+    }
+    fence_acq_rel_gpu();
+    return true;
+}
 
 template <int S, bool SPLIT>
 __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __grid_constant__ TcParams p) {
@@ -401,6 +426,7 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
         o.out_lo = p.out_lo;
         o.pg = pg;
         o.y0 = p.g.y0; o.y1 = p.g.y1; o.x0 = p.g.x0; o.x1 = p.g.x1;
+        o.ny = p.g.ny; o.nx = p.g.nx;
         bool stop = false;
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
         int i = 0;
@@ -673,6 +699,7 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
         o.out_lo = p.out_lo;
         o.pg = pg;
         o.y0 = p.g.y0; o.y1 = p.g.y1; o.x0 = p.g.x0; o.x1 = p.g.x1;
+        o.ny = p.g.ny; o.nx = p.g.nx;
         int G0 = 0;  // first global window of the tile
         // bounded wait for window w of the tile
         auto ready = [&](int w) {
@@ -693,6 +720,11 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
         int i = 0;
         TileWalk w;
         w.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
+        // the scale of the current step, and this warp's largest |u| in it
+        int cur = -1;
+        StepScale ss = step_scale(nullptr, 0);
+        float mx = 0.0f;
+        const unsigned per_row = (unsigned)(kRingEpiWarps * tiles_x);
         for (int k = blockIdx.x; k < n_items; k += gridDim.x, G0 += kTileWindows, i++, w.advance()) {
             const int step = w.step;
             const int Y0 = w.ty * kTile;
@@ -703,6 +735,20 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
                 o.in_lo = (step & 1) ? p.out_lo : p.in_lo;
                 o.out_hi = (step & 1) ? const_cast<uint16_t *>(p.in_hi) : p.out_hi;
                 o.out_lo = (step & 1) ? const_cast<uint16_t *>(p.in_lo) : p.out_lo;
+            }
+            if (step != cur && p.scale) {
+                if (MULTI && step >= 2 &&
+                    !wait_all_rows(p.rows_done, tiles_y, (unsigned)(step - 1) * per_row,
+                                   abort_flag)) {
+                    if (lane == 0) {
+                        record_error(&g_tc_error, kErrWaitDep);
+                        *abort_flag = 1;
+                    }
+                    break;
+                }
+                ss = step_scale(p.scale, p.t0 + step + 1);
+                cur = step;
+                mx = 0.0f;
             }
             const int y = Y0 + m;
             const bool fast = tile_inside(o, Y0, X0);
@@ -719,9 +765,17 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
                     mbar_arrive(&win_empty[Ga % kRingSlots]);
                     mbar_arrive(&win_empty[Gb % kRingSlots]);
                 }
-                store_block<true>(o, f, y, X0 + 16 * j, fast, row_in);
+                store_block_split(o, f, y, X0 + 16 * j, fast, row_in, ss, ss, mx);
             });
             if (!ok) break;
+            // the step's last item of this warp: its maximum and the step's
+            // exponent go out before the item is counted
+            if (p.scale) {
+                TileWalk nw = w;
+                nw.advance();
+                if (k + (int)gridDim.x >= n_items || nw.step != step)
+                    flush_step_max(p.scale, p.t0 + step + 1, ss, mx);
+            }
             if (MULTI) count_item(warp_done, warp - 1 - kRingIssuers, (uint32_t)(i + 1));
         }
     }
@@ -776,7 +830,8 @@ cudaError_t prepare_tc() {
 template <int S, bool SPLIT>
 cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
                       const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s,
-                      int steps = 1, unsigned *rows_done = nullptr, int tile_w = kTile) {
+                      int steps = 1, unsigned *rows_done = nullptr, int tile_w = kTile,
+                      SplitScale *scale = nullptr, int t0 = 0) {
     using C = Cfg<S, SPLIT>;
     if (!valid_tile_width(tile_w) || (SPLIT && tile_w != kTile)) return cudaErrorInvalidValue;
     cudaError_t pe = prepare_tc<S, SPLIT>();
@@ -794,6 +849,8 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     if (me != cudaSuccess) return me;
     p.out_hi = out_hi;
     p.out_lo = out_lo;
+    p.scale = SPLIT ? scale : nullptr;
+    p.t0 = t0;
     p.steps = 1;
     p.rows_done = nullptr;
     p.map_out = p.map_hi;
@@ -822,12 +879,13 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
 template <bool SPLIT>
 cudaError_t dispatch_tc(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
                         const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo, cudaStream_t s,
-                        int steps = 1, unsigned *rows_done = nullptr, int tile_w = kTile) {
+                        int steps = 1, unsigned *rows_done = nullptr, int tile_w = kTile,
+                        SplitScale *scale = nullptr, int t0 = 0) {
     switch (stencil) {
-    case TCS_STAR2D1R: return launch_tc<TCS_STAR2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w);
-    case TCS_STAR2D2R: return launch_tc<TCS_STAR2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w);
-    case TCS_BOX2D1R: return launch_tc<TCS_BOX2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w);
-    case TCS_BOX2D2R: return launch_tc<TCS_BOX2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w);
+    case TCS_STAR2D1R: return launch_tc<TCS_STAR2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w, scale, t0);
+    case TCS_STAR2D2R: return launch_tc<TCS_STAR2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w, scale, t0);
+    case TCS_BOX2D1R: return launch_tc<TCS_BOX2D1R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w, scale, t0);
+    case TCS_BOX2D2R: return launch_tc<TCS_BOX2D2R, SPLIT>(g, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done, tile_w, scale, t0);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -864,14 +922,17 @@ cudaError_t launch_tc_f16_steps(const GridGeom &g, int stencil, const float *B, 
 
 cudaError_t launch_tc_split_steps(const GridGeom &g, int stencil, const float *B,
                                   const uint16_t *in_hi, const uint16_t *in_lo, uint16_t *out_hi,
-                                  uint16_t *out_lo, int steps, unsigned *rows_done, cudaStream_t s) {
-    return dispatch_tc<true>(g, stencil, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done);
+                                  uint16_t *out_lo, int steps, unsigned *rows_done, cudaStream_t s,
+                                  SplitScale *scale, int t0) {
+    return dispatch_tc<true>(g, stencil, B, in_hi, in_lo, out_hi, out_lo, s, steps, rows_done,
+                             kTile, scale, t0);
 }
 
 cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
                             const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
-                            cudaStream_t s) {
-    return dispatch_tc<true>(g, stencil, B, in_hi, in_lo, out_hi, out_lo, s);
+                            cudaStream_t s, SplitScale *scale, int t0) {
+    return dispatch_tc<true>(g, stencil, B, in_hi, in_lo, out_hi, out_lo, s, 1, nullptr, kTile,
+                             scale, t0);
 }
 
 }  // namespace tcs

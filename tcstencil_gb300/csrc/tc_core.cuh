@@ -129,11 +129,92 @@ __device__ __forceinline__ float h_val(uint16_t b) {
     return __half2float(h);
 }
 
+// ------------------------------------------------ split scale, per step ---
+// (tcs_internal.h SplitScale.)  e(M): the frexp exponent of a positive FP32
+// M, M 2^-e in [0.5, 1); 0 for zero, subnormal or non-finite M (no change);
+// clamped to [-64, 64].
+__device__ __forceinline__ int split_exp_of(unsigned bits) {
+    const int b = (int)((bits >> 23) & 0xffu);
+    if (b == 0 || b == 0xff) return 0;
+    const int e = b - 126;
+    return e < -64 ? -64 : e > 64 ? 64 : e;
+}
+
+// Scale of step t (the step index within the run, from 1): s = 2^(11 + k_t)
+// turns the step's value v (units of 2^E_{t-1}) into u = v s, the new state
+// in units of 2^-11 of 2^E_t.  Without a scale record (sc null) k = 0.
+struct StepScale {
+    float s;
+    int k, e;
+};
+
+__device__ __forceinline__ int ld_exp(const SplitScale *sc, int t) {
+    return (int)ld_relaxed(reinterpret_cast<const unsigned *>(&sc->exp[t & (kScaleRing - 1)]));
+}
+__device__ __forceinline__ int exp_at(const SplitScale *sc, int t) {  // E_t, from step t-2
+    return ld_exp(sc, t - 2) + split_exp_of(ld_relaxed(&sc->maxbits[(t - 2) & (kScaleRing - 1)]));
+}
+
+__device__ __forceinline__ StepScale step_scale(const SplitScale *sc, int t) {
+    StepScale r;
+    r.s = 2048.0f;
+    r.k = 0;
+    r.e = 0;
+    if (!sc) return r;
+    r.e = exp_at(sc, t);
+    const int e1 = t == 1 ? ld_exp(sc, 0) : exp_at(sc, t - 1);
+    int k = e1 - r.e;
+    k = k < -64 ? -64 : k > 64 ? 64 : k;
+    r.k = k;
+    r.s = __int_as_float((127 + 11 + k) << 23);
+    return r;
+}
+
+// After a warp's last cells of step t: its largest |u| (units of 2^-11) into
+// M_t, E_t into slot t, and the maximum of slot t+3 cleared.
+__device__ __forceinline__ void flush_step_max(SplitScale *sc, int t, const StepScale &ss,
+                                               float mx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&sc->maxbits[t & (kScaleRing - 1)], __float_as_uint(mx * (1.0f / 2048.0f)));
+        sc->exp[t & (kScaleRing - 1)] = ss.e;
+        sc->maxbits[(t + 3) & (kScaleRing - 1)] = 0u;
+    }
+}
+
 // Fixed-point split of a value v (|v| about 1 or below): hi = fp16 of
 // rint(v 2^11) 2^-11, lo = fp16((v - hi) 2^11).
 __device__ __forceinline__ void split_fixed(float v, uint16_t &hi, uint16_t &lo) {
     hi = h_bits(rintf(v * 2048.0f) * (1.0f / 2048.0f));
     lo = h_bits((v - h_val(hi)) * 2048.0f);
+}
+
+// split_fixed of the value v 2^k, with s = 2^(11 + k) (StepScale): u = v s,
+// hi = fp16(rint(u) 2^-11), lo = fp16(u - hi 2^11), the same bits as
+// split_fixed(v) when k = 0; the largest |u| is kept in mx.
+__device__ __forceinline__ void split_fixed_s(float v, float s, uint16_t &hi, uint16_t &lo,
+                                              float &mx) {
+    const float u = v * s;
+    hi = h_bits(rintf(u) * (1.0f / 2048.0f));
+    lo = h_bits(u - h_val(hi) * 2048.0f);
+    mx = fmaxf(mx, fabsf(u));
+}
+
+// A stored (hi, lo) pair scaled by 2^k (k != 0), split again exactly: with
+// a = hi 2^(11+k) = ai + af (ai its integer part) and b = lo 2^k, the new
+// pair is hi' = (ai + rint(af + b)) 2^-11, lo' = (af + b) - rint(af + b),
+// every operation exact, so no bit of the value is lost.  (k = 0 keeps the
+// pair as it is.)
+__device__ __forceinline__ void resplit_pair(uint16_t &hi, uint16_t &lo, const StepScale &ss,
+                                             float &mx) {
+    const float a = h_val(hi) * ss.s;
+    const float ai = truncf(a);
+    const float bb = (a - ai) + h_val(lo) * (ss.s * (1.0f / 2048.0f));
+    const float rb = rintf(bb);
+    hi = h_bits((ai + rb) * (1.0f / 2048.0f));
+    lo = h_bits(bb - rb);
+    mx = fmaxf(mx, fabsf(ai + bb));
 }
 
 // Two FP32 values as packed FP16 (round to nearest even), v0 in the low half.
@@ -149,6 +230,27 @@ __device__ __forceinline__ uint32_t pack_h2(float v0, float v1) {
 // t 2^-11 is exact in FP16 and lo = u - t = (v - hi) 2^11 is exact; past that
 // (|v| slightly above 1, or NaN) hi rounds in FP16 and split_fixed's rule is
 // taken.
+// With s = 2^(11 + k) the pair is of v 2^k (StepScale), and the largest |u|
+// is kept in mx.
+__device__ __forceinline__ void split_pair_s(float v0, float v1, float s, uint32_t &hw,
+                                             uint32_t &lw, float &mx) {
+    constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
+    const float u0 = v0 * s, u1 = v1 * s;
+    mx = fmaxf(mx, fmaxf(fabsf(u0), fabsf(u1)));
+    const float t0 = copysignf(__fsub_rn(__fadd_rn(u0, kRound), kRound), u0);
+    const float t1 = copysignf(__fsub_rn(__fadd_rn(u1, kRound), kRound), u1);
+    if (fabsf(t0) <= 2048.0f && fabsf(t1) <= 2048.0f) {
+        hw = pack_h2(t0 * (1.0f / 2048.0f), t1 * (1.0f / 2048.0f));
+        lw = pack_h2(__fsub_rn(u0, t0), __fsub_rn(u1, t1));
+    } else {
+        uint16_t h0, l0, h1, l1;
+        split_fixed_s(v0, s, h0, l0, mx);
+        split_fixed_s(v1, s, h1, l1, mx);
+        hw = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        lw = (uint32_t)l0 | ((uint32_t)l1 << 16);
+    }
+}
+
 __device__ __forceinline__ void split_pair(float v0, float v1, uint32_t &hw, uint32_t &lw) {
     constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
     const float u0 = v0 * 2048.0f, u1 = v1 * 2048.0f;
@@ -381,6 +483,7 @@ struct TileOut {
     uint16_t *out_hi, *out_lo;
     PlaneGeom pg;
     int y0, y1, x0, x1;
+    int ny, nx;                     // the grid (split maxima cover its cells only)
 };
 
 // Epilogue walk over one step of split windows for block group g of ng
@@ -477,6 +580,56 @@ __device__ __forceinline__ void store_block(const TileOut &o, const float (&f)[1
         *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
         *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
     }
+}
+
+// store_block<true> of the values v 2^k (StepScale ss): fast blocks split in
+// pairs, others split each updated cell alone and copy the rest, re-split by
+// the copy scale cs when cs.k != 0 (cs = ss, except for a blocked pair's
+// second step, whose copies come from two steps back).  The largest |u| of
+// the stored grid cells is kept in mx (a fast block lies in the update
+// rectangle, hence in the grid; padding cells never count).
+__device__ __forceinline__ void store_block_split(const TileOut &o, const float (&f)[16], int y,
+                                                  int xb, bool fast, bool row_in,
+                                                  const StepScale &ss, const StepScale &cs,
+                                                  float &mx) {
+    const size_t off0 = plane_index(o.pg, y, xb);     // cells xb .. xb+7
+    const size_t off1 = off0 + (size_t)o.pg.nyp * 8;  // cells xb+8 .. xb+15
+    uint32_t hw[8], lw[8];
+    if (fast) {
+#pragma unroll
+        for (int c = 0; c < 8; c++) split_pair_s(f[2 * c], f[2 * c + 1], ss.s, hw[c], lw[c], mx);
+    } else {
+        const uint4 i0 = *reinterpret_cast<const uint4 *>(o.in_hi + off0);
+        const uint4 i1 = *reinterpret_cast<const uint4 *>(o.in_hi + off1);
+        const uint4 l0 = *reinterpret_cast<const uint4 *>(o.in_lo + off0);
+        const uint4 l1 = *reinterpret_cast<const uint4 *>(o.in_lo + off1);
+        const uint32_t iw[8] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w};
+        const uint32_t il[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            uint16_t hh[2], ll[2];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int x = xb + 2 * c + u;
+                if (row_in && x >= o.x0 && x < o.x1) {
+                    split_fixed_s(f[2 * c + u], ss.s, hh[u], ll[u], mx);
+                } else {
+                    hh[u] = (uint16_t)(iw[c] >> (16 * u));
+                    ll[u] = (uint16_t)(il[c] >> (16 * u));
+                    float m = 0.0f;
+                    if (cs.k != 0) resplit_pair(hh[u], ll[u], cs, m);
+                    else m = fabsf(fmaf(h_val(hh[u]), 2048.0f, h_val(ll[u])));
+                    if (y < o.ny && x < o.nx) mx = fmaxf(mx, m);
+                }
+            }
+            hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
+            lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
+        }
+    }
+    *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+    *reinterpret_cast<uint4 *>(o.out_lo + off0) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+    *reinterpret_cast<uint4 *>(o.out_lo + off1) = make_uint4(lw[4], lw[5], lw[6], lw[7]);
 }
 
 __device__ __forceinline__ bool tile_inside(const TileOut &o, int Y0, int X0) {

@@ -123,10 +123,14 @@ cudaError_t launch_cc_f32(const GridGeom &g, int stencil, const TapCoeffs &c, co
 
 // Reads and clears the tensor kernels' device error word.
 cudaError_t tc_take_error(int *code);
+struct SplitScale;
+// Split launches take the grid's per-step scale (SplitScale below; null: the
+// fixed scale of the planes as packed) and t0, the steps of the current run
+// done before the launch.
 // Two steps of the split form in one launch (temporal blocking), in -> out.
 cudaError_t launch_tc_split2(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
                              const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
-                             cudaStream_t s);
+                             cudaStream_t s, SplitScale *scale = nullptr, int t0 = 0);
 cudaError_t tb_take_error(int *code);
 // Configures the tensor kernel of (stencil, split) ahead of its first launch.
 cudaError_t tc_prepare(int stencil, bool split);
@@ -143,10 +147,11 @@ cudaError_t launch_tc_f16_steps(const GridGeom &g, int stencil, const float *B, 
                                 int tile_w = kTile);
 cudaError_t launch_tc_split_steps(const GridGeom &g, int stencil, const float *B,
                                   const uint16_t *in_hi, const uint16_t *in_lo, uint16_t *out_hi,
-                                  uint16_t *out_lo, int steps, unsigned *rows_done, cudaStream_t s);
+                                  uint16_t *out_lo, int steps, unsigned *rows_done, cudaStream_t s,
+                                  SplitScale *scale = nullptr, int t0 = 0);
 cudaError_t launch_tc_split(const GridGeom &g, int stencil, const float *B, const uint16_t *in_hi,
                             const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
-                            cudaStream_t s);
+                            cudaStream_t s, SplitScale *scale = nullptr, int t0 = 0);
 
 // --- layout kernels -------------------------------------------------------
 // pack/unpack between an FP32 row-major grid and an engine plane of the
@@ -172,6 +177,37 @@ cudaError_t launch_pack_split_dev(const float *in, int ny, int nx, const unsigne
 cudaError_t launch_unpack_split_dev(const uint16_t *hi, const uint16_t *lo, int ny, int nx,
                                     const int *exp_in, float *out, cudaStream_t s);
 cudaError_t launch_max_abs(const float *in, size_t n, unsigned *out_bits, cudaStream_t s);
+
+// ------------------------------------------------ split scale, per step ---
+// A split grid holds x' = x 2^-E as hi + lo 2^-11 with a fixed-point hi, so
+// its precision is about 2^-23 of 2^E.  E follows the grid's magnitude step
+// by step, so a field that decays keeps FP32-level relative precision:
+//   E_t = E_{t-2} + e(M_{t-2}),   k_t = E_{t-1} - E_t,
+// where M_t is the largest |x'| stored by step t (in step t's units, over
+// the grid's cells) and e(M) its frexp exponent (M 2^-e in [0.5, 1); 0 for
+// M = 0).  Step t multiplies its values by 2^k_t before the split (cells it
+// only copies are re-split by the same factor when k_t != 0).  Step t reads
+// only steps t-2 and t-3, which every form of the sweep (one launch per step,
+// several steps per launch, blocked pairs, batches) has completed by then,
+// so every form gives the same bits.  Slots are the step index within a run
+// (1..T) mod 8; slots 7 and 0 hold steps -1 and 0 (the run's starting
+// history), which launch_split_scale_end_run moves into place after each
+// run.  Step t writes M_t and E_t into slot t and clears the maximum of slot
+// t+3 (whose readers, steps t-3 and t-2, have finished, and whose next
+// writer, step t+3, starts after step t has).
+constexpr int kScaleRing = 8;
+struct SplitScale {
+    unsigned maxbits[kScaleRing];  // M_t as FP32 bits (atomicMax of non-negative floats)
+    int exp[kScaleRing];           // E_t
+};
+// From the max-|x| bits launch_max_abs left for a grid's input: E_0 = the
+// pack's exponent and M_0, as steps -1 and 0; the other maxima 0.
+cudaError_t launch_split_scale_init(SplitScale *sc, const unsigned *max_bits, cudaStream_t s);
+// After a run of `steps` steps: steps T-1 and T become slots 7 and 0, the
+// maxima of slots 1..6 are cleared.
+cudaError_t launch_split_scale_end_run(SplitScale *sc, int steps, cudaStream_t s);
+// The exponent of a split grid's state between runs (slot 0).
+inline const int *split_scale_exp_ptr(const SplitScale *sc) { return &sc->exp[0]; }
 // the reference's layout16 transforms (bricks of 16 x 16, row-major inside)
 cudaError_t launch_padding_2d(const uint16_t *in, uint16_t *out, int size, int halo,
                               uint16_t value, cudaStream_t s);

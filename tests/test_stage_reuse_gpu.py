@@ -147,8 +147,8 @@ def test_split_whole_grid_at_seven_tiles_per_cta(tcs, torch_cuda, stencil):
     assert tcs.device_error() == 0
     e = oracle.split_scale_exp(A)
     hi, lo = oracle.split(A.astype(np.float64), e)
-    h, l = oracle.sweep_split(hi, lo, B, stencil, steps)
-    contract = oracle.join(h, l, e)
+    h, l, e2 = oracle.sweep_split(hi, lo, B, stencil, steps, scale_exp=e)
+    contract = oracle.join(h, l, e2)
     # FP32 (not double) combination of the two accumulators: a few 2^-24 per step
     assert np.max(np.abs(got - contract)) <= steps * 2.0 ** (e - 22)
     f64 = oracle.sweep_f64(A.astype(np.float64), B.astype(np.float64), stencil, steps)

@@ -103,8 +103,8 @@ def test_tensor_split_contract_and_fp64_error(tcs, torch_cuda, stencil, shape):
     got = run_plan(tcs, A, B, stencil, steps, "tensor", "split").astype(np.float64)
     e = oracle.split_scale_exp(A)
     hi, lo = oracle.split(A.astype(np.float64), e)
-    h, l = oracle.sweep_split(hi, lo, B, stencil, steps)
-    contract = oracle.join(h, l, e)
+    h, l, e2 = oracle.sweep_split(hi, lo, B, stencil, steps, scale_exp=e)
+    contract = oracle.join(h, l, e2)
     # FP32 (not double) combination of the two accumulators: a few 2^-24 per step
     assert np.max(np.abs(got - contract)) <= steps * 2.0 ** (e - 22)
     ref64 = oracle.sweep_f64(A.astype(np.float64), B.astype(np.float64), stencil, steps)
