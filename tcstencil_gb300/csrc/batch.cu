@@ -54,6 +54,8 @@ constexpr int kRing = 8;  // published work items in flight
 // The work layout (step offsets, tile prefix) is copied into shared memory
 // when it fits, so decoding an item costs no global round trip.
 constexpr int kTableInts = 2048;
+// barriers, the item ring and the per-slot scale words, before the tables
+constexpr int kBarrierArea = 832;
 template <bool SPLIT>
 struct BatchCfg {
     // FP16: four stages, a multiple of the two issuers, so stage i % 4 holds
@@ -73,7 +75,7 @@ struct BatchCfg {
     static constexpr int EPI_WARP0 = 1 + ISSUERS;
     static constexpr int SIGNAL_WARP = EPI_WARP0 + EPI_WARPS;
     static constexpr int THREADS = 32 * (SIGNAL_WARP + 1);
-    static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 576 + kTableInts * 4;
+    static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + kBarrierArea + kTableInts * 4;
     static_assert(kRing > STAGES + 2, "a ring slot is reused only after its item's epilogue");
     static_assert(SMEM <= 232448, "shared memory budget");
     static_assert(STAGE_BYTES % 16 == 0, "bulk copy alignment");
@@ -164,15 +166,17 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
     BatchItem *ring = reinterpret_cast<BatchItem *>(ring_free + kRing);  // [kRing]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(ring + kRing);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-    // split: per ring slot, the item's largest |x'| (FP32 bits) and exponent,
-    // which the signal warp adds to the grid's scale record
-    unsigned *item_max = reinterpret_cast<unsigned *>(tmem_slot + 2);  // [kRing]
-    int *item_exp = reinterpret_cast<int *>(item_max + kRing);          // [kRing]
+    // split: per ring slot, the item's scale (producer -> epilogue, behind
+    // item_scaled) and its largest |x'| (FP32 bits), which the signal warp
+    // adds to the grid's scale record
+    uint64_t *item_scaled = reinterpret_cast<uint64_t *>(tmem_slot + 2);  // [kRing]
+    ItemScale *ring_scale = reinterpret_cast<ItemScale *>(item_scaled + kRing);  // [kRing]
+    unsigned *item_max = reinterpret_cast<unsigned *>(ring_scale + kRing);       // [kRing]
     volatile int *grid_error = p.error;
     static_assert((2 * NS + 2 * NACC + 1 + 3 * kRing) * 8 + kRing * sizeof(BatchItem) + 8 +
-                          8 * kRing <= 576,
+                          kRing * (8 + sizeof(ItemScale) + 4) <= kBarrierArea,
                   "barrier area");
-    int *tables = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(bars) + 576);
+    int *tables = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(bars) + kBarrierArea);
     const int n_table = p.n_steps + 1 + p.n_grids + 1;
     const bool tables_in_smem = n_table <= kTableInts;
 
@@ -195,8 +199,8 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             mbar_init(&item_ready[j], 1);
             mbar_init(&item_done[j], C::EPI_WARPS);
             mbar_init(&ring_free[j], 1);
+            mbar_init(&item_scaled[j], 1);
             item_max[j] = 0u;
-            item_exp[j] = 0;
         }
         *abort_flag = 0;
         fence_mbar_init();
@@ -232,6 +236,9 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             // (grid, step) whose dependency this thread has already seen met;
             // later items of the same pair need no further poll or fence
             int met_g = -1, met_t = -1;
+            // (grid, step) of the scale in iscale (split items)
+            int sc_g = -1, sc_t = -1;
+            ItemScale iscale{};
             const int grab = p.grab;
             int k = (int)atomicAdd(p.work_counter, (unsigned)grab);  // the item of this iteration
             int k_end = k + grab;                                   // end of its group
@@ -296,6 +303,12 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     met_g = it.g;
                     met_t = it.t;
                 }
+                // split: the step's scale, once per (grid, step).  Steps t-2
+                // and t-3 of the grid are final (step t-1 is, after the wait
+                // above); the loads are issued here and used after the copies.
+                ScaleWords sw{};
+                const bool fresh = SPLIT && g.scale && (it.g != sc_g || it.t != sc_t);
+                if (fresh) sw = scale_words(g.scale, it.t + 1);
                 const int band_bytes = batch_band_elems(g.r, SPLIT) * 2;
                 uint8_t *st = stage_base + (size_t)s * C::STAGE_BYTES;
                 mbar_arrive_expect_tx(&full[s], C::PLANES * SG::PLANE + band_bytes);
@@ -303,6 +316,19 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 const CUtensorMap *maps = g.maps + 2 * in;
                 load_tile_map(maps, maps + 1, C::PLANES, it.ty * kTile, it.tx * kTile, st, &full[s]);
                 bulk_load(st + C::PLANES * SG::PLANE, p.bands + g.band_base, band_bytes, &full[s]);
+                if (SPLIT) {
+                    if (fresh) {
+                        const StepScale ss = scale_of(sw, it.t + 1);
+                        iscale = ItemScale{ss.s, ss.k, ss.e, g.scale};
+                        sc_g = it.g;
+                        sc_t = it.t;
+                    } else if (!g.scale) {
+                        iscale = ItemScale{2048.0f, 0, 0, nullptr};
+                        sc_g = sc_t = -1;
+                    }
+                    ring_scale[j] = iscale;
+                    mbar_arrive(&item_scaled[j]);
+                }
                 last_issued = i;
                 // the next item: decoded, its descriptor loads in flight
                 const int g_prev = it.g;
@@ -437,6 +463,18 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
         if (lane == 0) {
             unsigned *pend = nullptr;
             unsigned n_pend = 0;
+            // split: the largest |x'| of the held items, for their (grid,
+            // step)'s scale record, added once before their counts go out
+            SplitScale *pend_sc = nullptr;
+            int pend_t = 0;
+            unsigned pend_max = 0u;
+            auto release = [&]() {
+                if (SPLIT && pend_sc)
+                    atomicMax(&pend_sc->maxbits[pend_t & (kScaleRing - 1)], pend_max);
+                red_release_add(pend, n_pend);
+                n_pend = 0;
+                pend_max = 0u;
+            };
             auto give_up = [&]() {
                 batch_fail(p, kErrWaitResult);
                 *abort_flag = 1;
@@ -451,32 +489,32 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 unsigned *ctr = nullptr;
                 if (it.g >= 0)
                     ctr = p.counters + (size_t)(p.grids[it.g].ctr_base + it.t) * kRowCounterStride;
-                if (n_pend && ctr != pend) {
-                    red_release_add(pend, n_pend);
-                    n_pend = 0;
-                }
+                if (n_pend && ctr != pend) release();
                 if (it.g < 0) break;
                 if (!mbar_wait(&item_done[j], (i / kRing) & 1, abort_flag, wait_lim)) {
                     give_up();
                     break;
                 }
                 if (SPLIT) {
-                    // the item's maximum and the step's exponent into the
-                    // grid's scale record, before its count is released
-                    SplitScale *sc = p.grids[it.g].scale;
-                    if (sc) {
-                        const int t = it.t + 1;  // the step within the run, from 1
-                        atomicMax(&sc->maxbits[t & (kScaleRing - 1)], item_max[j]);
-                        sc->exp[t & (kScaleRing - 1)] = item_exp[j];
+                    // the item's maximum joins the held one; the step's
+                    // exponent, and the clearing of slot t+3, come from the
+                    // step's tile 0 alone
+                    SplitScale *sc = ring_scale[j].sc;
+                    const int t = it.t + 1;  // the step within the run, from 1
+                    if (sc && it.tile == 0) {
+                        sc->exp[t & (kScaleRing - 1)] = ring_scale[j].e;
                         sc->maxbits[(t + 3) & (kScaleRing - 1)] = 0u;
                     }
+                    pend_sc = sc;
+                    pend_t = t;
+                    pend_max = max(pend_max, item_max[j]);
                     item_max[j] = 0u;
                 }
                 mbar_arrive(&ring_free[j]);
                 pend = ctr;
                 n_pend += C::EPI_WARPS;
             }
-            if (n_pend) red_release_add(pend, n_pend);
+            if (n_pend) release();
         }
     } else {
         // ------------------------------------------------------ epilogue ---
@@ -524,32 +562,17 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 const int y = Y0 + m;
                 const bool fast = tile_inside(o, Y0, X0);
                 const bool row_in = y >= o.y0 && y < o.y1;
-                // the step's scale: steps t-2 and t-3 of the grid have
-                // finished (the producer waited for all of step t-1 before
-                // this item's stage filled); one acquire of that count orders
-                // this warp's reads of the scale record after them
-                StepScale ss = step_scale(nullptr, 0);
-                if (g.scale) {
-                    if (it.t > 0) {
-                        const unsigned *ctr =
-                            p.counters + (size_t)(g.ctr_base + it.t - 1) * kRowCounterStride;
-                        const unsigned target = (unsigned)(g.n_tiles * C::EPI_WARPS);
-                        const uint64_t t0 = global_timer_ns();
-                        bool okc = true;
-                        while (ld_acquire(ctr) < target) {
-                            if (*abort_flag || global_timer_ns() - t0 > wait_lim) {
-                                okc = false;
-                                break;
-                            }
-                            __nanosleep(64);
-                        }
-                        if (!__all_sync(0xffffffffu, okc)) {
-                            fail_result();
-                            break;
-                        }
-                    }
-                    ss = step_scale(g.scale, it.t + 1);
+                // the step's scale, from the producer once the item's step
+                // could read the grid's scale record
+                bool oks = mbar_wait(&item_scaled[j], (i / kRing) & 1, abort_flag, wait_lim);
+                if (!__all_sync(0xffffffffu, oks)) {
+                    fail_result();
+                    break;
                 }
+                StepScale ss;
+                ss.s = ring_scale[j].s;
+                ss.k = ring_scale[j].k;
+                ss.e = ring_scale[j].e;
                 float mx = 0.0f;
                 auto ready = [&](int w) {
                     const int Gw = G0 + w;
@@ -596,10 +619,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
 #pragma unroll
                     for (int sh = 16; sh > 0; sh >>= 1)
                         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, sh));
-                    if (lane == 0) {
-                        atomicMax(&item_max[j], __float_as_uint(mx * (1.0f / 2048.0f)));
-                        item_exp[j] = ss.e;
-                    }
+                    if (lane == 0) atomicMax(&item_max[j], __float_as_uint(mx * (1.0f / 2048.0f)));
                 }
             } else {
                 uint32_t col;

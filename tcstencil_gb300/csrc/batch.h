@@ -47,6 +47,15 @@ struct BatchItem {
     int ty, tx;      // the tile's row and column (set by the producer when it publishes)
 };
 
+// Split items: the step's scale (StepScale of tc_core.cuh, as s, k, e) and
+// the grid's scale record, set by the producer once the step's inputs are
+// final (after the item is published, so a separate barrier per slot).
+struct ItemScale {
+    float s;
+    int k, e;
+    SplitScale *sc;
+};
+
 // One run's work: items are ordered step major and, within a step, by grid
 // then tile.  Grids are sorted by step count (descending), so the grids still
 // running at step t are a prefix of the array: step t holds the first

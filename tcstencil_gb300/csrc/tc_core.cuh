@@ -148,26 +148,48 @@ struct StepScale {
     int k, e;
 };
 
-__device__ __forceinline__ int ld_exp(const SplitScale *sc, int t) {
-    return (int)ld_relaxed(reinterpret_cast<const unsigned *>(&sc->exp[t & (kScaleRing - 1)]));
-}
-__device__ __forceinline__ int exp_at(const SplitScale *sc, int t) {  // E_t, from step t-2
-    return ld_exp(sc, t - 2) + split_exp_of(ld_relaxed(&sc->maxbits[(t - 2) & (kScaleRing - 1)]));
+// The words of step t's scale: E and M of steps t-2 and t-3, and E_0, in
+// one burst of relaxed GPU-scope loads (their latencies overlap, and a
+// caller can issue other work before it uses them).
+struct ScaleWords {
+    unsigned ea, ma, eb, mb, e0;
+};
+__device__ __forceinline__ ScaleWords scale_words(const SplitScale *sc, int t) {
+    const int a = (t - 2) & (kScaleRing - 1), b = (t - 3) & (kScaleRing - 1);
+    ScaleWords w;
+    asm volatile(
+        "ld.relaxed.gpu.global.u32 %0, [%5];\n\t"
+        "ld.relaxed.gpu.global.u32 %1, [%6];\n\t"
+        "ld.relaxed.gpu.global.u32 %2, [%7];\n\t"
+        "ld.relaxed.gpu.global.u32 %3, [%8];\n\t"
+        "ld.relaxed.gpu.global.u32 %4, [%9];"
+        : "=r"(w.ea), "=r"(w.ma), "=r"(w.eb), "=r"(w.mb), "=r"(w.e0)
+        : "l"(&sc->exp[a]), "l"(&sc->maxbits[a]), "l"(&sc->exp[b]), "l"(&sc->maxbits[b]),
+          "l"(&sc->exp[0])
+        : "memory");
+    return w;
 }
 
-__device__ __forceinline__ StepScale step_scale(const SplitScale *sc, int t) {
+__device__ __forceinline__ StepScale scale_of(const ScaleWords &w, int t) {
     StepScale r;
-    r.s = 2048.0f;
-    r.k = 0;
-    r.e = 0;
-    if (!sc) return r;
-    r.e = exp_at(sc, t);
-    const int e1 = t == 1 ? ld_exp(sc, 0) : exp_at(sc, t - 1);
+    r.e = (int)w.ea + split_exp_of(w.ma);                              // E_t
+    const int e1 = t == 1 ? (int)w.e0 : (int)w.eb + split_exp_of(w.mb);  // E_{t-1}
     int k = e1 - r.e;
     k = k < -64 ? -64 : k > 64 ? 64 : k;
     r.k = k;
     r.s = __int_as_float((127 + 11 + k) << 23);
     return r;
+}
+
+__device__ __forceinline__ StepScale step_scale(const SplitScale *sc, int t) {
+    if (!sc) {
+        StepScale r;
+        r.s = 2048.0f;
+        r.k = 0;
+        r.e = 0;
+        return r;
+    }
+    return scale_of(scale_words(sc, t), t);
 }
 
 // After a warp's last cells of step t: its largest |u| (units of 2^-11) into
@@ -235,13 +257,21 @@ __device__ __forceinline__ uint32_t pack_h2(float v0, float v1) {
 __device__ __forceinline__ void split_pair_s(float v0, float v1, float s, uint32_t &hw,
                                              uint32_t &lw, float &mx) {
     constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
-    const float u0 = v0 * s, u1 = v1 * s;
+    // packed FP32 operations on the pair: each lane rounds as the scalar
+    // operation would, so the bits are split_pair's
+    const float2 u = __fmul2_rn(make_float2(v0, v1), make_float2(s, s));
+    const float u0 = u.x, u1 = u.y;
     mx = fmaxf(mx, fmaxf(fabsf(u0), fabsf(u1)));
-    const float t0 = copysignf(__fsub_rn(__fadd_rn(u0, kRound), kRound), u0);
-    const float t1 = copysignf(__fsub_rn(__fadd_rn(u1, kRound), kRound), u1);
+    const float2 r = __fadd2_rn(__fadd2_rn(u, make_float2(kRound, kRound)),
+                                make_float2(-kRound, -kRound));
+    const float t0 = copysignf(r.x, u0);
+    const float t1 = copysignf(r.y, u1);
     if (fabsf(t0) <= 2048.0f && fabsf(t1) <= 2048.0f) {
-        hw = pack_h2(t0 * (1.0f / 2048.0f), t1 * (1.0f / 2048.0f));
-        lw = pack_h2(__fsub_rn(u0, t0), __fsub_rn(u1, t1));
+        const float2 t = make_float2(t0, t1);
+        const float2 h = __fmul2_rn(t, make_float2(1.0f / 2048.0f, 1.0f / 2048.0f));
+        const float2 l = __ffma2_rn(t, make_float2(-1.0f, -1.0f), u);  // u - t, exact
+        hw = pack_h2(h.x, h.y);
+        lw = pack_h2(l.x, l.y);
     } else {
         uint16_t h0, l0, h1, l1;
         split_fixed_s(v0, s, h0, l0, mx);
@@ -345,13 +375,18 @@ __device__ __forceinline__ void split_block_load(uint32_t region_a, uint32_t reg
         tmem_ld_x16(region_b + 32 * part, v[2 * part + 1]);
     }
     tmem_ld_wait();
+    // main (exact sum of ch.hi), correction in units of 2^-11; two columns
+    // per packed FP32 operation (each lane rounds as the scalar one would)
+    auto pr = [&](int part, int c) {
+        return make_float2(__uint_as_float(v[part][c]), __uint_as_float(v[part][c + 1]));
+    };
 #pragma unroll
-    for (int c = 0; c < 16; c++) {
-        // main (exact sum of ch.hi), correction in units of 2^-11
-        const float main = __uint_as_float(v[0][c]) + __uint_as_float(v[1][c]);
-        const float corr = (__uint_as_float(v[2][c]) + __uint_as_float(v[3][c])) +
-                           (__uint_as_float(v[4][c]) + __uint_as_float(v[5][c]));
-        f[c] = fmaf(corr, 1.0f / 2048.0f, main);
+    for (int c = 0; c < 16; c += 2) {
+        const float2 main = __fadd2_rn(pr(0, c), pr(1, c));
+        const float2 corr = __fadd2_rn(__fadd2_rn(pr(2, c), pr(3, c)), __fadd2_rn(pr(4, c), pr(5, c)));
+        const float2 r = __ffma2_rn(corr, make_float2(1.0f / 2048.0f, 1.0f / 2048.0f), main);
+        f[c] = r.x;
+        f[c + 1] = r.y;
     }
 }
 
@@ -616,10 +651,12 @@ __device__ __forceinline__ void store_block_split(const TileOut &o, const float 
                 } else {
                     hh[u] = (uint16_t)(iw[c] >> (16 * u));
                     ll[u] = (uint16_t)(il[c] >> (16 * u));
-                    float m = 0.0f;
-                    if (cs.k != 0) resplit_pair(hh[u], ll[u], cs, m);
-                    else m = fabsf(fmaf(h_val(hh[u]), 2048.0f, h_val(ll[u])));
-                    if (y < o.ny && x < o.nx) mx = fmaxf(mx, m);
+                    // grid cells outside the rectangle (a fixed border)
+                    // keep their value; padding cells are only copied
+                    if (y < o.ny && x < o.nx) {
+                        if (cs.k != 0) resplit_pair(hh[u], ll[u], cs, mx);
+                        else mx = fmaxf(mx, fabsf(fmaf(h_val(hh[u]), 2048.0f, h_val(ll[u]))));
+                    }
                 }
             }
             hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
