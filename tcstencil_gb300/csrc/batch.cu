@@ -239,6 +239,26 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
             // (grid, step) of the scale in iscale (split items)
             int sc_g = -1, sc_t = -1;
             ItemScale iscale{};
+            // split: the last issued item's scale is published at the top of
+            // the next iteration, before its dependency poll (which may wait
+            // for that item): its loads land meanwhile, and the thread never
+            // stalls on them before the next stage and ring waits
+            int pub_j = -1, pub_t = 0;
+            bool pub_fresh = false;
+            ScaleWords pub_sw{};
+            SplitScale *pub_sc = nullptr;
+            auto publish = [&]() {
+                if (!SPLIT || pub_j < 0) return;
+                if (pub_fresh) {
+                    const StepScale ss = scale_of(pub_sw, pub_t + 1);
+                    iscale = ItemScale{ss.s, ss.k, ss.e, pub_sc};
+                } else if (!pub_sc) {
+                    iscale = ItemScale{2048.0f, 0, 0, nullptr};
+                }
+                ring_scale[pub_j] = iscale;
+                mbar_arrive(&item_scaled[pub_j]);
+                pub_j = -1;
+            };
             const int grab = p.grab;
             int k = (int)atomicAdd(p.work_counter, (unsigned)grab);  // the item of this iteration
             int k_end = k + grab;                                   // end of its group
@@ -258,6 +278,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                     *abort_flag = 1;
                     break;
                 }
+                publish();
                 if (k >= p.n_items) {
                     ring[j] = BatchItem{-1, 0, 0};
                     mbar_arrive(&item_ready[j]);
@@ -305,7 +326,7 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 }
                 // split: the step's scale, once per (grid, step).  Steps t-2
                 // and t-3 of the grid are final (step t-1 is, after the wait
-                // above); the loads are issued here and used after the copies.
+                // above); the loads are issued here and used in publish().
                 ScaleWords sw{};
                 const bool fresh = SPLIT && g.scale && (it.g != sc_g || it.t != sc_t);
                 if (fresh) sw = scale_words(g.scale, it.t + 1);
@@ -317,17 +338,17 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                 load_tile_map(maps, maps + 1, C::PLANES, it.ty * kTile, it.tx * kTile, st, &full[s]);
                 bulk_load(st + C::PLANES * SG::PLANE, p.bands + g.band_base, band_bytes, &full[s]);
                 if (SPLIT) {
+                    pub_j = j;
+                    pub_t = it.t;
+                    pub_fresh = fresh;
+                    pub_sw = sw;
+                    pub_sc = g.scale;
                     if (fresh) {
-                        const StepScale ss = scale_of(sw, it.t + 1);
-                        iscale = ItemScale{ss.s, ss.k, ss.e, g.scale};
                         sc_g = it.g;
                         sc_t = it.t;
                     } else if (!g.scale) {
-                        iscale = ItemScale{2048.0f, 0, 0, nullptr};
                         sc_g = sc_t = -1;
                     }
-                    ring_scale[j] = iscale;
-                    mbar_arrive(&item_scaled[j]);
                 }
                 last_issued = i;
                 // the next item: decoded, its descriptor loads in flight

@@ -105,9 +105,14 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
     uint64_t *win_full = bars + 5;                 // [kTbRing]
     uint64_t *win_empty = bars + 5 + kTbRing;      // [kTbRing]
     uint64_t *drain = bars + 5 + 2 * kTbRing;      // [1]
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+    CtaScale cs;                                   // the CTA's side of the scale
+    cs.bar = drain + 1;                            // [2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cs.bar + 2);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-    static_assert((6 + 2 * kTbRing) * 8 + 8 <= 256, "barrier area");
+    cs.max = tmem_slot + 2;                        // [2]
+    cs.cnt = cs.max + 2;                           // [2]
+    cs.ss = reinterpret_cast<StepScale *>(cs.cnt + 2);  // [2]
+    static_assert((8 + 2 * kTbRing) * 8 + 8 + 16 + 2 * sizeof(StepScale) <= 256, "barrier area");
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -125,6 +130,7 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
             mbar_init(&win_empty[r], kTbEpiWarps);
         }
         mbar_init(drain, kTbIssuers);
+        cta_scale_init(cs);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -312,10 +318,21 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
             G0 += nwin;
         };
         // The pair's two scales, both from steps finished before the launch
-        // (step t reads steps t-2 and t-3); the second step's copies come
-        // from the input, two steps back, so they take both shifts.
-        const StepScale ss1 = step_scale(p.scale, p.t0 + 1);
-        const StepScale ss2 = step_scale(p.scale, p.t0 + 2);
+        // (step t reads steps t-2 and t-3), read by the first epilogue warp;
+        // the second step's copies come from the input, two steps back, so
+        // they take both shifts.
+        if (warp == 1 + kTbIssuers && lane == 0) {
+            cta_scale_publish(cs, 0, step_scale(p.scale, p.t0 + 1));
+            cta_scale_publish(cs, 1, step_scale(p.scale, p.t0 + 2));
+        }
+        StepScale ss1, ss2;
+        if (!cta_scale_take(cs, 0, ss1, abort_flag) || !cta_scale_take(cs, 1, ss2, abort_flag)) {
+            if (lane == 0) {
+                record_error(&g_tb_error, kErrWaitResult);
+                *abort_flag = 1;
+            }
+            stop = true;
+        }
         StepScale cs2 = ss2;
         cs2.k = ss1.k + ss2.k;
         cs2.s = __int_as_float((127 + 11 + cs2.k) << 23);
@@ -400,9 +417,9 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
                 });
             }
         }
-        if (!stop && p.scale) {
-            flush_step_max(p.scale, p.t0 + 1, ss1, mx1);
-            flush_step_max(p.scale, p.t0 + 2, ss2, mx2);
+        if (!stop && p.scale) {  // tile 0 is CTA 0's
+            cta_scale_flush<kTbEpiWarps>(cs, 0, p.scale, p.t0 + 1, ss1, mx1, blockIdx.x == 0);
+            cta_scale_flush<kTbEpiWarps>(cs, 1, p.scale, p.t0 + 2, ss2, mx2, blockIdx.x == 0);
         }
     }
 

@@ -230,20 +230,31 @@ struct TcParams {
     float coef[25];                 // n x n, row-major
 };
 
-// Several split steps per launch: before the first tile of launch step j >= 2
-// an epilogue warp waits (bounded, acquire) until every tile row has finished
-// launch step j - 2, whose maxima and exponents its scale reads (tiles only
+// Several split steps per launch: before publishing the scale of launch step
+// j >= 2 the CTA waits (bounded, acquire) until every tile row has finished
+// launch step j - 2, whose maxima and exponents the scale reads (tiles only
 // wait for their neighbouring rows of step j - 1).  No cycle: every tile of
 // step j - 2 is an earlier item of its CTA and depends only on earlier
-// items.  Returns false on give-up.
+// items.  The nl lanes of `mask` (this one is l of them) poll the rows, each
+// issuing all its loads before testing any, so that a satisfied wait costs
+// one round trip.  Returns false on give-up.
 __device__ __forceinline__ bool wait_all_rows(const unsigned *rows_done, int tiles_y,
-                                              unsigned target, const volatile int *abort_flag) {
+                                              unsigned target, const volatile int *abort_flag,
+                                              unsigned mask, int l, int nl) {
     const uint64_t t0 = global_timer_ns();
     for (;;) {
         bool done = true;
-        for (int r = (int)(threadIdx.x & 31); r < tiles_y; r += 32)
-            done = done && ld_relaxed(rows_done + r * kRowCounterStride) >= target;
-        if (__all_sync(0xffffffffu, done)) break;
+        for (int r0 = l; r0 < tiles_y; r0 += 4 * nl) {
+            unsigned v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int r = r0 + u * nl;
+                v[u] = r < tiles_y ? ld_relaxed(rows_done + r * kRowCounterStride) : target;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) done = done && v[u] >= target;
+        }
+        if (__all_sync(mask, done)) break;
         if (*abort_flag || *(volatile int *)&g_tc_error != 0 ||
             global_timer_ns() - t0 > kWaitLimitNs)
             return false;
@@ -507,11 +518,14 @@ __global__ void __launch_bounds__(Sweep<S>::THREADS, 1) tc_sweep_kernel(const __
 // others wait (measured per step at 8196²: box2d1r 124 -> 110 -> 109.5 us,
 // box2d2r 157 -> 117 -> 114 us for one, two, three issuers).  A region is
 // reused five windows later, by another issuer, after all twelve epilogue
-// warps have released it; an issuer's previous region wait (three windows
-// back) already covered the release before that, because every warp releases
-// windows in order, so no parity wait can alias.  Every issuer waits for
-// every stage fill in order, and a stage is free when all issuers' commits
-// for the tile have completed.
+// warps have released it; an issuer's previous region wait (two or three
+// windows back) already covered the release before that, because every warp
+// releases windows in order, so no parity wait can alias.  Every issuer
+// waits for every stage fill in order, and a stage is free when all issuers'
+// commits for the tile have completed.  The multi-step kernel (MULTI) has
+// two issuers: with a third its 17 warps leave 96 registers a thread, and
+// the epilogue spills (4098² box2d1r in one launch: 35.4 us per step with
+// three issuers, 29.4 with two).
 constexpr int kRingSlots = 5;
 constexpr int kRegionCols = 96;
 constexpr int kRingGroups = 3;                     // epilogue block groups
@@ -519,22 +533,58 @@ constexpr int kRingEpiWarps = 4 * kRingGroups;     // a lane quarter each
 #ifndef TCS_SPLIT_ISSUERS
 #define TCS_SPLIT_ISSUERS 3
 #endif
-constexpr int kRingIssuers = TCS_SPLIT_ISSUERS;   // MMA issuer warps 1 .. kRingIssuers
-constexpr int kRingSignalWarp = 1 + kRingIssuers + kRingEpiWarps;  // several steps: row counts
 // MULTI: the kernel runs several steps (p.steps) with the row counts and a
 // signal warp; without it, one step in the single-step kernel's exact form
 // (a kernel carrying the multi-step code ran single steps 8-11 % slower:
 // 8196² box2d1r 106.7 -> 114.9 us).
 template <bool MULTI>
-constexpr int ring_threads() { return 32 * (kRingSignalWarp + (MULTI ? 1 : 0)); }
+struct Ring {
+    static constexpr int ISSUERS = MULTI ? 2 : TCS_SPLIT_ISSUERS;  // MMA issuer warps 1 .. ISSUERS
+    static constexpr int EPI0 = 1 + ISSUERS;                        // first epilogue warp
+    static constexpr int SIGNAL_WARP = EPI0 + kRingEpiWarps;        // several steps: row counts
+    static constexpr int THREADS = 32 * (SIGNAL_WARP + (MULTI ? 1 : 0));
+};
 // Every tile computes all its windows: a runtime window count for the last
 // tile of a row slowed this epilogue-bound kernel by more than the skipped
 // MMAs saved (16386²: 380 -> 387 us per step).
 constexpr int kTileWindows = kTile / 16 + 1;
 static_assert(kRingSlots * kRegionCols <= kTmemCols, "window ring fits TMEM");
 
+// The multi-step kernel's scales: lanes 1..31 of the signal warp walk the
+// CTA's items and, at each step j it holds tiles in (the CTA's n-th), wait
+// for step j - 2 everywhere (j >= 2), read step j's scale and publish it as
+// the n-th.  Publishing the (n+2)-th waits for a step at or after the n-th's
+// to finish in every row, this CTA's tiles of it too, so every epilogue warp
+// has taken the n-th by then and its slot and phase are free.
+template <int NW>
+__device__ void publish_scales(const TcParams &p, const CtaScale &cs, int n_items, int tiles_x,
+                               int tiles_y, const volatile int *abort_flag) {
+    constexpr unsigned kMask = 0xfffffffeu;
+    const int l = (int)(threadIdx.x & 31) - 1;
+    const int n_tiles = tiles_x * tiles_y;
+    const unsigned per_row = (unsigned)(NW * tiles_x);
+    int n = 0;
+    for (int k = blockIdx.x, prev = -1; k < n_items; k += gridDim.x) {
+        const int step = k / n_tiles;
+        if (step == prev) continue;
+        prev = step;
+        if (step >= 2 && !wait_all_rows(p.rows_done, tiles_y, (unsigned)(step - 1) * per_row,
+                                        abort_flag, kMask, l, 31)) {
+            if (l == 0) {
+                record_error(&g_tc_error, kErrWaitDep);
+                *(volatile int *)abort_flag = 1;
+            }
+            return;
+        }
+        if (l == 0) cta_scale_publish(cs, n, step_scale(p.scale, p.t0 + step + 1));
+        __syncwarp(kMask);
+        n++;
+    }
+}
+
 template <int S, bool MULTI>
-__global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel(const __grid_constant__ TcParams p) {
+__global__ void __launch_bounds__(Ring<MULTI>::THREADS, 1) tc_split_ring_kernel(const __grid_constant__ TcParams p) {
+    using R = Ring<MULTI>;
     using C = Cfg<S, true>;
     using M = Mode<true>;
     constexpr int NS = C::STAGES;
@@ -552,10 +602,16 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
     uint64_t *win_full = bars + 2 * NS;                       // [kRingSlots]
     uint64_t *win_empty = bars + 2 * NS + kRingSlots;         // [kRingSlots]
     uint64_t *drain = bars + 2 * NS + 2 * kRingSlots;         // [1]
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+    CtaScale cs;                                              // the CTA's side of the scale
+    cs.bar = drain + 1;                                       // [2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cs.bar + 2);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     uint32_t *warp_done = tmem_slot + 2;  // [kRingEpiWarps] several steps: items stored
-    static_assert((2 * NS + 2 * kRingSlots + 1) * 8 + (2 + kRingEpiWarps) * 4 <= 256, "barrier area");
+    cs.max = warp_done + kRingEpiWarps;   // [2]
+    cs.cnt = cs.max + 2;                  // [2]
+    cs.ss = reinterpret_cast<StepScale *>(cs.cnt + 2);  // [2]
+    static_assert((2 * NS + 2 * kRingSlots + 3) * 8 + (2 + kRingEpiWarps + 4) * 4 +
+                          2 * sizeof(StepScale) <= 256, "barrier area");
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -564,13 +620,14 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], kRingIssuers);
+            mbar_init(&empty[s], R::ISSUERS);
         }
         for (int r = 0; r < kRingSlots; r++) {
             mbar_init(&win_full[r], 1);
             mbar_init(&win_empty[r], kRingEpiWarps);
         }
-        mbar_init(drain, kRingIssuers);
+        mbar_init(drain, R::ISSUERS);
+        cta_scale_init(cs);
         for (int w = 0; w < kRingEpiWarps; w++) warp_done[w] = 0;
         *abort_flag = 0;
         fence_mbar_init();
@@ -581,7 +638,7 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
         tmem_relinquish();
     }
     build_bands(reinterpret_cast<uint16_t *>(band_base), p.coef, C::R, C::BOX, true, threadIdx.x,
-                ring_threads<MULTI>());
+                R::THREADS);
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -639,10 +696,10 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
                 }
             }
         }
-    } else if (warp <= kRingIssuers) {
+    } else if (warp <= R::ISSUERS) {
         // --------------------------------------------------- MMA issuers ---
         if (lane == 0) {
-            const int id = warp - 1;  // takes the windows G with G % kRingIssuers == id
+            const int id = warp - 1;  // takes the windows G with G % R::ISSUERS == id
             int i = 0, G = 0;         // tiles, global windows
             bool stop = false;
             const uint32_t band = smem_u32(band_base);
@@ -657,7 +714,7 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
                     smem_u32(stage_base + (size_t)s * NP * SG::PLANE), SG::CHUNK, 128);
 #pragma unroll 1
                 for (int wg = 0; wg < kTileWindows; wg++, G++) {
-                    if (G % kRingIssuers != id) continue;
+                    if (G % R::ISSUERS != id) continue;
                     const int r = G % kRingSlots;
                     if (!mbar_wait(&win_empty[r], ((G / kRingSlots) & 1) ^ 1, abort_flag)) {
                         record_error(&g_tc_error, kErrWaitAccum);
@@ -682,14 +739,17 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
                 }
             }
         }
-    } else if (MULTI && warp == kRingSignalWarp) {
+    } else if (MULTI && warp == R::SIGNAL_WARP) {
         // -------------------------------------------------------- signal ---
+        // lane 0 the row counts, lanes 1..31 the scales of the CTA's steps
         if (lane == 0)
             signal_rows<kRingEpiWarps>(p.rows_done, n_items, n_tiles, tiles_x, warp_done, abort_flag);
+        else if (p.scale)
+            publish_scales<kRingEpiWarps>(p, cs, n_items, tiles_x, tiles_y, abort_flag);
     } else {
         // ------------------------------------------------------ epilogue ---
         const int q = warp & 3;                          // TMEM lane quarter
-        const int grp = (warp - 1 - kRingIssuers) >> 2;  // block group: blocks j with j % 3 == grp
+        const int grp = (warp - R::EPI0) >> 2;  // block group: blocks j with j % 3 == grp
         const int m = q * 32 + lane;
         const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
         TileOut o;
@@ -720,11 +780,15 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
         int i = 0;
         TileWalk w;
         w.init(blockIdx.x, gridDim.x, tiles_x, tiles_y);
-        // the scale of the current step, and this warp's largest |u| in it
-        int cur = -1;
+        // the scale of the current step, this warp's largest |u| in it, and
+        // whether the CTA holds the step's tile 0
+        int cur = -1, nst = -1;  // nst: the CTA's step ordinal
         StepScale ss = step_scale(nullptr, 0);
         float mx = 0.0f;
-        const unsigned per_row = (unsigned)(kRingEpiWarps * tiles_x);
+        bool own0 = false;
+        // one step per launch: the first epilogue warp reads the record for
+        // the CTA (several: the signal warp's lanes 1..31 do)
+        const bool scale_warp = !MULTI && warp == R::EPI0;
         for (int k = blockIdx.x; k < n_items; k += gridDim.x, G0 += kTileWindows, i++, w.advance()) {
             const int step = w.step;
             const int Y0 = w.ty * kTile;
@@ -737,19 +801,23 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
                 o.out_lo = (step & 1) ? const_cast<uint16_t *>(p.in_lo) : p.out_lo;
             }
             if (step != cur && p.scale) {
-                if (MULTI && step >= 2 &&
-                    !wait_all_rows(p.rows_done, tiles_y, (unsigned)(step - 1) * per_row,
-                                   abort_flag)) {
+                nst++;
+                if (scale_warp) {
+                    if (lane == 0) cta_scale_publish(cs, nst, step_scale(p.scale, p.t0 + step + 1));
+                    __syncwarp();
+                }
+                if (!cta_scale_take(cs, nst, ss, abort_flag)) {
                     if (lane == 0) {
                         record_error(&g_tc_error, kErrWaitDep);
                         *abort_flag = 1;
                     }
                     break;
                 }
-                ss = step_scale(p.scale, p.t0 + step + 1);
                 cur = step;
                 mx = 0.0f;
+                own0 = false;
             }
+            own0 = own0 || (w.ty == 0 && w.tx == 0);
             const int y = Y0 + m;
             const bool fast = tile_inside(o, Y0, X0);
             const bool row_in = y >= o.y0 && y < o.y1;
@@ -774,9 +842,10 @@ __global__ void __launch_bounds__(ring_threads<MULTI>(), 1) tc_split_ring_kernel
                 TileWalk nw = w;
                 nw.advance();
                 if (k + (int)gridDim.x >= n_items || nw.step != step)
-                    flush_step_max(p.scale, p.t0 + step + 1, ss, mx);
+                    cta_scale_flush<kRingEpiWarps>(cs, nst, p.scale, p.t0 + step + 1, ss, mx,
+                                                   own0);
             }
-            if (MULTI) count_item(warp_done, warp - 1 - kRingIssuers, (uint32_t)(i + 1));
+            if (MULTI) count_item(warp_done, warp - R::EPI0, (uint32_t)(i + 1));
         }
     }
 
@@ -869,8 +938,8 @@ cudaError_t launch_tc(const GridGeom &g, const float *B, const uint16_t *in_hi,
     const int grid = items < g_num_sms ? (int)items : g_num_sms;
     if constexpr (SPLIT)
         return p.steps > 1
-                   ? launch_step(tc_split_ring_kernel<S, true>, grid, ring_threads<true>(), C::SMEM, s, p, true)
-                   : launch_step(tc_split_ring_kernel<S, false>, grid, ring_threads<false>(), C::SMEM, s, p);
+                   ? launch_step(tc_split_ring_kernel<S, true>, grid, Ring<true>::THREADS, C::SMEM, s, p, true)
+                   : launch_step(tc_split_ring_kernel<S, false>, grid, Ring<false>::THREADS, C::SMEM, s, p);
     else
         return launch_step(tc_sweep_kernel<S, SPLIT>, grid, Sweep<S>::THREADS, C::SMEM, s, p,
                            p.steps > 1);

@@ -192,16 +192,69 @@ __device__ __forceinline__ StepScale step_scale(const SplitScale *sc, int t) {
     return scale_of(scale_words(sc, t), t);
 }
 
-// After a warp's last cells of step t: its largest |u| (units of 2^-11) into
-// M_t, E_t into slot t, and the maximum of slot t+3 cleared.
-__device__ __forceinline__ void flush_step_max(SplitScale *sc, int t, const StepScale &ss,
-                                               float mx) {
+// A CTA's side of the scale record.  Every CTA of a step reads the same
+// record and adds to the same maximum, so per warp these would be thousands
+// of accesses to one line at each step boundary (measured on GB300: a
+// 4098² split step in one launch per step, 30 -> 39 us; several steps per
+// launch, 28 -> 97 us).  Instead one warp of the CTA reads the scale and
+// publishes it in shared memory, and the epilogue warps' maxima meet in
+// shared memory, which the CTA's last warp to finish the step adds to the
+// record.  The slots go by the CTA's step ordinal n (the steps in which the
+// CTA holds tiles, counted from 0; every epilogue warp walks the same items,
+// so they agree on n), two of them: a CTA's warps are at most one step apart.
+struct CtaScale {
+    uint64_t *bar;   // [2] the step's scale published (one arrival)
+    StepScale *ss;   // [2]
+    unsigned *max;   // [2] the CTA's largest |u| 2^-11 in the step (FP32 bits)
+    unsigned *cnt;   // [2] epilogue warps done with the step
+};
+
+__device__ __forceinline__ void cta_scale_init(const CtaScale &c) {
+    for (int j = 0; j < 2; j++) {
+        mbar_init(&c.bar[j], 1);
+        c.max[j] = 0u;
+        c.cnt[j] = 0u;
+    }
+}
+
+// The scale warp's lane 0: the scale of the CTA's n-th step.
+__device__ __forceinline__ void cta_scale_publish(const CtaScale &c, int n, const StepScale &ss) {
+    c.ss[n & 1] = ss;
+    mbar_arrive(&c.bar[n & 1]);
+}
+
+// Every lane of an epilogue warp: the scale of the CTA's n-th step (bounded
+// wait; false on give-up or abort).  Slot n & 1 completes its phases in the
+// order of n, so the n-th step's is phase n >> 1 of it.
+__device__ __forceinline__ bool cta_scale_take(const CtaScale &c, int n, StepScale &ss,
+                                               const volatile int *abort_flag) {
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(&c.bar[n & 1], (n >> 1) & 1, abort_flag));
+    if (ok) ss = c.ss[n & 1];
+    return ok;
+}
+
+// After a warp's last cells of the CTA's n-th step (record step t): its
+// largest |u| joins the CTA's; the CTA's last warp of NW adds that to M_t
+// and, if the CTA held the step's tile 0 (own0), stores E_t in slot t and
+// clears the maximum of slot t+3.  Called by every lane.
+template <int NW>
+__device__ __forceinline__ void cta_scale_flush(const CtaScale &c, int n, SplitScale *sc, int t,
+                                                const StepScale &ss, float mx, bool own0) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) {
-        atomicMax(&sc->maxbits[t & (kScaleRing - 1)], __float_as_uint(mx * (1.0f / 2048.0f)));
-        sc->exp[t & (kScaleRing - 1)] = ss.e;
-        sc->maxbits[(t + 3) & (kScaleRing - 1)] = 0u;
+        atomicMax(&c.max[n & 1], __float_as_uint(mx * (1.0f / 2048.0f)));
+        __threadfence_block();
+        if (atomicAdd(&c.cnt[n & 1], 1u) == (unsigned)NW - 1) {
+            __threadfence_block();
+            const unsigned m = atomicExch(&c.max[n & 1], 0u);
+            atomicExch(&c.cnt[n & 1], 0u);
+            atomicMax(&sc->maxbits[t & (kScaleRing - 1)], m);
+            if (own0) {
+                sc->exp[t & (kScaleRing - 1)] = ss.e;
+                sc->maxbits[(t + 3) & (kScaleRing - 1)] = 0u;
+            }
+        }
     }
 }
 
@@ -617,12 +670,55 @@ __device__ __forceinline__ void store_block(const TileOut &o, const float (&f)[1
     }
 }
 
+// The grid cells of a 16-cell block that lie outside the update rectangle (a
+// fixed border), whose stored bits (iw, il) store_block_split copied: they
+// join mx, and when cs.k != 0 they are split again, scaled by 2^k, into
+// (hw, lw).  Taken only by blocks that hold such cells, and for the rescale
+// only on the steps whose scale moved (cs.k is the same for every thread).
+__device__ __forceinline__ void split_border_cells(const TileOut &o, int y, int xb, bool row_in,
+                                                   const uint32_t (&iw)[8],
+                                                   const uint32_t (&il)[8], const StepScale &cs,
+                                                   uint32_t (&hw)[8], uint32_t (&lw)[8],
+                                                   float &mx) {
+    uint32_t bm = 0;  // bit q: cell xb + q is a grid cell outside the update rectangle
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const int x = xb + q;
+        bm |= (x < o.nx && !(row_in && x >= o.x0 && x < o.x1)) ? 1u << q : 0u;
+    }
+    if (cs.k == 0) {
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const float2 hv = __half22float2(*reinterpret_cast<const __half2 *>(&iw[c]));
+            const float2 lv = __half22float2(*reinterpret_cast<const __half2 *>(&il[c]));
+            const float u0 = fmaf(hv.x, 2048.0f, lv.x), u1 = fmaf(hv.y, 2048.0f, lv.y);
+            mx = fmaxf(mx, fmaxf((bm >> (2 * c)) & 1u ? fabsf(u0) : 0.0f,
+                                 (bm >> (2 * c + 1)) & 1u ? fabsf(u1) : 0.0f));
+        }
+        return;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if ((bm >> (2 * c + u)) & 1u) {
+                uint16_t h = (uint16_t)(iw[c] >> (16 * u)), l = (uint16_t)(il[c] >> (16 * u));
+                resplit_pair(h, l, cs, mx);
+                const uint32_t keep = u ? 0x0000ffffu : 0xffff0000u;
+                hw[c] = (hw[c] & keep) | ((uint32_t)h << (16 * u));
+                lw[c] = (lw[c] & keep) | ((uint32_t)l << (16 * u));
+            }
+        }
+    }
+}
+
 // store_block<true> of the values v 2^k (StepScale ss): fast blocks split in
-// pairs, others split each updated cell alone and copy the rest, re-split by
-// the copy scale cs when cs.k != 0 (cs = ss, except for a blocked pair's
-// second step, whose copies come from two steps back).  The largest |u| of
-// the stored grid cells is kept in mx (a fast block lies in the update
-// rectangle, hence in the grid; padding cells never count).
+// pairs, others split each updated cell alone and copy the rest; the copied
+// grid cells (outside the update rectangle) are then re-split by the copy
+// scale cs when cs.k != 0 (cs = ss, except for a blocked pair's second step,
+// whose copies come from two steps back).  The largest |u| of the stored
+// grid cells is kept in mx (a fast block lies in the update rectangle, hence
+// in the grid; padding cells never count).
 __device__ __forceinline__ void store_block_split(const TileOut &o, const float (&f)[16], int y,
                                                   int xb, bool fast, bool row_in,
                                                   const StepScale &ss, const StepScale &cs,
@@ -651,17 +747,14 @@ __device__ __forceinline__ void store_block_split(const TileOut &o, const float 
                 } else {
                     hh[u] = (uint16_t)(iw[c] >> (16 * u));
                     ll[u] = (uint16_t)(il[c] >> (16 * u));
-                    // grid cells outside the rectangle (a fixed border)
-                    // keep their value; padding cells are only copied
-                    if (y < o.ny && x < o.nx) {
-                        if (cs.k != 0) resplit_pair(hh[u], ll[u], cs, mx);
-                        else mx = fmaxf(mx, fabsf(fmaf(h_val(hh[u]), 2048.0f, h_val(ll[u]))));
-                    }
                 }
             }
             hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
             lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
         }
+        // the block holds grid cells outside the update rectangle
+        if (y < o.ny && xb < o.nx && !(row_in && xb >= o.x0 && xb + 16 <= o.x1))
+            split_border_cells(o, y, xb, row_in, iw, il, cs, hw, lw, mx);
     }
     *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
     *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
