@@ -401,9 +401,6 @@ static void step_rows(const step_ctx *c, int i0, int i1) {
                         double bb = (a - ai) + H[l] * sc, rb = nearbyint(bb);
                         h = f64_to_f16((ai + rb) / 2048.0);
                         l = f64_to_f16(bb - rb);
-                        m = fmax(m, fabs(ai + bb));
-                    } else {
-                        m = fmax(m, fabs(H[h] * 2048.0 + H[l]));
                     }
                     Ch[o] = h;
                     Cl[o] = l;
@@ -635,21 +632,35 @@ int oracle_sweep_f16tc(uint16_t *grid, const float *B, int ny, int nx, int stenc
     return sweep16(oracle_step_f16tc, grid, B, ny, nx, stencil, steps, y0, y1, x0, x1);
 }
 
-/* e(M): the frexp exponent of M as an FP32 value (M 2^-e in [0.5, 1)), 0 for
- * zero, subnormal or non-finite M, clamped to [-64, 64] (the engine's rule). */
-static int split_exp_of(double M) {
-    float f = (float)M;
-    if (!(f > 0.0f) || !isfinite(f) || f < 1.17549435e-38f) return 0;
-    int e;
-    frexpf(f, &e);
+/* frexp exponent of a positive normal FP32 value (v 2^-e in [0.5, 1)) in
+ * *e; 0 for zero, subnormal or non-finite v (the part is absent). */
+static int f32_exp(float v, int *e) {
+    if (!(v >= 1.17549435e-38f) || !isfinite(v)) return 0;
+    frexpf(v, e);
+    return 1;
+}
+
+/* e(M) of M = max(m, b 2^d), m and b as FP32 values: the larger of the
+ * present parts' exponents, 0 for none or for a non-finite m (no change),
+ * clamped to [-64, 64] (the engine's rule). */
+static int split_exp_of(float m, float b, int d) {
+    if (!isfinite(m)) return 0;
+    int em = 0, eb = 0;
+    const int hm = f32_exp(m, &em), hb = f32_exp(b, &eb);
+    if (!hm && !hb) return 0;
+    eb += d;
+    int e = !hb ? em : !hm ? eb : (em > eb ? em : eb);
     return e < -64 ? -64 : e > 64 ? 64 : e;
 }
 
-/* A split sweep of one run with the engine's per-step scale: the planes start
- * in units of 2^E (*exp_io, the packing exponent) and end in units of 2^E_T
- * (written back to *exp_io).  Step t's exponent is E_t = E_{t-2} + e(M_{t-2})
- * (E_{-1} = E_0 = the input's, e(M_{-1}) = e(M_0) = 0), M_t the largest |x'|
- * the step stores; the step's values are multiplied by 2^(E_{t-1} - E_t). */
+/* A split sweep of one run with the engine's per-step scale, from planes as
+ * uploaded: they start in units of 2^E (*exp_io, the packing exponent) and
+ * end in units of 2^E_T (written back to *exp_io).  Step t's exponent is
+ * E_t = E_{t-2} + e(M_{t-2}) (E_{-1} = E_0 = the input's, e(M_{-1}) =
+ * e(M_0) = 0), M_t = max(m_t, B 2^(E_0 - E_t)) with m_t the largest |x'|
+ * the step stores in its update rectangle and B the largest |x'| of the
+ * input's cells outside it (|x'| 2^11 = |hi 2^11 + lo| rounded once to
+ * FP32); the step's values are multiplied by 2^(E_{t-1} - E_t). */
 int oracle_sweep_split(uint16_t *hi, uint16_t *lo, const float *B, int ny, int nx, int stencil,
                        int steps, int y0, int y1, int x0, int x1, int *exp_io) {
     long cells = (long)ny * nx;
@@ -662,6 +673,21 @@ int oracle_sweep_split(uint16_t *hi, uint16_t *lo, const float *B, int ny, int n
         free(th); free(tl); free(rowmax); free(E); free(eM);
         return -2;
     }
+    step_ctx c0;
+    if (ctx_init(&c0, K_SPLIT, ny, nx, stencil, y0, y1, x0, x1)) {
+        free(th); free(tl); free(rowmax); free(E); free(eM);
+        return -1;
+    }
+    const double *H = f16tab();
+    float bu = 0.0f; /* the border's largest |x'| 2^11 */
+    for (int i = 0; i < ny; i++)
+        for (int j = 0; j < nx; j++)
+            if (!inside(&c0, i, j)) {
+                long o = (long)i * nx + j;
+                bu = fmaxf(bu, (float)fabs(H[hi[o]] * 2048.0 + H[lo[o]]));
+            }
+    const float bm = bu / 2048.0f;
+    const int e_b = *exp_io;
     E[0] = E[1] = *exp_io; /* index t + 1 */
     eM[0] = eM[1] = 0;
     uint16_t *ch = hi, *cl = lo, *nh = th, *nl = tl;
@@ -680,7 +706,7 @@ int oracle_sweep_split(uint16_t *hi, uint16_t *lo, const float *B, int ny, int n
         double M = 0.0;
         for (int i = 0; i < ny; i++) M = fmax(M, rowmax[i]);
         E[t + 1] = et;
-        eM[t + 1] = split_exp_of(M);
+        eM[t + 1] = split_exp_of((float)M, bm, e_b - et);
         uint16_t *s = ch; ch = nh; nh = s;
         s = cl; cl = nl; nl = s;
     }

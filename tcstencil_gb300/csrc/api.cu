@@ -576,7 +576,9 @@ int tcs_plan_upload(tcs_plan p, const float *grid, int on_host, void *stream) {
                                                    static_cast<uint16_t *>(p->buf[0][1]), s),
                              "pack launch");
         if (st) return st;
-        e = launch_split_scale_init(p->d_scale, p->d_max, s);
+        e = launch_split_scale_init(p->d_scale, p->d_max, p->g,
+                                    static_cast<const uint16_t *>(p->buf[0][0]),
+                                    static_cast<const uint16_t *>(p->buf[0][1]), s);
     }
     else
         e = launch_pack_f16(src, p->prob.ny, p->prob.nx, 0, 0.0f, static_cast<uint16_t *>(p->buf[0][0]), s);

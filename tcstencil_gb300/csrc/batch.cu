@@ -1030,7 +1030,8 @@ int tcs_batch_upload(tcs_batch b, int index, const float *grid, int on_host, voi
         if (!st) st = cuda_status(launch_max_abs(src, cells, b->d_max, s), "max_abs launch");
         if (!st) st = cuda_status(launch_pack_split_dev(src, e.g.ny, e.g.nx, b->d_max, nullptr, hi,
                                                         b->pool + e.offset[cur][1], s), "pack launch");
-        if (!st) st = cuda_status(launch_split_scale_init(b->d_scales + index, b->d_max, s), "scale init");
+        if (!st) st = cuda_status(launch_split_scale_init(b->d_scales + index, b->d_max, e.g, hi,
+                                                          b->pool + e.offset[cur][1], s), "scale init");
     } else {
         st = cuda_status(launch_pack_f16(src, e.g.ny, e.g.nx, 0, 0.0f, hi, s), "pack launch");
     }

@@ -331,12 +331,44 @@ cudaError_t launch_unpack_f16(const uint16_t *plane, int ny, int nx, int pad, fl
 
 __global__ void split_scale_init_kernel(SplitScale *sc, const unsigned *max_bits) {
     const int e = scale_exp_of(*max_bits);
-    const float m = ldexpf(__uint_as_float(*max_bits), -e);
     for (int i = 0; i < kScaleRing; i++) {
         sc->maxbits[i] = 0;
         sc->exp[i] = e;
     }
-    sc->maxbits[0] = sc->maxbits[kScaleRing - 1] = __float_as_uint(isfinite(m) ? m : 0.0f);
+    sc->maxbits[0] = sc->maxbits[kScaleRing - 1] = kScaleNoMax;
+    sc->bmax = 0u;
+    sc->bexp = e;
+}
+
+// B: the largest |x'| 2^-11 stored in the grid's cells outside the update
+// rectangle, as FP32 bits, over the index space of the rows outside
+// [y0, y1) (every column) followed by the rows inside (the columns outside
+// [x0, x1)).  |x'| 2^11 = |hi 2^11 + lo| rounded once to FP32.
+__global__ void split_border_max_kernel(SplitScale *sc, GridGeom g, const uint16_t *__restrict__ hi,
+                                        const uint16_t *__restrict__ lo) {
+    const int out_rows = g.y0 + (g.ny - g.y1);
+    const int out_cols = g.x0 + (g.nx - g.x1);
+    const size_t na = (size_t)out_rows * g.nx;
+    const size_t n = na + (size_t)(g.y1 - g.y0) * out_cols;
+    float m = 0.0f;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        int y, x;
+        if (i < na) {
+            const int r = (int)(i / g.nx);
+            x = (int)(i - (size_t)r * g.nx);
+            y = r < g.y0 ? r : g.y1 + (r - g.y0);
+        } else {
+            const size_t j = i - na;
+            const int r = (int)(j / out_cols), c = (int)(j - (size_t)r * out_cols);
+            y = g.y0 + r;
+            x = c < g.x0 ? c : g.x1 + (c - g.x0);
+        }
+        const size_t idx = plane_index(g.p16, y, x);
+        m = fmaxf(m, fabsf(fmaf(h2f_bits(hi[idx]), 2048.0f, h2f_bits(lo[idx]))));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&sc->bmax, __float_as_uint(m * (1.0f / 2048.0f)));
 }
 
 __global__ void split_scale_end_run_kernel(SplitScale *sc, int steps) {
@@ -351,8 +383,16 @@ __global__ void split_scale_end_run_kernel(SplitScale *sc, int steps) {
     sc->exp[0] = e0;
 }
 
-cudaError_t launch_split_scale_init(SplitScale *sc, const unsigned *max_bits, cudaStream_t s) {
+cudaError_t launch_split_scale_init(SplitScale *sc, const unsigned *max_bits, const GridGeom &g,
+                                    const uint16_t *hi, const uint16_t *lo, cudaStream_t s) {
     split_scale_init_kernel<<<1, 1, 0, s>>>(sc, max_bits);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const size_t n = (size_t)g.ny * g.nx - (size_t)(g.y1 - g.y0) * (g.x1 - g.x0);
+    if (n == 0) return cudaSuccess;
+    const size_t want = blocks_for(n);
+    split_border_max_kernel<<<static_cast<unsigned>(want < 1024 ? want : 1024), kThreads, 0, s>>>(
+        sc, g, hi, lo);
     return cudaGetLastError();
 }
 

@@ -386,7 +386,7 @@ void tcs_server_s::admit() {
             st = cuda_status(cudaMemsetAsync(mx, 0, sizeof(unsigned), upload), "max clear");
             if (!st) st = cuda_status(launch_max_abs(stg, cells, mx, upload), "max_abs launch");
             if (!st) st = cuda_status(launch_pack_split_dev(stg, q->g.ny, q->g.nx, mx, nullptr, plane(q, 0, 0), plane(q, 0, 1), upload), "pack launch");
-            if (!st) st = cuda_status(launch_split_scale_init(d_scale + q->slot, mx, upload), "scale init");
+            if (!st) st = cuda_status(launch_split_scale_init(d_scale + q->slot, mx, q->g, plane(q, 0, 0), plane(q, 0, 1), upload), "scale init");
         } else if (!st) {
             st = cuda_status(launch_pack_f16(stg, q->g.ny, q->g.nx, 0, 0.0f, plane(q, 0, 0), upload), "pack launch");
         }

@@ -372,11 +372,7 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
                                 } else {
                                     hh[u2] = (uint16_t)(iw[c] >> (16 * u2));
                                     ll[u2] = (uint16_t)(il[c] >> (16 * u2));
-                                    float mc = 0.0f;
-                                    if (ss1.k != 0) resplit_pair(hh[u2], ll[u2], ss1, mc);
-                                    else mc = fabsf(fmaf(h_val(hh[u2]), 2048.0f, h_val(ll[u2])));
-                                    if (y >= 0 && y < p.g.ny && x >= 0 && x < p.g.nx)
-                                        mx1 = fmaxf(mx1, mc);
+                                    if (ss1.k != 0) resplit_pair(hh[u2], ll[u2], ss1);
                                 }
                             }
                             hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);

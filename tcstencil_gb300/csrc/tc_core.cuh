@@ -130,13 +130,18 @@ __device__ __forceinline__ float h_val(uint16_t b) {
 }
 
 // ------------------------------------------------ split scale, per step ---
-// (tcs_internal.h SplitScale.)  e(M): the frexp exponent of a positive FP32
-// M, M 2^-e in [0.5, 1); 0 for zero, subnormal or non-finite M (no change);
-// clamped to [-64, 64].
-__device__ __forceinline__ int split_exp_of(unsigned bits) {
-    const int b = (int)((bits >> 23) & 0xffu);
-    if (b == 0 || b == 0xff) return 0;
-    const int e = b - 126;
+// (tcs_internal.h SplitScale.)  e(M) of M = max(m, B 2^d) from the FP32
+// bits of m and B: the larger of the present parts' frexp exponents (a zero
+// or subnormal part is absent), 0 for none or for a non-finite m (no
+// change), clamped to [-64, 64].
+__device__ __forceinline__ int split_exp_of(unsigned mbits, unsigned bbits, int d) {
+    const int bm = (int)((mbits >> 23) & 0xffu);
+    if (bm == 0xff) return 0;
+    const int bb = (int)((bbits >> 23) & 0xffu);
+    const bool hm = bm != 0, hb = bb != 0 && bb != 0xff;
+    if (!hm && !hb) return 0;
+    const int em = bm - 126, eb = bb - 126 + d;
+    const int e = !hb ? em : !hm ? eb : (em > eb ? em : eb);
     return e < -64 ? -64 : e > 64 ? 64 : e;
 }
 
@@ -148,32 +153,35 @@ struct StepScale {
     int k, e;
 };
 
-// The words of step t's scale: E and M of steps t-2 and t-3, and E_0, in
-// one burst of relaxed GPU-scope loads (their latencies overlap, and a
-// caller can issue other work before it uses them).
+// The words of step t's scale: E and m of steps t-2 and t-3, E_0, and the
+// border's B and E_B, in one burst of relaxed GPU-scope loads (their
+// latencies overlap, and a caller can issue other work before it uses them).
 struct ScaleWords {
-    unsigned ea, ma, eb, mb, e0;
+    unsigned ea, ma, eb, mb, e0, bm, be;
 };
 __device__ __forceinline__ ScaleWords scale_words(const SplitScale *sc, int t) {
     const int a = (t - 2) & (kScaleRing - 1), b = (t - 3) & (kScaleRing - 1);
     ScaleWords w;
     asm volatile(
-        "ld.relaxed.gpu.global.u32 %0, [%5];\n\t"
-        "ld.relaxed.gpu.global.u32 %1, [%6];\n\t"
-        "ld.relaxed.gpu.global.u32 %2, [%7];\n\t"
-        "ld.relaxed.gpu.global.u32 %3, [%8];\n\t"
-        "ld.relaxed.gpu.global.u32 %4, [%9];"
-        : "=r"(w.ea), "=r"(w.ma), "=r"(w.eb), "=r"(w.mb), "=r"(w.e0)
+        "ld.relaxed.gpu.global.u32 %0, [%7];\n\t"
+        "ld.relaxed.gpu.global.u32 %1, [%8];\n\t"
+        "ld.relaxed.gpu.global.u32 %2, [%9];\n\t"
+        "ld.relaxed.gpu.global.u32 %3, [%10];\n\t"
+        "ld.relaxed.gpu.global.u32 %4, [%11];\n\t"
+        "ld.relaxed.gpu.global.u32 %5, [%12];\n\t"
+        "ld.relaxed.gpu.global.u32 %6, [%13];"
+        : "=r"(w.ea), "=r"(w.ma), "=r"(w.eb), "=r"(w.mb), "=r"(w.e0), "=r"(w.bm), "=r"(w.be)
         : "l"(&sc->exp[a]), "l"(&sc->maxbits[a]), "l"(&sc->exp[b]), "l"(&sc->maxbits[b]),
-          "l"(&sc->exp[0])
+          "l"(&sc->exp[0]), "l"(&sc->bmax), "l"(&sc->bexp)
         : "memory");
     return w;
 }
 
 __device__ __forceinline__ StepScale scale_of(const ScaleWords &w, int t) {
     StepScale r;
-    r.e = (int)w.ea + split_exp_of(w.ma);                              // E_t
-    const int e1 = t == 1 ? (int)w.e0 : (int)w.eb + split_exp_of(w.mb);  // E_{t-1}
+    const int ea = (int)w.ea, eb = (int)w.eb, be = (int)w.be;
+    r.e = ea + split_exp_of(w.ma, w.bm, be - ea);                              // E_t
+    const int e1 = t == 1 ? (int)w.e0 : eb + split_exp_of(w.mb, w.bm, be - eb);  // E_{t-1}
     int k = e1 - r.e;
     k = k < -64 ? -64 : k > 64 ? 64 : k;
     r.k = k;
@@ -281,15 +289,13 @@ __device__ __forceinline__ void split_fixed_s(float v, float s, uint16_t &hi, ui
 // pair is hi' = (ai + rint(af + b)) 2^-11, lo' = (af + b) - rint(af + b),
 // every operation exact, so no bit of the value is lost.  (k = 0 keeps the
 // pair as it is.)
-__device__ __forceinline__ void resplit_pair(uint16_t &hi, uint16_t &lo, const StepScale &ss,
-                                             float &mx) {
+__device__ __forceinline__ void resplit_pair(uint16_t &hi, uint16_t &lo, const StepScale &ss) {
     const float a = h_val(hi) * ss.s;
     const float ai = truncf(a);
     const float bb = (a - ai) + h_val(lo) * (ss.s * (1.0f / 2048.0f));
     const float rb = rintf(bb);
     hi = h_bits((ai + rb) * (1.0f / 2048.0f));
     lo = h_bits(bb - rb);
-    mx = fmaxf(mx, fabsf(ai + bb));
 }
 
 // Two FP32 values as packed FP16 (round to nearest even), v0 in the low half.
@@ -671,39 +677,22 @@ __device__ __forceinline__ void store_block(const TileOut &o, const float (&f)[1
 }
 
 // The grid cells of a 16-cell block that lie outside the update rectangle (a
-// fixed border), whose stored bits (iw, il) store_block_split copied: they
-// join mx, and when cs.k != 0 they are split again, scaled by 2^k, into
-// (hw, lw).  Taken only by blocks that hold such cells, and for the rescale
-// only on the steps whose scale moved (cs.k is the same for every thread).
+// fixed border), whose stored bits (iw, il) store_block_split copied, split
+// again, scaled by 2^k, into (hw, lw): taken only on the steps whose scale
+// moved (cs.k != 0, the same for every thread) and by blocks that hold such
+// cells.
 __device__ __forceinline__ void split_border_cells(const TileOut &o, int y, int xb, bool row_in,
                                                    const uint32_t (&iw)[8],
                                                    const uint32_t (&il)[8], const StepScale &cs,
-                                                   uint32_t (&hw)[8], uint32_t (&lw)[8],
-                                                   float &mx) {
-    uint32_t bm = 0;  // bit q: cell xb + q is a grid cell outside the update rectangle
-#pragma unroll
-    for (int q = 0; q < 16; q++) {
-        const int x = xb + q;
-        bm |= (x < o.nx && !(row_in && x >= o.x0 && x < o.x1)) ? 1u << q : 0u;
-    }
-    if (cs.k == 0) {
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-            const float2 hv = __half22float2(*reinterpret_cast<const __half2 *>(&iw[c]));
-            const float2 lv = __half22float2(*reinterpret_cast<const __half2 *>(&il[c]));
-            const float u0 = fmaf(hv.x, 2048.0f, lv.x), u1 = fmaf(hv.y, 2048.0f, lv.y);
-            mx = fmaxf(mx, fmaxf((bm >> (2 * c)) & 1u ? fabsf(u0) : 0.0f,
-                                 (bm >> (2 * c + 1)) & 1u ? fabsf(u1) : 0.0f));
-        }
-        return;
-    }
+                                                   uint32_t (&hw)[8], uint32_t (&lw)[8]) {
 #pragma unroll
     for (int c = 0; c < 8; c++) {
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-            if ((bm >> (2 * c + u)) & 1u) {
+            const int x = xb + 2 * c + u;
+            if (x < o.nx && !(row_in && x >= o.x0 && x < o.x1)) {
                 uint16_t h = (uint16_t)(iw[c] >> (16 * u)), l = (uint16_t)(il[c] >> (16 * u));
-                resplit_pair(h, l, cs, mx);
+                resplit_pair(h, l, cs);
                 const uint32_t keep = u ? 0x0000ffffu : 0xffff0000u;
                 hw[c] = (hw[c] & keep) | ((uint32_t)h << (16 * u));
                 lw[c] = (lw[c] & keep) | ((uint32_t)l << (16 * u));
@@ -716,9 +705,9 @@ __device__ __forceinline__ void split_border_cells(const TileOut &o, int y, int 
 // pairs, others split each updated cell alone and copy the rest; the copied
 // grid cells (outside the update rectangle) are then re-split by the copy
 // scale cs when cs.k != 0 (cs = ss, except for a blocked pair's second step,
-// whose copies come from two steps back).  The largest |u| of the stored
-// grid cells is kept in mx (a fast block lies in the update rectangle, hence
-// in the grid; padding cells never count).
+// whose copies come from two steps back).  The largest |u| of the updated
+// cells is kept in mx (the border's share of the step maximum is the
+// record's B; padding cells never count).
 __device__ __forceinline__ void store_block_split(const TileOut &o, const float (&f)[16], int y,
                                                   int xb, bool fast, bool row_in,
                                                   const StepScale &ss, const StepScale &cs,
@@ -752,9 +741,9 @@ __device__ __forceinline__ void store_block_split(const TileOut &o, const float 
             hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
             lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
         }
-        // the block holds grid cells outside the update rectangle
-        if (y < o.ny && xb < o.nx && !(row_in && xb >= o.x0 && xb + 16 <= o.x1))
-            split_border_cells(o, y, xb, row_in, iw, il, cs, hw, lw, mx);
+        // the scale moved and the block holds grid cells outside the update rectangle
+        if (cs.k != 0 && y < o.ny && xb < o.nx && !(row_in && xb >= o.x0 && xb + 16 <= o.x1))
+            split_border_cells(o, y, xb, row_in, iw, il, cs, hw, lw);
     }
     *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
     *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);

@@ -183,26 +183,37 @@ cudaError_t launch_max_abs(const float *in, size_t n, unsigned *out_bits, cudaSt
 // its precision is about 2^-23 of 2^E.  E follows the grid's magnitude step
 // by step, so a field that decays keeps FP32-level relative precision:
 //   E_t = E_{t-2} + e(M_{t-2}),   k_t = E_{t-1} - E_t,
-// where M_t is the largest |x'| stored by step t (in step t's units, over
-// the grid's cells) and e(M) its frexp exponent (M 2^-e in [0.5, 1); 0 for
-// M = 0).  Step t multiplies its values by 2^k_t before the split (cells it
-// only copies are re-split by the same factor when k_t != 0).  Step t reads
-// only steps t-2 and t-3, which every form of the sweep (one launch per step,
-// several steps per launch, blocked pairs, batches) has completed by then,
-// so every form gives the same bits.  Slots are the step index within a run
-// (1..T) mod 8; slots 7 and 0 hold steps -1 and 0 (the run's starting
-// history), which launch_split_scale_end_run moves into place after each
-// run.  Step t writes M_t and E_t into slot t and clears the maximum of slot
-// t+3 (whose readers, steps t-3 and t-2, have finished, and whose next
-// writer, step t+3, starts after step t has).
+// where M_t = max(the largest |x'| step t stores in its update rectangle,
+// B 2^(E_B - E_t)) in step t's units, B the largest |x'| of the grid's
+// cells outside the update rectangle (its fixed border) as uploaded, in the
+// units of the upload's exponent E_B, and e(M) the frexp exponent of M
+// (M 2^-e in [0.5, 1)), taken as max(e(m), e(B) + E_B - E_t) of the parts
+// present (a zero or subnormal part is absent; no part, or a non-finite m:
+// 0), clamped to [-64, 64].  The border keeps its values, so its share of M
+// needs no pass over its cells.  Step t multiplies its values by 2^k_t
+// before the split (cells it only copies are re-split by the same factor
+// when k_t != 0).  Step t reads only steps t-2 and t-3, which every form of
+// the sweep (one launch per step, several steps per launch, blocked pairs,
+// batches) has completed by then, so every form gives the same bits.  Slots
+// are the step index within a run (1..T) mod 8; slots 7 and 0 hold steps -1
+// and 0 (the run's starting history), which launch_split_scale_end_run moves
+// into place after each run; after an upload their maxima are the non-finite
+// mark, e = 0.  Step t writes M_t (its part m) and E_t into slot t and clears
+// the maximum of slot t+3 (whose readers, steps t-3 and t-2, have finished,
+// and whose next writer, step t+3, starts after step t has).
 constexpr int kScaleRing = 8;
+constexpr unsigned kScaleNoMax = 0xffffffffu;  // a slot's maximum before any step: e = 0
 struct SplitScale {
-    unsigned maxbits[kScaleRing];  // M_t as FP32 bits (atomicMax of non-negative floats)
+    unsigned maxbits[kScaleRing];  // m of M_t as FP32 bits (atomicMax of non-negative floats)
     int exp[kScaleRing];           // E_t
+    unsigned bmax;                 // B as FP32 bits
+    int bexp;                      // E_B
 };
-// From the max-|x| bits launch_max_abs left for a grid's input: E_0 = the
-// pack's exponent and M_0, as steps -1 and 0; the other maxima 0.
-cudaError_t launch_split_scale_init(SplitScale *sc, const unsigned *max_bits, cudaStream_t s);
+// From the max-|x| bits launch_max_abs left for a grid's input: E_0 = E_B =
+// the pack's exponent, steps -1 and 0 marked as unmeasured, and B from the
+// packed planes (hi, lo) of the grid g.
+cudaError_t launch_split_scale_init(SplitScale *sc, const unsigned *max_bits, const GridGeom &g,
+                                    const uint16_t *hi, const uint16_t *lo, cudaStream_t s);
 // After a run of `steps` steps: steps T-1 and T become slots 7 and 0, the
 // maxima of slots 1..6 are cleared.
 cudaError_t launch_split_scale_end_run(SplitScale *sc, int steps, cudaStream_t s);

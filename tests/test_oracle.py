@@ -155,3 +155,27 @@ def test_error_metrics_match_the_reference(golden):
     assert any(g[f"{c}_rel_reported"].size for c in cases)
     assert any(not g[f"{c}_abs_reported"].size for c in cases)
     assert any(not g[f"{c}_abs_max_line"].size and g[f"{c}_abs_reported"].size for c in cases)
+
+
+def test_split_scale_rule_follows_the_field_and_its_fixed_border():
+    """The oracle's per-step split scale: E_t follows the largest value of
+    the update rectangle, or of the fixed border where that is larger (the
+    border keeps its values, so it pins E).  A decaying zero-border field's
+    exponent comes down and the run stays within 1e-6 of FP64; with a 0.75
+    border around the same field it stays at the input's."""
+    from helpers import normalized_coeffs
+    rng = np.random.default_rng(5)
+    B = normalized_coeffs(rng, "box2d2r")
+    noise = rng.uniform(-1, 1, (76, 86))
+    for border, expect_drop in ((0.0, True), (0.75, False)):
+        A = np.full((80, 90), border, np.float32)
+        A[2:-2, 2:-2] = noise
+        e0 = oracle.split_scale_exp(A)
+        hi, lo = oracle.split(A.astype(np.float64), e0)
+        h, l, e = oracle.sweep_split(hi, lo, B, "box2d2r", 60, scale_exp=e0)
+        assert (e < e0) == expect_drop, (border, e0, e)
+        got = oracle.join(h, l, e)
+        f64 = oracle.sweep_f64(A.astype(np.float64), B.astype(np.float64), "box2d2r", 60)
+        assert np.linalg.norm(got - f64) / np.linalg.norm(f64) <= 1e-6
+        # the border keeps its values
+        np.testing.assert_allclose(got[:2], A[:2], rtol=0, atol=2.0 ** (e0 - 23))
