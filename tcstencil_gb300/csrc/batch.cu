@@ -629,8 +629,10 @@ __global__ void __launch_bounds__(BatchCfg<SPLIT>::THREADS, 1) tc_batch_kernel(c
                         mbar_arrive(&acc_empty[Ga % kBatchRingSlots]);
                         mbar_arrive(&acc_empty[Gb % kBatchRingSlots]);
                     }
-                    store_block_split(o, f, y, X0 + 16 * jb, fast, row_in, ss, ss, mx);
+                    store_block_split(o, f, y, X0 + 16 * jb, fast, row_in, ss, mx);
                 });
+                if (ok && ss.k != 0 && !fast && !rows_out)
+                    resplit_border(o, y, X0, grp, C::GROUPS, nwin - 1, ss);
                 G0 += nwin;
                 if (!ok) {
                     stop = true;

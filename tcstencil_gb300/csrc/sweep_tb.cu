@@ -408,9 +408,10 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_split_tb_kernel(const TbPara
                 const bool row_in = y >= o.y0 && y < o.y1;
                 run_step(kS2Windows, [&](int j, const float (&f)[16]) {
                     const int xb = X0 + 16 * j;
-                    if (mine && xb < p.g.nx)
-                        store_block_split(o, f, y, xb, fast, row_in, ss2, cs2, mx2);
+                    if (mine && xb < p.g.nx) store_block_split(o, f, y, xb, fast, row_in, ss2, mx2);
                 });
+                if (!stop && mine && cs2.k != 0 && !fast)
+                    resplit_border(o, y, X0, grp, kTbGroups, kS2Windows - 1, cs2);
             }
         }
         if (!stop && p.scale) {  // tile 0 is CTA 0's

@@ -833,9 +833,10 @@ __global__ void __launch_bounds__(Ring<MULTI>::THREADS, 1) tc_split_ring_kernel(
                     mbar_arrive(&win_empty[Ga % kRingSlots]);
                     mbar_arrive(&win_empty[Gb % kRingSlots]);
                 }
-                store_block_split(o, f, y, X0 + 16 * j, fast, row_in, ss, ss, mx);
+                store_block_split(o, f, y, X0 + 16 * j, fast, row_in, ss, mx);
             });
             if (!ok) break;
+            if (ss.k != 0 && !fast) resplit_border(o, y, X0, grp, kRingGroups, kTileWindows - 1, ss);
             // the step's last item of this warp: its maximum and the step's
             // exponent go out before the item is counted
             if (p.scale) {

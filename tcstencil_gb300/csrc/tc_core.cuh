@@ -676,42 +676,63 @@ __device__ __forceinline__ void store_block(const TileOut &o, const float (&f)[1
     }
 }
 
-// The grid cells of a 16-cell block that lie outside the update rectangle (a
-// fixed border), whose stored bits (iw, il) store_block_split copied, split
-// again, scaled by 2^k, into (hw, lw): taken only on the steps whose scale
-// moved (cs.k != 0, the same for every thread) and by blocks that hold such
-// cells.
-__device__ __forceinline__ void split_border_cells(const TileOut &o, int y, int xb, bool row_in,
-                                                   const uint32_t (&iw)[8],
-                                                   const uint32_t (&il)[8], const StepScale &cs,
-                                                   uint32_t (&hw)[8], uint32_t (&lw)[8]) {
+// After a warp has stored its blocks of a tile (row y, blocks X0 + 16 j for
+// j = j0, j0 + dj, ... < nblk), on a step whose copies change scale
+// (cs.k != 0, the same for every thread): the grid cells among them outside
+// the update rectangle (a fixed border), which the stores copied, are split
+// again from the input planes, scaled by 2^k.  A pass of its own with rolled
+// loops (each 8-cell panel row's input words loaded at once, then taken two
+// cells at a time from the front of the word arrays): such steps are few,
+// and this code inside the unrolled stores slowed every step of the
+// epilogue-bound kernels (measured on GB300: 512 mixed split grids
+// 5.66 -> 6.15 ms, 16386² 378 -> 386 us per step).
+__device__ __forceinline__ void resplit_border(const TileOut &o, int y, int X0, int j0, int dj,
+                                               int nblk, const StepScale &cs) {
+    if (y >= o.ny) return;
+    const bool row_in = y >= o.y0 && y < o.y1;
+#pragma unroll 1
+    for (int j = j0; j < nblk; j += dj) {
+        const int xb = X0 + 16 * j;
+        if (xb >= o.nx || (row_in && xb >= o.x0 && xb + 16 <= o.x1)) continue;
+#pragma unroll 1
+        for (int hf = 0; hf < 2; hf++) {
+            const int xh = xb + 8 * hf;  // a panel row: cells xh .. xh+7
+            if (xh >= o.nx || (row_in && xh >= o.x0 && xh + 8 <= o.x1)) continue;
+            const size_t off = plane_index(o.pg, y, xh);
+            const uint4 a = *reinterpret_cast<const uint4 *>(o.in_hi + off);
+            const uint4 b = *reinterpret_cast<const uint4 *>(o.in_lo + off);
+            uint32_t hw[4] = {a.x, a.y, a.z, a.w}, lw[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll 1
+            for (int q = 0; q < 8; q += 2) {
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
+                for (int u = 0; u < 2; u++) {
+                    const int x = xh + q + u;
+                    if (x < o.nx && !(row_in && x >= o.x0 && x < o.x1)) {
+                        uint16_t h = (uint16_t)(hw[0] >> (16 * u));
+                        uint16_t l = (uint16_t)(lw[0] >> (16 * u));
+                        resplit_pair(h, l, cs);
+                        o.out_hi[off + q + u] = h;
+                        o.out_lo[off + q + u] = l;
+                    }
+                }
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const int x = xb + 2 * c + u;
-            if (x < o.nx && !(row_in && x >= o.x0 && x < o.x1)) {
-                uint16_t h = (uint16_t)(iw[c] >> (16 * u)), l = (uint16_t)(il[c] >> (16 * u));
-                resplit_pair(h, l, cs);
-                const uint32_t keep = u ? 0x0000ffffu : 0xffff0000u;
-                hw[c] = (hw[c] & keep) | ((uint32_t)h << (16 * u));
-                lw[c] = (lw[c] & keep) | ((uint32_t)l << (16 * u));
+                for (int c = 0; c < 3; c++) {
+                    hw[c] = hw[c + 1];
+                    lw[c] = lw[c + 1];
+                }
             }
         }
     }
 }
 
 // store_block<true> of the values v 2^k (StepScale ss): fast blocks split in
-// pairs, others split each updated cell alone and copy the rest; the copied
-// grid cells (outside the update rectangle) are then re-split by the copy
-// scale cs when cs.k != 0 (cs = ss, except for a blocked pair's second step,
-// whose copies come from two steps back).  The largest |u| of the updated
-// cells is kept in mx (the border's share of the step maximum is the
-// record's B; padding cells never count).
+// pairs, others split each updated cell alone and copy the rest (on a step
+// whose copies change scale, resplit_border then rewrites the grid's copied
+// cells).  The largest |u| of the updated cells is kept in mx (the border's
+// share of the step maximum is the record's B; padding cells never count).
 __device__ __forceinline__ void store_block_split(const TileOut &o, const float (&f)[16], int y,
                                                   int xb, bool fast, bool row_in,
-                                                  const StepScale &ss, const StepScale &cs,
-                                                  float &mx) {
+                                                  const StepScale &ss, float &mx) {
     const size_t off0 = plane_index(o.pg, y, xb);     // cells xb .. xb+7
     const size_t off1 = off0 + (size_t)o.pg.nyp * 8;  // cells xb+8 .. xb+15
     uint32_t hw[8], lw[8];
@@ -741,9 +762,6 @@ __device__ __forceinline__ void store_block_split(const TileOut &o, const float 
             hw[c] = (uint32_t)hh[0] | ((uint32_t)hh[1] << 16);
             lw[c] = (uint32_t)ll[0] | ((uint32_t)ll[1] << 16);
         }
-        // the scale moved and the block holds grid cells outside the update rectangle
-        if (cs.k != 0 && y < o.ny && xb < o.nx && !(row_in && xb >= o.x0 && xb + 16 <= o.x1))
-            split_border_cells(o, y, xb, row_in, iw, il, cs, hw, lw);
     }
     *reinterpret_cast<uint4 *>(o.out_hi + off0) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
     *reinterpret_cast<uint4 *>(o.out_hi + off1) = make_uint4(hw[4], hw[5], hw[6], hw[7]);
