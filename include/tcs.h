@@ -44,6 +44,7 @@ extern "C" {
 #define TCS_ERR_UNSUPPORTED 3 /* valid request this build/device cannot run   */
 #define TCS_ERR_NOMEM 4       /* device allocation failed or budget exceeded  */
 #define TCS_ERR_TIMEOUT 5     /* a bounded device wait gave up                */
+#define TCS_ERR_CANCELLED 6   /* a server request was cancelled (tcs_server_cancel) */
 
 enum tcs_stencil { TCS_STAR2D1R = 0, TCS_STAR2D2R = 1, TCS_BOX2D1R = 2, TCS_BOX2D2R = 3 };
 /* TENSOR: tcgen05 banded-matrix kernel; CUDACORE: FP32 FMA warp-strip kernel */
@@ -357,6 +358,7 @@ typedef struct tcs_server_stats {
     /* round launch: host build of the round, compute-stream enqueue, and the
      * enqueue of finished requests' downloads (total and worst), seconds */
     double launch_total_s[3], launch_max_s[3];
+    long long cancelled;       /* requests ended by tcs_server_cancel */
 } tcs_server_stats;
 
 int tcs_server_create(const tcs_server_config *config, tcs_server *out);
@@ -372,6 +374,14 @@ int tcs_server_submit(tcs_server server, const tcs_problem *problem, int steps, 
 int tcs_server_poll(tcs_server server, long long ticket, int *state, int *status);
 /* Blocks until the ticket is done or failed, or until timeout_s (< 0: no limit). */
 int tcs_server_wait(tcs_server server, long long ticket, double timeout_s);
+/* Cancels a request.  A queued one is dropped at once; a resident one takes
+ * part in no further round and is retired (its memory freed) once its
+ * rounds and upload are done.  Either way the ticket ends failed with
+ * TCS_ERR_CANCELLED and h_out is left as it was.  TCS_ERR_INVALID when the
+ * ticket is unknown, done, failed, already cancelled, or finishing (its
+ * result being downloaded: it completes normally).  With tcs_server_wait's
+ * timeout this gives a deadline: wait, and cancel on TCS_ERR_TIMEOUT. */
+int tcs_server_cancel(tcs_server server, long long ticket);
 /* Seconds, on the server's clock, of the ticket's submission, admission and
  * completion (its result in h_out). */
 int tcs_server_times(tcs_server server, long long ticket, double *submitted, double *admitted,
@@ -379,6 +389,38 @@ int tcs_server_times(tcs_server server, long long ticket, double *submitted, dou
 /* The server's clock (seconds since creation). */
 double tcs_server_clock(tcs_server server);
 int tcs_server_get_stats(tcs_server server, tcs_server_stats *stats);
+
+/* ------------------------------------- allocation hook and guard regions ---
+ * Test and debug aids; neither is needed in production.  No reference
+ * counterpart (the reference's allocations exit on failure,
+ * common/common.hpp:10-16).
+ *
+ * Every device and pinned-host allocation the library makes (plans, batches,
+ * the server, the drift check, tcs_sweep_host, host_code) first asks the
+ * hook, if one is installed: hook(bytes, what, user) != 0 makes that
+ * allocation fail as out of memory, so the call that needed it returns
+ * TCS_ERR_NOMEM with `what` in tcs_last_error(), after freeing what it had
+ * allocated.  NULL removes the hook.  The hook runs on the allocating
+ * thread (the server's scheduler thread for round buffers).
+ *
+ * tcs_set_guard_bytes(n): allocations made from now on carry n bytes
+ * (rounded up to a multiple of 256; 0 turns it off) of a canary pattern
+ * before and after them; batches and the server also put n canary bytes
+ * between the planes of their pools and around each request, and
+ * tcs_sweep_steps_noalloc after the part of its scratch a call uses.
+ * tcs_guard_check waits for the device, compares every live guard region
+ * with the canary and sets *damaged to the number found changed, counting
+ * those found changed when their memory was freed since the last check; a
+ * non-zero count names the regions in tcs_last_error().  A changed guard
+ * means a kernel or copy wrote out of bounds.
+ *
+ * tcs_alloc_stats: the library's live allocations, count and bytes (a test
+ * of error paths can compare them before and after a failed call). */
+typedef int (*tcs_alloc_hook)(size_t bytes, const char *what, void *user);
+int tcs_set_alloc_hook(tcs_alloc_hook hook, void *user);
+int tcs_set_guard_bytes(size_t bytes);
+int tcs_guard_check(long long *damaged);
+int tcs_alloc_stats(long long *live_count, size_t *live_bytes);
 
 #ifdef __cplusplus
 }

@@ -30,7 +30,8 @@ RADIUS = {"star2d1r": 1, "star2d2r": 2, "box2d1r": 1, "box2d2r": 2}
 ENGINES = {"tensor": 0, "cudacore": 1}
 PRECISIONS = {"f16": 0, "split": 1, "f32": 2}
 
-TCS_OK, TCS_ERR_INVALID, TCS_ERR_CUDA, TCS_ERR_UNSUPPORTED, TCS_ERR_NOMEM, TCS_ERR_TIMEOUT = range(6)
+(TCS_OK, TCS_ERR_INVALID, TCS_ERR_CUDA, TCS_ERR_UNSUPPORTED, TCS_ERR_NOMEM, TCS_ERR_TIMEOUT,
+ TCS_ERR_CANCELLED) = range(7)
 
 LIB_PATH = _build.LIB
 
@@ -68,7 +69,11 @@ class ServerStats(ctypes.Structure):
                 ("peak_bytes_in_use", ctypes.c_size_t), ("active", ctypes.c_int),
                 ("queued", ctypes.c_int), ("sched_total_s", ctypes.c_double * 4),
                 ("sched_max_s", ctypes.c_double * 4), ("launch_total_s", ctypes.c_double * 3),
-                ("launch_max_s", ctypes.c_double * 3)]
+                ("launch_max_s", ctypes.c_double * 3), ("cancelled", ctypes.c_longlong)]
+
+
+# int hook(size_t bytes, const char *what, void *user): non-zero fails the allocation
+ALLOC_HOOK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_void_p)
 
 
 _lib = None
@@ -150,6 +155,11 @@ SIGNATURES = {
     "tcs_server_times": (_I, [_P, ctypes.c_longlong, ctypes.POINTER(ctypes.c_double),
                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "tcs_server_clock": (ctypes.c_double, [_P]),
+    "tcs_server_cancel": (_I, [_P, ctypes.c_longlong]),
+    "tcs_set_alloc_hook": (_I, [ALLOC_HOOK, _P]),
+    "tcs_set_guard_bytes": (_I, [_SZ]),
+    "tcs_guard_check": (_I, [ctypes.POINTER(ctypes.c_longlong)]),
+    "tcs_alloc_stats": (_I, [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_SZ)]),
     "tcs_server_get_stats": (_I, [_P, ctypes.POINTER(ServerStats)]),
 }
 
@@ -590,6 +600,10 @@ class Server:
         _check(lib().tcs_server_wait(self._h, ticket, float(timeout)))
         self._held.pop(ticket, None)
 
+    def cancel(self, ticket: int) -> None:
+        """tcs_server_cancel: the ticket ends failed with TCS_ERR_CANCELLED."""
+        _check(lib().tcs_server_cancel(self._h, ticket))
+
     def times(self, ticket: int):
         """(submitted, admitted, completed) on the server clock, seconds."""
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
@@ -605,6 +619,42 @@ class Server:
         _check(lib().tcs_server_get_stats(self._h, ctypes.byref(o)))
         return {k: (list(getattr(o, k)) if k.startswith(("sched_", "launch_")) else getattr(o, k))
                 for k, _ in ServerStats._fields_}
+
+
+_hook_ref = None  # the installed allocation hook's ctypes callback, kept alive
+
+
+def set_alloc_hook(fn) -> None:
+    """tcs_set_alloc_hook: fn(bytes, what) -> True to fail that allocation
+    (TCS_ERR_NOMEM from the call that needed it); None removes the hook."""
+    global _hook_ref
+    if fn is None:
+        _check(lib().tcs_set_alloc_hook(ALLOC_HOOK(), None))
+        _hook_ref = None
+        return
+    cb = ALLOC_HOOK(lambda n, what, user: 1 if fn(int(n), what.decode()) else 0)
+    _check(lib().tcs_set_alloc_hook(cb, None))
+    _hook_ref = cb
+
+
+def set_guard_bytes(n: int) -> None:
+    """tcs_set_guard_bytes: canary regions of n bytes (rounded up to 256)
+    around allocations made from now on; 0 turns them off."""
+    _check(lib().tcs_set_guard_bytes(int(n)))
+
+
+def guard_check() -> int:
+    """tcs_guard_check: the number of guard regions found changed (0: none)."""
+    n = ctypes.c_longlong()
+    _check(lib().tcs_guard_check(ctypes.byref(n)))
+    return n.value
+
+
+def alloc_stats():
+    """tcs_alloc_stats: (live allocations, live bytes) of the library."""
+    c, b = ctypes.c_longlong(), ctypes.c_size_t()
+    _check(lib().tcs_alloc_stats(ctypes.byref(c), ctypes.byref(b)))
+    return c.value, b.value
 
 
 def sweep_host(h_in: np.ndarray, steps: int, stencil: str, coeffs, engine: str = "tensor",

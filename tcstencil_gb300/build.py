@@ -23,7 +23,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT = os.path.join(PKG, "_build")
 
-CU_SOURCES = ["layout.cu", "sweep_cc.cu", "sweep_tc.cu", "api.cu", "sweep_noalloc.cu", "batch.cu", "server.cu", "sweep_tb.cu", "drift.cu"]
+CU_SOURCES = ["layout.cu", "sweep_cc.cu", "sweep_tc.cu", "api.cu", "sweep_noalloc.cu", "batch.cu", "server.cu", "sweep_tb.cu", "drift.cu", "memory.cu"]
 HEADERS = ["tcs_device.cuh", "tcs_internal.h", "tc_core.cuh", "batch.h", "tile_walk.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-Wall",

@@ -150,6 +150,7 @@ const char *tcs_status_string(int status) {
     case TCS_ERR_UNSUPPORTED: return "unsupported";
     case TCS_ERR_NOMEM: return "out of device memory";
     case TCS_ERR_TIMEOUT: return "device wait timed out";
+    case TCS_ERR_CANCELLED: return "cancelled";
     default: return "unknown status";
     }
 }
@@ -235,12 +236,12 @@ int tcs_max_abs_f32(const float *d_in, size_t n, float *h_max, void *stream) {
     if (!d_in || !h_max) return fail(TCS_ERR_INVALID, "tcs_max_abs_f32: null argument");
     cudaStream_t s = (cudaStream_t)stream;
     unsigned *d = nullptr, bits = 0;
-    int st = cuda_status(cudaMalloc(&d, sizeof(unsigned)), "cudaMalloc(max)");
+    int st = dev_alloc_t(&d, sizeof(unsigned), "max");
     if (!st) st = cuda_status(cudaMemsetAsync(d, 0, sizeof(unsigned), s), "memset(max)");
     if (!st) st = cuda_status(launch_max_abs(d_in, n, d, s), "max_abs launch");
     if (!st) st = cuda_status(cudaMemcpyAsync(&bits, d, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "max copy");
     if (!st) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-    if (d) cudaFree(d);
+    if (d) dev_free(d);
     if (!st) std::memcpy(h_max, &bits, sizeof(float));
     return st;
 }
@@ -366,11 +367,11 @@ struct tcs_plan_s {
         drop_graphs();
         for (auto &s : buf)
             for (auto &p : s)
-                if (p) cudaFree(p);
-        if (staging) cudaFree(staging);
-        if (d_max) cudaFree(d_max);
-        if (d_scale) cudaFree(d_scale);
-        if (rows_done) cudaFree(rows_done);
+                if (p) dev_free(p);
+        if (staging) dev_free(staging);
+        if (d_max) dev_free(d_max);
+        if (d_scale) dev_free(d_scale);
+        if (rows_done) dev_free(rows_done);
         if (capture_stream) cudaStreamDestroy(capture_stream);
     }
 
@@ -479,8 +480,7 @@ namespace {
 
 int ensure_staging(tcs_plan p) {
     if (p->staging) return TCS_OK;
-    return cuda_status(cudaMalloc(&p->staging, (size_t)p->prob.ny * p->prob.nx * sizeof(float)),
-                       "cudaMalloc(staging)");
+    return dev_alloc_t(&p->staging, (size_t)p->prob.ny * p->prob.nx * sizeof(float), "staging");
 }
 
 }  // namespace
@@ -507,12 +507,12 @@ int tcs_plan_create(const tcs_problem *pr, tcs_plan *out) {
     // zero band entry times a NaN would still poison an MMA sum.
     for (int s = 0; s < 2; s++)
         for (int pl = 0; pl < p->planes(); pl++) {
-            st = cuda_status(cudaMalloc(&p->buf[s][pl], p->plane_bytes), "cudaMalloc(plane)");
+            st = dev_alloc_t(&p->buf[s][pl], p->plane_bytes, "plane");
             if (!st) st = cuda_status(cudaMemset(p->buf[s][pl], 0, p->plane_bytes), "cudaMemset(plane)");
             if (st) return st;
         }
     if (pr->precision == TCS_PREC_SPLIT) {
-        st = cuda_status(cudaMalloc(&p->d_scale, sizeof(SplitScale)), "cudaMalloc(scale)");
+        st = dev_alloc_t(&p->d_scale, sizeof(SplitScale), "scale");
         if (!st) st = cuda_status(cudaMemset(p->d_scale, 0, sizeof(SplitScale)), "cudaMemset(scale)");
         if (st) return st;
     }
@@ -521,8 +521,7 @@ int tcs_plan_create(const tcs_problem *pr, tcs_plan *out) {
         if (st) return st;
         {
             const int tiles_y = (pr->ny + kTile - 1) / kTile;
-            st = cuda_status(cudaMalloc(&p->rows_done, (size_t)tiles_y * kRowCounterStride * sizeof(unsigned)),
-                             "cudaMalloc(rows)");
+            st = dev_alloc_t(&p->rows_done, (size_t)tiles_y * kRowCounterStride * sizeof(unsigned), "row counters");
             if (st) return st;
         }
     }
@@ -567,7 +566,7 @@ int tcs_plan_upload(tcs_plan p, const float *grid, int on_host, void *stream) {
         // scale so that max |x| 2^-E < 1, all on the device: the maximum, the
         // packing with its exponent, and the scale record's starting history
         int st = TCS_OK;
-        if (!p->d_max) st = cuda_status(cudaMalloc(&p->d_max, sizeof(unsigned)), "cudaMalloc(max)");
+        if (!p->d_max) st = dev_alloc_t(&p->d_max, sizeof(unsigned), "max");
         if (!st) st = cuda_status(cudaMemsetAsync(p->d_max, 0, sizeof(unsigned), s), "memset(max)");
         if (!st) st = cuda_status(launch_max_abs(src, (size_t)p->prob.ny * p->prob.nx, p->d_max, s), "max_abs launch");
         if (!st)
@@ -862,15 +861,15 @@ int tcs_host_code(float *h_A, float *h_B, float *h_C, int N, int n, int stencil,
     uint16_t *d_A = nullptr, *d_C = nullptr;
     cudaEvent_t start = nullptr, stop = nullptr;
     auto cleanup = [&]() {
-        if (d_f32) cudaFree(d_f32);
-        if (d_A) cudaFree(d_A);
-        if (d_C) cudaFree(d_C);
+        if (d_f32) dev_free(d_f32);
+        if (d_A) dev_free(d_A);
+        if (d_C) dev_free(d_C);
         if (start) cudaEventDestroy(start);
         if (stop) cudaEventDestroy(stop);
     };
-    st = cuda_status(cudaMalloc(&d_f32, cells * sizeof(float)), "Failed to allocate device memory for A");
-    if (!st) st = cuda_status(cudaMalloc(&d_A, plane), "Failed to allocate device memory for A");
-    if (!st) st = cuda_status(cudaMalloc(&d_C, plane), "Failed to allocate device memory for C");
+    st = dev_alloc_t(&d_f32, cells * sizeof(float), "Failed to allocate device memory for A");
+    if (!st) st = dev_alloc_t(&d_A, plane, "Failed to allocate device memory for A");
+    if (!st) st = dev_alloc_t(&d_C, plane, "Failed to allocate device memory for C");
     if (!st) st = cuda_status(cudaMemset(d_C, 0, plane), "cudaMemset(C)");
     if (!st) st = cuda_status(cudaMemcpy(d_f32, h_A, cells * sizeof(float), cudaMemcpyHostToDevice), "H2D copy of A");
     // array_float2half + padding_2D(pad 16, value 1.0) + brick_layout_2D

@@ -781,6 +781,7 @@ struct tcs_batch_s {
     std::vector<Entry> entries;
     uint16_t *pool = nullptr;
     size_t pool_elems = 0;
+    std::vector<uint16_t *> guards;  // guard regions between the planes (guard mode)
     // all grids, FP16 ones first then split ones, each part sorted by steps
     // (descending); one launch per part
     BatchGrid *d_grids = nullptr;
@@ -808,11 +809,13 @@ struct tcs_batch_s {
     ~tcs_batch_s() {
         if (graph) cudaGraphExecDestroy(graph);
         if (capture_stream) cudaStreamDestroy(capture_stream);
+        if (!guards.empty()) cudaDeviceSynchronize();
+        for (uint16_t *g : guards) guard_forget(g, true);
         for (void *p : {(void *)pool, (void *)d_grids, (void *)d_maps, (void *)part[0].d_layout,
                         (void *)part[0].d_counters, (void *)part[1].d_layout,
                         (void *)part[1].d_counters, (void *)d_bands, (void *)d_coefs,
                         (void *)d_staging, (void *)d_max, (void *)d_scales})
-            if (p) cudaFree(p);
+            if (p) dev_free(p);
     }
 
     int state_of(const Entry &e) const { return (runs * (e.steps & 1)) & 1; }
@@ -823,7 +826,10 @@ namespace {
 int batch_build(tcs_batch b) {
     if (b->built) return TCS_OK;
     if (b->entries.empty()) return fail(TCS_ERR_INVALID, "tcs_batch: no grids");
-    // device plane pool (zeroed: padding must be finite)
+    // device plane pool (zeroed: padding must be finite); in guard mode a
+    // guard region before every plane and after the last
+    const size_t gel = guard_bytes() / sizeof(uint16_t);
+    std::vector<size_t> gaps;
     size_t total = 0;
     for (auto &e : b->entries)
         for (int s = 0; s < 2; s++)
@@ -832,12 +838,24 @@ int batch_build(tcs_batch b) {
                     e.offset[s][pl] = 0;
                     continue;
                 }
+                if (gel) {
+                    gaps.push_back(total);
+                    total += gel;
+                }
                 e.offset[s][pl] = total;
                 total += (e.plane_elems + 127) / 128 * 128;  // 256-byte aligned planes
             }
-    int st = cuda_status(cudaMalloc(&b->pool, total * sizeof(uint16_t)), "cudaMalloc(batch planes)");
+    if (gel) {
+        gaps.push_back(total);
+        total += gel;
+    }
+    int st = dev_alloc_t(&b->pool, total * sizeof(uint16_t), "batch planes");
     if (!st) st = cuda_status(cudaMemset(b->pool, 0, total * sizeof(uint16_t)), "cudaMemset(batch planes)");
-    if (!st) st = cuda_status(cudaMalloc(&b->d_scales, b->entries.size() * sizeof(SplitScale)), "cudaMalloc(scales)");
+    for (size_t k = 0; k < gaps.size() && !st; k++) {
+        st = guard_place(b->pool + gaps[k], gel * sizeof(uint16_t), "batch plane guard", 0);
+        if (!st) b->guards.push_back(b->pool + gaps[k]);
+    }
+    if (!st) st = dev_alloc_t(&b->d_scales, b->entries.size() * sizeof(SplitScale), "scales");
     if (!st) st = cuda_status(cudaMemset(b->d_scales, 0, b->entries.size() * sizeof(SplitScale)), "cudaMemset(scales)");
     if (st) return st;
     b->pool_elems = total;
@@ -904,23 +922,23 @@ int batch_build(tcs_batch b) {
                                                layout.data() + P.n_steps + 1);
         if (n_items < 0) return fail(TCS_ERR_INVALID, "tcs_batch: more than 2^31 work items per run");
         P.n_items = (int)n_items;
-        st = cuda_status(cudaMalloc(&P.d_layout, layout.size() * sizeof(int)), "cudaMalloc(layout)");
-        if (!st) st = cuda_status(cudaMalloc(&P.d_counters, (size_t)(P.n_counters + 2) * kRowCounterStride * sizeof(unsigned)), "cudaMalloc(counters)");
+        st = dev_alloc_t(&P.d_layout, layout.size() * sizeof(int), "layout");
+        if (!st) st = dev_alloc_t(&P.d_counters, (size_t)(P.n_counters + 2) * kRowCounterStride * sizeof(unsigned), "counters");
         if (!st) st = cuda_status(cudaMemcpy(P.d_layout, layout.data(), layout.size() * sizeof(int), cudaMemcpyHostToDevice), "layout copy");
         if (st) return st;
     }
     // tensor maps of every grid's planes, then the descriptors that point at them
     std::vector<CUtensorMap> maps(4 * grids.size());
-    st = cuda_status(cudaMalloc(&b->d_maps, maps.size() * sizeof(CUtensorMap)), "cudaMalloc(maps)");
+    st = dev_alloc_t(&b->d_maps, maps.size() * sizeof(CUtensorMap), "maps");
     for (size_t i = 0; i < grids.size() && !st; i++) {
         st = cuda_status(encode_grid_maps(grids[i], &maps[4 * i]), "tensor map encode");
         grids[i].maps = b->d_maps + 4 * i;
     }
     if (!st) st = cuda_status(cudaMemcpy(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "maps copy");
     if (st) return st;
-    st = cuda_status(cudaMalloc(&b->d_grids, grids.size() * sizeof(BatchGrid)), "cudaMalloc(grids)");
-    if (!st) st = cuda_status(cudaMalloc(&b->d_bands, std::max(band, 1) * sizeof(uint16_t)), "cudaMalloc(bands)");
-    if (!st) st = cuda_status(cudaMalloc(&b->d_coefs, coefs.size() * sizeof(float)), "cudaMalloc(coefs)");
+    st = dev_alloc_t(&b->d_grids, grids.size() * sizeof(BatchGrid), "grids");
+    if (!st) st = dev_alloc_t(&b->d_bands, std::max(band, 1) * sizeof(uint16_t), "bands");
+    if (!st) st = dev_alloc_t(&b->d_coefs, coefs.size() * sizeof(float), "coefs");
     if (!st) st = cuda_status(cudaMemcpy(b->d_grids, grids.data(), grids.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice), "grids copy");
     if (!st) st = cuda_status(cudaMemcpy(b->d_coefs, coefs.data(), coefs.size() * sizeof(float), cudaMemcpyHostToDevice), "coefs copy");
     if (st) return st;
@@ -963,10 +981,10 @@ int batch_enqueue(tcs_batch b, cudaStream_t s) {
 
 int ensure_staging(tcs_batch b, size_t elems) {
     if (b->staging_elems >= elems) return TCS_OK;
-    if (b->d_staging) cudaFree(b->d_staging);
+    if (b->d_staging) dev_free(b->d_staging);
     b->d_staging = nullptr;
     b->staging_elems = 0;
-    int st = cuda_status(cudaMalloc(&b->d_staging, elems * sizeof(float)), "cudaMalloc(staging)");
+    int st = dev_alloc_t(&b->d_staging, elems * sizeof(float), "staging");
     if (!st) b->staging_elems = elems;
     return st;
 }
@@ -1027,7 +1045,7 @@ int tcs_batch_upload(tcs_batch b, int index, const float *grid, int on_host, voi
     if (e.prob.precision == TCS_PREC_SPLIT) {
         // scale so that max |x| 2^-E < 1, on the device: the maximum, the
         // packing with its exponent, and the scale record's starting history
-        if (!b->d_max) st = cuda_status(cudaMalloc(&b->d_max, sizeof(unsigned)), "cudaMalloc(max)");
+        if (!b->d_max) st = dev_alloc_t(&b->d_max, sizeof(unsigned), "max");
         if (!st) st = cuda_status(cudaMemsetAsync(b->d_max, 0, sizeof(unsigned), s), "memset(max)");
         if (!st) st = cuda_status(launch_max_abs(src, cells, b->d_max, s), "max_abs launch");
         if (!st) st = cuda_status(launch_pack_split_dev(src, e.g.ny, e.g.nx, b->d_max, nullptr, hi,

@@ -83,7 +83,7 @@ struct tcs_drift_s {
     float *staging = nullptr;
     ~tcs_drift_s() {
         for (void *p : {(void *)buf[0], (void *)buf[1], (void *)d_acc, (void *)staging})
-            if (p) cudaFree(p);
+            if (p) dev_free(p);
     }
 };
 
@@ -104,8 +104,8 @@ int tcs_drift_create(const tcs_problem *pr, tcs_drift *out) {
         d->taps.c[k] = (double)pr->coeffs[(d->taps.dy[k] + r) * n + d->taps.dx[k] + r];
     }
     const size_t bytes = (size_t)pr->ny * pr->nx * sizeof(double);
-    for (int s = 0; s < 2 && !st; s++) st = cuda_status(cudaMalloc(&d->buf[s], bytes), "cudaMalloc(drift)");
-    if (!st) st = cuda_status(cudaMalloc(&d->d_acc, 3 * sizeof(double)), "cudaMalloc(drift acc)");
+    for (int s = 0; s < 2 && !st; s++) st = dev_alloc_t(&d->buf[s], bytes, "drift");
+    if (!st) st = dev_alloc_t(&d->d_acc, 3 * sizeof(double), "drift acc");
     if (st) return st;
     *out = d.release();
     return TCS_OK;
@@ -123,7 +123,7 @@ int tcs_drift_upload(tcs_drift d, const float *grid, int grid_on_host, void *str
     const float *src = grid;
     int st = TCS_OK;
     if (grid_on_host) {
-        if (!d->staging) st = cuda_status(cudaMalloc(&d->staging, n * sizeof(float)), "cudaMalloc(drift staging)");
+        if (!d->staging) st = dev_alloc_t(&d->staging, n * sizeof(float), "drift staging");
         if (!st) st = cuda_status(cudaMemcpyAsync(d->staging, grid, n * sizeof(float), cudaMemcpyHostToDevice, s), "drift upload");
         if (st) return st;
         src = d->staging;

@@ -118,12 +118,20 @@ struct Request {
     const float *h_in = nullptr;
     float *h_out = nullptr;
     size_t plane_bytes = 0, bytes = 0, off = 0;
+    size_t guard = 0;  // guard mode: canary bytes before and after the request's memory
     int slot = -1;
     bool waited = false;  // the compute stream already waits on `ready`
     cudaEvent_t ready = nullptr;  // upload and pack done
     cudaEvent_t done = nullptr;   // result and error word in host memory
     int state = kQueued;  // guarded by the server mutex
     int status = TCS_OK;
+    // Cancellation of a resident request (tcs_server_cancel): asked by the
+    // caller; the scheduler leaves it out of later rounds and retires it once
+    // its last round (last_round, a round index) and its upload are done.
+    std::atomic<bool> cancel{false};
+    bool finishing = false;     // its download is enqueued (guarded by mu)
+    bool cancel_done = false;   // scheduler thread only
+    long long last_round = -1;  // scheduler thread only
     double t_submit = 0, t_admit = 0, t_done = 0;
     long long updates() const {
         return (long long)(g.y1 - g.y0) * (g.x1 - g.x0) * steps;
@@ -170,6 +178,7 @@ struct tcs_server_s {
         bool pending = false;
     } rb[2];
     long long round_idx = 0;
+    long long rounds_done = 0;  // scheduler thread only: rounds seen complete, in order
 
     std::mutex mu;
     std::condition_variable cv_sched, cv_done;
@@ -186,7 +195,7 @@ struct tcs_server_s {
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
 
     // stats, guarded by mu
-    long long submitted = 0, completed = 0, failed = 0, rounds = 0;
+    long long submitted = 0, completed = 0, failed = 0, rounds = 0, cancelled = 0;
     long long point_updates = 0, alg_bytes = 0;
     double busy_s = 0.0;
     int n_active = 0;
@@ -195,10 +204,10 @@ struct tcs_server_s {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     uint16_t *plane(const Request *q, int s, int pl) const {
-        return reinterpret_cast<uint16_t *>(pool + q->off + (size_t)(2 * s + pl) * q->plane_bytes);
+        return reinterpret_cast<uint16_t *>(pool + q->off + q->guard + (size_t)(2 * s + pl) * q->plane_bytes);
     }
     float *staging(const Request *q) const {
-        return reinterpret_cast<float *>(pool + q->off + 4 * q->plane_bytes);
+        return reinterpret_cast<float *>(pool + q->off + q->guard + 4 * q->plane_bytes);
     }
 
     void loop();
@@ -206,6 +215,7 @@ struct tcs_server_s {
     void admit();
     void poll_rounds();
     bool poll_downloads();
+    bool retire_cancelled();
     bool launch_round();
     cudaEvent_t take_event();
     int finish(Request *q, int cur, bool wait_round, cudaEvent_t round_end);
@@ -222,7 +232,7 @@ int grow_pinned(T **h, size_t *cap, size_t want, Retired &ret) {
     if (*cap >= want) return TCS_OK;
     const size_t n = std::max(want, *cap * 2);
     T *p = nullptr;
-    int st = cuda_status(cudaMallocHost(reinterpret_cast<void **>(&p), n * sizeof(T)), "cudaMallocHost(round)");
+    int st = host_alloc_t(&p, n * sizeof(T), "round");
     if (st) return st;
     if (*h) ret.host.push_back(*h);
     *h = p;
@@ -235,7 +245,7 @@ int grow_device(T **d, size_t *cap, size_t want, Retired &ret) {
     if (*cap >= want) return TCS_OK;
     const size_t n = std::max(want, *cap * 2);
     T *p = nullptr;
-    int st = cuda_status(cudaMalloc(reinterpret_cast<void **>(&p), n * sizeof(T)), "cudaMalloc(round)");
+    int st = dev_alloc_t(&p, n * sizeof(T), "round");
     if (st) return st;
     if (*d) ret.dev.push_back(*d);
     *d = p;
@@ -325,6 +335,11 @@ void tcs_server_s::fail_request(Request *q, int status) {
 void tcs_server_s::reap(std::vector<Request *> &done) {
     for (Request *q : done) {
         if (q->slot >= 0) {
+            if (q->guard) {  // its work is complete; the upload stream may hold its fills
+                cudaStreamSynchronize(upload);
+                guard_forget(pool + q->off, true);
+                guard_forget(pool + q->off + q->bytes - q->guard, true);
+            }
             alloc.release(q->off, q->bytes);
             free_slots.push_back(q->slot);
             q->slot = -1;
@@ -371,6 +386,10 @@ void tcs_server_s::admit() {
         q->slot = free_slots.back();
         free_slots.pop_back();
         active.push_back(q);
+        if (q->guard) {
+            guard_place(pool + off, q->guard, "server request guard", upload);
+            guard_place(pool + off + q->bytes - q->guard, q->guard, "server request guard", upload);
+        }
         {
             std::lock_guard<std::mutex> lk(mu);
             n_active = (int)active.size();
@@ -422,6 +441,7 @@ void tcs_server_s::poll_rounds() {
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, b.start, b.end);
         b.pending = false;
+        rounds_done++;
         std::lock_guard<std::mutex> lk(mu);
         busy_s += ms * 1e-3;
         rounds++;
@@ -436,7 +456,7 @@ bool tcs_server_s::launch_round() {
     if (b.pending) return false;  // its previous round still runs
     std::vector<Request *> part;
     for (Request *q : active)
-        if (q->state == kResident && q->done_steps < q->steps) part.push_back(q);
+        if (q->state == kResident && q->done_steps < q->steps && !q->cancel) part.push_back(q);
     if (part.empty()) return false;
 
     // FP16 grids first, then split grids (one batched launch each), each part
@@ -559,6 +579,7 @@ bool tcs_server_s::launch_round() {
         return true;
     }
     b.pending = true;
+    for (Request *q : part) q->last_round = round_idx;
     round_idx++;
     const double t_enq = now();
     bool waited_round = false;
@@ -566,6 +587,12 @@ bool tcs_server_s::launch_round() {
         Request *q = part[i];
         q->done_steps += run_steps[i];
         if (q->done_steps < q->steps) continue;
+        {
+            // a cancellation asked for before now wins: no download
+            std::lock_guard<std::mutex> lk(mu);
+            if (q->cancel) continue;
+            q->finishing = true;
+        }
         // finished in this round: unpack and download behind it
         const int rs = finish(q, q->done_steps & 1, !waited_round, b.end);
         waited_round = true;
@@ -579,6 +606,31 @@ bool tcs_server_s::launch_round() {
         note_launch(2, t_fin - t_enq);
     }
     return true;
+}
+
+// Retires cancelled resident requests whose rounds and upload are done;
+// true when any was.
+bool tcs_server_s::retire_cancelled() {
+    bool any = false;
+    for (Request *q : active) {
+        if (!q->cancel || q->cancel_done) continue;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            if (q->finishing) continue;  // too late: it completes normally
+        }
+        if (q->last_round >= rounds_done) continue;
+        if (q->ready && cudaEventQuery(q->ready) != cudaSuccess) continue;
+        q->cancel_done = true;
+        any = true;
+        std::lock_guard<std::mutex> lk(mu);
+        q->status = TCS_ERR_CANCELLED;
+        q->state = kFailed;
+        q->t_done = now();
+        finished.push_back(q);
+        cancelled++;
+    }
+    if (any) cv_done.notify_all();
+    return any;
 }
 
 void tcs_server_s::loop() {
@@ -606,6 +658,7 @@ void tcs_server_s::loop() {
         t[2] = now();
         poll_rounds();
         const bool landed = poll_downloads();
+        const bool retired = retire_cancelled();
         t[3] = now();
         const bool launched = launch_round();
         t[4] = now();
@@ -616,7 +669,7 @@ void tcs_server_s::loop() {
                 phase_max[i] = std::max(phase_max[i], t[i + 1] - t[i]);
             }
         }
-        progressed = reaped || landed || launched || active.size() != before;
+        progressed = reaped || landed || retired || launched || active.size() != before;
     }
 }
 
@@ -633,21 +686,18 @@ int tcs_server_create(const tcs_server_config *config, tcs_server *out) {
     if (s->cfg.max_active == 0) s->cfg.max_active = 1024;
     s->cfg.hbm_budget_bytes = align_up(s->cfg.hbm_budget_bytes);
     int st = cuda_status(batch_prepare(&s->sms), "batch kernel set-up");
-    if (!st) st = cuda_status(cudaMalloc(&s->pool, s->cfg.hbm_budget_bytes), "cudaMalloc(server budget)");
-    if (st) {
-        if (st == TCS_ERR_CUDA) return fail(TCS_ERR_NOMEM, "cannot reserve %zu bytes of device memory", s->cfg.hbm_budget_bytes);
-        return st;
-    }
+    if (!st) st = dev_alloc_t(&s->pool, s->cfg.hbm_budget_bytes, "server budget");
+    if (st) return st;
     s->alloc.reset(s->cfg.hbm_budget_bytes);
     const int slots = s->cfg.max_active;
-    if (!st) st = cuda_status(cudaMalloc(&s->d_bands, (size_t)slots * kBatchMaxBandElems * sizeof(uint16_t)), "cudaMalloc(bands)");
-    if (!st) st = cuda_status(cudaMalloc(&s->d_maps, (size_t)slots * 4 * sizeof(CUtensorMap)), "cudaMalloc(maps)");
-    if (!st) st = cuda_status(cudaMallocHost(&s->h_maps, (size_t)slots * 4 * sizeof(CUtensorMap)), "cudaMallocHost(maps)");
-    if (!st) st = cuda_status(cudaMalloc(&s->d_maxbits, slots * sizeof(unsigned)), "cudaMalloc(max)");
-    if (!st) st = cuda_status(cudaMalloc(&s->d_scale, slots * sizeof(SplitScale)), "cudaMalloc(scales)");
-    if (!st) st = cuda_status(cudaMalloc(&s->d_err, sizeof(int)), "cudaMalloc(error)");
+    if (!st) st = dev_alloc_t(&s->d_bands, (size_t)slots * kBatchMaxBandElems * sizeof(uint16_t), "bands");
+    if (!st) st = dev_alloc_t(&s->d_maps, (size_t)slots * 4 * sizeof(CUtensorMap), "maps");
+    if (!st) st = host_alloc_t(&s->h_maps, (size_t)slots * 4 * sizeof(CUtensorMap), "maps");
+    if (!st) st = dev_alloc_t(&s->d_maxbits, slots * sizeof(unsigned), "max");
+    if (!st) st = dev_alloc_t(&s->d_scale, slots * sizeof(SplitScale), "scales");
+    if (!st) st = dev_alloc_t(&s->d_err, sizeof(int), "error");
     if (!st) st = cuda_status(cudaMemset(s->d_err, 0, sizeof(int)), "cudaMemset(error)");
-    if (!st) st = cuda_status(cudaMallocHost(&s->h_slot_err, slots * sizeof(int)), "cudaMallocHost(errors)");
+    if (!st) st = host_alloc_t(&s->h_slot_err, slots * sizeof(int), "errors");
     if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking), "cudaStreamCreate");
     if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->upload, cudaStreamNonBlocking), "cudaStreamCreate");
     if (!st) st = cuda_status(cudaStreamCreateWithFlags(&s->download, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -698,22 +748,22 @@ int tcs_server_destroy(tcs_server s) {
     for (auto &b : s->rb) {
         if (b.start) cudaEventDestroy(b.start);
         if (b.end) cudaEventDestroy(b.end);
-        if (b.h_grids) cudaFreeHost(b.h_grids);
-        if (b.h_layout) cudaFreeHost(b.h_layout);
+        if (b.h_grids) host_free(b.h_grids);
+        if (b.h_layout) host_free(b.h_layout);
         for (void *p : {(void *)b.d_grids, (void *)b.d_layout, (void *)b.d_counters})
-            if (p) cudaFree(p);
+            if (p) dev_free(p);
     }
     for (auto &kv : s->tickets)
         for (cudaEvent_t e : {kv.second->ready, kv.second->done})
             if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
-    for (void *p : s->retired.host) cudaFreeHost(p);
-    for (void *p : s->retired.dev) cudaFree(p);
+    for (void *p : s->retired.host) host_free(p);
+    for (void *p : s->retired.dev) dev_free(p);
     for (void *p : {(void *)s->pool, (void *)s->d_bands, (void *)s->d_maps, (void *)s->d_maxbits,
                     (void *)s->d_scale, (void *)s->d_err})
-        if (p) cudaFree(p);
-    if (s->h_slot_err) cudaFreeHost(s->h_slot_err);
-    if (s->h_maps) cudaFreeHost(s->h_maps);
+        if (p) dev_free(p);
+    if (s->h_slot_err) host_free(s->h_slot_err);
+    if (s->h_maps) host_free(s->h_maps);
     if (s->compute) cudaStreamDestroy(s->compute);
     if (s->upload) cudaStreamDestroy(s->upload);
     if (s->download) cudaStreamDestroy(s->download);
@@ -743,7 +793,8 @@ int tcs_server_submit(tcs_server s, const tcs_problem *pr, int steps, const floa
     q->h_out = h_out;
     q->srv = s;
     q->plane_bytes = align_up(plane_elems(q->g.p16) * sizeof(uint16_t));
-    q->bytes = 4 * q->plane_bytes + align_up((size_t)q->g.ny * q->g.nx * sizeof(float));
+    q->guard = guard_bytes();
+    q->bytes = 4 * q->plane_bytes + align_up((size_t)q->g.ny * q->g.nx * sizeof(float)) + 2 * q->guard;
     if (q->bytes > s->cfg.hbm_budget_bytes)
         return fail(TCS_ERR_NOMEM, "request needs %zu bytes, the server budget is %zu", q->bytes, s->cfg.hbm_budget_bytes);
     {
@@ -783,6 +834,30 @@ int tcs_server_wait(tcs_server s, long long ticket, double timeout_s) {
     return q->state == kDone ? TCS_OK : q->status;
 }
 
+int tcs_server_cancel(tcs_server s, long long ticket) {
+    if (!s) return fail(TCS_ERR_INVALID, "tcs_server_cancel: null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return fail(TCS_ERR_INVALID, "unknown ticket %lld", ticket);
+    Request *q = it->second.get();
+    if (q->state == kDone || q->state == kFailed || q->finishing || q->cancel)
+        return fail(TCS_ERR_INVALID, "ticket %lld is finished, finishing or already cancelled", ticket);
+    if (q->state == kQueued) {  // never admitted: nothing of it is on the device
+        s->queued.erase(std::find(s->queued.begin(), s->queued.end(), q));
+        q->status = TCS_ERR_CANCELLED;
+        q->state = kFailed;
+        q->t_done = s->now();
+        s->finished.push_back(q);
+        s->cancelled++;
+        s->cv_done.notify_all();
+    } else {
+        q->cancel = true;
+        s->new_work = true;
+    }
+    s->cv_sched.notify_one();
+    return TCS_OK;
+}
+
 int tcs_server_times(tcs_server s, long long ticket, double *submitted, double *admitted,
                      double *completed) {
     if (!s) return fail(TCS_ERR_INVALID, "tcs_server_times: null server");
@@ -811,6 +886,7 @@ int tcs_server_get_stats(tcs_server s, tcs_server_stats *o) {
     o->peak_bytes_in_use = s->peak_bytes;
     o->active = s->n_active;
     o->queued = (int)s->queued.size();
+    o->cancelled = s->cancelled;
     for (int i = 0; i < 4; i++) {
         o->sched_total_s[i] = s->phase_total[i];
         o->sched_max_s[i] = s->phase_max[i];

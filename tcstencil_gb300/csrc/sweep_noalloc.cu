@@ -26,8 +26,12 @@ namespace {
 // 32 MiB: one FP16 plane of up to 16,777,216 cells, padding included
 // (tcs_plane_elems gives a grid's plane size): square grids up to 3968 x 3968.
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+// Room for guard regions (guard mode, tcs_set_guard_bytes): before the
+// plane, and after it when a call uses all of it.
+constexpr size_t kScratchGuard = 4096;
 
-static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static __device__ __align__(256) unsigned char
+    g_noalloc_scratch[kScratchGuard + kNoAllocScratchBytes + kScratchGuard];
 
 // Device address of g_noalloc_scratch per device ordinal, looked up once per
 // device with that device current.  (In host code the array's name is only a
@@ -37,8 +41,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 void *g_scratch_ptr[kMaxDevices] = {};
+void *g_scratch_tail[kMaxDevices] = {};  // guard mode: the last call's trailing guard
 
-int scratch_for_current_device(void **out) {
+int scratch_for_current_device(void **out, int *dev_out) {
     int dev = 0;
     int st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
     if (st) return st;
@@ -52,7 +57,24 @@ int scratch_for_current_device(void **out) {
         g_scratch_ptr[dev] = p;
     }
     *out = g_scratch_ptr[dev];
+    *dev_out = dev;
     return TCS_OK;
+}
+
+// Guard mode: canary before the scratch plane and right after the part of
+// it this call uses, filled on the call's stream (the previous call's
+// trailing region is dropped unchecked: this call's plane may cover it).
+int place_scratch_guards(unsigned char *base, int dev, size_t plane_bytes, cudaStream_t s) {
+    if (!guard_bytes()) return TCS_OK;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (g_scratch_tail[dev]) guard_forget(g_scratch_tail[dev], false);
+    g_scratch_tail[dev] = nullptr;
+    int st = guard_place(base, kScratchGuard, "no-alloc scratch guard", s);
+    if (st) return st;
+    unsigned char *tail = base + kScratchGuard + plane_bytes;
+    st = guard_place(tail, kScratchGuard, "no-alloc scratch guard", s);
+    if (!st) g_scratch_tail[dev] = tail;
+    return st;
 }
 
 }  // namespace
@@ -88,8 +110,12 @@ int tcs_sweep_steps_noalloc(const tcs_step_args *a, const void *d_in, void *d_ou
     if (steps == 0)
         return cuda_status(cudaMemcpyAsync(d_out, d_in, plane_bytes, cudaMemcpyDeviceToDevice, s),
                            "no-alloc copy");
-    void *scratch = nullptr;
-    st = scratch_for_current_device(&scratch);
+    void *scratch_base = nullptr;
+    int dev = 0;
+    st = scratch_for_current_device(&scratch_base, &dev);
+    if (st) return st;
+    void *scratch = static_cast<unsigned char *>(scratch_base) + kScratchGuard;
+    st = place_scratch_guards(static_cast<unsigned char *>(scratch_base), dev, plane_bytes, s);
     if (st) return st;
     if (a->engine == TCS_ENGINE_TENSOR) {
         st = cuda_status(tc_prepare(a->stencil, false), "tensor kernel set-up");

@@ -103,6 +103,31 @@ int fail(int status, const char *fmt, ...);
 // Maps a CUDA runtime error to TCS_ERR_CUDA with a message (TCS_OK if none).
 int cuda_status(cudaError_t e, const char *what);
 
+// The library's device and pinned-host allocations (memory.cu): the
+// allocation hook and guard regions of include/tcs.h apply to them.  A
+// failure returns TCS_ERR_NOMEM (or TCS_ERR_CUDA) with *p null and the
+// message naming `what`.
+int dev_alloc(void **p, size_t bytes, const char *what);
+int host_alloc(void **p, size_t bytes, const char *what);
+void dev_free(void *p);
+void host_free(void *p);
+// Guard regions inside the library's own memory: the guard size in force
+// (0: off); guard_place fills bytes at p with the canary on stream s and
+// has tcs_guard_check watch them; guard_forget stops watching, after
+// comparing them with the canary (check; the work that touched them must be
+// complete) and counting a damaged region.
+size_t guard_bytes();
+int guard_place(void *p, size_t bytes, const char *what, cudaStream_t s);
+void guard_forget(void *p, bool check);
+template <typename T>
+int dev_alloc_t(T **p, size_t bytes, const char *what) {
+    return dev_alloc(reinterpret_cast<void **>(p), bytes, what);
+}
+template <typename T>
+int host_alloc_t(T **p, size_t bytes, const char *what) {
+    return host_alloc(reinterpret_cast<void **>(p), bytes, what);
+}
+
 // Fills `geom` (validating the rectangle) for a stencil; returns a status.
 int make_geom(int ny, int nx, int stencil, int y0, int y1, int x0, int x1, GridGeom *geom);
 // Gold's coefficients for a stencil from an n x n row-major matrix.

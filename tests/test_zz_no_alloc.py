@@ -100,3 +100,38 @@ def test_noalloc_rejects_grids_beyond_the_static_scratch(tcs, torch_cuda):
     B = normalized_coeffs(rng, "box2d1r")
     got = noalloc16(tcs, torch, oracle.f32_to_f16(A), B, "box2d1r", 3, "tensor")
     np.testing.assert_array_equal(got, plan_result16(tcs, A, B, "box2d1r", 3, "tensor"))
+
+
+def test_noalloc_writes_stay_inside_the_planes(tcs, torch_cuda):
+    """Guard regions: canary bytes around the caller's input and output
+    planes, and (guard mode) the library's canaries before the shared scratch
+    plane and after the part of it each call uses, stay intact over calls of
+    growing and shrinking shapes on both engines; the results keep the plan
+    path's bits."""
+    torch = torch_cuda
+    rng = np.random.default_rng(80)
+    G = 4096
+    tcs.set_guard_bytes(G)
+    try:
+        cases = [("box2d2r", (300, 411), 5, "tensor"), ("star2d1r", (1030, 130), 4, "tensor"),
+                 ("box2d1r", (129, 131), 3, "cudacore"), ("star2d2r", (257, 190), 6, "tensor")]
+        for stencil, (ny, nx), steps, engine in cases:
+            A = grid(rng, ny, nx)
+            B = normalized_coeffs(rng, stencil)
+            p16 = plane16(torch, oracle.f32_to_f16(A))
+            n = p16.numel() * 2
+            bufs = [torch.full((G + n + G,), 0xA5, dtype=torch.uint8, device="cuda") for _ in range(2)]
+            bufs[0][G:G + n].copy_(p16.view(torch.uint8))
+            tcs.sweep_steps_noalloc(bufs[0].data_ptr() + G, bufs[1].data_ptr() + G, ny, nx, stencil,
+                                    B, steps, engine=engine)
+            torch.cuda.synchronize()
+            assert tcs.device_error() == 0
+            for k, b in enumerate(bufs):
+                for part in (b[:G], b[G + n:]):
+                    assert bool((part == 0xA5).all()), f"caller guard of plane {k}, {stencil} {ny}x{nx}"
+            assert tcs.guard_check() == 0, tcs.lib().tcs_last_error().decode()
+            out = bufs[1][G:G + n].view(torch.int16)
+            np.testing.assert_array_equal(grid16(out, ny, nx),
+                                          plan_result16(tcs, A, B, stencil, steps, engine))
+    finally:
+        tcs.set_guard_bytes(0)
