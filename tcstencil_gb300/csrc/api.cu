@@ -184,6 +184,9 @@ int tcs_device_error(int *code) {
     st = cuda_status(tb_take_error(&cb), "reading the blocked-sweep error word");
     if (st) return st;
     if (!c) c = cb;
+    st = cuda_status(cc_take_error(&cb), "reading the CUDA-core error word");
+    if (st) return st;
+    if (!c) c = cb;
     if (code) *code = c;
     return c ? fail(TCS_ERR_TIMEOUT, "device wait timed out (code %d)", c) : TCS_OK;
 }

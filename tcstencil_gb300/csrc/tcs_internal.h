@@ -157,6 +157,8 @@ cudaError_t launch_tc_split2(const GridGeom &g, int stencil, const float *B, con
                              const uint16_t *in_lo, uint16_t *out_hi, uint16_t *out_lo,
                              cudaStream_t s, SplitScale *scale = nullptr, int t0 = 0);
 cudaError_t tb_take_error(int *code);
+// Reads and clears the CUDA-core kernels' device error word.
+cudaError_t cc_take_error(int *code);
 // Configures the tensor kernel of (stencil, split) ahead of its first launch.
 cudaError_t tc_prepare(int stencil, bool split);
 
