@@ -5,16 +5,21 @@
 // One thread stages the tile's rows, with four halo rows above and below,
 // and the panel on each side, as 18 bulk copies (a panel's rows are one
 // contiguous run) into shared memory, where runs sit 2192 bytes apart so
-// that the 16 panels of a row fall on different banks.  The copies go by
-// the copy engine, not the load pipeline, which was this kernel's limit
-// when it loaded through L1 (79 % of the L1 throughput at 0.43 of HBM).
-// Four warps then take 32 rows each.  Lane l owns half a panel: cells
-// [x_l, x_l + H) with H = 4 (FP16) or 2 (FP32), 8 bytes of each panel row;
-// horizontal halo cells come from lanes l-1 and l+1 by shuffle (the same
-// shuffle for every lane) and, for the outer lanes, from the side panels'
-// runs.  The vertical taps come from a register window of six rows, two
-// rows per step, and each lane stores its own 8 bytes of both rows.  Five
-// such CTAs fit an SM, so about five tiles' copies are in flight per SM.
+// that the 16 panels of a row fall on different banks.  Four warps then
+// take 32 rows each.  Lane l owns half a panel: cells [x_l, x_l + H) with
+// H = 4 (FP16) or 2 (FP32), 8 bytes of each panel row; horizontal halo
+// cells come from lanes l-1 and l+1 by shuffle (the same shuffle for every
+// lane) and, for the outer lanes, from the side panels' runs.  The vertical
+// taps come from a register window of six rows, two rows per step.  Each
+// warp first reads the rows it shares with its neighbours, then writes its
+// results over its own rows of the stage, and one thread stores the 16
+// panels' rows back with 16 bulk copies.  Both directions go by the copy
+// engine, not the load/store pipeline, which was this kernel's limit when
+// it moved its rows through L1 (79 % of the L1 throughput at 0.43 of HBM;
+// measured on GB300 at 8196², us per step, L1 -> bulk loads -> bulk loads
+// and stores: star2d1r FP16 111.7 -> 73.9 -> 61.4, FP32 182 -> 124 -> 97.6).
+// Five such CTAs fit an SM.  (Persistent CTAs walking tiles through two or
+// three stages measured no faster.)
 //
 // Arithmetic follows gold's tap order (common/gold_*.cpp):
 //  - FP16 storage: acc = fmaf chain from 0, FP32 coefficients, RNE to FP16.
@@ -54,6 +59,21 @@ __device__ __forceinline__ uint2 lds_v2(uint32_t addr) {
     uint2 v;
     asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(addr));
     return v;
+}
+__device__ __forceinline__ void sts_v2(uint32_t addr, uint2 v) {
+    asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(addr), "r"(v.x), "r"(v.y) : "memory");
+}
+// 1-D bulk copy of `bytes` (a multiple of 16) from shared to global memory,
+// both addresses 16-byte aligned, in this thread's bulk group.
+__device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(
+                     reinterpret_cast<uint64_t>(dst)),
+                 "r"(smem_u32(src)), "r"(bytes)
+                 : "memory");
+}
+// Waits until this thread's bulk stores have read their shared memory.
+__device__ __forceinline__ void bulk_store_commit_and_wait_read() {
+    asm volatile("cp.async.bulk.commit_group;\n\tcp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 __device__ __forceinline__ uint32_t lds_u32(uint32_t addr) {
     uint32_t v;
@@ -102,8 +122,8 @@ __global__ void __launch_bounds__(kCcWarps * 32)
                       in + ((ptrdiff_t)(chunk0 + q) * nyp + Y0) * V, kCcRunBytes, bar);
     }
     __syncthreads();
-    if (!mbar_wait(bar, 0, &g_cc_error)) {
-        record_error(&g_cc_error, kErrWaitFull);
+    if (!__syncthreads_and(mbar_wait(bar, 0, &g_cc_error))) {  // every thread leaves, or none
+        if (threadIdx.x == 0) record_error(&g_cc_error, kErrWaitFull);
         return;
     }
 
@@ -114,13 +134,12 @@ __global__ void __launch_bounds__(kCcWarps * 32)
     const int xl = chunk * V + (lane & 1) * H;  // first column this lane computes
     const int ys = Y0 + warp * kCcWarpRows;
     const int ye = min(ys + kCcWarpRows, p.g.ny);
-    if (ys >= p.g.ny) return;
+    const bool has_rows = ys < p.g.ny;  // the same for the whole warp
     // shared address of tile row r (from -4) of this lane's half panel, and of
     // the outer lanes' edge words
     const uint32_t own0 = runs + (1 + (lane >> 1)) * kCcRunStride + 4 * 16 + (lane & 1) * 8;
     const uint32_t edge0 = lane == 0 ? runs + 4 * 16 + (V - HC) * (uint32_t)sizeof(T)
                                      : runs + (kCcPanels + 1) * kCcRunStride + 4 * 16;
-    const ptrdiff_t gbase = ((ptrdiff_t)(chunk + 1) * nyp + 4) * V + (lane & 1) * H;
 
     // Window columns [0, W) of grid row y: cells xl-R .. xl+H+R-1.
     auto to_window = [&](int y, float (&w)[W]) {
@@ -164,66 +183,104 @@ __global__ void __launch_bounds__(kCcWarps * 32)
     // this lane's cells of the update rectangle
     const bool cols_in = xl >= p.g.x0 && xl + H <= p.g.x1;
 
+    // Results go back into the stage, over the rows they replace, and leave
+    // by bulk stores: so each warp first reads the rows it shares with its
+    // neighbours (two above its rows, two below), and only then, after a
+    // barrier, overwrites its own rows.
     // window: pair slot j holds rows (y0-2+2j, y0-1+2j), rotated over steps
     float win[3][2][W];
-    to_window(ys - 2, win[0][0]);
-    to_window(ys - 1, win[0][1]);
-    to_window(ys, win[1][0]);
-    to_window(ys + 1, win[1][1]);
+    float below[2][W];  // rows ye, ye+1
+    if (has_rows) {
+        to_window(ys - 2, win[0][0]);
+        to_window(ys - 1, win[0][1]);
+        to_window(ys, win[1][0]);
+        to_window(ys + 1, win[1][1]);
+        to_window(ye, below[0]);
+        to_window(ye + 1, below[1]);
+    }
+    __syncthreads();
 
-    for (int y = ys; y < ye; y += 6) {
+    if (has_rows) {
+        for (int y = ys; y < ye; y += 6) {
 #pragma unroll
-        for (int u = 0; u < 3; u++) {
-            const int y0 = y + 2 * u;
-            if (y0 < ye) {
-                to_window(y0 + 2, win[(u + 2) % 3][0]);
-                to_window(y0 + 3, win[(u + 2) % 3][1]);
+            for (int u = 0; u < 3; u++) {
+                const int y0 = y + 2 * u;
+                if (y0 < ye) {
+                    float (&n0)[W] = win[(u + 2) % 3][0];
+                    float (&n1)[W] = win[(u + 2) % 3][1];
+                    // rows from ye on belong to the next warp, which may have
+                    // written them by now, unless the grid ends at ye (then
+                    // no warp writes them, and a warp of an odd row count
+                    // reads up to ye + 2)
+                    if (y0 + 2 < ye || ye == p.g.ny) {
+                        to_window(y0 + 2, n0);
+                        to_window(y0 + 3, n1);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < W; k++) {
+                            n0[k] = below[0][k];
+                            n1[k] = below[1][k];
+                        }
+                    }
 
-                float acc[2][H];
+                    float acc[2][H];
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    {
-                        constexpr int dy0 = tap_dy(S, 0), dx0 = tap_dx(S, 0);
-                        const int wr = 2 + q + dy0;  // window row of y0 + q + dy
+                    for (int q = 0; q < 2; q++) {
+                        {
+                            constexpr int dy0 = tap_dy(S, 0), dx0 = tap_dx(S, 0);
+                            const int wr = 2 + q + dy0;  // window row of y0 + q + dy
 #pragma unroll
-                        for (int i = 0; i < H; i++) {
-                            const float x0 = win[(u + wr / 2) % 3][wr % 2][R + i + dx0];
-                            if constexpr (F32) acc[q][i] = BOX ? __fadd_rn(0.0f, __fmul_rn(x0, c.c[0]))
-                                                               : __fmul_rn(x0, c.c[0]);
-                            else acc[q][i] = fmaf(x0, c.c[0], 0.0f);
+                            for (int i = 0; i < H; i++) {
+                                const float x0 = win[(u + wr / 2) % 3][wr % 2][R + i + dx0];
+                                if constexpr (F32) acc[q][i] = BOX ? __fadd_rn(0.0f, __fmul_rn(x0, c.c[0]))
+                                                                   : __fmul_rn(x0, c.c[0]);
+                                else acc[q][i] = fmaf(x0, c.c[0], 0.0f);
+                            }
                         }
-                    }
 #pragma unroll
-                    for (int k = 1; k < NT; k++) {
-                        const int dy = tap_dy(S, k), dx = tap_dx(S, k);
-                        const int wr = 2 + q + dy;
+                        for (int k = 1; k < NT; k++) {
+                            const int dy = tap_dy(S, k), dx = tap_dx(S, k);
+                            const int wr = 2 + q + dy;
 #pragma unroll
-                        for (int i = 0; i < H; i++) {
-                            const float x = win[(u + wr / 2) % 3][wr % 2][R + i + dx];
-                            if constexpr (F32) acc[q][i] = __fadd_rn(acc[q][i], __fmul_rn(x, c.c[k]));
-                            else acc[q][i] = fmaf(x, c.c[k], acc[q][i]);
+                            for (int i = 0; i < H; i++) {
+                                const float x = win[(u + wr / 2) % 3][wr % 2][R + i + dx];
+                                if constexpr (F32) acc[q][i] = __fadd_rn(acc[q][i], __fmul_rn(x, c.c[k]));
+                                else acc[q][i] = fmaf(x, c.c[k], acc[q][i]);
+                            }
                         }
-                    }
-                    // cells outside the update rectangle keep their value
-                    const int yy = y0 + q;
-                    const bool row_in = yy >= p.g.y0 && yy < p.g.y1;
-                    if (!(row_in && cols_in)) {
+                        // cells outside the update rectangle keep their value
+                        const int yy = y0 + q;
+                        const bool row_in = yy >= p.g.y0 && yy < p.g.y1;
+                        if (!(row_in && cols_in)) {
 #pragma unroll
-                        for (int i = 0; i < H; i++) {
-                            const int x = xl + i;
-                            if (!(row_in && x >= p.g.x0 && x < p.g.x1))
-                                acc[q][i] = win[(u + (2 + q) / 2) % 3][(2 + q) % 2][R + i];
+                            for (int i = 0; i < H; i++) {
+                                const int x = xl + i;
+                                if (!(row_in && x >= p.g.x0 && x < p.g.x1))
+                                    acc[q][i] = win[(u + (2 + q) / 2) % 3][(2 + q) % 2][R + i];
+                            }
                         }
-                    }
-                    if (active && yy < ye) {
-                        uint2 v;
-                        if constexpr (F32) v = make_uint2(__float_as_uint(acc[q][0]), __float_as_uint(acc[q][1]));
-                        else v = make_uint2(pack_half2(acc[q][0], acc[q][1]), pack_half2(acc[q][2], acc[q][3]));
-                        *reinterpret_cast<uint2 *>(out + gbase + (ptrdiff_t)yy * V) = v;
+                        if (active && yy < ye) {
+                            uint2 v;
+                            if constexpr (F32) v = make_uint2(__float_as_uint(acc[q][0]), __float_as_uint(acc[q][1]));
+                            else v = make_uint2(pack_half2(acc[q][0], acc[q][1]), pack_half2(acc[q][2], acc[q][3]));
+                            sts_v2(own0 + (uint32_t)(yy - Y0) * 16, v);
+                        }
                     }
                 }
             }
         }
+    }
+    // the stage's rows Y0 .. Y0+127 of the 16 panels (results, and the input
+    // where nothing was computed: rows past the grid, panels past its cells)
+    // to the output plane
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nq = min(kCcPanels + 1, p.p.npan - chunk0);
+        for (int q = 1; q < nq; q++)
+            bulk_store(out + ((ptrdiff_t)(chunk0 + q) * nyp + Y0 + 4) * V,
+                       smem + kCcRunsOffset + q * kCcRunStride + 4 * 16, kCcTileRows * 16);
+        bulk_store_commit_and_wait_read();
     }
 }
 
