@@ -370,6 +370,11 @@ void tcs_server_s::admit() {
         if (!alloc.alloc(q->bytes, &off)) return;  // head of line waits for memory
         {
             std::lock_guard<std::mutex> lk(mu);
+            // tcs_server_cancel may have dropped q since it was looked at
+            if (queued.empty() || queued.front() != q) {
+                alloc.release(off, q->bytes);
+                continue;
+            }
             queued.pop_front();
             q->state = kResident;
             q->t_admit = now();
@@ -616,7 +621,8 @@ bool tcs_server_s::retire_cancelled() {
         if (!q->cancel || q->cancel_done) continue;
         {
             std::lock_guard<std::mutex> lk(mu);
-            if (q->finishing) continue;  // too late: it completes normally
+            // too late (it completes normally), or already ended by a failure
+            if (q->finishing || q->state != kResident) continue;
         }
         if (q->last_round >= rounds_done) continue;
         if (q->ready && cudaEventQuery(q->ready) != cudaSuccess) continue;
