@@ -344,3 +344,47 @@ def test_server_deadline_by_wait_and_cancel(tcs, torch_cuda):
     srv.wait(srv.submit(C, out_c, "star2d1r", B, 13, "split"), 60.0)
     np.testing.assert_array_equal(out_c, plan_bits(tcs, C, B, "star2d1r", 13, "tensor", "split"))
     srv.close()
+
+
+def test_server_cancels_under_load(tcs, torch_cuda):
+    """Cancels racing admission, rounds and downloads: every third of 45
+    mixed requests is cancelled right after submission. A cancel either
+    succeeds (the ticket ends cancelled, its output untouched) or is refused
+    because the request is already finishing (it then completes); every
+    other request keeps its plan-path bits, and the server ends idle."""
+    rng = np.random.default_rng(907)
+    srv = tcs.Server(256 << 20, max_active=6, round_steps=4)
+    base = srv.stats()
+    reqs = []
+    for k in range(45):
+        st = ("star2d1r", "star2d2r", "box2d1r", "box2d2r")[k % 4]
+        prec = "split" if k % 3 == 1 else "f16"
+        A = grid(rng, int(rng.integers(64, 400)), int(rng.integers(64, 400)))
+        B = normalized_coeffs(rng, st)
+        steps = int(rng.integers(5, 60))
+        out = np.full_like(A, np.nan)
+        reqs.append((A, B, st, steps, prec, out, srv.submit(A, out, st, B, steps, prec)))
+    cancelled = set()
+    for k, r in enumerate(reqs):
+        if k % 3 == 0:
+            try:
+                srv.cancel(r[6])
+                cancelled.add(k)
+            except tcs.TcsError as e:
+                assert e.status == tcs.TCS_ERR_INVALID
+    for k, (A, B, st, steps, prec, out, t) in enumerate(reqs):
+        if k in cancelled:
+            with pytest.raises(tcs.TcsError) as e:
+                srv.wait(t, 60.0)
+            assert e.value.status == tcs.TCS_ERR_CANCELLED
+            assert np.all(np.isnan(out))
+        else:
+            srv.wait(t, 60.0)
+            np.testing.assert_array_equal(out, plan_bits(tcs, A, B, st, steps, "tensor", prec),
+                                          err_msg=f"request {k}")
+    s = srv.stats()
+    assert s["cancelled"] - base["cancelled"] == len(cancelled)
+    assert s["completed"] - base["completed"] == len(reqs) - len(cancelled)
+    assert s["active"] == 0 and s["queued"] == 0
+    srv.close()
+    assert tcs.device_error() == 0
