@@ -420,13 +420,14 @@ struct tcs_plan_s {
         if (multistep >= 0) return multistep == 1;
         const long long tiles = this->tiles();
         const long long sms = device_sms();
-        // Split, box2d1r, us per step, one launch per step -> one launch:
-        // 2048² 11.1 -> 8.8, 4096² 30.4 -> 27.1, 8196² 103.3 -> 107.0, 16386²
-        // 379.6 -> 417.5: the multi-step split kernel spends ~10 % more per
-        // tile, which only the mid sizes' step overheads repay (the sweep
-        // harness: 4800², 9.5 tiles per SM, 44.5 us per step in one launch,
-        // slower than 3200² and 7200² per point).
-        if (prob.precision == TCS_PREC_SPLIT) return tiles > sms && tiles <= 8 * sms;
+        // Split, us per step, one launch per step -> one launch (box2d1r /
+        // box2d2r): 2400² 16.5 -> 11.8 / 16.5 -> 12.6, 3200² 22.2 -> 16.3 /
+        // 23.0 -> 17.2, 4800² 51.8 -> 46.2 / 53.0 -> 47.0, 6400² 65.9 -> 60.5
+        // / 66.4 -> 64.3, 8196² 104.0 -> 100.8 / 104.7 -> 107.2, 12000² 206.0
+        // -> 208.9 / 207.5 -> 222.3, 16386² 378.6 -> 391.1 / 380.1 -> 416.9:
+        // the multi-step kernel spends a little more per tile, which the step
+        // overheads repay up to about 20 tiles per SM.
+        if (prob.precision == TCS_PREC_SPLIT) return tiles > sms && tiles <= 20 * sms;
         return tiles > 2 * sms;
     }
     int steps_in_one(int steps, int from, cudaStream_t s) {
