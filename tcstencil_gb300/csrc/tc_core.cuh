@@ -120,6 +120,14 @@ struct AccSlots {
     }
 };
 
+// plane_index of an FP16 (or split) plane, 8 cells per panel row: the
+// panel and the cell in it by shifts, not by a division by the plane's cpp
+// (x >= -8).
+__device__ __forceinline__ size_t plane_index16(const PlaneGeom &p, int y, int x) {
+    const int xs = x + 8;
+    return ((size_t)(xs >> 3) * p.nyp + (size_t)(y + kPadTop)) * 8 + (size_t)(xs & 7);
+}
+
 __device__ __forceinline__ uint16_t h_bits(float v) {
     __half h = __float2half_rn(v);
     return *reinterpret_cast<uint16_t *>(&h);
@@ -620,7 +628,7 @@ __device__ __forceinline__ bool walk_windows(int g, int ng, int nwin, Ready &&re
 template <bool SPLIT>
 __device__ __forceinline__ void store_block(const TileOut &o, const float (&f)[16], int y, int xb,
                                             bool fast, bool row_in) {
-    const size_t off0 = plane_index(o.pg, y, xb);     // cells xb .. xb+7
+    const size_t off0 = plane_index16(o.pg, y, xb);     // cells xb .. xb+7
     const size_t off1 = off0 + (size_t)o.pg.nyp * 8;  // cells xb+8 .. xb+15
     uint32_t hw[8], lw[8];
     if constexpr (SPLIT) {
@@ -698,7 +706,7 @@ __device__ __forceinline__ void resplit_border(const TileOut &o, int y, int X0, 
         for (int hf = 0; hf < 2; hf++) {
             const int xh = xb + 8 * hf;  // a panel row: cells xh .. xh+7
             if (xh >= o.nx || (row_in && xh >= o.x0 && xh + 8 <= o.x1)) continue;
-            const size_t off = plane_index(o.pg, y, xh);
+            const size_t off = plane_index16(o.pg, y, xh);
             const uint4 a = *reinterpret_cast<const uint4 *>(o.in_hi + off);
             const uint4 b = *reinterpret_cast<const uint4 *>(o.in_lo + off);
             uint32_t hw[4] = {a.x, a.y, a.z, a.w}, lw[4] = {b.x, b.y, b.z, b.w};
@@ -733,7 +741,7 @@ __device__ __forceinline__ void resplit_border(const TileOut &o, int y, int X0, 
 __device__ __forceinline__ void store_block_split(const TileOut &o, const float (&f)[16], int y,
                                                   int xb, bool fast, bool row_in,
                                                   const StepScale &ss, float &mx) {
-    const size_t off0 = plane_index(o.pg, y, xb);     // cells xb .. xb+7
+    const size_t off0 = plane_index16(o.pg, y, xb);     // cells xb .. xb+7
     const size_t off1 = off0 + (size_t)o.pg.nyp * 8;  // cells xb+8 .. xb+15
     uint32_t hw[8], lw[8];
     if (fast) {
