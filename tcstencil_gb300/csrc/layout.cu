@@ -36,16 +36,61 @@ __device__ __forceinline__ float padded_cell(const float *in, int ny, int nx, in
     return (iy >= 0 && iy < ny && ix >= 0 && ix < nx) ? in[(size_t)iy * nx + ix] : pad_value;
 }
 
-// A panel row: thread id -> (panel, row) -> first cell (Y, X0).
+// A panel row: thread id -> (plane row, panel) -> first cell (Y, X0) of the
+// padded grid and the row's index q in the plane.  Consecutive threads take
+// consecutive panels of one plane row, so that the row-major FP32 side of a
+// warp's accesses is one contiguous run (the plane side is one 16-byte panel
+// row per thread; the next plane row of a panel follows a few warps later).
 struct PanelRow {
     int Y, X0;
+    size_t q;
 };
 __device__ __forceinline__ PanelRow panel_row(size_t id, const PlaneGeom &p) {
     PanelRow r;
-    const int pan = static_cast<int>(id / p.nyp);
-    r.Y = static_cast<int>(id % p.nyp) - kPadTop;
+    const int yq = static_cast<int>(id / p.npan);
+    const int pan = static_cast<int>(id - (size_t)yq * p.npan);
+    r.Y = yq - kPadTop;
     r.X0 = (pan - 1) * p.cpp;
+    r.q = (size_t)pan * p.nyp + yq;
     return r;
+}
+
+// The N cells (Y, X0 .. X0+N-1) of the padded grid (padded_cell), by 16-byte
+// loads where they are all interior and 16-byte aligned.
+template <int N>
+__device__ __forceinline__ void load_cells(const float *__restrict__ in, int ny, int nx, int pad,
+                                           float pad_value, int Y, int X0, float (&c)[N]) {
+    const int iy = Y - pad, ix = X0 - pad;
+    const size_t e = (size_t)iy * nx + ix;
+    if (iy >= 0 && iy < ny && ix >= 0 && ix + N <= nx && (e & 3) == 0) {
+#pragma unroll
+        for (int k = 0; k < N; k += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(in + e + k);
+            c[k] = v.x; c[k + 1] = v.y; c[k + 2] = v.z; c[k + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++) c[i] = padded_cell(in, ny, nx, pad, pad_value, Y, X0 + i);
+    }
+}
+
+// Stores the grid cells among (Y, X0 .. X0+N-1) of the padded grid into the
+// ny x nx row-major output, by 16-byte stores where all N are and aligned.
+template <int N>
+__device__ __forceinline__ void store_cells(float *__restrict__ out, int ny, int nx, int pad,
+                                            int Y, int X0, const float (&c)[N]) {
+    const int iy = Y - pad, ix = X0 - pad;
+    if (iy < 0 || iy >= ny) return;
+    const size_t e = (size_t)iy * nx + ix;
+    if (ix >= 0 && ix + N <= nx && (e & 3) == 0) {
+#pragma unroll
+        for (int k = 0; k < N; k += 4)
+            *reinterpret_cast<float4 *>(out + e + k) = make_float4(c[k], c[k + 1], c[k + 2], c[k + 3]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            if (ix + i >= 0 && ix + i < nx) out[(size_t)iy * nx + (ix + i)] = c[i];
+    }
 }
 
 // Split storage of x: x' = x 2^-E, hi = fp16(rint(x' 2^11) 2^-11) (fixed
@@ -63,14 +108,12 @@ __global__ void pack_f16_kernel(const float *__restrict__ in, int ny, int nx, in
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_rows) return;
     const PanelRow r = panel_row(id, p);
+    float c[8];
+    load_cells<8>(in, ny, nx, pad, pad_value, r.Y, r.X0, c);
     uint32_t w[4];
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const uint32_t a = f2h_bits(padded_cell(in, ny, nx, pad, pad_value, r.Y, r.X0 + 2 * i));
-        const uint32_t b = f2h_bits(padded_cell(in, ny, nx, pad, pad_value, r.Y, r.X0 + 2 * i + 1));
-        w[i] = a | (b << 16);
-    }
-    reinterpret_cast<uint4 *>(out)[id] = make_uint4(w[0], w[1], w[2], w[3]);
+    for (int i = 0; i < 4; i++) w[i] = f2h_bits(c[2 * i]) | ((uint32_t)f2h_bits(c[2 * i + 1]) << 16);
+    reinterpret_cast<uint4 *>(out)[r.q] = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
 __global__ void unpack_f16_kernel(const uint16_t *__restrict__ in, int ny, int nx, int pad,
@@ -80,14 +123,12 @@ __global__ void unpack_f16_kernel(const uint16_t *__restrict__ in, int ny, int n
     const PanelRow r = panel_row(id, p);
     const int iy = r.Y - pad;
     if (iy < 0 || iy >= ny) return;
-    const uint4 v = reinterpret_cast<const uint4 *>(in)[id];
+    const uint4 v = reinterpret_cast<const uint4 *>(in)[r.q];
     const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    float c[8];
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const int ix = r.X0 + i - pad;
-        if (ix >= 0 && ix < nx)
-            out[(size_t)iy * nx + ix] = h2f_bits((uint16_t)(w[i >> 1] >> (16 * (i & 1))));
-    }
+    for (int i = 0; i < 8; i++) c[i] = h2f_bits((uint16_t)(w[i >> 1] >> (16 * (i & 1))));
+    store_cells<8>(out, ny, nx, pad, r.Y, r.X0, c);
 }
 
 __global__ void pack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
@@ -97,9 +138,8 @@ __global__ void pack_f32_kernel(const float *__restrict__ in, int ny, int nx, in
     if (id >= n_rows) return;
     const PanelRow r = panel_row(id, p);
     float v[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) v[i] = padded_cell(in, ny, nx, pad, pad_value, r.Y, r.X0 + i);
-    reinterpret_cast<float4 *>(out)[id] = make_float4(v[0], v[1], v[2], v[3]);
+    load_cells<4>(in, ny, nx, pad, pad_value, r.Y, r.X0, v);
+    reinterpret_cast<float4 *>(out)[r.q] = make_float4(v[0], v[1], v[2], v[3]);
 }
 
 __global__ void unpack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
@@ -109,13 +149,9 @@ __global__ void unpack_f32_kernel(const float *__restrict__ in, int ny, int nx, 
     const PanelRow r = panel_row(id, p);
     const int iy = r.Y - pad;
     if (iy < 0 || iy >= ny) return;
-    const float4 v = reinterpret_cast<const float4 *>(in)[id];
-    const float f[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int ix = r.X0 + i - pad;
-        if (ix >= 0 && ix < nx) out[(size_t)iy * nx + ix] = f[i];
-    }
+    const float4 v = reinterpret_cast<const float4 *>(in)[r.q];
+    const float c[4] = {v.x, v.y, v.z, v.w};
+    store_cells<4>(out, ny, nx, pad, r.Y, r.X0, c);
 }
 
 // Scale exponent E of a grid whose max |x| has float bits `bits`: the
@@ -142,19 +178,19 @@ __global__ void pack_split_kernel(const float *__restrict__ in, int ny, int nx, 
     }
     if (id >= n_rows) return;
     const PanelRow r = panel_row(id, p);
+    float c[8];
+    load_cells<8>(in, ny, nx, pad, pad_value, r.Y, r.X0, c);
     uint32_t wh[4], wl[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         uint16_t h[2], l[2];
 #pragma unroll
-        for (int j = 0; j < 2; j++)
-            split_value(padded_cell(in, ny, nx, pad, pad_value, r.Y, r.X0 + 2 * i + j), scale,
-                        h[j], l[j]);
+        for (int j = 0; j < 2; j++) split_value(c[2 * i + j], scale, h[j], l[j]);
         wh[i] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
         wl[i] = (uint32_t)l[0] | ((uint32_t)l[1] << 16);
     }
-    reinterpret_cast<uint4 *>(hi)[id] = make_uint4(wh[0], wh[1], wh[2], wh[3]);
-    reinterpret_cast<uint4 *>(lo)[id] = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+    reinterpret_cast<uint4 *>(hi)[r.q] = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+    reinterpret_cast<uint4 *>(lo)[r.q] = make_uint4(wl[0], wl[1], wl[2], wl[3]);
 }
 
 __global__ void unpack_split_kernel(const uint16_t *__restrict__ hi,
@@ -167,19 +203,18 @@ __global__ void unpack_split_kernel(const uint16_t *__restrict__ hi,
     const PanelRow r = panel_row(id, p);
     const int iy = r.Y - pad;
     if (iy < 0 || iy >= ny) return;
-    const uint4 vh = reinterpret_cast<const uint4 *>(hi)[id];
-    const uint4 vl = reinterpret_cast<const uint4 *>(lo)[id];
+    const uint4 vh = reinterpret_cast<const uint4 *>(hi)[r.q];
+    const uint4 vl = reinterpret_cast<const uint4 *>(lo)[r.q];
     const uint32_t wh[4] = {vh.x, vh.y, vh.z, vh.w};
     const uint32_t wl[4] = {vl.x, vl.y, vl.z, vl.w};
+    float c[8];
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-        const int ix = r.X0 + i - pad;
-        if (ix >= 0 && ix < nx) {
-            const float h = h2f_bits((uint16_t)(wh[i >> 1] >> (16 * (i & 1))));
-            const float l = h2f_bits((uint16_t)(wl[i >> 1] >> (16 * (i & 1))));
-            out[(size_t)iy * nx + ix] = fmaf(l, 1.0f / 2048.0f, h) * scale;
-        }
+        const float h = h2f_bits((uint16_t)(wh[i >> 1] >> (16 * (i & 1))));
+        const float l = h2f_bits((uint16_t)(wl[i >> 1] >> (16 * (i & 1))));
+        c[i] = fmaf(l, 1.0f / 2048.0f, h) * scale;
     }
+    store_cells<8>(out, ny, nx, pad, r.Y, r.X0, c);
 }
 
 // max |x| as float bits (non-negative floats order like their bit patterns).
