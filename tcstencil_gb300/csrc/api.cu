@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <memory>
 #include <string>
@@ -355,6 +356,11 @@ struct tcs_plan_s {
     SplitScale *d_scale = nullptr;  // split form: per-step scale; the planes hold x 2^-E
     unsigned *d_max = nullptr;      // split form: max |x| scratch (float bits)
     float *staging = nullptr;   // ny*nx FP32, for host/row-major transfers
+    // host transfers in row bands: packing (unpacking) of one band on `aux`
+    // while the next band's copy runs on the caller's stream
+    static constexpr int kBands = 4;
+    cudaStream_t aux = nullptr;
+    cudaEvent_t band_ev[kBands + 1] = {};
     cudaStream_t capture_stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (steps, start state)
     unsigned *rows_done = nullptr;  // plain tensor form: per tile row, for multi-step launches
@@ -375,7 +381,32 @@ struct tcs_plan_s {
         if (d_max) dev_free(d_max);
         if (d_scale) dev_free(d_scale);
         if (rows_done) dev_free(rows_done);
+        for (cudaEvent_t e : band_ev)
+            if (e) cudaEventDestroy(e);
+        if (aux) cudaStreamDestroy(aux);
         if (capture_stream) cudaStreamDestroy(capture_stream);
+    }
+
+    // FP16 and FP32 grids of at least 8 MB move in bands; split grids need
+    // their maximum before packing, and small ones gain nothing.
+    bool banded() const {
+        return prob.precision != TCS_PREC_SPLIT &&
+               (size_t)prob.ny * prob.nx * sizeof(float) >= ((size_t)8 << 20);
+    }
+    int ensure_bands() {
+        if (aux) return TCS_OK;
+        int st = cuda_status(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (int k = 0; k <= kBands && !st; k++)
+            st = cuda_status(cudaEventCreateWithFlags(&band_ev[k], cudaEventDisableTiming), "cudaEventCreate");
+        return st;
+    }
+    // band k: plane rows [q0, q1) and the grid rows [r0, r1) they hold
+    void band(int k, int &q0, int &q1, int &r0, int &r1) const {
+        const int nyp = g.p16.nyp;
+        q0 = (int)((long long)nyp * k / kBands);
+        q1 = (int)((long long)nyp * (k + 1) / kBands);
+        r0 = std::max(0, q0 - kPadTop);
+        r1 = std::min(prob.ny, q1 - kPadTop);
     }
 
     // Tile columns of the plain FP16 tensor sweeps (64, 96 or 128,
@@ -554,6 +585,30 @@ int tcs_plan_upload(tcs_plan p, const float *grid, int on_host, void *stream) {
     if (!p || !grid) return fail(TCS_ERR_INVALID, "tcs_plan_upload: null argument");
     cudaStream_t s = (cudaStream_t)stream;
     const float *src = grid;
+    if (on_host && p->banded()) {
+        int st = ensure_staging(p);
+        if (!st) st = p->ensure_bands();
+        if (st) return st;
+        p->cur = 0;
+        const size_t row = (size_t)p->prob.nx;
+        const bool f32 = p->prob.precision == TCS_PREC_F32;
+        for (int k = 0; k < tcs_plan_s::kBands && !st; k++) {
+            int q0, q1, r0, r1;
+            p->band(k, q0, q1, r0, r1);
+            if (r1 > r0)
+                st = cuda_status(cudaMemcpyAsync(p->staging + r0 * row, grid + r0 * row,
+                                                 (size_t)(r1 - r0) * row * sizeof(float),
+                                                 cudaMemcpyHostToDevice, s), "upload copy");
+            if (!st) st = cuda_status(cudaEventRecord(p->band_ev[k], s), "cudaEventRecord");
+            if (!st) st = cuda_status(cudaStreamWaitEvent(p->aux, p->band_ev[k], 0), "cudaStreamWaitEvent");
+            if (!st)
+                st = cuda_status(launch_pack_rows(p->staging, p->prob.ny, p->prob.nx, f32,
+                                                  p->buf[0][0], q0, q1, p->aux), "pack launch");
+        }
+        if (!st) st = cuda_status(cudaEventRecord(p->band_ev[tcs_plan_s::kBands], p->aux), "cudaEventRecord");
+        if (!st) st = cuda_status(cudaStreamWaitEvent(s, p->band_ev[tcs_plan_s::kBands], 0), "cudaStreamWaitEvent");
+        return st;
+    }
     if (on_host) {
         int st = ensure_staging(p);
         if (st) return st;
@@ -591,6 +646,28 @@ int tcs_plan_upload(tcs_plan p, const float *grid, int on_host, void *stream) {
 int tcs_plan_download(tcs_plan p, float *grid, int on_host, void *stream) {
     if (!p || !grid) return fail(TCS_ERR_INVALID, "tcs_plan_download: null argument");
     cudaStream_t s = (cudaStream_t)stream;
+    if (on_host && p->banded()) {
+        int st = ensure_staging(p);
+        if (!st) st = p->ensure_bands();
+        if (st) return st;
+        const size_t row = (size_t)p->prob.nx;
+        const bool f32 = p->prob.precision == TCS_PREC_F32;
+        st = cuda_status(cudaEventRecord(p->band_ev[tcs_plan_s::kBands], s), "cudaEventRecord");
+        if (!st) st = cuda_status(cudaStreamWaitEvent(p->aux, p->band_ev[tcs_plan_s::kBands], 0), "cudaStreamWaitEvent");
+        for (int k = 0; k < tcs_plan_s::kBands && !st; k++) {
+            int q0, q1, r0, r1;
+            p->band(k, q0, q1, r0, r1);
+            st = cuda_status(launch_unpack_rows(p->buf[p->cur][0], p->prob.ny, p->prob.nx, f32,
+                                                p->staging, q0, q1, p->aux), "unpack launch");
+            if (!st) st = cuda_status(cudaEventRecord(p->band_ev[k], p->aux), "cudaEventRecord");
+            if (!st) st = cuda_status(cudaStreamWaitEvent(s, p->band_ev[k], 0), "cudaStreamWaitEvent");
+            if (!st && r1 > r0)
+                st = cuda_status(cudaMemcpyAsync(grid + r0 * row, p->staging + r0 * row,
+                                                 (size_t)(r1 - r0) * row * sizeof(float),
+                                                 cudaMemcpyDeviceToHost, s), "download copy");
+        }
+        return st;
+    }
     float *dst = grid;
     if (on_host) {
         int st = ensure_staging(p);

@@ -45,10 +45,11 @@ struct PanelRow {
     int Y, X0;
     size_t q;
 };
-__device__ __forceinline__ PanelRow panel_row(size_t id, const PlaneGeom &p) {
+__device__ __forceinline__ PanelRow panel_row(size_t id, const PlaneGeom &p, int q0 = 0) {
     PanelRow r;
-    const int yq = static_cast<int>(id / p.npan);
-    const int pan = static_cast<int>(id - (size_t)yq * p.npan);
+    const int yl = static_cast<int>(id / p.npan);  // row within the range
+    const int yq = q0 + yl;
+    const int pan = static_cast<int>(id - (size_t)yl * p.npan);
     r.Y = yq - kPadTop;
     r.X0 = (pan - 1) * p.cpp;
     r.q = (size_t)pan * p.nyp + yq;
@@ -104,10 +105,10 @@ __device__ __forceinline__ void split_value(float x, float scale, uint16_t &h, u
 
 __global__ void pack_f16_kernel(const float *__restrict__ in, int ny, int nx, int pad,
                                 float pad_value, uint16_t *__restrict__ out, PlaneGeom p,
-                                size_t n_rows) {
+                                size_t n_rows, int q0) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_rows) return;
-    const PanelRow r = panel_row(id, p);
+    const PanelRow r = panel_row(id, p, q0);
     float c[8];
     load_cells<8>(in, ny, nx, pad, pad_value, r.Y, r.X0, c);
     uint32_t w[4];
@@ -117,10 +118,10 @@ __global__ void pack_f16_kernel(const float *__restrict__ in, int ny, int nx, in
 }
 
 __global__ void unpack_f16_kernel(const uint16_t *__restrict__ in, int ny, int nx, int pad,
-                                  float *__restrict__ out, PlaneGeom p, size_t n_rows) {
+                                  float *__restrict__ out, PlaneGeom p, size_t n_rows, int q0) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_rows) return;
-    const PanelRow r = panel_row(id, p);
+    const PanelRow r = panel_row(id, p, q0);
     const int iy = r.Y - pad;
     if (iy < 0 || iy >= ny) return;
     const uint4 v = reinterpret_cast<const uint4 *>(in)[r.q];
@@ -133,20 +134,20 @@ __global__ void unpack_f16_kernel(const uint16_t *__restrict__ in, int ny, int n
 
 __global__ void pack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
                                 float pad_value, float *__restrict__ out, PlaneGeom p,
-                                size_t n_rows) {
+                                size_t n_rows, int q0) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_rows) return;
-    const PanelRow r = panel_row(id, p);
+    const PanelRow r = panel_row(id, p, q0);
     float v[4];
     load_cells<4>(in, ny, nx, pad, pad_value, r.Y, r.X0, v);
     reinterpret_cast<float4 *>(out)[r.q] = make_float4(v[0], v[1], v[2], v[3]);
 }
 
 __global__ void unpack_f32_kernel(const float *__restrict__ in, int ny, int nx, int pad,
-                                  float *__restrict__ out, PlaneGeom p, size_t n_rows) {
+                                  float *__restrict__ out, PlaneGeom p, size_t n_rows, int q0) {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n_rows) return;
-    const PanelRow r = panel_row(id, p);
+    const PanelRow r = panel_row(id, p, q0);
     const int iy = r.Y - pad;
     if (iy < 0 || iy >= ny) return;
     const float4 v = reinterpret_cast<const float4 *>(in)[r.q];
@@ -352,7 +353,7 @@ cudaError_t launch_pack_f16(const float *in, int ny, int nx, int pad, float pad_
                             uint16_t *plane, cudaStream_t s) {
     const PackShape ps = pack_shape(ny, nx, pad, 8);
     pack_f16_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, plane,
-                                                             ps.p, ps.rows);
+                                                             ps.p, ps.rows, 0);
     return cudaGetLastError();
 }
 
@@ -360,7 +361,7 @@ cudaError_t launch_unpack_f16(const uint16_t *plane, int ny, int nx, int pad, fl
                               cudaStream_t s) {
     const PackShape ps = pack_shape(ny, nx, pad, 8);
     unpack_f16_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(plane, ny, nx, pad, out, ps.p,
-                                                               ps.rows);
+                                                               ps.rows, 0);
     return cudaGetLastError();
 }
 
@@ -441,7 +442,7 @@ cudaError_t launch_pack_f32(const float *in, int ny, int nx, int pad, float pad_
                             float *plane, cudaStream_t s) {
     const PackShape ps = pack_shape(ny, nx, pad, 4);
     pack_f32_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(in, ny, nx, pad, pad_value, plane,
-                                                             ps.p, ps.rows);
+                                                             ps.p, ps.rows, 0);
     return cudaGetLastError();
 }
 
@@ -449,7 +450,40 @@ cudaError_t launch_unpack_f32(const float *plane, int ny, int nx, int pad, float
                               cudaStream_t s) {
     const PackShape ps = pack_shape(ny, nx, pad, 4);
     unpack_f32_kernel<<<blocks_for(ps.rows), kThreads, 0, s>>>(plane, ny, nx, pad, out, ps.p,
-                                                               ps.rows);
+                                                               ps.rows, 0);
+    return cudaGetLastError();
+}
+
+// Plane rows [q0, q1) only (every panel), pad 0: the grid rows they hold are
+// [q0 - 4, q1 - 4) clipped to the grid; the pad rows above and below belong
+// to the first and last ranges.
+cudaError_t launch_pack_rows(const float *in, int ny, int nx, bool f32, void *plane, int q0,
+                             int q1, cudaStream_t s) {
+    const PackShape ps = pack_shape(ny, nx, 0, f32 ? 4 : 8);
+    if (q0 < 0 || q1 > ps.p.nyp || q0 >= q1) return cudaErrorInvalidValue;
+    const size_t rows = (size_t)(q1 - q0) * ps.p.npan;
+    if (f32)
+        pack_f32_kernel<<<blocks_for(rows), kThreads, 0, s>>>(in, ny, nx, 0, 0.0f,
+                                                              static_cast<float *>(plane), ps.p,
+                                                              rows, q0);
+    else
+        pack_f16_kernel<<<blocks_for(rows), kThreads, 0, s>>>(in, ny, nx, 0, 0.0f,
+                                                              static_cast<uint16_t *>(plane),
+                                                              ps.p, rows, q0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_rows(const void *plane, int ny, int nx, bool f32, float *out, int q0,
+                               int q1, cudaStream_t s) {
+    const PackShape ps = pack_shape(ny, nx, 0, f32 ? 4 : 8);
+    if (q0 < 0 || q1 > ps.p.nyp || q0 >= q1) return cudaErrorInvalidValue;
+    const size_t rows = (size_t)(q1 - q0) * ps.p.npan;
+    if (f32)
+        unpack_f32_kernel<<<blocks_for(rows), kThreads, 0, s>>>(static_cast<const float *>(plane),
+                                                                ny, nx, 0, out, ps.p, rows, q0);
+    else
+        unpack_f16_kernel<<<blocks_for(rows), kThreads, 0, s>>>(
+            static_cast<const uint16_t *>(plane), ny, nx, 0, out, ps.p, rows, q0);
     return cudaGetLastError();
 }
 

@@ -204,6 +204,13 @@ cudaError_t launch_pack_split_dev(const float *in, int ny, int nx, const unsigne
 cudaError_t launch_unpack_split_dev(const uint16_t *hi, const uint16_t *lo, int ny, int nx,
                                     const int *exp_in, float *out, cudaStream_t s);
 cudaError_t launch_max_abs(const float *in, size_t n, unsigned *out_bits, cudaStream_t s);
+// FP16 (f32 false) or FP32 plane rows [q0, q1) from / to an ny x nx
+// row-major grid, no padding; the grid rows involved are [q0 - 4, q1 - 4)
+// clipped to [0, ny).
+cudaError_t launch_pack_rows(const float *in, int ny, int nx, bool f32, void *plane, int q0,
+                             int q1, cudaStream_t s);
+cudaError_t launch_unpack_rows(const void *plane, int ny, int nx, bool f32, float *out, int q0,
+                               int q1, cudaStream_t s);
 
 // ------------------------------------------------ split scale, per step ---
 // A split grid holds x' = x 2^-E as hi + lo 2^-11 with a fixed-point hi, so
