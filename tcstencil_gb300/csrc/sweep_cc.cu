@@ -19,7 +19,13 @@
 // measured on GB300 at 8196², us per step, L1 -> bulk loads -> bulk loads
 // and stores: star2d1r FP16 111.7 -> 73.9 -> 61.4, FP32 182 -> 124 -> 97.6).
 // Five such CTAs fit an SM.  (Persistent CTAs walking tiles through two or
-// three stages measured no faster.)
+// three stages measured no faster.)  A warp whose rows and whose tile's
+// columns all lie in the update rectangle (most warps of a large grid) runs
+// its rows with no per-row tests and immediate row offsets; with that,
+// star2d1r FP16 runs 57.9 -> 49.5 us per step at 8196², star2d2r 66.3 ->
+// 55.0, box2d2r 95.1 -> 83.5 (FP32 97.7 -> 87.3, 109.4 -> 90.9, 160.1 -> 134.5),
+// from the row overhead each lane carried: about 62 instructions per row
+// beside the FMAs.
 //
 // Arithmetic follows gold's tap order (common/gold_*.cpp):
 //  - FP16 storage: acc = fmaf chain from 0, FP32 coefficients, RNE to FP16.
@@ -82,7 +88,7 @@ __device__ __forceinline__ uint32_t lds_u32(uint32_t addr) {
 }
 
 template <int S, bool F32>
-__global__ void __launch_bounds__(kCcWarps * 32)
+__global__ void __launch_bounds__(kCcWarps * 32, 5)
     cc_sweep_kernel(const void *__restrict__ in_, void *__restrict__ out_, CcParams p,
                     TapCoeffs c) {
     constexpr int R = stencil_r(S);
@@ -141,9 +147,10 @@ __global__ void __launch_bounds__(kCcWarps * 32)
     const uint32_t edge0 = lane == 0 ? runs + 4 * 16 + (V - HC) * (uint32_t)sizeof(T)
                                      : runs + (kCcPanels + 1) * kCcRunStride + 4 * 16;
 
-    // Window columns [0, W) of grid row y: cells xl-R .. xl+H+R-1.
-    auto to_window = [&](int y, float (&w)[W]) {
-        const uint32_t r16 = (uint32_t)(y - Y0) * 16;
+    const bool is_l = lane == 0, is_r = lane == 31;
+    // Window columns [0, W) of the stage row at byte offset r16 = (y - Y0) * 16:
+    // cells xl-R .. xl+H+R-1 of grid row y.
+    auto to_window = [&](uint32_t r16, float (&w)[W]) {
         const uint2 v = lds_v2(own0 + r16);
         const uint32_t own[2] = {v.x, v.y};
         uint32_t left[HW], right[HW];
@@ -151,14 +158,12 @@ __global__ void __launch_bounds__(kCcWarps * 32)
         for (int k = 0; k < HW; k++) {
             left[k] = __shfl_up_sync(0xffffffffu, own[2 - HW + k], 1);
             right[k] = __shfl_down_sync(0xffffffffu, own[k], 1);
-        }
-        if (lane == 0 || lane == 31) {
-#pragma unroll
-            for (int k = 0; k < HW; k++) {
-                const uint32_t e = lds_u32(edge0 + r16 + 4 * k);
-                if (lane == 0) left[k] = e;
-                else right[k] = e;
-            }
+            // the outer lanes' halo words are in the side panels' runs: every
+            // lane loads one (the inner lanes all the same word, discarded), so
+            // the warp does not branch
+            const uint32_t e = lds_u32(edge0 + r16 + 4 * k);
+            left[k] = is_l ? e : left[k];
+            right[k] = is_r ? e : right[k];
         }
         float cells[HC + H + HC];
         if constexpr (F32) {
@@ -180,98 +185,139 @@ __global__ void __launch_bounds__(kCcWarps * 32)
         for (int k = 0; k < W; k++) w[k] = cells[HC - R + k];
     };
 
+    // Rows y0, y0+1 from the window rows y0-2 .. y0+3, held as three row
+    // pairs p0, p1, p2, in gold's tap order.
+    auto compute = [&](const float (&p0)[2][W], const float (&p1)[2][W], const float (&p2)[2][W],
+                       float (&acc)[2][H]) {
+        auto row = [&](int wr) -> const float (&)[W] {
+            return wr < 2 ? p0[wr] : wr < 4 ? p1[wr - 2] : p2[wr - 4];
+        };
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            if constexpr (!F32 && R == 1) {
+                // packed FP32 FMAs on cell pairs: each lane rounds as fmaf
+                // does, so the bits are the same (measured at 8196²: star2d1r
+                // 61.4 -> 57.9 us, box2d1r 66.4 -> 63.4; slower for radius 2,
+                // whose windows then crowd the registers)
+                float2 a2[H / 2];
+#pragma unroll
+                for (int k = 0; k < NT; k++) {
+                    const int dy = tap_dy(S, k), dx = tap_dx(S, k);
+                    const float (&x)[W] = row(2 + q + dy);
+                    const float2 cc = make_float2(c.c[k], c.c[k]);
+#pragma unroll
+                    for (int i = 0; i < H; i += 2) {
+                        const float2 x2 = make_float2(x[R + i + dx], x[R + i + 1 + dx]);
+                        a2[i / 2] = __ffma2_rn(x2, cc, k == 0 ? make_float2(0.0f, 0.0f) : a2[i / 2]);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < H; i += 2) {
+                    acc[q][i] = a2[i / 2].x;
+                    acc[q][i + 1] = a2[i / 2].y;
+                }
+            } else {
+                constexpr int dy0 = tap_dy(S, 0), dx0 = tap_dx(S, 0);
+                const float (&x0)[W] = row(2 + q + dy0);
+#pragma unroll
+                for (int i = 0; i < H; i++) {
+                    if constexpr (F32) acc[q][i] = BOX ? __fadd_rn(0.0f, __fmul_rn(x0[R + i + dx0], c.c[0]))
+                                                       : __fmul_rn(x0[R + i + dx0], c.c[0]);
+                    else acc[q][i] = fmaf(x0[R + i + dx0], c.c[0], 0.0f);
+                }
+#pragma unroll
+                for (int k = 1; k < NT; k++) {
+                    const int dy = tap_dy(S, k), dx = tap_dx(S, k);
+                    const float (&x)[W] = row(2 + q + dy);
+#pragma unroll
+                    for (int i = 0; i < H; i++) {
+                        if constexpr (F32) acc[q][i] = __fadd_rn(acc[q][i], __fmul_rn(x[R + i + dx], c.c[k]));
+                        else acc[q][i] = fmaf(x[R + i + dx], c.c[k], acc[q][i]);
+                    }
+                }
+            }
+        }
+    };
+    auto store_row = [&](uint32_t r16, const float (&a)[H]) {
+        uint2 v;
+        if constexpr (F32) v = make_uint2(__float_as_uint(a[0]), __float_as_uint(a[1]));
+        else v = make_uint2(pack_half2(a[0], a[1]), pack_half2(a[2], a[3]));
+        sts_v2(own0 + r16, v);
+    };
+
     // this lane's cells of the update rectangle
     const bool cols_in = xl >= p.g.x0 && xl + H <= p.g.x1;
+    // A warp whose 32 rows and whose tile's 128 columns all lie in the update
+    // rectangle takes a path with no per-row checks and immediate row offsets
+    // (the general path tests rows, columns and the grid's end on every row).
+    const bool fast = __all_sync(0xffffffffu, active && cols_in) && ys >= p.g.y0 &&
+                      ys + kCcWarpRows <= p.g.y1;
 
     // Results go back into the stage, over the rows they replace, and leave
     // by bulk stores: so each warp first reads the rows it shares with its
     // neighbours (two above its rows, two below), and only then, after a
     // barrier, overwrites its own rows.
     // window: pair slot j holds rows (y0-2+2j, y0-1+2j), rotated over steps
+    const uint32_t rs = (uint32_t)(ys - Y0) * 16;  // this warp's first row
     float win[3][2][W];
     float below[2][W];  // rows ye, ye+1
     if (has_rows) {
-        to_window(ys - 2, win[0][0]);
-        to_window(ys - 1, win[0][1]);
-        to_window(ys, win[1][0]);
-        to_window(ys + 1, win[1][1]);
-        to_window(ye, below[0]);
-        to_window(ye + 1, below[1]);
+        to_window(rs - 2 * 16, win[0][0]);
+        to_window(rs - 1 * 16, win[0][1]);
+        to_window(rs, win[1][0]);
+        to_window(rs + 16, win[1][1]);
+        to_window((uint32_t)(ye - Y0) * 16, below[0]);
+        to_window((uint32_t)(ye + 1 - Y0) * 16, below[1]);
     }
     __syncthreads();
 
-    if (has_rows) {
+    if (fast) {
+        // 16 row pairs: five rounds of three (the window's three slots), then
+        // the last pair, whose next rows are the next warp's, read before the
+        // barrier
+        static_assert(kCcWarpRows == 32, "five rounds of three row pairs and one more");
+        uint32_t r = rs;
+        for (int round = 0; round < 5; round++, r += 6 * 16) {
+#pragma unroll
+            for (int u = 0; u < 3; u++) {
+                float (&n)[2][W] = win[(u + 2) % 3];
+                to_window(r + (2 * u + 2) * 16, n[0]);
+                to_window(r + (2 * u + 3) * 16, n[1]);
+                float acc[2][H];
+                compute(win[u], win[(u + 1) % 3], n, acc);
+                store_row(r + 2 * u * 16, acc[0]);
+                store_row(r + (2 * u + 1) * 16, acc[1]);
+            }
+        }
+        float acc[2][H];
+        compute(win[0], win[1], below, acc);
+        store_row(r, acc[0]);
+        store_row(r + 16, acc[1]);
+    } else if (has_rows) {
         for (int y = ys; y < ye; y += 6) {
 #pragma unroll
             for (int u = 0; u < 3; u++) {
                 const int y0 = y + 2 * u;
                 if (y0 < ye) {
-                    float (&n0)[W] = win[(u + 2) % 3][0];
-                    float (&n1)[W] = win[(u + 2) % 3][1];
+                    float (&n)[2][W] = win[(u + 2) % 3];
                     // rows from ye on belong to the next warp, which may have
                     // written them by now, unless the grid ends at ye (then
                     // no warp writes them, and a warp of an odd row count
                     // reads up to ye + 2)
                     if (y0 + 2 < ye || ye == p.g.ny) {
-                        to_window(y0 + 2, n0);
-                        to_window(y0 + 3, n1);
+                        to_window((uint32_t)(y0 + 2 - Y0) * 16, n[0]);
+                        to_window((uint32_t)(y0 + 3 - Y0) * 16, n[1]);
                     } else {
 #pragma unroll
                         for (int k = 0; k < W; k++) {
-                            n0[k] = below[0][k];
-                            n1[k] = below[1][k];
+                            n[0][k] = below[0][k];
+                            n[1][k] = below[1][k];
                         }
                     }
-
                     float acc[2][H];
+                    compute(win[u], win[(u + 1) % 3], n, acc);
 #pragma unroll
                     for (int q = 0; q < 2; q++) {
-                        if constexpr (!F32 && R == 1) {
-                            // packed FP32 FMAs on cell pairs: each lane rounds
-                            // as fmaf does, so the bits are the same (measured
-                            // at 8196²: star2d1r 61.4 -> 57.9 us, box2d1r 66.4
-                            // -> 63.4; slower for radius 2, whose windows then
-                            // crowd the registers)
-                            float2 a2[H / 2];
-#pragma unroll
-                            for (int k = 0; k < NT; k++) {
-                                const int dy = tap_dy(S, k), dx = tap_dx(S, k);
-                                const int wr = 2 + q + dy;
-                                const float2 cc = make_float2(c.c[k], c.c[k]);
-#pragma unroll
-                                for (int i = 0; i < H; i += 2) {
-                                    const float2 x2 = make_float2(win[(u + wr / 2) % 3][wr % 2][R + i + dx],
-                                                                  win[(u + wr / 2) % 3][wr % 2][R + i + 1 + dx]);
-                                    a2[i / 2] = __ffma2_rn(x2, cc, k == 0 ? make_float2(0.0f, 0.0f) : a2[i / 2]);
-                                }
-                            }
-#pragma unroll
-                            for (int i = 0; i < H; i += 2) {
-                                acc[q][i] = a2[i / 2].x;
-                                acc[q][i + 1] = a2[i / 2].y;
-                            }
-                        } else {
-                            constexpr int dy0 = tap_dy(S, 0), dx0 = tap_dx(S, 0);
-                            const int wr = 2 + q + dy0;  // window row of y0 + q + dy
-#pragma unroll
-                            for (int i = 0; i < H; i++) {
-                                const float x0 = win[(u + wr / 2) % 3][wr % 2][R + i + dx0];
-                                if constexpr (F32) acc[q][i] = BOX ? __fadd_rn(0.0f, __fmul_rn(x0, c.c[0]))
-                                                                   : __fmul_rn(x0, c.c[0]);
-                                else acc[q][i] = fmaf(x0, c.c[0], 0.0f);
-                            }
-#pragma unroll
-                            for (int k = 1; k < NT; k++) {
-                                const int dy = tap_dy(S, k), dx = tap_dx(S, k);
-                                const int wr = 2 + q + dy;
-#pragma unroll
-                                for (int i = 0; i < H; i++) {
-                                    const float x = win[(u + wr / 2) % 3][wr % 2][R + i + dx];
-                                    if constexpr (F32) acc[q][i] = __fadd_rn(acc[q][i], __fmul_rn(x, c.c[k]));
-                                    else acc[q][i] = fmaf(x, c.c[k], acc[q][i]);
-                                }
-                            }
-                        }
                         // cells outside the update rectangle keep their value
                         const int yy = y0 + q;
                         const bool row_in = yy >= p.g.y0 && yy < p.g.y1;
@@ -280,15 +326,10 @@ __global__ void __launch_bounds__(kCcWarps * 32)
                             for (int i = 0; i < H; i++) {
                                 const int x = xl + i;
                                 if (!(row_in && x >= p.g.x0 && x < p.g.x1))
-                                    acc[q][i] = win[(u + (2 + q) / 2) % 3][(2 + q) % 2][R + i];
+                                    acc[q][i] = win[(u + 1) % 3][q][R + i];
                             }
                         }
-                        if (active && yy < ye) {
-                            uint2 v;
-                            if constexpr (F32) v = make_uint2(__float_as_uint(acc[q][0]), __float_as_uint(acc[q][1]));
-                            else v = make_uint2(pack_half2(acc[q][0], acc[q][1]), pack_half2(acc[q][2], acc[q][3]));
-                            sts_v2(own0 + (uint32_t)(yy - Y0) * 16, v);
-                        }
+                        if (active && yy < ye) store_row((uint32_t)(yy - Y0) * 16, acc[q]);
                     }
                 }
             }
