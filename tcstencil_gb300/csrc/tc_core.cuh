@@ -834,16 +834,8 @@ __device__ __forceinline__ void plain_epilogue(const TileOut &o, uint32_t lane_c
 
 // Launches a single-grid step kernel with programmatic stream serialization:
 // the next step's CTAs do their set-up (barriers, TMEM, bands) while this
-// step's last tiles finish, and wait in pdl_wait() before touching a plane.
-// Setting TCS_PDL=0 in the environment launches in plain stream order.
-inline bool pdl_enabled() {
-    static const bool on = [] {
-        const char *e = getenv("TCS_PDL");
-        return !(e && e[0] == '0');
-    }();
-    return on;
-}
-
+// step's last tiles finish, and wait in pdl_wait() before touching a plane
+// (pdl_enabled: TCS_PDL=0 in the environment launches in plain stream order).
 // cooperative: a launch of several steps, whose CTAs wait on one another's
 // tile rows, must have all its CTAs resident at once (and is not overlapped).
 template <typename Params>

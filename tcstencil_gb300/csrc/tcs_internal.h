@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "../../include/tcs.h"
 
@@ -253,6 +254,18 @@ cudaError_t launch_split_scale_init(SplitScale *sc, const unsigned *max_bits, co
 cudaError_t launch_split_scale_end_run(SplitScale *sc, int steps, cudaStream_t s);
 // The exponent of a split grid's state between runs (slot 0).
 inline const int *split_scale_exp_ptr(const SplitScale *sc) { return &sc->exp[0]; }
+
+// Whether step kernels launch with programmatic stream serialization (the
+// next step's CTAs set up while the previous step's last tiles finish, and
+// wait in griddepcontrol.wait before touching a plane).  TCS_PDL=0 in the
+// environment launches in plain stream order.
+inline bool pdl_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("TCS_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
 // the reference's layout16 transforms (bricks of 16 x 16, row-major inside)
 cudaError_t launch_padding_2d(const uint16_t *in, uint16_t *out, int size, int halo,
                               uint16_t value, cudaStream_t s);

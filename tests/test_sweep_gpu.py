@@ -53,6 +53,26 @@ def test_cudacore_f32_bit_exact_with_gold(tcs, torch_cuda, stencil, shape):
     np.testing.assert_array_equal(got.view(np.uint32), expect.view(np.uint32))
 
 
+@pytest.mark.parametrize("precision", ["f16", "f32"])
+@pytest.mark.parametrize("stencil", STENCILS)
+def test_cudacore_interior_and_edge_warps(tcs, torch_cuda, stencil, precision):
+    """An update rectangle that cuts through tiles, so that warps whose 32 rows
+    and whose tile's columns all lie inside it (the interior path, no per-row
+    tests) sit beside warps with rows or columns outside (the general path):
+    bit-exact with the oracle, both storage types, over several steps."""
+    rng = np.random.default_rng(77)
+    A = grid(rng, 420, 700)
+    B = normalized_coeffs(rng, stencil)
+    rect = (37, 350, 140, 650)
+    got = run_plan(tcs, A, B, stencil, 5, "cudacore", precision, rect=rect)
+    if precision == "f16":
+        expect = oracle.sweep_f16cc(oracle.f32_to_f16(A), B, stencil, 5, rect=rect)
+        np.testing.assert_array_equal(oracle.f32_to_f16(got), expect)
+    else:
+        expect = oracle.sweep_f32(A, B, stencil, 5, rect=rect)
+        np.testing.assert_array_equal(got.view(np.uint32), expect.view(np.uint32))
+
+
 @pytest.mark.parametrize("stencil", ["box2d2r", "star2d2r"])
 def test_tensor_single_taps(tcs, torch_cuda, stencil):
     """Each tap alone (coefficient 1.0) shifts the grid exactly; a failure names
