@@ -97,13 +97,18 @@ import tcstencil_gb300 as tcs
 from helpers import grid, normalized_coeffs
 rng = np.random.default_rng(5)
 out = []
-for (ny, nx), st, prec in (((700, 500), "box2d2r", "f16"), ((700, 500), "star2d1r", "f16"),
-                           ((700, 500), "box2d1r", "split"), ((2100, 1500), "box2d1r", "f16"),
-                           ((2100, 1500), "star2d2r", "f16")):
+for (ny, nx), st, prec, eng in (((700, 500), "box2d2r", "f16", "tensor"),
+                                ((700, 500), "star2d1r", "f16", "tensor"),
+                                ((700, 500), "box2d1r", "split", "tensor"),
+                                ((2100, 1500), "box2d1r", "f16", "tensor"),
+                                ((2100, 1500), "star2d2r", "f16", "tensor"),
+                                ((700, 500), "star2d2r", "f16", "cudacore"),
+                                ((2100, 1500), "box2d2r", "f32", "cudacore")):
     A = grid(rng, ny, nx)
     B = normalized_coeffs(rng, st)
-    p = tcs.Plan(ny, nx, st, B, engine="tensor", precision=prec, temporal_depth=1)
-    p.set_multistep(1)
+    p = tcs.Plan(ny, nx, st, B, engine=eng, precision=prec, temporal_depth=1)
+    if eng == "tensor":
+        p.set_multistep(1)
     p.upload(A); p.run(9)
     o = np.empty_like(A); p.download(o); p.close()
     out.append(o.ravel())
@@ -115,8 +120,9 @@ np.save(sys.argv[2], np.concatenate(out))
 @pytest.mark.parametrize("env", [{}, {"TCS_PDL": "0"}, {"TCS_MULTI": "0"},
                                  {"TCS_PDL": "0", "TCS_MULTI": "0"}])
 def test_launch_switches_change_no_bits(tmp_path, torch_cuda, env):
-    """The same sweeps with overlapped step launches and multi-step launches
-    switched off (environment switches read once per process)."""
+    """The same sweeps (tensor and CUDA-core steps) with overlapped step
+    launches and multi-step launches switched off (environment switches read
+    once per process)."""
     def run(e, name):
         path = tmp_path / name
         full = dict(os.environ, **e)
