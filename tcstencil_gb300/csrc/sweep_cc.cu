@@ -196,13 +196,42 @@ __global__ void __launch_bounds__(kCcWarps * 32, 5)
         auto row = [&](int wr) -> const float (&)[W] {
             return wr < 2 ? p0[wr] : wr < 4 ? p1[wr - 2] : p2[wr - 4];
         };
+        if constexpr (!F32 && R == 2 && !BOX) {
+            // packed FP32 FMAs on cell pairs, taps outside the rows so that
+            // one coefficient pair serves both rows; each lane rounds as
+            // fmaf does, so the bits are the same (measured at 8196²:
+            // star2d2r 55.0 -> 51.8 us; box2d2r, whose 25 taps then spill
+            // registers, 83.0 -> 92.5, keeps the scalar chain)
+            float2 a2[2][H / 2];
+#pragma unroll
+            for (int k = 0; k < NT; k++) {
+                const int dy = tap_dy(S, k), dx = tap_dx(S, k);
+                const float2 cc = make_float2(c.c[k], c.c[k]);
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const float (&x)[W] = row(2 + q + dy);
+#pragma unroll
+                    for (int i = 0; i < H; i += 2) {
+                        const float2 x2 = make_float2(x[R + i + dx], x[R + i + 1 + dx]);
+                        a2[q][i / 2] = __ffma2_rn(x2, cc, k == 0 ? make_float2(0.0f, 0.0f) : a2[q][i / 2]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++)
+#pragma unroll
+                for (int i = 0; i < H; i += 2) {
+                    acc[q][i] = a2[q][i / 2].x;
+                    acc[q][i + 1] = a2[q][i / 2].y;
+                }
+            return;
+        }
 #pragma unroll
         for (int q = 0; q < 2; q++) {
             if constexpr (!F32 && R == 1) {
                 // packed FP32 FMAs on cell pairs: each lane rounds as fmaf
                 // does, so the bits are the same (measured at 8196²: star2d1r
-                // 61.4 -> 57.9 us, box2d1r 66.4 -> 63.4; slower for radius 2,
-                // whose windows then crowd the registers)
+                // 61.4 -> 57.9 us, box2d1r 66.4 -> 63.4)
                 float2 a2[H / 2];
 #pragma unroll
                 for (int k = 0; k < NT; k++) {
