@@ -196,12 +196,14 @@ __global__ void __launch_bounds__(kCcWarps * 32, 5)
         auto row = [&](int wr) -> const float (&)[W] {
             return wr < 2 ? p0[wr] : wr < 4 ? p1[wr - 2] : p2[wr - 4];
         };
-        if constexpr (!F32 && R == 2 && !BOX) {
+        if constexpr (!F32 && (R == 1 || !BOX)) {
             // packed FP32 FMAs on cell pairs, taps outside the rows so that
             // one coefficient pair serves both rows; each lane rounds as
-            // fmaf does, so the bits are the same (measured at 8196²:
-            // star2d2r 55.0 -> 51.8 us; box2d2r, whose 25 taps then spill
-            // registers, 83.0 -> 92.5, keeps the scalar chain)
+            // fmaf does, so the bits are the same (measured at 8196², us per
+            // step: star2d1r 61.4 -> 57.9 and box2d1r 66.4 -> 63.4 before
+            // the interior path, star2d2r 55.0 -> 51.8 after it; box2d2r,
+            // whose 25 taps then spill registers, 83.0 -> 92.5, keeps the
+            // scalar chain)
             float2 a2[2][H / 2];
 #pragma unroll
             for (int k = 0; k < NT; k++) {
@@ -226,47 +228,26 @@ __global__ void __launch_bounds__(kCcWarps * 32, 5)
                 }
             return;
         }
+        // scalar chains: FP32 storage (gold's unfused products and sums) and
+        // the FP16 box2d2r
 #pragma unroll
         for (int q = 0; q < 2; q++) {
-            if constexpr (!F32 && R == 1) {
-                // packed FP32 FMAs on cell pairs: each lane rounds as fmaf
-                // does, so the bits are the same (measured at 8196²: star2d1r
-                // 61.4 -> 57.9 us, box2d1r 66.4 -> 63.4)
-                float2 a2[H / 2];
+            constexpr int dy0 = tap_dy(S, 0), dx0 = tap_dx(S, 0);
+            const float (&x0)[W] = row(2 + q + dy0);
 #pragma unroll
-                for (int k = 0; k < NT; k++) {
-                    const int dy = tap_dy(S, k), dx = tap_dx(S, k);
-                    const float (&x)[W] = row(2 + q + dy);
-                    const float2 cc = make_float2(c.c[k], c.c[k]);
+            for (int i = 0; i < H; i++) {
+                if constexpr (F32) acc[q][i] = BOX ? __fadd_rn(0.0f, __fmul_rn(x0[R + i + dx0], c.c[0]))
+                                                   : __fmul_rn(x0[R + i + dx0], c.c[0]);
+                else acc[q][i] = fmaf(x0[R + i + dx0], c.c[0], 0.0f);
+            }
 #pragma unroll
-                    for (int i = 0; i < H; i += 2) {
-                        const float2 x2 = make_float2(x[R + i + dx], x[R + i + 1 + dx]);
-                        a2[i / 2] = __ffma2_rn(x2, cc, k == 0 ? make_float2(0.0f, 0.0f) : a2[i / 2]);
-                    }
-                }
-#pragma unroll
-                for (int i = 0; i < H; i += 2) {
-                    acc[q][i] = a2[i / 2].x;
-                    acc[q][i + 1] = a2[i / 2].y;
-                }
-            } else {
-                constexpr int dy0 = tap_dy(S, 0), dx0 = tap_dx(S, 0);
-                const float (&x0)[W] = row(2 + q + dy0);
+            for (int k = 1; k < NT; k++) {
+                const int dy = tap_dy(S, k), dx = tap_dx(S, k);
+                const float (&x)[W] = row(2 + q + dy);
 #pragma unroll
                 for (int i = 0; i < H; i++) {
-                    if constexpr (F32) acc[q][i] = BOX ? __fadd_rn(0.0f, __fmul_rn(x0[R + i + dx0], c.c[0]))
-                                                       : __fmul_rn(x0[R + i + dx0], c.c[0]);
-                    else acc[q][i] = fmaf(x0[R + i + dx0], c.c[0], 0.0f);
-                }
-#pragma unroll
-                for (int k = 1; k < NT; k++) {
-                    const int dy = tap_dy(S, k), dx = tap_dx(S, k);
-                    const float (&x)[W] = row(2 + q + dy);
-#pragma unroll
-                    for (int i = 0; i < H; i++) {
-                        if constexpr (F32) acc[q][i] = __fadd_rn(acc[q][i], __fmul_rn(x[R + i + dx], c.c[k]));
-                        else acc[q][i] = fmaf(x[R + i + dx], c.c[k], acc[q][i]);
-                    }
+                    if constexpr (F32) acc[q][i] = __fadd_rn(acc[q][i], __fmul_rn(x[R + i + dx], c.c[k]));
+                    else acc[q][i] = fmaf(x[R + i + dx], c.c[k], acc[q][i]);
                 }
             }
         }
